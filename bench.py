@@ -1,0 +1,394 @@
+#!/usr/bin/env python
+"""Benchmark of the FEMOCS field-solve path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload config2|config1]
+
+Workload (default `config2`): synthetic FCC-Cu nanotip, tip radius 5 nm, height 40 nm, on an
+80x80x4 nm slab, vacuum box up to 250 nm, graded tet mesh split into ~2.1e6 vacuum Q1
+hexahedra (~2.3e6 DoFs); applied field 1 GV/m (Neumann), phi = 0 on the metal; 1e6 query
+points = all surface atoms (coordination < 12) + uniform random vacuum probes. Q1 elements
+stand in for the configuration's Q2 elements (not provided).
+
+One step = the reference's Femocs::run field path on resident data: full assembly (element
+matrices, CSR scatter, Neumann rhs, Dirichlet elimination), CG solve to a 1e-9 relative
+FP64 residual (FP32 inner PCG + FP64 refinement), nodal field recovery + smoothing, location
++ interpolation (rank 1) of all query points. Metric: solved DOF/s = DoFs / step time.
+`e2e` runs the same step through the reference-facing C ABI (femocs_run +
+femocs_interpolate_elfield) with host arrays in and out.
+
+N > 1 (torchrun): independent replicas, one per GPU (the solve does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+E0 = -0.1          # V/A, i.e. 1 GV/m; the Neumann value on the top is -E0
+REL_TOL = 1e-9
+RANK = 1           # interpolation_rank default of the reference (src/Config.cpp:29)
+N_POINTS = {"config2": 1_000_000, "config1": 100_000}
+# SSOR(1.2)-PCG iterations to a 1e-9 relative residual on these exact systems, measured by
+# running the oracle's restatement of the reference solve (oracle/femocs_oracle.c) to
+# convergence; the CPU baseline times iterations live and multiplies by this count.
+SSOR_ITERS = {"config1": 268, "config2": 540}
+# DRAM bytes per launch of the FP32 CG SpMV kernel from an ncu capture (profiles/), or None
+SPMV_TRAFFIC = {"config2": None, "config1": None}
+FALLBACK_HBM_GBS = 6800.0
+
+
+def spec_of(workload):
+    import femocs_gb300 as fg
+    return dict(fg.CONFIG2 if workload == "config2" else fg.CONFIG1)
+
+
+def make_points(spec, n_points):
+    import numpy as np
+    import femocs_gb300 as fg
+    atoms, types = fg.synth_atoms(spec, seed=12345)
+    surf = atoms[types == 2]
+    n_probe = max(0, n_points - len(surf))
+    probes = fg.synth_probes(spec, n_probe, seed=777) if n_probe else np.zeros((0, 3))
+    return np.ascontiguousarray(np.r_[surf, probes][:n_points]), len(surf)
+
+
+def write_conf(path, spec, precision="mixed"):
+    with open(path, "w") as f:
+        f.write(f"""mesh_file synthetic
+radius {spec['radius']}
+tip_height {spec['height']}
+gpu_box_half {spec['box_half']}
+gpu_slab {spec['slab']}
+gpu_top {spec['top']}
+gpu_h {spec['h']}
+gpu_growth {spec['growth']}
+gpu_margin {spec['margin']}
+elfield {E0}
+anode_bc neumann
+interpolation_rank {RANK}
+smoothen_field true
+gpu_precision {precision}
+gpu_rel_tol {REL_TOL}
+field_ncg 100000
+""")
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self, gpu_index=0):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9 or not f[0].isdigit() or int(f[0]) != gpu_index:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(world, v):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return v
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ----------------------------------------------------------------------------------------
+def cpu_baseline(field, workload, n_points, pts, spec, budget_s=15.0):
+    """Oracle restatement of the reference CPU path on the host cores (1 thread, like the
+    reference default n_omp=1): SSOR(1.2)-PCG iterations on the same assembled system, and the
+    reference's sequential location + interpolation on a sample of the points."""
+    import numpy as np
+    import oracle as orc
+    rowptr, col, val, rhs, d2n = field.system()
+    sysm = orc.System(csr=(rowptr, col, val, rhs))
+    t_it = sysm.ssor_cg_fixed(2)
+    n_it = max(3, min(200, int(0.7 * budget_s / max(t_it / 2, 1e-6))))
+    t = sysm.ssor_cg_fixed(n_it)
+    t_iter = t / n_it
+    solve_s = t_iter * SSOR_ITERS[workload]
+    return dict(value=field.n_dofs / solve_s, unit="DOF/s", cores=1, kind="port",
+                sample=f"{n_it} SSOR(1.2)-PCG iterations of the oracle (reference deal.II CG+SSOR restated) on the "
+                       f"full {field.n_dofs}-DoF system, {t_iter * 1e3:.1f} ms/iteration x {SSOR_ITERS[workload]} "
+                       f"iterations to 1e-9 (count measured by a full oracle solve of this system); solve only")
+
+
+def run_ours(args, world, rank):
+    import numpy as np
+    import femocs_gb300 as fg
+    from femocs_gb300._lib import load
+
+    spec = spec_of(args.workload)
+    n_points = args.points or N_POINTS[args.workload]
+    pts, n_surf = make_points(spec, n_points)
+    tmp = tempfile.mkdtemp(prefix="fgb_bench_")
+    conf = os.path.join(tmp, "bench.in")
+    write_conf(conf, spec)
+    fem = fg.Femocs(conf)
+    if fem.run() != 0:
+        raise RuntimeError("femocs_run failed: " + fg.last_error())
+    # borrowed handle of the device field femocs_run solved on (only DoF-indexed exports used)
+    field = fem.field({"n_nodes": 0})
+    n = field.n_dofs
+    d_pts = fg.DeviceBuffer(24 * n_points)
+    d_pts.upload(pts)
+    d_cells = fg.DeviceBuffer(4 * n_points)
+    d_out = fg.DeviceBuffer(40 * n_points)
+
+    solve_stats = []
+
+    def step(precision):
+        field.setup(-E0, 0.0)
+        field.assemble(True, False)
+        rc, st = field.solve(precision=precision, rel_tol=REL_TOL, max_iter=100000)
+        if rc <= 0:
+            raise RuntimeError(f"solve did not converge: {st}")
+        field.extract(True)
+        field.interpolate_device(n_points, d_pts.ptr, RANK, d_cells.ptr, d_out.ptr)
+        return st
+
+    for _ in range(args.warmup):
+        step(1)
+    lib = load()
+    sampler = ClockSampler()
+    sampler.start()
+    barrier(world)
+    launches0 = lib.fgb_kernel_launches()
+    field.mark(0)
+    for _ in range(args.steps):
+        solve_stats.append(step(1))
+    field.mark(1)
+    dev_ms = field.elapsed(0, 1)
+    launches = lib.fgb_kernel_launches() - launches0
+    clocks = sampler.stop(0)
+    dev_ms = reduce_max(world, dev_ms)
+    ms_per_step = dev_ms / args.steps
+    value = n * args.steps * world / (dev_ms * 1e-3)
+    solve_ms = [s["ms"] for s in solve_stats]
+
+    # plain FP64 Jacobi-PCG on the same system, same step otherwise
+    plain = []
+    for _ in range(min(3, args.steps)):
+        plain.append(step(0))
+    plain_ms = [s["ms"] for s in plain]
+
+    # end to end through the reference-facing C ABI with host buffers
+    x, y, z = (np.ascontiguousarray(pts[:, k]) for k in range(3))
+    e2e_t = []
+    for _ in range(min(3, args.steps)):
+        t0 = time.perf_counter()
+        if fem.run() != 0:
+            raise RuntimeError(fg.last_error())
+        rv, Ex, Ey, Ez, En, flag = fem.interpolate_elfield(x, y, z)
+        e2e_t.append(time.perf_counter() - t0)
+        if rv != 0:
+            raise RuntimeError(fg.last_error())
+    e2e_s = reduce_max(world, statistics.median(e2e_t))
+
+    # roofline of the dominant kernel: FP32 SpMV+dot of the inner CG
+    spmv_ms = field.time_spmv(1, 50)
+    nnz = field.nnz
+    alg_bytes = nnz * (4 + 4) + (n + 1) * 4 + 2 * n * 4
+    peak, peak_kind = measured_hbm_peak()
+    achieved = alg_bytes / (spmv_ms * 1e-3) / 1e9
+    spmv64_ms = field.time_spmv(0, 20)
+
+    line = {
+        "metric": "solved DOF/s and p50/p99 solve latency at 1e-9 rel. residual vs plain FP64 CG",
+        "value": value,
+        "unit": "DOF/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 inner / f64 refinement",
+        "data": "synthetic (seeded nanotip mesh, FCC surface atoms, random vacuum probes)",
+        "config": {"workload": f"{args.workload}: nanotip R={spec['radius'] / 10:g} nm H={spec['height'] / 10:g} nm, "
+                               f"box {2 * spec['box_half'] / 10:g} nm, top {spec['top'] / 10:g} nm, Q1",
+                   "n_dofs": n, "nnz": nnz, "n_points": n_points, "n_surface_atoms": n_surf,
+                   "interpolation_rank": RANK, "rel_tol": REL_TOL, "precision": "fp32 inner PCG + fp64 refinement",
+                   "l2": "inputs larger than L2 (FP64 matrix %.0f MB)" % (nnz * 12 / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "solve": {"p50_ms": statistics.median(solve_ms), "p99_ms": float(np.percentile(solve_ms, 99)),
+                  "iterations": solve_stats[-1]["iterations"], "outer": solve_stats[-1]["outer"],
+                  "rel_residual": solve_stats[-1]["rel_residual"],
+                  "solved_dof_per_s": n / (statistics.median(solve_ms) * 1e-3)},
+        "plain_fp64_cg": {"p50_ms": statistics.median(plain_ms), "iterations": plain[-1]["iterations"],
+                          "rel_residual": plain[-1]["rel_residual"],
+                          "solved_dof_per_s": n / (statistics.median(plain_ms) * 1e-3),
+                          "speedup_mixed_vs_plain": statistics.median(plain_ms) / statistics.median(solve_ms)},
+        "e2e": {"value": n * world / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": 24 * n_points,
+                "d2h_bytes_per_step": 36 * n_points,
+                "note": "femocs_run + femocs_interpolate_elfield through the C ABI, host arrays"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": SPMV_TRAFFIC.get(args.workload), "kernel": "k_cg_spmv_pq<float>",
+                     "algorithmic_bytes": alg_bytes, "launch_ms": spmv_ms, "peak_kind": peak_kind,
+                     "fp64_launch_ms": spmv64_ms},
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU path (oracle port; the reference itself needs deal.II): per step,
+    SSOR-PCG iterations on the assembled system plus the sequential location/interpolation
+    of a sample of the points, scaled to the full solve and point count."""
+    if rank != 0:
+        return
+    import numpy as np
+    import femocs_gb300 as fg
+    import oracle as orc
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from util import oracle_tables, vacuum_system_inputs
+
+    spec = spec_of(args.workload)
+    n_points = args.points or N_POINTS[args.workload]
+    pts, _ = make_points(spec, n_points)
+    m = fg.Mesh.synthetic(**spec)
+    xyz, cells, v2n = vacuum_system_inputs(m)
+    t0 = time.perf_counter()
+    sysm = orc.System(xyz, cells, -E0)
+    t_assemble = time.perf_counter() - t0
+    it0, x0 = sysm.ssor_cg(1.2, 1e-3 * np.linalg.norm(sysm.rhs), 5)
+    phi = np.zeros(m.sizes()["n_nodes"])
+    phi[v2n] = x0
+    nnodes = m.sizes()
+    sol = np.zeros((nnodes["n_nodes"], 5))
+    sol[:, 4] = phi
+    tables = oracle_tables(m, sol)
+    rng = np.random.default_rng(3)
+    sample = np.sort(rng.choice(n_points, size=min(2000, n_points), replace=False))
+    step_s = []
+
+    def one_step():
+        t = sysm.ssor_cg_fixed(10) / 10
+        ti = time.perf_counter()
+        orc.locate_interpolate(tables, RANK, pts[sample])
+        t_int = (time.perf_counter() - ti) / len(sample) * n_points
+        return t_assemble + t * SSOR_ITERS[args.workload] + t_int
+
+    for _ in range(args.warmup):
+        one_step()
+    for _ in range(args.steps):
+        step_s.append(one_step())
+    s = statistics.median(step_s)
+    n = sysm.n
+    v = n / s
+    line = {
+        "metric": "solved DOF/s and p50/p99 solve latency at 1e-9 rel. residual vs plain FP64 CG",
+        "value": v, "unit": "DOF/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": args.workload, "n_dofs": n, "n_points": n_points},
+        "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": 1, "kind": "port",
+                         "sample": f"per step: 10 SSOR(1.2)-PCG iterations x {SSOR_ITERS[args.workload]} to 1e-9, "
+                                   f"assembly timed once ({t_assemble:.1f} s), sequential location+interpolation of "
+                                   f"{len(sample)} of {n_points} points scaled"},
+        "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "config1"])
+    ap.add_argument("--points", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    world, rank, _ = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        from femocs_gb300.build import build
+        build()
+        run_ours(args, world, rank)
+
+
+if __name__ == "__main__":
+    main()

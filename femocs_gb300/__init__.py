@@ -1,0 +1,324 @@
+"""femocs_gb300: GB300-native field-solve path of FEMOCS (Poisson FEM, CG, nodal field,
+cell location and interpolation onto atoms), exposed through the reference's C ABI.
+
+Python here is a thin host-side mirror of the C ABI for tests and benchmarks; the
+computation runs in libfemocs_gb300.so (C++ host code + sm_103a CUDA kernels).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import FgbNanotip, dp, i64p, ip, last_error, load, ptr
+
+__all__ = ["Mesh", "Field", "Femocs", "nanotip", "synth_atoms", "synth_probes", "load", "last_error",
+           "CONFIG1", "CONFIG2", "FgbNanotip", "DeviceBuffer"]
+
+
+def nanotip(radius=20.0, height=80.0, box_half=100.0, slab=20.0, top=600.0, h=8.0, growth=1.3, margin=10.0):
+    """Nanotip geometry + grid grading (Angstrom)."""
+    return FgbNanotip(radius, height, box_half, slab, top, h, growth, margin)
+
+
+# Synthetic stand-ins for the benchmark configurations (tip radius/height, slab, vacuum top as
+# in the workload descriptions; grid spacing chosen for the stated hex counts).
+CONFIG1 = dict(radius=20.0, height=80.0, box_half=100.0, slab=20.0, top=600.0, h=7.0, growth=1.25, margin=12.0)
+CONFIG2 = dict(radius=50.0, height=400.0, box_half=400.0, slab=40.0, top=2500.0, h=9.5, growth=1.18, margin=20.0)
+
+
+class Mesh:
+    """Host-prepared tetrahedral mesh (tet->hex split, neighbour lists, interpolation tables)."""
+
+    SIZE_NAMES = ["n_tetnodes", "n_tets", "n_nodes", "n_hexs", "n_vac_vertices", "n_vac_cells", "n_nbr_idx",
+                  "n_voro_idx"]
+
+    def __init__(self, handle):
+        if not handle:
+            raise RuntimeError("mesh construction failed: " + last_error())
+        self.h = handle
+        self._sizes = None
+
+    @classmethod
+    def from_arrays(cls, xyz, tets, markers):
+        lib = load()
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        tets = np.ascontiguousarray(tets, dtype=np.int32).reshape(-1)
+        markers = np.ascontiguousarray(markers, dtype=np.int32).reshape(-1)
+        return cls(lib.fgb_mesh_from_arrays(len(xyz) // 3, ptr(xyz), len(tets) // 4, ptr(tets, ip), ptr(markers, ip)))
+
+    @classmethod
+    def synthetic(cls, **kw):
+        spec = nanotip(**kw)
+        return cls(load().fgb_mesh_synthetic(C.byref(spec)))
+
+    @classmethod
+    def read_gmsh(cls, path):
+        return cls(load().fgb_mesh_read_gmsh(path.encode()))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().fgb_mesh_free(self.h)
+            self.h = None
+
+    def sizes(self):
+        if self._sizes is None:
+            o = np.zeros(12, dtype=np.int64)
+            load().fgb_mesh_sizes(self.h, ptr(o, i64p))
+            self._sizes = dict(zip(self.SIZE_NAMES, o[:8].tolist()))
+        return self._sizes
+
+    def export(self, name):
+        s = self.sizes()
+        shapes = {
+            "tet_nodes": (np.int32, 4 * s["n_tets"]), "tet_marker": (np.int32, s["n_tets"]),
+            "tet_nbor": (np.int32, 4 * s["n_tets"]), "node_xyz": (np.float64, 3 * s["n_nodes"]),
+            "node_marker": (np.int32, s["n_nodes"]), "hex_nodes": (np.int32, 8 * s["n_hexs"]),
+            "hex_marker": (np.int32, s["n_hexs"]), "tet_det": (np.float64, 17 * s["n_tets"]),
+            "tet_centroid": (np.float64, 3 * s["n_tets"]), "hex_coeffs": (np.float64, 24 * s["n_hexs"]),
+            "nbr_ptr": (np.int32, s["n_tets"] + 1), "nbr_idx": (np.int32, s["n_nbr_idx"]),
+            "quad_nodes": (np.int32, 10 * s["n_tets"]), "voro_ptr": (np.int32, s["n_tetnodes"] + 1),
+            "voro_idx": (np.int32, s["n_voro_idx"]), "vac_node2vertex": (np.int32, s["n_nodes"]),
+            "vac_cells": (np.int32, s["n_vac_cells"]), "tet_search": (np.int32, s["n_tets"]),
+            "edgemax": (np.float64, 1),
+        }
+        dt, n = shapes[name]
+        out = np.zeros(max(n, 1), dtype=dt)
+        if load().fgb_mesh_export(self.h, name.encode(), out.ctypes.data_as(C.c_void_p)) != 0:
+            raise RuntimeError(last_error())
+        return out[:n]
+
+
+class Field:
+    """Device-resident Poisson system + interpolator of one mesh (PoissonSolver verbs)."""
+
+    def __init__(self, mesh: Mesh):
+        self.mesh = mesh
+        self.h = load().fgb_field_create(mesh.h)
+        if not self.h:
+            raise RuntimeError("field creation failed: " + last_error())
+        o = np.zeros(4, dtype=np.int64)
+        load().fgb_field_sizes(self.h, ptr(o, i64p))
+        self.n_dofs, self.nnz, self.n_top_faces, self.n_sell = (int(v) for v in o)
+
+    @classmethod
+    def borrowed(cls, handle, mesh_sizes):
+        """Wrap a field handle owned elsewhere (e.g. femocs_field of a FEMOCS instance)."""
+        if not handle:
+            raise RuntimeError(last_error())
+        f = cls.__new__(cls)
+        f.mesh = None
+        f._mesh_sizes = mesh_sizes
+        f.h = handle
+        o = np.zeros(4, dtype=np.int64)
+        load().fgb_field_sizes(f.h, ptr(o, i64p))
+        f.n_dofs, f.nnz, f.n_top_faces, f.n_sell = (int(v) for v in o)
+        return f
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().fgb_field_free(self.h)
+            self.h = None
+
+    def _n_nodes(self):
+        return self.mesh.sizes()["n_nodes"] if self.mesh is not None else self._mesh_sizes["n_nodes"]
+
+    def _ok(self, rc):
+        if rc != 0:
+            raise RuntimeError(last_error())
+
+    def setup(self, applied_field, applied_potential=0.0):
+        self._ok(load().fgb_field_setup(self.h, applied_field, applied_potential))
+
+    def assemble(self, full_run=True, anode_dirichlet=False):
+        self._ok(load().fgb_field_assemble(self.h, int(full_run), int(anode_dirichlet)))
+
+    def solve(self, precision=1, rel_tol=1e-9, abs_tol=0.0, max_iter=10000, inner_tol=1e-4):
+        st = np.zeros(6)
+        rc = load().fgb_field_solve(self.h, precision, rel_tol, abs_tol, max_iter, inner_tol, ptr(st))
+        if rc == -(2 ** 31):
+            raise RuntimeError(last_error())
+        return rc, dict(iterations=int(st[0]), outer=int(st[1]), status=int(st[2]), rel_residual=st[3],
+                        bnorm=st[4], ms=st[5])
+
+    def extract(self, smoothen=True):
+        self._ok(load().fgb_field_extract(self.h, int(smoothen)))
+
+    def phi_nodes(self):
+        out = np.zeros(self._n_nodes())
+        self._ok(load().fgb_field_export_phi_nodes(self.h, ptr(out)))
+        return out
+
+    def set_phi_nodes(self, phi):
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        self._ok(load().fgb_field_import_phi_nodes(self.h, ptr(phi)))
+
+    def nodal(self):
+        out = np.zeros(5 * self._n_nodes())
+        self._ok(load().fgb_field_get_nodal(self.h, ptr(out)))
+        return out.reshape(-1, 5)
+
+    def set_nodal(self, sol5):
+        sol5 = np.ascontiguousarray(sol5, dtype=np.float64).reshape(-1)
+        self._ok(load().fgb_field_set_nodal(self.h, ptr(sol5)))
+
+    def interpolate(self, xyz, rank=3, stats=False):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        n = len(xyz) // 3
+        cells = np.zeros(max(n, 1), dtype=np.int32)
+        out = np.zeros(max(5 * n, 1))
+        st = np.zeros(5, dtype=np.int64)
+        self._ok(load().fgb_field_interpolate(self.h, n, ptr(xyz), rank, ptr(cells, ip), ptr(out), ptr(st, i64p)))
+        res = (cells[:n], out[:5 * n].reshape(-1, 5))
+        if stats:
+            return res + (dict(zip(["n", "walk_failed", "fallback", "dependent", "longest_run"], st.tolist())),)
+        return res
+
+    def mark(self, slot):
+        """Record CUDA event `slot` (0..7) on the field's stream."""
+        self._ok(load().fgb_field_mark(self.h, slot))
+
+    def elapsed(self, a, b):
+        """Milliseconds between events a and b (waits for b)."""
+        return load().fgb_field_elapsed(self.h, a, b)
+
+    def interpolate_device(self, n, d_xyz, rank, d_cells, d_out):
+        self._ok(load().fgb_field_interpolate_device(self.h, n, d_xyz, rank, d_cells, d_out))
+
+    def system(self):
+        rowptr = np.zeros(self.n_dofs + 1, dtype=np.int64)
+        col = np.zeros(self.nnz, dtype=np.int32)
+        val = np.zeros(self.nnz)
+        rhs = np.zeros(self.n_dofs)
+        d2n = np.zeros(self.n_dofs, dtype=np.int32)
+        self._ok(load().fgb_field_export_system(self.h, ptr(rowptr, i64p), ptr(col, ip), ptr(val), ptr(rhs),
+                                                ptr(d2n, ip)))
+        return rowptr, col, val, rhs, d2n
+
+    def time_spmv(self, precision, reps=20):
+        return load().fgb_field_time_spmv(self.h, precision, reps)
+
+
+class Femocs:
+    """Mirror of the reference's C wrapper (create_femocs / femocs_run / femocs_interpolate_*)."""
+
+    def __init__(self, conf_path: str):
+        self.lib = load()
+        self.h = self.lib.create_femocs(conf_path.encode())
+        if not self.h:
+            raise RuntimeError("create_femocs failed: " + last_error())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.delete_femocs(self.h)
+            self.h = None
+
+    def run(self, timestep=-1, time=-1.0):
+        rv = C.c_int(0)
+        self.lib.femocs_run(self.h, C.byref(rv), timestep, time)
+        return rv.value
+
+    def import_mesh(self, xyz, tets, markers):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        tets = np.ascontiguousarray(tets, dtype=np.int32).reshape(-1)
+        markers = np.ascontiguousarray(markers, dtype=np.int32).reshape(-1)
+        rv = C.c_int(0)
+        self.lib.femocs_import_mesh(self.h, C.byref(rv), len(xyz) // 3, ptr(xyz), len(tets) // 4, ptr(tets, ip),
+                                    ptr(markers, ip))
+        return rv.value
+
+    def import_atoms(self, x, y, z, types):
+        x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        rv = C.c_int(0)
+        self.lib.femocs_import_atoms(self.h, C.byref(rv), len(x), ptr(x), ptr(y), ptr(z), ptr(types, ip))
+        return rv.value
+
+    def interpolate_elfield(self, x, y, z):
+        x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+        n = len(x)
+        Ex, Ey, Ez, En = (np.zeros(n) for _ in range(4))
+        flag = np.zeros(n, dtype=np.int32)
+        rv = C.c_int(0)
+        self.lib.femocs_interpolate_elfield(self.h, C.byref(rv), n, ptr(x), ptr(y), ptr(z), ptr(Ex), ptr(Ey), ptr(Ez),
+                                            ptr(En), ptr(flag, ip))
+        return rv.value, Ex, Ey, Ez, En, flag
+
+    def interpolate_phi(self, x, y, z):
+        x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+        n = len(x)
+        phi = np.zeros(n)
+        flag = np.zeros(n, dtype=np.int32)
+        rv = C.c_int(0)
+        self.lib.femocs_interpolate_phi(self.h, C.byref(rv), n, ptr(x), ptr(y), ptr(z), ptr(phi), ptr(flag, ip))
+        return rv.value, phi, flag
+
+    def export_data(self, n, label):
+        data = np.zeros(3 * n if label.lower() == "elfield" else n)
+        rv = C.c_int(0)
+        self.lib.femocs_export_data(self.h, C.byref(rv), ptr(data), n, label.encode())
+        return rv.value, data
+
+    def field(self, mesh_sizes):
+        """Borrowed device field of this instance (valid after run())."""
+        return Field.borrowed(self.lib.femocs_field(self.h), mesh_sizes)
+
+    def last_solve(self):
+        out = np.zeros(8)
+        rv = C.c_int(0)
+        self.lib.femocs_last_solve(self.h, C.byref(rv), ptr(out))
+        return dict(iterations=int(out[0]), outer=int(out[1]), status=int(out[2]), rel_residual=out[3], ms=out[4],
+                    n_dofs=int(out[5]))
+
+    def parse_double(self, cmd):
+        v = C.c_double(0)
+        rv = C.c_int(0)
+        self.lib.femocs_parse_double(self.h, C.byref(rv), cmd.encode(), C.byref(v))
+        return rv.value, v.value
+
+
+class DeviceBuffer:
+    """Plain device allocation (cudaMalloc) used by tests and the benchmark."""
+
+    def __init__(self, nbytes):
+        self.nbytes = int(nbytes)
+        self.ptr = load().fgb_device_alloc(self.nbytes)
+        if not self.ptr:
+            raise MemoryError(last_error())
+
+    def upload(self, a: np.ndarray):
+        a = np.ascontiguousarray(a)
+        assert a.nbytes <= self.nbytes
+        if load().fgb_memcpy_htod(self.ptr, a.ctypes.data_as(C.c_void_p), a.nbytes) != 0:
+            raise RuntimeError(last_error())
+
+    def download(self, a: np.ndarray):
+        assert a.flags.c_contiguous and a.nbytes <= self.nbytes
+        if load().fgb_memcpy_dtoh(a.ctypes.data_as(C.c_void_p), self.ptr, a.nbytes) != 0:
+            raise RuntimeError(last_error())
+        return a
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            load().fgb_device_free(self.ptr)
+            self.ptr = None
+
+
+def synth_atoms(spec_kw, latconst=3.615, sigma=0.05, cutoff=3.1, seed=12345):
+    spec = nanotip(**spec_kw)
+    lib = load()
+    n = lib.fgb_synth_atoms(C.byref(spec), latconst, sigma, cutoff, seed, None, None)
+    if n < 0:
+        raise RuntimeError(last_error())
+    xyz = np.zeros(3 * n)
+    types = np.zeros(n, dtype=np.int32)
+    lib.fgb_synth_atoms(C.byref(spec), latconst, sigma, cutoff, seed, ptr(xyz), ptr(types, ip))
+    return xyz.reshape(-1, 3), types
+
+
+def synth_probes(spec_kw, n, seed=777):
+    spec = nanotip(**spec_kw)
+    xyz = np.zeros(3 * n)
+    if load().fgb_synth_probes(C.byref(spec), n, seed, ptr(xyz)) < 0:
+        raise RuntimeError(last_error())
+    return xyz.reshape(-1, 3)

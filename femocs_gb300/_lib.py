@@ -1,0 +1,111 @@
+"""ctypes binding of libfemocs_gb300.so (the C ABI declared in include/femocs_gb300.h).
+
+The library is built in-tree by femocs_gb300.build; loading fails loudly when it is missing
+-- there is no CPU fallback for the field path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfemocs_gb300.so")
+
+_lib = None
+
+dp = C.POINTER(C.c_double)
+ip = C.POINTER(C.c_int)
+i64p = C.POINTER(C.c_int64)
+vp = C.c_void_p
+
+
+class FgbNanotip(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("radius", "height", "box_half", "slab", "top", "h", "growth", "margin")]
+
+
+_PROTOS = {
+    # Part 1
+    "create_femocs": (vp, [C.c_char_p]),
+    "delete_femocs": (None, [vp]),
+    "femocs_run": (None, [vp, ip, C.c_int, C.c_double]),
+    "femocs_import_file": (None, [vp, ip, C.c_char_p]),
+    "femocs_import_parcas": (None, [vp, ip, C.c_int, dp, dp, dp, ip]),
+    "femocs_import_atoms": (None, [vp, ip, C.c_int, dp, dp, dp, ip]),
+    "femocs_import_mesh": (None, [vp, ip, C.c_int, dp, C.c_int, ip, ip]),
+    "femocs_interpolate_elfield": (None, [vp, ip, C.c_int, dp, dp, dp, dp, dp, dp, dp, ip]),
+    "femocs_interpolate_surface_elfield": (None, [vp, ip, C.c_int, dp, dp, dp, dp, dp, dp, dp, ip]),
+    "femocs_interpolate_phi": (None, [vp, ip, C.c_int, dp, dp, dp, dp, ip]),
+    "femocs_export_data": (None, [vp, ip, dp, C.c_int, C.c_char_p]),
+    "femocs_export_int": (None, [vp, ip, ip, C.c_int, C.c_char_p]),
+    "femocs_interpolate": (None, [vp, ip, dp, ip, C.c_int, C.c_char_p, C.c_int, dp, dp, dp]),
+    "femocs_parse_int": (None, [vp, ip, C.c_char_p, ip]),
+    "femocs_parse_double": (None, [vp, ip, C.c_char_p, dp]),
+    "femocs_parse_string": (None, [vp, ip, C.c_char_p, C.c_char_p]),
+    "femocs_last_solve": (None, [vp, ip, dp]),
+    "femocs_last_error": (C.c_char_p, []),
+    "fgb_kernel_launches": (C.c_longlong, []),
+    # Part 2
+    "fgb_mesh_from_arrays": (vp, [C.c_int, dp, C.c_int, ip, ip]),
+    "fgb_mesh_read_gmsh": (vp, [C.c_char_p]),
+    "fgb_mesh_synthetic": (vp, [C.POINTER(FgbNanotip)]),
+    "fgb_mesh_free": (None, [vp]),
+    "fgb_mesh_sizes": (C.c_int, [vp, i64p]),
+    "fgb_mesh_export": (C.c_int, [vp, C.c_char_p, vp]),
+    "fgb_synth_atoms": (C.c_int64, [C.POINTER(FgbNanotip), C.c_double, C.c_double, C.c_double, C.c_uint64, dp, ip]),
+    "fgb_synth_probes": (C.c_int64, [C.POINTER(FgbNanotip), C.c_int, C.c_uint64, dp]),
+    "fgb_field_create": (vp, [vp]),
+    "fgb_field_free": (None, [vp]),
+    "fgb_field_sizes": (C.c_int, [vp, i64p]),
+    "fgb_field_setup": (C.c_int, [vp, C.c_double, C.c_double]),
+    "fgb_field_assemble": (C.c_int, [vp, C.c_int, C.c_int]),
+    "fgb_field_solve": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, dp]),
+    "fgb_field_export_phi_nodes": (C.c_int, [vp, dp]),
+    "fgb_field_import_phi_nodes": (C.c_int, [vp, dp]),
+    "fgb_field_extract": (C.c_int, [vp, C.c_int]),
+    "fgb_field_get_nodal": (C.c_int, [vp, dp]),
+    "fgb_field_set_nodal": (C.c_int, [vp, dp]),
+    "fgb_field_interpolate": (C.c_int, [vp, C.c_int, dp, C.c_int, ip, dp, i64p]),
+    "fgb_field_interpolate_device": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp]),
+    "fgb_field_export_system": (C.c_int, [vp, i64p, ip, dp, dp, ip]),
+    "fgb_field_time_spmv": (C.c_double, [vp, C.c_int, C.c_int]),
+    "fgb_field_stream": (vp, [vp]),
+    "femocs_field": (vp, [vp]),
+    "fgb_field_mark": (C.c_int, [vp, C.c_int]),
+    "fgb_field_elapsed": (C.c_double, [vp, C.c_int, C.c_int]),
+    "fgb_device_alloc": (vp, [C.c_size_t]),
+    "fgb_device_free": (None, [vp]),
+    "fgb_memcpy_htod": (C.c_int, [vp, vp, C.c_size_t]),
+    "fgb_memcpy_dtoh": (C.c_int, [vp, vp, C.c_size_t]),
+}
+
+
+def exported_symbols():
+    return list(_PROTOS)
+
+
+def load():
+    """Load the shared library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run femocs_gb300.build.build() first "
+                           "(the field path has no CPU fallback)")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    e = load().femocs_last_error()
+    return e.decode() if e else ""
+
+
+def ptr(a: np.ndarray, kind=dp):
+    return a.ctypes.data_as(kind)

@@ -1,0 +1,458 @@
+// extern "C" shims over the C++ classes; no exception crosses this boundary. Failures are
+// reported through retval = 1 (reference convention) or a NULL / negative return, with the
+// message available from femocs_last_error().
+#include <cstring>
+#include <memory>
+
+#include "facade.h"
+#include "femocs_gb300.h"
+#include "synth.h"
+
+using namespace fgb;
+
+struct FEMOCS {
+    std::unique_ptr<FemocsFacade> f;
+};
+struct FGB_MESH {
+    std::shared_ptr<PreparedMesh> pm;
+};
+struct FGB_FIELD {
+    ~FGB_FIELD() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    cudaEvent_t ev[8] = {};
+    std::unique_ptr<Field> owned;
+    Field* f = nullptr;  // owned.get(), or a field borrowed from a FEMOCS handle
+    std::shared_ptr<const PreparedMesh> pm;
+    const PreparedMesh* mesh = nullptr;
+    SolveStats last;
+};
+
+namespace {
+template <typename F>
+int guarded(F&& fn) {
+    try {
+        return fn();
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return 1;
+    } catch (...) {
+        set_last_error("unknown error");
+        return 1;
+    }
+}
+template <typename F>
+void guarded_rv(int* retval, F&& fn) {
+    const int rc = guarded(fn);
+    if (retval) *retval = rc;
+}
+NanotipSpec to_spec(const FgbNanotip* s) {
+    NanotipSpec n;
+    if (!s) return n;
+    n.radius = s->radius;
+    n.height = s->height;
+    n.box_half = s->box_half;
+    n.slab = s->slab;
+    n.top = s->top;
+    n.h = s->h;
+    n.growth = s->growth;
+    n.margin = s->margin;
+    return n;
+}
+}  // namespace
+
+extern "C" {
+
+const char* femocs_last_error(void) { return last_error(); }
+long long fgb_kernel_launches(void) { return g_kernel_launches.load(); }
+
+// ---------------------------------------------------------------- Part 1
+FEMOCS* create_femocs(const char* conf_file) {
+    FEMOCS* h = new FEMOCS;
+    const int rc = guarded([&] {
+        h->f.reset(new FemocsFacade(conf_file ? conf_file : ""));
+        return 0;
+    });
+    if (rc) {
+        delete h;
+        return nullptr;
+    }
+    return h;
+}
+void delete_femocs(FEMOCS* h) { delete h; }
+
+void femocs_run(FEMOCS* h, int* retval, int timestep, double time) {
+    guarded_rv(retval, [&] { return h->f->run(timestep, time); });
+}
+void femocs_import_file(FEMOCS* h, int* retval, const char* file_name) {
+    guarded_rv(retval, [&] { return h->f->import_file(file_name ? file_name : ""); });
+}
+void femocs_import_parcas(FEMOCS*, int* retval, int, const double*, const double*, const double*, const int*) {
+    set_last_error("PARCAS import is not provided by this library");
+    if (retval) *retval = 1;
+}
+void femocs_import_atoms(FEMOCS* h, int* retval, int n, const double* x, const double* y, const double* z,
+                         const int* types) {
+    guarded_rv(retval, [&] { return h->f->import_atoms(n, x, y, z, types); });
+}
+void femocs_import_mesh(FEMOCS* h, int* retval, int n_nodes, const double* xyz, int n_tets, const int* tets,
+                        const int* markers) {
+    guarded_rv(retval, [&] { return h->f->import_mesh(n_nodes, xyz, n_tets, tets, markers); });
+}
+void femocs_interpolate_elfield(FEMOCS* h, int* retval, int n, const double* x, const double* y, const double* z,
+                                double* Ex, double* Ey, double* Ez, double* En, int* flag) {
+    guarded_rv(retval, [&] { return h->f->interpolate_elfield(n, x, y, z, Ex, Ey, Ez, En, flag); });
+}
+void femocs_interpolate_surface_elfield(FEMOCS* h, int* retval, int n, const double* x, const double* y,
+                                        const double* z, double* Ex, double* Ey, double* Ez, double* En, int* flag) {
+    (void)Ex; (void)Ey; (void)Ez; (void)En;
+    guarded_rv(retval, [&] {
+        std::vector<double> d(3 * (size_t)std::max(n, 0));
+        return h->f->interpolate(d.data(), flag, n, "Elfield", true, x, y, z);
+    });
+}
+void femocs_interpolate_phi(FEMOCS* h, int* retval, int n, const double* x, const double* y, const double* z,
+                            double* phi, int* flag) {
+    guarded_rv(retval, [&] { return h->f->interpolate_phi(n, x, y, z, phi, flag); });
+}
+void femocs_export_data(FEMOCS* h, int* retval, double* data, int n, const char* type) {
+    guarded_rv(retval, [&] { return h->f->export_data(data, n, type ? type : ""); });
+}
+void femocs_export_int(FEMOCS* h, int* retval, int* data, int n, const char* type) {
+    guarded_rv(retval, [&] { return h->f->export_int(data, n, type ? type : ""); });
+}
+void femocs_interpolate(FEMOCS* h, int* retval, double* data, int* flag, int n, const char* type, int near_surface,
+                        const double* x, const double* y, const double* z) {
+    guarded_rv(retval, [&] { return h->f->interpolate(data, flag, n, type ? type : "", near_surface != 0, x, y, z); });
+}
+void femocs_parse_int(FEMOCS* h, int* retval, const char* cmd, int* arg) {
+    guarded_rv(retval, [&] { return h->f->parse(cmd, arg); });
+}
+void femocs_parse_double(FEMOCS* h, int* retval, const char* cmd, double* arg) {
+    guarded_rv(retval, [&] { return h->f->parse(cmd, arg); });
+}
+void femocs_parse_string(FEMOCS* h, int* retval, const char* cmd, char* arg) {
+    guarded_rv(retval, [&] {
+        std::string s;
+        const int rc = h->f->parse(cmd, s);
+        if (!rc) s.copy(arg, s.length());  // like Femocs::parse_command: no terminator appended
+        return rc;
+    });
+}
+void femocs_last_solve(FEMOCS* h, int* retval, double* out8) {
+    guarded_rv(retval, [&] {
+        const SolveStats& s = h->f->last_stats();
+        out8[0] = s.iterations;
+        out8[1] = s.outer;
+        out8[2] = s.status;
+        out8[3] = s.rel_residual;
+        out8[4] = s.ms;
+        out8[5] = h->f->n_dofs();
+        out8[6] = s.bnorm;
+        out8[7] = 0;
+        return 0;
+    });
+}
+
+// ---------------------------------------------------------------- Part 2: meshes
+FGB_MESH* fgb_mesh_from_arrays(int n_nodes, const double* xyz, int n_tets, const int* tets, const int* markers) {
+    FGB_MESH* m = new FGB_MESH;
+    const int rc = guarded([&] {
+        TetMesh tm;
+        tm.xyz.assign(xyz, xyz + 3 * (size_t)n_nodes);
+        tm.tets.assign(tets, tets + 4 * (size_t)n_tets);
+        tm.marker.assign(markers, markers + n_tets);
+        m->pm = std::make_shared<PreparedMesh>(prepare_mesh(std::move(tm)));
+        return 0;
+    });
+    if (rc) { delete m; return nullptr; }
+    return m;
+}
+FGB_MESH* fgb_mesh_read_gmsh(const char* path) {
+    FGB_MESH* m = new FGB_MESH;
+    const int rc = guarded([&] {
+        m->pm = std::make_shared<PreparedMesh>(prepare_mesh(read_gmsh(path)));
+        return 0;
+    });
+    if (rc) { delete m; return nullptr; }
+    return m;
+}
+FGB_MESH* fgb_mesh_synthetic(const FgbNanotip* spec) {
+    FGB_MESH* m = new FGB_MESH;
+    const int rc = guarded([&] {
+        m->pm = std::make_shared<PreparedMesh>(prepare_mesh(make_nanotip_mesh(to_spec(spec))));
+        return 0;
+    });
+    if (rc) { delete m; return nullptr; }
+    return m;
+}
+void fgb_mesh_free(FGB_MESH* m) { delete m; }
+
+int fgb_mesh_sizes(const FGB_MESH* m, int64_t* o) {
+    return guarded([&] {
+        const PreparedMesh& p = *m->pm;
+        o[0] = p.hex.n_tetnodes;
+        o[1] = p.tet.n_tets();
+        o[2] = p.hex.n_nodes();
+        o[3] = p.hex.n_hexs();
+        o[4] = (int64_t)p.vac.vertex2node.size();
+        o[5] = (int64_t)p.vac.cells.size();
+        o[6] = (int64_t)p.tt.nbr_idx.size();
+        o[7] = (int64_t)p.voro_idx.size();
+        for (int k = 8; k < 12; ++k) o[k] = 0;
+        return 0;
+    });
+}
+
+int fgb_mesh_export(const FGB_MESH* m, const char* name, void* out) {
+    return guarded([&] {
+        const PreparedMesh& p = *m->pm;
+        const std::string n = name ? name : "";
+        auto cp = [&](const auto& v) {
+            std::memcpy(out, v.data(), v.size() * sizeof(v[0]));
+            return 0;
+        };
+        if (n == "tet_nodes") return cp(p.tet.tets);
+        if (n == "tet_marker") return cp(p.tet.marker);
+        if (n == "tet_nbor") return cp(p.face_nbr);
+        if (n == "node_xyz") return cp(p.hex.xyz);
+        if (n == "node_marker") {
+            std::vector<int32_t> v(p.hex.node_marker.begin(), p.hex.node_marker.end());
+            return cp(v);
+        }
+        if (n == "hex_nodes") return cp(p.hex.hexs);
+        if (n == "hex_marker") return cp(p.hex.hex_marker);
+        if (n == "tet_det") return cp(p.tt.det);
+        if (n == "tet_centroid") return cp(p.tt.centroid);
+        if (n == "hex_coeffs") return cp(p.hex_coeffs);
+        if (n == "nbr_ptr") return cp(p.tt.nbr_ptr);
+        if (n == "nbr_idx") return cp(p.tt.nbr_idx);
+        if (n == "quad_nodes") return cp(p.tt.quad_nodes);
+        if (n == "voro_ptr") return cp(p.voro_ptr);
+        if (n == "voro_idx") return cp(p.voro_idx);
+        if (n == "vac_node2vertex") return cp(p.vac.node2vertex);
+        if (n == "vac_cells") return cp(p.vac.cells);
+        if (n == "tet_search") {
+            std::vector<int32_t> v(p.tt.search.begin(), p.tt.search.end());
+            return cp(v);
+        }
+        if (n == "edgemax") {
+            std::memcpy(out, &p.edgemax, sizeof(double));
+            return 0;
+        }
+        set_last_error("unknown table " + n);
+        return 1;
+    });
+}
+
+int64_t fgb_synth_atoms(const FgbNanotip* spec, double a, double sigma, double cutoff, uint64_t seed, double* xyz,
+                        int* type) {
+    try {
+        AtomSet at = make_nanotip_atoms(to_spec(spec), a, sigma, cutoff, seed);
+        const int64_t n = (int64_t)at.type.size();
+        if (xyz) std::memcpy(xyz, at.xyz.data(), sizeof(double) * 3 * n);
+        if (type) std::memcpy(type, at.type.data(), sizeof(int) * n);
+        return n;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return -1;
+    }
+}
+
+int64_t fgb_synth_probes(const FgbNanotip* spec, int n, uint64_t seed, double* xyz) {
+    try {
+        std::vector<double> p = make_vacuum_probes(to_spec(spec), n, seed);
+        if (xyz) std::memcpy(xyz, p.data(), sizeof(double) * p.size());
+        return n;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return -1;
+    }
+}
+
+// ---------------------------------------------------------------- Part 2: device field
+FGB_FIELD* fgb_field_create(const FGB_MESH* m) {
+    FGB_FIELD* f = new FGB_FIELD;
+    const int rc = guarded([&] {
+        f->pm = m->pm;
+        f->owned.reset(new Field(f->pm));
+        f->f = f->owned.get();
+        f->mesh = f->pm.get();
+        return 0;
+    });
+    if (rc) { delete f; return nullptr; }
+    return f;
+}
+void fgb_field_free(FGB_FIELD* f) { delete f; }
+
+int fgb_field_sizes(const FGB_FIELD* f, int64_t* o) {
+    return guarded([&] {
+        const FemStructure& s = f->f->fem().structure();
+        o[0] = s.n_dofs;
+        o[1] = s.nnz();
+        o[2] = s.n_top_faces();
+        o[3] = s.slice_ptr.back();
+        return 0;
+    });
+}
+int fgb_field_setup(FGB_FIELD* f, double applied_field, double applied_potential) {
+    return guarded([&] { f->f->fem().setup(applied_field, applied_potential); return 0; });
+}
+int fgb_field_assemble(FGB_FIELD* f, int full_run, int anode_dirichlet) {
+    return guarded([&] { f->f->fem().assemble(full_run != 0, anode_dirichlet != 0); return 0; });
+}
+int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol, int max_iter, double inner_tol,
+                    double* stats6) {
+    int rc = 0;
+    const int g = guarded([&] {
+        SolveOptions o;
+        o.precision = precision;
+        o.rel_tol = rel_tol;
+        o.abs_tol = abs_tol;
+        o.max_iter = max_iter;
+        if (inner_tol > 0) o.inner_tol = inner_tol;
+        rc = f->f->fem().solve(o, &f->last);
+        if (stats6) {
+            stats6[0] = f->last.iterations;
+            stats6[1] = f->last.outer;
+            stats6[2] = f->last.status;
+            stats6[3] = f->last.rel_residual;
+            stats6[4] = f->last.bnorm;
+            stats6[5] = f->last.ms;
+        }
+        return 0;
+    });
+    return g ? INT32_MIN : rc;
+}
+int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi) {
+    return guarded([&] {
+        FemDevice& fem = f->f->fem();
+        std::vector<double> x(fem.n_dofs());
+        FGB_CUDA(cudaMemcpyAsync(x.data(), fem.d_solution(), sizeof(double) * x.size(), cudaMemcpyDeviceToHost, fem.stream()));
+        FGB_CUDA(cudaStreamSynchronize(fem.stream()));
+        const FemStructure& s = fem.structure();
+        std::fill(phi, phi + f->mesh->hex.n_nodes(), 0.0);
+        for (int d = 0; d < s.n_dofs; ++d) phi[s.dof2node[d]] = x[d];
+        return 0;
+    });
+}
+int fgb_field_import_phi_nodes(FGB_FIELD* f, const double* phi) {
+    return guarded([&] {
+        FemDevice& fem = f->f->fem();
+        const FemStructure& s = fem.structure();
+        std::vector<double> x(s.n_dofs);
+        for (int d = 0; d < s.n_dofs; ++d) x[d] = phi[s.dof2node[d]];
+        FGB_CUDA(cudaMemcpyAsync(fem.d_solution(), x.data(), sizeof(double) * x.size(), cudaMemcpyHostToDevice, fem.stream()));
+        FGB_CUDA(cudaStreamSynchronize(fem.stream()));
+        return 0;
+    });
+}
+int fgb_field_extract(FGB_FIELD* f, int smoothen) {
+    return guarded([&] {
+        f->f->extract(smoothen != 0);
+        FGB_CUDA(cudaStreamSynchronize(f->f->stream()));
+        return 0;
+    });
+}
+int fgb_field_get_nodal(FGB_FIELD* f, double* sol5) {
+    return guarded([&] { f->f->interp().get_solution(sol5); return 0; });
+}
+int fgb_field_set_nodal(FGB_FIELD* f, const double* sol5) {
+    return guarded([&] {
+        f->f->interp().set_solution(sol5);
+        FGB_CUDA(cudaStreamSynchronize(f->f->stream()));
+        return 0;
+    });
+}
+int fgb_field_interpolate(FGB_FIELD* f, int n, const double* xyz, int rank, int* cells, double* out5, int64_t* st5) {
+    return guarded([&] {
+        LocateStats ls;
+        f->f->interpolate_host(n, xyz, rank, cells, out5, st5 ? &ls : nullptr);
+        if (st5) {
+            st5[0] = ls.n_points;
+            st5[1] = ls.n_walk_failed;
+            st5[2] = ls.n_fallback;
+            st5[3] = ls.n_dependent;
+            st5[4] = ls.longest_run;
+        }
+        return 0;
+    });
+}
+int fgb_field_interpolate_device(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells, double* d_out5) {
+    return guarded([&] {
+        f->f->interp().locate_interpolate(n, d_xyz, rank, d_cells, d_out5, nullptr);
+        return 0;
+    });
+}
+int fgb_field_export_system(FGB_FIELD* f, int64_t* rowptr, int* col, double* val, double* rhs, int* dof2node) {
+    return guarded([&] {
+        FemDevice& fem = f->f->fem();
+        const FemStructure& s = fem.structure();
+        std::vector<double> v, b;
+        fem.download_matrix(v, b);
+        if (rowptr) std::memcpy(rowptr, s.rowptr.data(), sizeof(int64_t) * s.rowptr.size());
+        if (col) std::memcpy(col, s.col.data(), sizeof(int32_t) * s.col.size());
+        if (val) std::memcpy(val, v.data(), sizeof(double) * v.size());
+        if (rhs) std::memcpy(rhs, b.data(), sizeof(double) * b.size());
+        if (dof2node) std::memcpy(dof2node, s.dof2node.data(), sizeof(int32_t) * s.dof2node.size());
+        return 0;
+    });
+}
+double fgb_field_time_spmv(FGB_FIELD* f, int precision, int reps) {
+    double ms = -1;
+    guarded([&] { ms = f->f->fem().time_spmv(precision, reps); return 0; });
+    return ms;
+}
+void* fgb_field_stream(FGB_FIELD* f) { return (void*)f->f->stream(); }
+
+int fgb_field_mark(FGB_FIELD* f, int slot) {
+    return guarded([&] {
+        FGB_REQUIRE(slot >= 0 && slot < 8, "event slot out of range");
+        if (!f->ev[slot]) FGB_CUDA(cudaEventCreate(&f->ev[slot]));
+        FGB_CUDA(cudaEventRecord(f->ev[slot], f->f->stream()));
+        return 0;
+    });
+}
+double fgb_field_elapsed(FGB_FIELD* f, int a, int b) {
+    double ms = -1;
+    guarded([&] {
+        FGB_REQUIRE(a >= 0 && a < 8 && b >= 0 && b < 8 && f->ev[a] && f->ev[b], "unrecorded event slot");
+        FGB_CUDA(cudaEventSynchronize(f->ev[b]));
+        float m = 0;
+        FGB_CUDA(cudaEventElapsedTime(&m, f->ev[a], f->ev[b]));
+        ms = m;
+        return 0;
+    });
+    return ms;
+}
+void* fgb_device_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        set_last_error("cudaMalloc failed");
+        return nullptr;
+    }
+    return p;
+}
+void fgb_device_free(void* p) { cudaFree(p); }
+int fgb_memcpy_htod(void* dst, const void* src, size_t bytes) {
+    return guarded([&] { FGB_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice)); return 0; });
+}
+int fgb_memcpy_dtoh(void* dst, const void* src, size_t bytes) {
+    return guarded([&] { FGB_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost)); return 0; });
+}
+
+FGB_FIELD* femocs_field(FEMOCS* h) {
+    FGB_FIELD* f = new FGB_FIELD;
+    const int rc = guarded([&] {
+        Field* fd = h->f->field();
+        if (!fd) throw Error("no field yet: call femocs_run first");
+        f->f = fd;
+        f->mesh = &fd->mesh();
+        return 0;
+    });
+    if (rc) { delete f; return nullptr; }
+    return f;
+}
+
+}  // extern "C"

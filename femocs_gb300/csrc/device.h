@@ -1,0 +1,82 @@
+// Device memory and error helpers shared by the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+#include "common.h"
+
+namespace fgb {
+
+// Count of kernels this library has launched (reported by the benchmark).
+extern std::atomic<long long> g_kernel_launches;
+#define FGB_LAUNCH(...)                                                              \
+    do {                                                                             \
+        __VA_ARGS__;                                                                 \
+        ::fgb::g_kernel_launches.fetch_add(1, std::memory_order_relaxed);           \
+    } while (0)
+
+#define FGB_CUDA(call)                                                                    \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            throw ::fgb::Error(std::string(__FILE__) + ":" + std::to_string(__LINE__) +  \
+                               ": " #call " -> " + cudaGetErrorString(e_));               \
+    } while (0)
+
+// Owning device buffer (cudaMalloc'd, freed on destruction).
+template <typename T>
+class DBuf {
+public:
+    DBuf() = default;
+    explicit DBuf(size_t n) { resize(n); }
+    ~DBuf() { release(); }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) { release(); p_ = o.p_; n_ = o.n_; o.p_ = nullptr; o.n_ = 0; }
+        return *this;
+    }
+    void resize(size_t n) {
+        if (n == n_) return;
+        release();
+        if (n) FGB_CUDA(cudaMalloc(&p_, n * sizeof(T)));
+        n_ = n;
+    }
+    void release() {
+        if (p_) cudaFree(p_);
+        p_ = nullptr;
+        n_ = 0;
+    }
+    void upload(const T* h, size_t n, cudaStream_t s = 0) {
+        resize(n);
+        if (n) FGB_CUDA(cudaMemcpyAsync(p_, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T>& v, cudaStream_t s = 0) { upload(v.data(), v.size(), s); }
+    void download(T* h, size_t n, cudaStream_t s = 0) const {
+        if (n) FGB_CUDA(cudaMemcpyAsync(h, p_, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+    std::vector<T> to_host(cudaStream_t s = 0) const {
+        std::vector<T> v(n_);
+        download(v.data(), n_, s);
+        FGB_CUDA(cudaStreamSynchronize(s));
+        return v;
+    }
+    void zero(cudaStream_t s = 0) {
+        if (n_) FGB_CUDA(cudaMemsetAsync(p_, 0, n_ * sizeof(T), s));
+    }
+    T* get() { return p_; }
+    const T* get() const { return p_; }
+    size_t size() const { return n_; }
+    size_t bytes() const { return n_ * sizeof(T); }
+
+private:
+    T* p_ = nullptr;
+    size_t n_ = 0;
+};
+
+inline int grid_for(long long n, int block) { return (int)((n + block - 1) / block); }
+
+}  // namespace fgb

@@ -1,0 +1,673 @@
+// Device assembly and CG solvers of the vacuum Poisson system (sm_103a).
+//
+//   k_cell_stiffness   Q1 element matrices, 2x2x2 Gauss, trilinear map
+//                      (PoissonSolver::assemble_local_cell, src/PoissonSolver.cpp:239-263)
+//   k_assemble_rows    deterministic row-owned scatter of the element matrices into CSR
+//                      (DealSolver::copy_global_cell, src/DealSolver.cpp:65-72)
+//   k_neumann_rows     2x2 Gauss face integral of the applied field on the top faces
+//                      (DealSolver::assemble_rhs, src/DealSolver.cpp:390-430)
+//   k_dirichlet_rows   symmetric elimination of the copper (and anode) values, writes the
+//                      SELL-32 FP64/FP32 matrices and the Jacobi diagonal
+//                      (MatrixTools::apply_boundary_values via src/DealSolver.cpp:433-440)
+//   k_sell_spmv        y = A x, SELL-32, one row per thread, coalesced value/column streams
+//   k_cg_*             fused Jacobi-PCG iteration (SpMV+dot, update+dots, direction), all
+//                      scalars in device memory, replayed from a CUDA graph
+//   mixed precision    FP32 inner PCG inside FP64 iterative refinement; the true residual,
+//                      the refinement update and the boundary values stay FP64
+#include <algorithm>
+#include <cmath>
+
+#include "fem_device.h"
+
+namespace fgb {
+
+std::atomic<long long> g_kernel_launches{0};
+
+namespace {
+
+constexpr int kBlock = 256;
+__constant__ double c_hx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+__constant__ double c_hy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+__constant__ double c_hz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+
+__global__ void __launch_bounds__(128) k_cell_stiffness(int nc, const int32_t* __restrict__ cd,
+                                                        const double* __restrict__ dxyz, double* __restrict__ ke) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    double X[8][3];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int d = cd[8 * (size_t)c + k];
+        X[k][0] = dxyz[3 * (size_t)d];
+        X[k][1] = dxyz[3 * (size_t)d + 1];
+        X[k][2] = dxyz[3 * (size_t)d + 2];
+    }
+    double K[36];
+#pragma unroll
+    for (int i = 0; i < 36; ++i) K[i] = 0.0;
+    const double g = 0.57735026918962576451;
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+        const double xi = (q & 1) ? g : -g, eta = (q & 2) ? g : -g, zeta = (q & 4) ? g : -g;
+        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        double dN[8][3];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const double ax = c_hx[k], ay = c_hy[k], az = c_hz[k];
+            dN[k][0] = ax * (1 + eta * ay) * (1 + zeta * az) * 0.125;
+            dN[k][1] = (1 + xi * ax) * ay * (1 + zeta * az) * 0.125;
+            dN[k][2] = (1 + xi * ax) * (1 + eta * ay) * az * 0.125;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) J[a][b] += X[k][a] * dN[k][b];
+        }
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const double id = 1.0 / det;
+        // inverse(J)[b][a]; grad_x N = inv^T grad_xi N
+        double inv[3][3];
+        inv[0][0] = c00 * id;
+        inv[1][0] = c01 * id;
+        inv[2][0] = c02 * id;
+        inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+        double G[8][3];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                G[k][a] = inv[a][0] * dN[k][0] + inv[a][1] * dN[k][1] + inv[a][2] * dN[k][2];
+        const double w = fabs(det);
+        int t = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = i; j < 8; ++j, ++t)
+                K[t] += w * (G[i][0] * G[j][0] + G[i][1] * G[j][1] + G[i][2] * G[j][2]);
+    }
+    double* o = ke + 64 * (size_t)c;
+    int t = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = i; j < 8; ++j, ++t) {
+            o[8 * i + j] = K[t];
+            o[8 * j + i] = K[t];
+        }
+}
+
+__global__ void k_assemble_rows(int n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                const int32_t* __restrict__ r2c_ptr, const int32_t* __restrict__ r2c_item,
+                                const int32_t* __restrict__ cd, const double* __restrict__ ke, double* __restrict__ kval) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int64_t b = rowptr[r], e = rowptr[r + 1];
+    for (int64_t k = b; k < e; ++k) kval[k] = 0.0;
+    for (int p = r2c_ptr[r]; p < r2c_ptr[r + 1]; ++p) {
+        const int item = r2c_item[p];
+        const int c = item >> 3, loc = item & 7;
+        const double* kr = ke + 64 * (size_t)c + 8 * loc;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int cj = cd[8 * (size_t)c + j];
+            int64_t lo = b, hi = e - 1;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (col[mid] < cj) lo = mid + 1; else hi = mid;
+            }
+            kval[lo] += kr[j];
+        }
+    }
+}
+
+__global__ void k_neumann_rows(int n, const int32_t* __restrict__ r2f_ptr, const int32_t* __restrict__ r2f_item,
+                               const int32_t* __restrict__ top, const double* __restrict__ dxyz, double bc,
+                               const double* __restrict__ extra, double* __restrict__ rhs) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double acc = 0.0;
+    const double g = 0.57735026918962576451;
+    for (int p = r2f_ptr[r]; p < r2f_ptr[r + 1]; ++p) {
+        const int f = r2f_item[p] >> 2, q = r2f_item[p] & 3;
+        double P[4][3];
+        for (int k = 0; k < 4; ++k)
+            for (int a = 0; a < 3; ++a) P[k][a] = dxyz[3 * (size_t)top[4 * (size_t)f + k] + a];
+        for (int qp = 0; qp < 4; ++qp) {
+            const double s = (qp & 1) ? g : -g, t = (qp & 2) ? g : -g;
+            const double N[4] = {0.25 * (1 - s) * (1 - t), 0.25 * (1 + s) * (1 - t), 0.25 * (1 + s) * (1 + t),
+                                 0.25 * (1 - s) * (1 + t)};
+            double ds[3], dt[3];
+            for (int a = 0; a < 3; ++a) {
+                ds[a] = 0.25 * (-(1 - t) * P[0][a] + (1 - t) * P[1][a] + (1 + t) * P[2][a] - (1 + t) * P[3][a]);
+                dt[a] = 0.25 * (-(1 - s) * P[0][a] - (1 + s) * P[1][a] + (1 + s) * P[2][a] + (1 - s) * P[3][a]);
+            }
+            const double cx = ds[1] * dt[2] - ds[2] * dt[1], cy = ds[2] * dt[0] - ds[0] * dt[2],
+                         cz = ds[0] * dt[1] - ds[1] * dt[0];
+            acc += N[q] * bc * sqrt(cx * cx + cy * cy + cz * cz);
+        }
+    }
+    if (extra) acc += extra[r];
+    rhs[r] = acc;
+}
+
+__device__ __forceinline__ bool is_fixed(int8_t k, bool anode) { return k == 1 || (k == 2 && anode); }
+
+__global__ void k_dirichlet_rows(int n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                 const double* __restrict__ kval, const int8_t* __restrict__ bc, int anode, double v0,
+                                 const int64_t* __restrict__ csr2sell, double* __restrict__ s64, float* __restrict__ s32,
+                                 double* __restrict__ dinv64, float* __restrict__ dinv32, double* __restrict__ rhs,
+                                 double* __restrict__ x) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int64_t b = rowptr[r], e = rowptr[r + 1];
+    double diag = 1.0;
+    for (int64_t k = b; k < e; ++k)
+        if (col[k] == r) diag = kval[k];
+    const bool fr = is_fixed(bc[r], anode);
+    if (fr) {
+        const double gr = bc[r] == 2 ? v0 : 0.0;
+        for (int64_t k = b; k < e; ++k) {
+            const double a = col[k] == r ? kval[k] : 0.0;
+            s64[csr2sell[k]] = a;
+            s32[csr2sell[k]] = (float)a;
+        }
+        rhs[r] = gr * diag;
+        x[r] = gr;
+    } else {
+        double acc = rhs[r];
+        for (int64_t k = b; k < e; ++k) {
+            const int c = col[k];
+            double a = kval[k];
+            if (is_fixed(bc[c], anode)) {
+                const double gc = bc[c] == 2 ? v0 : 0.0;
+                acc -= a * gc;
+                a = 0.0;
+            }
+            s64[csr2sell[k]] = a;
+            s32[csr2sell[k]] = (float)a;
+        }
+        rhs[r] = acc;
+    }
+    dinv64[r] = 1.0 / diag;
+    dinv32[r] = (float)(1.0 / diag);
+}
+
+// ---------------------------------------------------------------- SpMV / CG
+template <typename T>
+__device__ __forceinline__ T sell_row(int r, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                      const int32_t* __restrict__ scol, const T* __restrict__ sval,
+                                      const T* __restrict__ x) {
+    const int s = r >> 5;
+    const int64_t base = sptr[s] + (r & 31);
+    const int len = slen[s];
+    T a0 = 0, a1 = 0;
+    int j = 0;
+    for (; j + 1 < len; j += 2) {
+        const int64_t o0 = base + (int64_t)j * 32, o1 = o0 + 32;
+        const int c0 = __ldg(scol + o0), c1 = __ldg(scol + o1);
+        a0 += __ldg(sval + o0) * __ldg(x + c0);
+        a1 += __ldg(sval + o1) * __ldg(x + c1);
+    }
+    if (j < len) {
+        const int64_t o0 = base + (int64_t)j * 32;
+        a0 += __ldg(sval + o0) * __ldg(x + __ldg(scol + o0));
+    }
+    return a0 + a1;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_sell_spmv(int n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                                      const int32_t* __restrict__ scol, const T* __restrict__ sval,
+                                                      const T* __restrict__ x, T* __restrict__ y) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    y[r] = sell_row(r, sptr, slen, scol, sval, x);
+}
+
+template <int NV>
+__device__ __forceinline__ void block_reduce(double (&v)[NV], double* sh) {
+    // sh: NV * 32 doubles
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double a = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) sh[k * 32 + wid] = a;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double a = lane < nw ? sh[k * 32 + lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            v[k] = a;
+        }
+    }
+}
+
+// Writes the block's NV partial sums; the last block to finish reduces all partials in a
+// fixed order (deterministic) and returns true in thread 0 with the totals in v.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* partial, unsigned int* ticket) {
+    __shared__ double sh[NV * 32];
+    __shared__ bool last;
+    block_reduce<NV>(v, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) partial[(size_t)NV * blockIdx.x + k] = v[k];
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += ((volatile double*)partial)[(size_t)NV * b + k];
+    __syncthreads();
+    block_reduce<NV>(acc, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = acc[k];
+        *ticket = 0;
+        return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void cg_check(CgState* st, double rr) {
+    st->rr = rr;
+    if (!(rr == rr)) { st->done = 1; st->status = -2; return; }
+    if (rr <= st->tol2) { st->done = 1; st->status = 1; return; }
+    if (st->iter >= st->max_iter) { st->done = 1; st->status = -1; }
+}
+
+// r = b - A x (x may be null: zero guess), z = D^-1 r, p = z; rz, rr
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_init(int n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                                    const int32_t* __restrict__ scol, const T* __restrict__ sval,
+                                                    const T* __restrict__ x, const T* __restrict__ b, const T* __restrict__ dinv,
+                                                    T* __restrict__ r, T* __restrict__ z, T* __restrict__ p,
+                                                    double* partial, CgState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (i < n) {
+        T ri = b[i];
+        if (x) ri -= sell_row(i, sptr, slen, scol, sval, x);
+        const T zi = dinv[i] * ri;
+        r[i] = ri;
+        z[i] = zi;
+        p[i] = zi;
+        v[0] = (double)ri * (double)zi;
+        v[1] = (double)ri * (double)ri;
+    }
+    if (grid_reduce<2>(v, partial, &st->ticket)) {
+        st->rz = v[0];
+        st->rr0 = v[1];
+        st->iter = 0;
+        st->done = 0;
+        st->status = 0;
+        cg_check(st, v[1]);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv_pq(int n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                                       const int32_t* __restrict__ scol, const T* __restrict__ sval,
+                                                       const T* __restrict__ p, T* __restrict__ q, double* partial, CgState* st) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n) {
+        const T qi = sell_row(i, sptr, slen, scol, sval, p);
+        q[i] = qi;
+        v[0] = (double)p[i] * (double)qi;
+    }
+    if (grid_reduce<1>(v, partial, &st->ticket)) {
+        st->pq = v[0];
+        st->alpha = st->rz / v[0];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_update(int n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                                                      const T* __restrict__ q, const T* __restrict__ dinv, T* __restrict__ z,
+                                                      double* partial, CgState* st) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const T alpha = (T)st->alpha;
+    double v[2] = {0.0, 0.0};
+    if (i < n) {
+        x[i] += alpha * p[i];
+        const T ri = r[i] - alpha * q[i];
+        const T zi = dinv[i] * ri;
+        r[i] = ri;
+        z[i] = zi;
+        v[0] = (double)ri * (double)zi;
+        v[1] = (double)ri * (double)ri;
+    }
+    if (grid_reduce<2>(v, partial, &st->ticket)) {
+        st->beta = v[0] / st->rz;
+        st->rz = v[0];
+        st->iter += 1;
+        cg_check(st, v[1]);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_direction(int n, const T* __restrict__ z, T* __restrict__ p, const CgState* st) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    p[i] = z[i] + (T)st->beta * p[i];
+}
+
+// FP64 residual r = b - A x with its squared norm; also writes the FP32 scaled copy
+// r32 = r / ||r|| used as the right-hand side of the inner solve.
+__global__ void __launch_bounds__(kBlock) k_residual64(int n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                                       const int32_t* __restrict__ scol, const double* __restrict__ sval,
+                                                       const double* __restrict__ x, const double* __restrict__ b,
+                                                       double* __restrict__ r, double* partial, CgState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n) {
+        const double ri = b[i] - sell_row(i, sptr, slen, scol, sval, x);
+        r[i] = ri;
+        v[0] = ri * ri;
+    }
+    if (grid_reduce<1>(v, partial, &st->ticket)) st->rr = v[0];
+}
+
+__global__ void k_norm2(int n, const double* __restrict__ a, double* partial, CgState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n) v[0] = a[i] * a[i];
+    if (grid_reduce<1>(v, partial, &st->ticket)) st->rr = v[0];
+}
+
+__global__ void k_scale_to32(int n, const double* __restrict__ r, const CgState* st, float* __restrict__ r32,
+                             float* __restrict__ d32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double s = 1.0 / sqrt(st->rr);
+    r32[i] = (float)(r[i] * s);
+    d32[i] = 0.0f;
+}
+
+__global__ void k_refine(int n, double* __restrict__ x, const float* __restrict__ d, const CgState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] += sqrt(st->rr) * (double)d[i];
+}
+
+}  // namespace
+
+// ==================================================================== FemDevice
+FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t stream)
+    : fs_(std::move(fs)), stream_(stream), n_(fs_.n_dofs), nc_(fs_.n_cells) {
+    cudaStream_t s = stream_;
+    cell_dofs_.upload(fs_.cell_dofs, s);
+    r2c_ptr_.upload(fs_.r2c_ptr, s);
+    r2c_item_.upload(fs_.r2c_item, s);
+    r2f_ptr_.upload(fs_.r2f_ptr, s);
+    r2f_item_.upload(fs_.r2f_item, s);
+    if (!fs_.top_faces.empty()) top_faces_.upload(fs_.top_faces, s);
+    dof2node_.upload(fs_.dof2node, s);
+    rowptr_.upload(fs_.rowptr, s);
+    col_.upload(fs_.col, s);
+    slice_ptr_.upload(fs_.slice_ptr, s);
+    slice_len_.upload(fs_.slice_len, s);
+    sell_col_.upload(fs_.sell_col, s);
+    csr2sell_.upload(fs_.csr2sell, s);
+    bc_.upload(fs_.bc_kind, s);
+    std::vector<double> dxyz(3 * (size_t)n_);
+    for (int d = 0; d < n_; ++d)
+        for (int c = 0; c < 3; ++c) dxyz[3 * (size_t)d + c] = pm.hex.xyz[3 * (size_t)fs_.dof2node[d] + c];
+    dof_xyz_.upload(dxyz, s);
+    ke_.resize(64 * (size_t)nc_);
+    kval_.resize(fs_.nnz());
+    sell64_.resize(fs_.slice_ptr.back());
+    sell32_.resize(fs_.slice_ptr.back());
+    sell64_.zero(s);
+    sell32_.zero(s);
+    dinv64_.resize(n_);
+    dinv32_.resize(n_);
+    rhs_.resize(n_);
+    x_.resize(n_);
+    x_.zero(s);
+    r64_.resize(n_); p64_.resize(n_); q64_.resize(n_); z64_.resize(n_);
+    r32_.resize(n_); p32_.resize(n_); q32_.resize(n_); z32_.resize(n_); d32_.resize(n_);
+    partial_.resize(2 * (size_t)grid_for(n_, kBlock) + 64);
+    state_.resize(2);
+    state_.zero(s);
+    FGB_CUDA(cudaMallocHost(&h_state_, 2 * sizeof(CgState)));
+    FGB_CUDA(cudaEventCreate(&ev0_));
+    FGB_CUDA(cudaEventCreate(&ev1_));
+    FGB_CUDA(cudaStreamSynchronize(s));
+    // the host copies of the structure that only the device needs are dropped
+    fs_.r2c_item.clear(); fs_.r2c_item.shrink_to_fit();
+    fs_.csr2sell.clear(); fs_.csr2sell.shrink_to_fit();
+    fs_.sell_col.clear(); fs_.sell_col.shrink_to_fit();
+}
+
+FemDevice::~FemDevice() {
+    if (h_state_) cudaFreeHost(h_state_);
+    cudaEventDestroy(ev0_);
+    cudaEventDestroy(ev1_);
+}
+
+void FemDevice::setup(double applied_field, double applied_potential) {
+    applied_field_ = applied_field;
+    applied_potential_ = applied_potential;
+    x_.zero(stream_);  // solution = dirichlet_bc_value (0), src/DealSolver.cpp:384
+}
+
+void FemDevice::set_space_charge(const double* d_extra) {
+    if (!d_extra) { has_extra_ = false; return; }
+    rhs_extra_.resize(n_);
+    FGB_CUDA(cudaMemcpyAsync(rhs_extra_.get(), d_extra, sizeof(double) * n_, cudaMemcpyDeviceToDevice, stream_));
+    has_extra_ = true;
+}
+
+void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
+    anode_dirichlet_ = anode_dirichlet;
+    const int gb = grid_for(n_, kBlock);
+    if (full_run) {
+        FGB_LAUNCH(k_cell_stiffness<<<grid_for(nc_, 128), 128, 0, stream_>>>(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get()));
+        FGB_LAUNCH(k_assemble_rows<<<gb, kBlock, 0, stream_>>>(n_, rowptr_.get(), col_.get(), r2c_ptr_.get(), r2c_item_.get(),
+                                                    cell_dofs_.get(), ke_.get(), kval_.get()));
+        FGB_CUDA(cudaGetLastError());
+    }
+    // Neumann rhs (or zero when the anode is a Dirichlet boundary)
+    const double bc = anode_dirichlet ? 0.0 : applied_field_;
+    FGB_LAUNCH(k_neumann_rows<<<gb, kBlock, 0, stream_>>>(n_, r2f_ptr_.get(), r2f_item_.get(), top_faces_.get(), dof_xyz_.get(), bc,
+                                               has_extra_ ? rhs_extra_.get() : nullptr, rhs_.get()));
+    FGB_LAUNCH(k_dirichlet_rows<<<gb, kBlock, 0, stream_>>>(n_, rowptr_.get(), col_.get(), kval_.get(), bc_.get(), anode_dirichlet ? 1 : 0,
+                                                 applied_potential_, csr2sell_.get(), sell64_.get(), sell32_.get(),
+                                                 dinv64_.get(), dinv32_.get(), rhs_.get(), x_.get()));
+    FGB_CUDA(cudaGetLastError());
+}
+
+void FemDevice::spmv64(const double* x, double* y) {
+    FGB_LAUNCH(k_sell_spmv<double><<<grid_for(n_, kBlock), kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                                      sell64_.get(), x, y));
+}
+
+double FemDevice::time_spmv(int precision, int reps) {
+    // times the SpMV+dot kernel of the CG iteration on a scratch state (done = 0, rz = 1)
+    const int gb = grid_for(n_, kBlock);
+    CgState* ds = state_.get() + 1;
+    CgState init{};
+    init.rz = 1.0;
+    init.max_iter = 1 << 30;
+    FGB_CUDA(cudaMemcpyAsync(ds, &init, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
+    if (precision) { FGB_CUDA(cudaMemsetAsync(p32_.get(), 0, sizeof(float) * n_, stream_)); }
+    else { FGB_CUDA(cudaMemsetAsync(p64_.get(), 0, sizeof(double) * n_, stream_)); }
+    auto launch = [&]() {
+        if (precision)
+            FGB_LAUNCH(k_cg_spmv_pq<float><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                            sell32_.get(), p32_.get(), q32_.get(), partial_.get(), ds));
+        else
+            FGB_LAUNCH(k_cg_spmv_pq<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                             sell64_.get(), p64_.get(), q64_.get(), partial_.get(), ds));
+    };
+    for (int i = 0; i < 3; ++i) launch();
+    FGB_CUDA(cudaEventRecord(ev0_, stream_));
+    for (int i = 0; i < reps; ++i) launch();
+    FGB_CUDA(cudaEventRecord(ev1_, stream_));
+    FGB_CUDA(cudaEventSynchronize(ev1_));
+    float ms = 0;
+    FGB_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    return ms / reps;
+}
+
+void FemDevice::download_matrix(std::vector<double>& vals, std::vector<double>& rhs) {
+    // CSR order values after Dirichlet elimination, gathered back from the SELL layout
+    std::vector<double> s = sell64_.to_host(stream_);
+    std::vector<int64_t> c2s(fs_.nnz());
+    // rebuild the CSR->SELL map on the host (kept only on the device after upload)
+    for (int r = 0; r < n_; ++r) {
+        const int sl = r / 32, lane = r % 32;
+        for (int64_t k = fs_.rowptr[r]; k < fs_.rowptr[r + 1]; ++k)
+            c2s[k] = fs_.slice_ptr[sl] + (k - fs_.rowptr[r]) * 32 + lane;
+    }
+    vals.resize(fs_.nnz());
+    for (int64_t k = 0; k < fs_.nnz(); ++k) vals[k] = s[c2s[k]];
+    rhs = rhs_.to_host(stream_);
+}
+
+void FemDevice::run_cg(bool fp32, CgState* d_state, int max_iter, int chunk) {
+    const int gb = grid_for(n_, kBlock);
+    CgState* h = h_state_ + (fp32 ? 1 : 0);
+    // one chunk = `chunk` iterations, launched back to back; kernels become no-ops once done.
+    // The device sets done at max_iter at the latest; the host bound is a second guard.
+    const long long max_chunks = (long long)max_iter / chunk + 2;
+    for (long long c = 0;; ++c) {
+        FGB_REQUIRE(c <= max_chunks, "CG did not report completion within its iteration budget");
+        for (int it = 0; it < chunk; ++it) {
+            if (fp32) {
+                FGB_LAUNCH(k_cg_spmv_pq<float><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                                sell32_.get(), p32_.get(), q32_.get(), partial_.get(), d_state));
+                FGB_LAUNCH(k_cg_update<float><<<gb, kBlock, 0, stream_>>>(n_, d32_.get(), r32_.get(), p32_.get(), q32_.get(), dinv32_.get(),
+                                                               z32_.get(), partial_.get(), d_state));
+                FGB_LAUNCH(k_cg_direction<float><<<gb, kBlock, 0, stream_>>>(n_, z32_.get(), p32_.get(), d_state));
+            } else {
+                FGB_LAUNCH(k_cg_spmv_pq<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                                 sell64_.get(), p64_.get(), q64_.get(), partial_.get(), d_state));
+                FGB_LAUNCH(k_cg_update<double><<<gb, kBlock, 0, stream_>>>(n_, x_.get(), r64_.get(), p64_.get(), q64_.get(), dinv64_.get(),
+                                                                z64_.get(), partial_.get(), d_state));
+                FGB_LAUNCH(k_cg_direction<double><<<gb, kBlock, 0, stream_>>>(n_, z64_.get(), p64_.get(), d_state));
+            }
+        }
+        FGB_CUDA(cudaMemcpyAsync(h, d_state, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        if (h->done) break;
+    }
+    FGB_CUDA(cudaGetLastError());
+}
+
+int FemDevice::solve(const SolveOptions& opt, SolveStats* st) {
+    SolveStats local;
+    if (!st) st = &local;
+    *st = SolveStats();
+    FGB_CUDA(cudaEventRecord(ev0_, stream_));
+    int rc = opt.precision == 0 ? solve_plain(opt, st) : solve_mixed(opt, st);
+    FGB_CUDA(cudaEventRecord(ev1_, stream_));
+    FGB_CUDA(cudaEventSynchronize(ev1_));
+    float ms = 0;
+    FGB_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    st->ms = ms;
+    return rc;
+}
+
+static double tol2_of(const SolveOptions& opt, double bnorm) {
+    const double t = std::max(opt.rel_tol * bnorm, opt.abs_tol);
+    return t * t;
+}
+
+int FemDevice::solve_plain(const SolveOptions& opt, SolveStats* st) {
+    const int gb = grid_for(n_, kBlock);
+    CgState* ds = state_.get();
+    // ||b||
+    FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
+    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    const double bnorm = std::sqrt(h_state_->rr);
+    st->bnorm = bnorm;
+    CgState init{};
+    init.tol2 = tol2_of(opt, bnorm);
+    init.max_iter = opt.max_iter;
+    FGB_CUDA(cudaMemcpyAsync(ds, &init, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
+    FGB_LAUNCH(k_cg_init<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(),
+                                                  x_.get(), rhs_.get(), dinv64_.get(), r64_.get(), z64_.get(), p64_.get(),
+                                                  partial_.get(), ds));
+    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    if (!h_state_->done) run_cg(false, ds, opt.max_iter, std::max(1, opt.chunk));
+    st->iterations = h_state_->iter;
+    const int cg_status = h_state_->status;
+    // true residual
+    FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(), x_.get(),
+                                             rhs_.get(), r64_.get(), partial_.get(), ds));
+    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    const double rn = std::sqrt(h_state_->rr);
+    st->rel_residual = bnorm > 0 ? rn / bnorm : rn;
+    st->status = bnorm == 0 ? 1 : cg_status;
+    return st->status == 1 ? st->iterations : -st->iterations;
+}
+
+int FemDevice::solve_mixed(const SolveOptions& opt, SolveStats* st) {
+    const int gb = grid_for(n_, kBlock);
+    CgState* ds = state_.get();       // outer scalars
+    CgState* di = state_.get() + 1;   // inner CG scalars
+    FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
+    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    const double bnorm = std::sqrt(h_state_->rr);
+    st->bnorm = bnorm;
+    const double tol2 = tol2_of(opt, bnorm);
+    int total = 0;
+    st->status = -1;
+    for (int outer = 0; outer <= opt.max_outer; ++outer) {
+        FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(),
+                                                 x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
+        FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        const double rr = h_state_->rr;
+        st->rel_residual = bnorm > 0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
+        st->outer = outer;
+        if (rr <= tol2 || bnorm == 0) { st->status = 1; break; }
+        if (!(rr == rr)) { st->status = -2; break; }
+        if (total >= opt.max_iter || outer == opt.max_outer) break;
+        FGB_LAUNCH(k_scale_to32<<<gb, kBlock, 0, stream_>>>(n_, r64_.get(), ds, r32_.get(), d32_.get()));
+        CgState init{};
+        init.tol2 = opt.inner_tol * opt.inner_tol;
+        init.max_iter = std::max(1, opt.max_iter - total);
+        FGB_CUDA(cudaMemcpyAsync(di, &init, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
+        FGB_LAUNCH(k_cg_init<float><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
+                                                     nullptr, r32_.get(), dinv32_.get(), r32_.get(), z32_.get(), p32_.get(),
+                                                     partial_.get(), di));
+        run_cg(true, di, init.max_iter, std::max(1, opt.chunk));
+        total += h_state_[1].iter;
+        FGB_LAUNCH(k_refine<<<gb, kBlock, 0, stream_>>>(n_, x_.get(), d32_.get(), ds));
+    }
+    st->iterations = total;
+    return st->status == 1 ? total : -total;
+}
+
+}  // namespace fgb

@@ -1,0 +1,101 @@
+// Device-resident Poisson system of one mesh and its solvers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.h"
+#include "fem.h"
+
+namespace fgb {
+
+// Scalars of one CG run, kept in device memory so that a whole chunk of iterations can be
+// replayed from a CUDA graph without host round trips.
+struct CgState {
+    double rz, rz_new, pq, alpha, beta, rr, rr0, tol2;
+    int iter, max_iter, done, status;  // status: 1 converged, -1 max_iter, -2 breakdown/NaN
+    unsigned int ticket;
+    int pad;
+};
+
+struct SolveOptions {
+    int precision = 1;        // 0: plain FP64 Jacobi-PCG; 1: FP32 inner PCG + FP64 refinement
+    double rel_tol = 1e-9;    // on ||b - A x||_2 / ||b||_2 (FP64 true residual)
+    double abs_tol = 0.0;     // optional absolute floor (reference field_cgtol semantics)
+    int max_iter = 10000;     // total CG iterations (inner + plain)
+    double inner_tol = 1e-4;  // relative reduction per refinement sweep
+    int max_outer = 50;
+    int chunk = 16;           // iterations per graph launch
+};
+
+struct SolveStats {
+    int iterations = 0;       // total CG iterations (all refinement sweeps)
+    int outer = 0;            // refinement sweeps (0 for plain FP64)
+    int status = 0;           // 1 converged, -1 not converged, -2 breakdown
+    double rel_residual = 0;  // final ||b-Ax||/||b|| in FP64
+    double bnorm = 0;
+    double ms = 0;            // device time of the solve (CUDA events)
+};
+
+class FemDevice {
+public:
+    FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t stream);
+    ~FemDevice();
+
+    // PoissonSolver::setup + assemble verbs (src/PoissonSolver.cpp:162-210)
+    void setup(double applied_field, double applied_potential);   // zeroes the solution
+    void assemble(bool full_run, bool anode_dirichlet);
+    // adds a space-charge contribution rhs[dof] += w * N(point) to the unconstrained rhs
+    // before Dirichlet application; values given per dof (already summed)
+    void set_space_charge(const double* d_rhs_extra);
+    int solve(const SolveOptions& opt, SolveStats* st);
+
+    // solution by dof / by mesh node
+    const double* d_solution() const { return x_.get(); }
+    double* d_solution() { return x_.get(); }
+    const FemStructure& structure() const { return fs_; }
+    int n_dofs() const { return fs_.n_dofs; }
+    int64_t nnz() const { return fs_.nnz(); }
+    const int32_t* d_dof2node() const { return dof2node_.get(); }
+    double last_spmv_ms(int precision) const { return precision ? spmv32_ms_ : spmv64_ms_; }
+    // measure: average device time of one SpMV (64 or 32 bit values) over `reps` launches
+    double time_spmv(int precision, int reps);
+    void download_matrix(std::vector<double>& vals, std::vector<double>& rhs);
+    cudaStream_t stream() const { return stream_; }
+
+private:
+    void spmv64(const double* x, double* y);
+    int solve_plain(const SolveOptions& opt, SolveStats* st);
+    int solve_mixed(const SolveOptions& opt, SolveStats* st);
+    void run_cg(bool fp32, CgState* d_state, int max_iter, int chunk);
+
+    FemStructure fs_;
+    cudaStream_t stream_;
+    int n_, nc_;
+    double applied_field_ = 0, applied_potential_ = 0;
+    bool anode_dirichlet_ = false;
+    // structure
+    DBuf<int32_t> cell_dofs_, r2c_ptr_, r2c_item_, r2f_ptr_, r2f_item_, top_faces_, dof2node_;
+    DBuf<int64_t> rowptr_, slice_ptr_, csr2sell_;
+    DBuf<int32_t> col_, slice_len_, sell_col_;
+    DBuf<int8_t> bc_;
+    DBuf<double> dof_xyz_;
+    // values
+    DBuf<double> ke_;        // 64 per cell
+    DBuf<double> kval_;      // CSR values before Dirichlet (saved matrix)
+    DBuf<double> sell64_;    // SELL values after Dirichlet
+    DBuf<float> sell32_;
+    DBuf<double> dinv64_;
+    DBuf<float> dinv32_;
+    DBuf<double> rhs_, rhs_extra_, x_;
+    bool has_extra_ = false;
+    // work vectors
+    DBuf<double> r64_, p64_, q64_, z64_;
+    DBuf<float> r32_, p32_, q32_, z32_, d32_;
+    DBuf<double> partial_;
+    DBuf<CgState> state_;
+    CgState* h_state_ = nullptr;  // pinned mirror
+    double spmv64_ms_ = 0, spmv32_ms_ = 0;
+    cudaEvent_t ev0_, ev1_;
+};
+
+}  // namespace fgb

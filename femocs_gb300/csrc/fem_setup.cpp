@@ -1,0 +1,247 @@
+// Host construction of the vacuum FEM structure.
+//
+// DoF numbering: the reference lets deal.II number DoFs (DoFHandler::distribute_dofs) and
+// maps them back to mesh vertices (src/DealSolver.cpp:318-341); only the per-vertex
+// solution is observable. Here the vacuum vertices are ordered along a Morton curve and,
+// inside windows of 256 rows, by decreasing row length, so that (a) rows close in index are
+// close in space (the SpMV gathers hit cache) and (b) each 32-row SELL slice holds rows of
+// similar length (little padding).
+#include "fem.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace fgb {
+
+namespace {
+
+inline uint64_t spread3(uint64_t v) {
+    v &= 0x1fffff;
+    v = (v | v << 32) & 0x1f00000000ffffull;
+    v = (v | v << 16) & 0x1f0000ff0000ffull;
+    v = (v | v << 8) & 0x100f00f00f00f00full;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+    v = (v | v << 2) & 0x1249249249249249ull;
+    return v;
+}
+
+// the six faces of a femocs-ordered hex, vertices in cyclic order
+const int kHexFace[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 3, 7, 4}, {1, 2, 6, 5}, {0, 1, 5, 4}, {3, 2, 6, 7}};
+
+struct BFace {
+    int32_t s[4];  // sorted dofs
+    int32_t cell;
+    int8_t face;
+};
+
+}  // namespace
+
+FemStructure build_fem_structure(const PreparedMesh& pm) {
+    FemStructure fs;
+    const int nv = (int)pm.vac.vertex2node.size();
+    const int nc = (int)pm.vac.cells.size();
+    FGB_REQUIRE(nv > 0 && nc > 0, "mesh has no vacuum hexahedra");
+    fs.n_dofs = nv;
+    fs.n_cells = nc;
+    const std::vector<double>& X = pm.hex.xyz;
+
+    // cells in vertex numbering
+    std::vector<int32_t> cv(8 * (size_t)nc);
+    for (int c = 0; c < nc; ++c)
+        for (int k = 0; k < 8; ++k)
+            cv[8 * (size_t)c + k] = pm.vac.node2vertex[pm.hex.hexs[8 * (size_t)pm.vac.cells[c] + k]];
+
+    // vertex -> cells
+    std::vector<int32_t> v2c_ptr(nv + 1, 0);
+    for (int32_t v : cv) v2c_ptr[v + 1]++;
+    for (int i = 0; i < nv; ++i) v2c_ptr[i + 1] += v2c_ptr[i];
+    std::vector<int32_t> v2c(v2c_ptr[nv]);
+    {
+        std::vector<int32_t> pos(v2c_ptr.begin(), v2c_ptr.end() - 1);
+        for (int c = 0; c < nc; ++c)
+            for (int k = 0; k < 8; ++k) v2c[pos[cv[8 * (size_t)c + k]]++] = 8 * c + k;
+    }
+
+    // neighbour sets (vertex numbering) and degrees
+    std::vector<int32_t> deg(nv);
+    std::vector<std::vector<int32_t>> nb(nv);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int v = 0; v < nv; ++v) {
+        std::vector<int32_t>& l = nb[v];
+        l.reserve(8 * (v2c_ptr[v + 1] - v2c_ptr[v]));
+        for (int p = v2c_ptr[v]; p < v2c_ptr[v + 1]; ++p) {
+            const int c = v2c[p] / 8;
+            for (int k = 0; k < 8; ++k) l.push_back(cv[8 * (size_t)c + k]);
+        }
+        std::sort(l.begin(), l.end());
+        l.erase(std::unique(l.begin(), l.end()), l.end());
+        deg[v] = (int32_t)l.size();
+    }
+
+    // Morton order, then windows of 256 sorted by decreasing degree
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int v = 0; v < nv; ++v)
+        for (int c = 0; c < 3; ++c) {
+            const double x = X[3 * (size_t)pm.vac.vertex2node[v] + c];
+            mn[c] = std::min(mn[c], x);
+            mx[c] = std::max(mx[c], x);
+        }
+    std::vector<std::pair<uint64_t, int32_t>> key(nv);
+    for (int v = 0; v < nv; ++v) {
+        uint64_t code = 0;
+        for (int c = 0; c < 3; ++c) {
+            const double span = mx[c] > mn[c] ? mx[c] - mn[c] : 1.0;
+            double t = (X[3 * (size_t)pm.vac.vertex2node[v] + c] - mn[c]) / span;
+            uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, std::floor(t * 2097151.0)));
+            code |= spread3(q) << c;
+        }
+        key[v] = {code, v};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int32_t> dof2v(nv);
+    for (int i = 0; i < nv; ++i) dof2v[i] = key[i].second;
+    const int W = 256;
+    for (int w0 = 0; w0 < nv; w0 += W) {
+        const int w1 = std::min(nv, w0 + W);
+        std::stable_sort(dof2v.begin() + w0, dof2v.begin() + w1,
+                         [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+    }
+    std::vector<int32_t> v2dof(nv);
+    for (int d = 0; d < nv; ++d) v2dof[dof2v[d]] = d;
+
+    fs.dof2node.resize(nv);
+    fs.node2dof.assign(pm.hex.n_nodes(), -1);
+    for (int d = 0; d < nv; ++d) {
+        fs.dof2node[d] = pm.vac.vertex2node[dof2v[d]];
+        fs.node2dof[fs.dof2node[d]] = d;
+    }
+    fs.cell_dofs.resize(8 * (size_t)nc);
+    for (size_t i = 0; i < cv.size(); ++i) fs.cell_dofs[i] = v2dof[cv[i]];
+
+    // CSR in dof numbering
+    fs.rowptr.assign(nv + 1, 0);
+    fs.row_len.resize(nv);
+    for (int d = 0; d < nv; ++d) {
+        fs.row_len[d] = deg[dof2v[d]];
+        fs.rowptr[d + 1] = fs.rowptr[d] + fs.row_len[d];
+    }
+    fs.col.resize(fs.rowptr[nv]);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int d = 0; d < nv; ++d) {
+        const std::vector<int32_t>& l = nb[dof2v[d]];
+        int32_t* o = &fs.col[fs.rowptr[d]];
+        for (size_t k = 0; k < l.size(); ++k) o[k] = v2dof[l[k]];
+        std::sort(o, o + l.size());
+    }
+    nb.clear();
+    nb.shrink_to_fit();
+
+    // row -> (cell, local), ascending cell
+    fs.r2c_ptr.assign(nv + 1, 0);
+    for (int d = 0; d < nv; ++d) fs.r2c_ptr[d + 1] = fs.r2c_ptr[d] + (v2c_ptr[dof2v[d] + 1] - v2c_ptr[dof2v[d]]);
+    fs.r2c_item.resize(fs.r2c_ptr[nv]);
+    for (int d = 0; d < nv; ++d) {
+        const int v = dof2v[d];
+        std::copy(v2c.begin() + v2c_ptr[v], v2c.begin() + v2c_ptr[v + 1], fs.r2c_item.begin() + fs.r2c_ptr[d]);
+    }
+
+    // ---- boundary faces (src/DealSolver.cpp:461-518 via PoissonSolver::mark_mesh)
+    std::vector<BFace> faces(6 * (size_t)nc);
+    for (int c = 0; c < nc; ++c)
+        for (int f = 0; f < 6; ++f) {
+            BFace& b = faces[6 * (size_t)c + f];
+            for (int q = 0; q < 4; ++q) b.s[q] = fs.cell_dofs[8 * (size_t)c + kHexFace[f][q]];
+            std::sort(b.s, b.s + 4);
+            b.cell = c;
+            b.face = (int8_t)f;
+        }
+    std::sort(faces.begin(), faces.end(), [](const BFace& a, const BFace& b) {
+        for (int k = 0; k < 4; ++k)
+            if (a.s[k] != b.s[k]) return a.s[k] < b.s[k];
+        return a.cell < b.cell;
+    });
+    std::vector<BFace> bnd;
+    for (size_t i = 0; i < faces.size();) {
+        size_t j = i + 1;
+        while (j < faces.size() && std::equal(faces[j].s, faces[j].s + 4, faces[i].s)) ++j;
+        if (j - i == 1) bnd.push_back(faces[i]);
+        i = j;
+    }
+    faces.clear();
+    faces.shrink_to_fit();
+    std::sort(bnd.begin(), bnd.end(), [](const BFace& a, const BFace& b) {
+        return a.cell != b.cell ? a.cell < b.cell : a.face < b.face;
+    });
+    auto dof_x = [&](int32_t d, int c) { return X[3 * (size_t)fs.dof2node[d] + c]; };
+    double bmn[3] = {1e16, 1e16, 1e16}, bmx[3] = {-1e16, -1e16, -1e16};
+    std::vector<double> ctr(3 * bnd.size());
+    for (size_t i = 0; i < bnd.size(); ++i) {
+        for (int c = 0; c < 3; ++c) {
+            double s = 0.0;
+            for (int q = 0; q < 4; ++q) s += dof_x(fs.cell_dofs[8 * (size_t)bnd[i].cell + kHexFace[bnd[i].face][q]], c);
+            ctr[3 * i + c] = s / 4.0;
+            bmn[c] = std::min(bmn[c], ctr[3 * i + c]);
+            bmx[c] = std::max(bmx[c], ctr[3 * i + c]);
+        }
+    }
+    const double eps = 1e-6;
+    fs.bc_kind.assign(nv, 0);
+    std::vector<int32_t> top;
+    for (size_t i = 0; i < bnd.size(); ++i) {
+        const double x = ctr[3 * i], y = ctr[3 * i + 1], z = ctr[3 * i + 2];
+        const bool side = std::fabs(x - bmn[0]) <= eps || std::fabs(x - bmx[0]) <= eps ||
+                          std::fabs(y - bmn[1]) <= eps || std::fabs(y - bmx[1]) <= eps;
+        if (side) continue;
+        int32_t fd[4];
+        for (int q = 0; q < 4; ++q) fd[q] = fs.cell_dofs[8 * (size_t)bnd[i].cell + kHexFace[bnd[i].face][q]];
+        if (std::fabs(z - bmx[2]) <= eps) {
+            top.insert(top.end(), fd, fd + 4);
+        } else {
+            for (int q = 0; q < 4; ++q) fs.bc_kind[fd[q]] = 1;
+        }
+    }
+    fs.top_faces = top;
+    for (int32_t d : top)
+        if (fs.bc_kind[d] == 0) fs.bc_kind[d] = 2;
+    const int nt = fs.n_top_faces();
+    fs.r2f_ptr.assign(nv + 1, 0);
+    for (int32_t d : top) fs.r2f_ptr[d + 1]++;
+    for (int i = 0; i < nv; ++i) fs.r2f_ptr[i + 1] += fs.r2f_ptr[i];
+    fs.r2f_item.resize(fs.r2f_ptr[nv]);
+    {
+        std::vector<int32_t> pos(fs.r2f_ptr.begin(), fs.r2f_ptr.end() - 1);
+        for (int f = 0; f < nt; ++f)
+            for (int q = 0; q < 4; ++q) fs.r2f_item[pos[top[4 * (size_t)f + q]]++] = 4 * f + q;
+    }
+
+    // ---- SELL-32
+    const int C = 32;
+    const int ns = (nv + C - 1) / C;
+    fs.slice_ptr.assign(ns + 1, 0);
+    fs.slice_len.assign(ns, 0);
+    for (int s = 0; s < ns; ++s) {
+        int m = 0;
+        for (int r = s * C; r < std::min(nv, (s + 1) * C); ++r) m = std::max(m, fs.row_len[r]);
+        fs.slice_len[s] = m;
+        fs.slice_ptr[s + 1] = fs.slice_ptr[s] + (int64_t)m * C;
+    }
+    fs.sell_col.assign(fs.slice_ptr[ns], 0);
+    fs.csr2sell.resize(fs.nnz());
+    for (int s = 0; s < ns; ++s)
+        for (int lane = 0; lane < C; ++lane) {
+            const int r = s * C + lane;
+            for (int j = 0; j < fs.slice_len[s]; ++j) {
+                const int64_t pos = fs.slice_ptr[s] + (int64_t)j * C + lane;
+                if (r < nv && j < fs.row_len[r]) {
+                    fs.sell_col[pos] = fs.col[fs.rowptr[r] + j];
+                    fs.csr2sell[fs.rowptr[r] + j] = pos;
+                } else {
+                    fs.sell_col[pos] = r < nv ? r : 0;
+                }
+            }
+        }
+    return fs;
+}
+
+}  // namespace fgb

@@ -1,0 +1,41 @@
+// One mesh on the device: the Poisson system (FemDevice) and the interpolator (DeviceMesh)
+// sharing a CUDA stream. This is the GPU counterpart of the reference's PoissonSolver<3>
+// plus the vacuum Interpolator of ProjectRunaway.
+#pragma once
+
+#include <memory>
+
+#include "fem_device.h"
+#include "interp.h"
+
+namespace fgb {
+
+class Field {
+public:
+    explicit Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream = nullptr);
+    ~Field();
+
+    const PreparedMesh& mesh() const { return *pm_; }
+    FemDevice& fem() { return *fem_; }
+    DeviceMesh& interp() { return *dm_; }
+    cudaStream_t stream() const { return stream_; }
+
+    // ProjectRunaway::solve_laplace (src/ProjectRunaway.cpp:422-447): setup(-E0,V0),
+    // assemble(true), solve, extract_solution
+    int solve_laplace(double E0, double V0, bool anode_dirichlet, const SolveOptions& opt, bool smoothen, SolveStats* st);
+
+    // host-pointer interpolation through reusable device buffers
+    void interpolate_host(int n, const double* xyz, int rank, int32_t* cells, double* out5, LocateStats* ls);
+    void extract(bool smoothen);
+
+private:
+    std::shared_ptr<const PreparedMesh> pm_;
+    cudaStream_t stream_;
+    bool own_stream_ = false;
+    std::unique_ptr<FemDevice> fem_;
+    std::unique_ptr<DeviceMesh> dm_;
+    DBuf<double> pts_, out_;
+    DBuf<int32_t> cells_;
+};
+
+}  // namespace fgb

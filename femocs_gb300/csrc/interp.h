@@ -1,0 +1,79 @@
+// Device-resident interpolator of one mesh: nodal solution (E, charge density, phi per
+// hex-mesh node), nodal-field recovery and smoothing, point location and interpolation.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.h"
+#include "prepared.h"
+
+namespace fgb {
+
+// Uniform grid over the mesh box: a seed tet per grid cell (start of the location walk) and
+// the tets bucketed by centroid (exact nearest-centroid fallback search).
+struct SeedGrid {
+    int dim[3] = {1, 1, 1};
+    double origin[3] = {0, 0, 0};
+    double step[3] = {1, 1, 1};
+    std::vector<int32_t> seed;       // per grid cell
+    std::vector<int32_t> ptr, tets;  // tets bucketed by centroid, ascending within a bucket
+    std::vector<double> cxyz;        // centroids in bucket order
+};
+SeedGrid build_seed_grid(const PreparedMesh& pm);
+
+struct LocateStats {
+    int n_points = 0;
+    int n_walk_failed = 0;   // located by the exhaustive scan
+    int n_fallback = 0;      // no searchable tet contains the point (nearest-centroid result)
+    int n_dependent = 0;     // points whose result depends on the previous point's cell
+    int longest_run = 0;
+};
+
+class DeviceMesh {
+public:
+    DeviceMesh(const PreparedMesh& pm, cudaStream_t stream);
+
+    // nodal solution from the FEM solution (phi by dof); recovers E (src/Interpolator.cpp:172-190)
+    void extract_solution(const double* d_phi_dof, const int32_t* d_dof2node, int n_dofs, bool smoothen,
+                          const double* d_charge_dof = nullptr);
+    // overwrite the nodal solution (5 doubles per node) from the host
+    void set_solution(const double* h_sol5);
+    void get_solution(double* h_sol5);
+    // max |E| over the nodes (FieldReader::max_field, src/SolutionReader.cpp:558-566)
+    double max_field_norm();
+    // Locate and interpolate n points (device pointers, xyz interleaved); rank 1 lin-tet,
+    // 2 quad-tet, 3 lin-hex; cells and out (5 per point) on the device.
+    void locate_interpolate(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out,
+                            LocateStats* stats = nullptr);
+    // Interpolate with cells already known (SolutionReader::calc_interpolation with mapped atoms)
+    void interpolate_known(int n, const double* d_pts, int rank, const int32_t* d_cells, double* d_out);
+
+    int n_nodes() const { return n_nodes_; }
+    int n_tets() const { return n_tets_; }
+    double* d_sol() { return sol_.get(); }
+    cudaStream_t stream() const { return stream_; }
+    const double* d_node_xyz() const { return xyz_.get(); }
+    const int32_t* d_hexs() const { return hexs_.get(); }
+    const double* d_hex_coeffs() const { return hexf_.get(); }
+
+private:
+    void ensure_scratch(int n);
+    cudaStream_t stream_;
+    int n_nodes_, n_tets_, n_tetnodes_;
+    double decay_;
+    double bb_lo_[3], bb_hi_[3];
+    SeedGrid grid_;
+    DBuf<int32_t> tet_nodes_, face_nbr_, nbr_ptr_, nbr_idx_, quad_;
+    DBuf<int8_t> search_;
+    DBuf<double> det_, centroid_;
+    DBuf<int32_t> hexs_, n2c_ptr_, n2c_item_, voro_ptr_, voro_idx_;
+    DBuf<double> hexf_, xyz_;
+    DBuf<int32_t> seed_, gptr_, gtets_;
+    DBuf<double> gcxyz_;
+    DBuf<double> sol_;
+    // per-point scratch
+    DBuf<int32_t> v_, nin_, f_, res_, dep_, counters_;
+    int scratch_n_ = 0;
+};
+
+}  // namespace fgb

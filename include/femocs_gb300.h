@@ -1,0 +1,156 @@
+/*
+ * femocs_gb300 -- C ABI of the GB300 field-solve library.
+ *
+ * Part 1 reproduces the reference's C wrapper (include/Femocs_wrap.h:12-50 of FEMOCS) symbol
+ * for symbol, so an MD code (or the Fortran module src/Femocs_wrap.f90) can link this
+ * library in place of the deal.II CPU build. Conventions are the reference's: an opaque
+ * handle, caller-owned SoA arrays of length n, status through int* retval
+ * (0 = current solution used / success, 1 = previous solution / failure), n <= 0 disables
+ * the call, no exceptions cross the boundary.
+ *
+ * Part 2 exposes the inner operator interface (the reference's PoissonSolver<3> verbs
+ * setup / assemble / solve / export_solution, include/PoissonSolver.h:25-105, and the
+ * Interpolator's extract_solution / locate / interpolate) on device-resident state, plus
+ * mesh import and the seeded synthetic workloads used by the tests and the benchmark.
+ *
+ * All entry points are host functions; pointers are host pointers unless the name ends
+ * in _device.
+ */
+#ifndef FEMOCS_GB300_H
+#define FEMOCS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* =============================== Part 1: reference C wrapper =============================== */
+typedef struct FEMOCS FEMOCS;
+
+/* replaces create_femocs, include/Femocs_wrap.h:14 -- reads the configuration script */
+FEMOCS* create_femocs(const char* conf_file);
+/* replaces delete_femocs, include/Femocs_wrap.h:17 */
+void delete_femocs(FEMOCS* femocs);
+/* replaces femocs_run, include/Femocs_wrap.h:19 -- field solve (Femocs::run, src/Femocs.cpp:72) */
+void femocs_run(FEMOCS* femocs, int* retval, int timestep, double time);
+/* replaces femocs_import_file, include/Femocs_wrap.h:21 -- xyz/ckx atom files */
+void femocs_import_file(FEMOCS* femocs, int* retval, const char* file_name);
+/* replaces femocs_import_parcas, include/Femocs_wrap.h:23 -- not supported (sets retval=1) */
+void femocs_import_parcas(FEMOCS* femocs, int* retval, int n_atoms, const double* x0, const double* x1,
+                          const double* box, const int* nborlist);
+/* replaces femocs_import_atoms, include/Femocs_wrap.h:26 */
+void femocs_import_atoms(FEMOCS* femocs, int* retval, int n_atoms, const double* x, const double* y,
+                         const double* z, const int* types);
+/* replaces femocs_interpolate_elfield, include/Femocs_wrap.h:29 */
+void femocs_interpolate_elfield(FEMOCS* femocs, int* retval, int n_points, const double* x, const double* y,
+                                const double* z, double* Ex, double* Ey, double* Ez, double* Enorm, int* flag);
+/* replaces femocs_interpolate_surface_elfield, include/Femocs_wrap.h:33 */
+void femocs_interpolate_surface_elfield(FEMOCS* femocs, int* retval, int n_points, const double* x,
+                                        const double* y, const double* z, double* Ex, double* Ey, double* Ez,
+                                        double* Enorm, int* flag);
+/* replaces femocs_interpolate_phi, include/Femocs_wrap.h:37 */
+void femocs_interpolate_phi(FEMOCS* femocs, int* retval, int n_points, const double* x, const double* y,
+                            const double* z, double* phi, int* flag);
+/* replaces femocs_export_data, include/Femocs_wrap.h:41 */
+void femocs_export_data(FEMOCS* femocs, int* retval, double* data, int n_points, const char* data_type);
+/* replaces femocs_export_int, include/Femocs_wrap.h:43 */
+void femocs_export_int(FEMOCS* femocs, int* retval, int* data, int n_points, const char* data_type);
+/* replaces femocs_interpolate, include/Femocs_wrap.h:45 */
+void femocs_interpolate(FEMOCS* femocs, int* retval, double* data, int* flag, int n_points, const char* data_type,
+                        int near_surface, const double* x, const double* y, const double* z);
+/* replace femocs_parse_int/double/string, include/Femocs_wrap.h:48-52 */
+void femocs_parse_int(FEMOCS* femocs, int* retval, const char* command, int* arg);
+void femocs_parse_double(FEMOCS* femocs, int* retval, const char* command, double* arg);
+void femocs_parse_string(FEMOCS* femocs, int* retval, const char* command, char* arg);
+
+/* Library extensions of the facade (no counterpart in Femocs_wrap.h). */
+/* Tetrahedral mesh from arrays: nodes xyz (3*n_nodes), tets (4*n_tets, 0-based), region
+ * markers (3 = vacuum, anything else = material); replaces the TetGen step of Femocs::run. */
+void femocs_import_mesh(FEMOCS* femocs, int* retval, int n_nodes, const double* xyz, int n_tets, const int* tets,
+                        const int* markers);
+/* Statistics of the last femocs_run: iterations, refinement sweeps, status, relative
+ * residual, solve milliseconds, #dofs (as doubles). */
+void femocs_last_solve(FEMOCS* femocs, int* retval, double* out8);
+const char* femocs_last_error(void);
+/* number of CUDA kernels the library has launched so far (all handles) */
+long long fgb_kernel_launches(void);
+
+/* =============================== Part 2: inner operator API =============================== */
+typedef struct FGB_MESH FGB_MESH;    /* host-prepared mesh */
+typedef struct FGB_FIELD FGB_FIELD;  /* device-resident Poisson system + interpolator */
+
+typedef struct {
+    double radius, height, box_half, slab, top, h, growth, margin; /* Angstrom */
+} FgbNanotip;
+
+/* mesh construction (host); returns NULL on error (see femocs_last_error) */
+FGB_MESH* fgb_mesh_from_arrays(int n_nodes, const double* xyz, int n_tets, const int* tets, const int* markers);
+FGB_MESH* fgb_mesh_read_gmsh(const char* path);
+FGB_MESH* fgb_mesh_synthetic(const FgbNanotip* spec);
+void fgb_mesh_free(FGB_MESH* m);
+/* sizes: [n_tetnodes, n_tets, n_nodes, n_hexs, n_vac_vertices, n_vac_cells, n_nbr_idx, n_voro_idx,
+ *         n_dofs, nnz, n_top_faces, n_sell] (n_dofs.. are 0 until a field is created) */
+int fgb_mesh_sizes(const FGB_MESH* m, int64_t* out12);
+/* copy a named host table into `out` (caller sized from fgb_mesh_sizes):
+ * tet_nodes tet_marker tet_nbor node_xyz node_marker hex_nodes hex_marker tet_det
+ * tet_centroid hex_coeffs nbr_ptr nbr_idx quad_nodes voro_ptr voro_idx vac_node2vertex
+ * vac_cells edgemax(double) */
+int fgb_mesh_export(const FGB_MESH* m, const char* name, void* out);
+
+/* synthetic atoms/probes for a nanotip spec; two-call pattern: pass out=NULL to get the count */
+int64_t fgb_synth_atoms(const FgbNanotip* spec, double latconst, double sigma, double cutoff, uint64_t seed,
+                        double* xyz_out, int* type_out);
+int64_t fgb_synth_probes(const FgbNanotip* spec, int n, uint64_t seed, double* xyz_out);
+
+/* device field */
+FGB_FIELD* fgb_field_create(const FGB_MESH* m);
+void fgb_field_free(FGB_FIELD* f);
+int fgb_field_sizes(const FGB_FIELD* f, int64_t* out4); /* n_dofs, nnz, n_top_faces, sell_entries */
+/* PoissonSolver::setup(field, potential): applied_field is the Neumann value on the top
+ * boundary (the reference passes -E0), applied_potential the anode value; zeroes phi */
+int fgb_field_setup(FGB_FIELD* f, double applied_field, double applied_potential);
+/* PoissonSolver::assemble(full_run); anode_dirichlet selects anode_bc = dirichlet */
+int fgb_field_assemble(FGB_FIELD* f, int full_run, int anode_dirichlet);
+/* CG solve; precision 0 = plain FP64 Jacobi-PCG, 1 = FP32 inner + FP64 refinement.
+ * stats (may be NULL): iterations, outer, status, rel_residual, bnorm, ms.
+ * Returns #iterations (>0) or -#iterations when not converged. */
+int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol, int max_iter, double inner_tol,
+                    double* stats6);
+/* phi per vacuum dof order is internal; these export per hex-mesh node (n_nodes values) */
+int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi_nodes);
+int fgb_field_import_phi_nodes(FGB_FIELD* f, const double* phi_nodes);
+/* Interpolator::extract_solution: nodal E from phi, optional smoothing */
+int fgb_field_extract(FGB_FIELD* f, int smoothen);
+/* nodal solution, 5 doubles per node: Ex Ey Ez charge_density phi */
+int fgb_field_get_nodal(FGB_FIELD* f, double* sol5);
+int fgb_field_set_nodal(FGB_FIELD* f, const double* sol5);
+/* locate + interpolate n points (xyz interleaved, host), rank 1/2/3; cells (n) and out (5n) */
+int fgb_field_interpolate(FGB_FIELD* f, int n, const double* xyz, int rank, int* cells, double* out5,
+                          int64_t* stats5);
+/* same with device pointers (no copies) */
+int fgb_field_interpolate_device(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells, double* d_out5);
+/* matrix after Dirichlet elimination in CSR (sorted columns) with the rhs, by dof;
+ * dof2node maps dofs to mesh nodes */
+int fgb_field_export_system(FGB_FIELD* f, int64_t* rowptr, int* col, double* val, double* rhs, int* dof2node);
+/* average device time [ms] of one SpMV with FP64 (precision 0) or FP32 (1) values */
+double fgb_field_time_spmv(FGB_FIELD* f, int precision, int reps);
+/* device stream the field works on (cudaStream_t) */
+void* fgb_field_stream(FGB_FIELD* f);
+/* borrowed handle to the device field a FEMOCS instance solved on (valid after femocs_run,
+ * until the FEMOCS handle is deleted); free it with fgb_field_free (the field survives) */
+FGB_FIELD* femocs_field(FEMOCS* femocs);
+/* CUDA events on the field's stream (slots 0..7) for device-side timing */
+int fgb_field_mark(FGB_FIELD* f, int slot);
+double fgb_field_elapsed(FGB_FIELD* f, int slot_a, int slot_b);
+/* plain device memory for callers without a CUDA runtime binding */
+void* fgb_device_alloc(size_t bytes);
+void fgb_device_free(void* p);
+int fgb_memcpy_htod(void* dst, const void* src, size_t bytes);
+int fgb_memcpy_dtoh(void* dst, const void* src, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,100 @@
+/* CPU oracle for the femocs_gb300 field-solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY: this is the checker (and the timed CPU baseline in bench.py),
+ * never part of the product. It restates, in plain C, the reference FEMOCS algorithms for
+ * the path; every function cites the reference file:line it follows. Parity of the FEM
+ * solve (assembly, boundary conditions, SSOR-CG) is UNPINNED against the reference itself,
+ * because that part of the reference runs inside deal.II 9.2, which is not available; the
+ * cell-location, interpolation, nodal-field and smoothing parts are pinned against golden
+ * vectors produced by the reference's own compiled sources (oracle/ref_driver.cpp).
+ */
+#ifndef FEMOCS_ORACLE_H
+#define FEMOCS_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------- tet tables (src/InterpolatorCells.cpp:523-629) ---------- */
+void orc_tet_tables(int n_tets, const int32_t* tets, const double* xyz,
+                    double* det /* 17*n_tets */, double* centroid /* 3*n_tets */);
+
+/* ---------- FEM system on the vacuum hexes ----------
+ * cells: 8 vertex ids per cell (femocs hex order), vertex coordinates xyz (3*n_vert).
+ * Builds the CSR pattern (sorted columns), the Q1 stiffness (src/PoissonSolver.cpp:239-263),
+ * boundary marking (src/DealSolver.cpp:461-518), Neumann rhs on the top (src/DealSolver.cpp:390-430)
+ * and the Dirichlet elimination (deal.II MatrixTools::apply_boundary_values, called from
+ * src/DealSolver.cpp:438). The caller frees the CSR arrays with orc_free. */
+typedef struct {
+    int n;
+    int64_t nnz;
+    int64_t* rowptr;
+    int32_t* col;
+    double* val;
+    double* rhs;
+    double* x;              /* initial guess / solution, Dirichlet values preset */
+    int8_t* constrained;    /* 1 if Dirichlet */
+    int n_top_faces;
+} OrcSystem;
+
+int orc_build_system(int n_vert, const double* xyz, int n_cells, const int32_t* cells,
+                     double applied_field, int anode_dirichlet, double applied_potential,
+                     OrcSystem* sys);
+void orc_free_system(OrcSystem* sys);
+/* wrap a CSR system assembled elsewhere (arrays copied); diagonal must be present */
+int orc_system_from_csr(int n, const int64_t* rowptr, const int32_t* col, const double* val, const double* rhs,
+                        const double* x0, OrcSystem* sys);
+
+/* deal.II SolverCG + PreconditionSSOR(omega) (src/DealSolver.cpp:443-459); omega <= 0 gives
+ * the identity preconditioner. Stop when ||b-Ax||_2 <= tol. Returns #iterations or
+ * -#iterations when max_it is reached. */
+int orc_ssor_cg(const OrcSystem* sys, double* x, double omega, double tol, int max_it);
+/* Jacobi-preconditioned CG with the same stop test (plain GPU-CG counterpart). */
+int orc_jacobi_cg(const OrcSystem* sys, double* x, double tol, int max_it);
+/* timing helper: run exactly n_it SSOR-CG iterations regardless of convergence */
+double orc_ssor_cg_fixed(const OrcSystem* sys, double* x, double omega, int n_it);
+void orc_spmv(const OrcSystem* sys, const double* x, double* y);
+
+/* ---------- nodal field (src/Interpolator.cpp:125-140 + src/InterpolatorCells.cpp:1462-1505) ----
+ * phi: per node of the hex mesh; out E: 3 per node, only nodes with is_vac[node] are set.  */
+void orc_nodal_field(int n_nodes, const double* xyz, int n_hexs, const int32_t* hexs,
+                     const int32_t* hex_marker, const int8_t* is_vac, const double* phi, double* E);
+/* smoothing (src/Interpolator.cpp:142-170) with the pseudo-Voronoi stencils */
+void orc_smooth_field(int n_tetnodes, const double* xyz, const int32_t* vptr, const int32_t* vidx,
+                      double decay_factor, double* E);
+
+/* ---------- location + interpolation (src/InterpolatorCells.cpp:269-307, 631-661,
+ * 795-816, 1272-1353, 1536-1562; src/SolutionReader.cpp:136-165) ----------
+ * rank 1/2 return tet indices, rank 3 hex indices, negative = outside. The chain starts
+ * from a fresh reader (cell = -1). sol: 5 doubles per node (E, scalar1, phi).
+ * out: 5 doubles per point. */
+typedef struct {
+    int n_tets;
+    const int32_t* tets;
+    const int8_t* search;       /* 1 for tets in the searched region (vacuum) */
+    const double* det;          /* 17 per tet */
+    const double* centroid;     /* 3 per tet */
+    const int32_t* nbr_ptr;     /* candidate lists after a failed guess */
+    const int32_t* nbr_idx;
+    const int32_t* hexs;        /* 8 per hex */
+    const double* hexf;         /* 24 per hex */
+    const int32_t* quad_nodes;  /* 10 per tet */
+    const double* sol;          /* 5 per node */
+} OrcInterp;
+
+void orc_locate_interpolate(const OrcInterp* m, int rank, int n_pts, const double* pts,
+                            int32_t* cells, double* out);
+
+/* neighbour lists exactly as the reference stores them (face neighbours, then
+ * vertex-sharing tets with repeats), src/InterpolatorCells.cpp:537-558 */
+int orc_tet_neighbour_lists(int n_nodes, int n_tets, const int32_t* tets, const int32_t* face_nbr,
+                            int32_t* ptr /* n_tets+1 */, int32_t* idx /* capacity */, int capacity);
+
+void orc_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,112 @@
+"""CUDA assembly and solvers against the oracle's restatement of the reference FEM.
+
+Tolerances: matrix entries and rhs within 1e-12 relative (FP64 summation order differs);
+solutions compared after both solvers reach the stated relative residual."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import femocs_gb300 as fg
+import oracle as orc
+from util import vacuum_system_inputs
+
+pytestmark = pytest.mark.gpu
+TIP = dict(radius=8.0, height=25.0, box_half=30.0, slab=6.0, top=80.0, h=4.0, growth=1.4, margin=4.0)
+FLAT = dict(radius=0.0, height=0.0, box_half=30.0, slab=6.0, top=60.0, h=6.0, growth=1.3, margin=0.0)
+
+
+@pytest.fixture(scope="module")
+def tip():
+    m = fg.Mesh.synthetic(**TIP)
+    return m, fg.Field(m)
+
+
+def gpu_matrix_in_vertex_order(m, f):
+    rowptr, col, val, rhs, d2n = f.system()
+    n2v = m.export("vac_node2vertex")
+    d2v = n2v[d2n]
+    A = sp.csr_matrix((val, col, rowptr), shape=(f.n_dofs, f.n_dofs)).tocoo()
+    P = sp.csr_matrix((val, (d2v[A.row], d2v[A.col])), shape=A.shape)
+    b = np.zeros(f.n_dofs)
+    b[d2v] = rhs
+    return P, b, d2v
+
+
+@pytest.mark.parametrize("anode", [False, True])
+def test_assembled_system_matches_oracle(tip, anode):
+    m, f = tip
+    f.setup(0.1, 3.0)
+    f.assemble(True, anode)
+    A, b, _ = gpu_matrix_in_vertex_order(m, f)
+    xyz, cells, _ = vacuum_system_inputs(m)
+    s = orc.System(xyz, cells, 0.1, anode, 3.0)
+    R = sp.csr_matrix((s.val, s.col, s.rowptr), shape=(s.n, s.n))
+    assert abs(A - R).max() <= 1e-12 * abs(R).max()
+    np.testing.assert_allclose(b, s.rhs, rtol=0, atol=1e-12 * np.abs(s.rhs).max())
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("tol", [1e-9, 1e-12])
+def test_solve_matches_oracle(tip, precision, tol):
+    m, f = tip
+    f.setup(0.1)
+    f.assemble(True, False)
+    rc, st = f.solve(precision=precision, rel_tol=tol, max_iter=20000)
+    assert rc > 0 and st["status"] == 1
+    assert st["rel_residual"] <= tol * 1.05
+    xyz, cells, v2n = vacuum_system_inputs(m)
+    s = orc.System(xyz, cells, 0.1)
+    it, x = s.ssor_cg(1.2, 1e-13 * np.linalg.norm(s.rhs), 50000)
+    phi = f.phi_nodes()[v2n]
+    # error bound of a solve at relative residual tol on this (moderately conditioned) system
+    assert np.abs(phi - x).max() <= 2e3 * tol * np.abs(x).max()
+
+
+def test_mixed_beats_plain_iteration_economy(tip):
+    m, f = tip
+    f.setup(0.1)
+    f.assemble(True, False)
+    rc0, s0 = f.solve(precision=0, rel_tol=1e-9)
+    f.setup(0.1)
+    f.assemble(False, False)
+    rc1, s1 = f.solve(precision=1, rel_tol=1e-9)
+    assert s0["status"] == 1 and s1["status"] == 1
+    assert s1["outer"] >= 1
+    # refinement restarts cost iterations but not more than twice the FP64 count
+    assert s1["iterations"] <= 2 * s0["iterations"] + 50
+
+
+def test_warm_start_and_reassembly(tip):
+    m, f = tip
+    f.setup(0.1)
+    f.assemble(True, False)
+    rc, st = f.solve(precision=1, rel_tol=1e-10)
+    # PoissonSolver::assemble(false) keeps the matrix; the converged phi is a warm start
+    f.assemble(False, False)
+    rc2, st2 = f.solve(precision=1, rel_tol=1e-10)
+    assert st2["iterations"] == 0 and st2["status"] == 1
+
+
+def test_flat_known_answer():
+    m = fg.Mesh.synthetic(**FLAT)
+    f = fg.Field(m)
+    f.setup(0.1)
+    f.assemble(True, False)
+    rc, st = f.solve(precision=1, rel_tol=1e-12)
+    assert rc > 0
+    xyz = m.export("node_xyz").reshape(-1, 3)
+    n2v = m.export("vac_node2vertex")
+    phi = f.phi_nodes()
+    vac = n2v >= 0
+    assert np.abs(phi[vac] - 0.1 * xyz[vac, 2]).max() < 1e-8
+    f.extract(smoothen=True)
+    E = f.nodal()[vac, :3]
+    assert np.abs(E[:, 2] + 0.1).max() < 1e-7 and np.abs(E[:, :2]).max() < 1e-7
+
+
+def test_nonconvergence_reports_failure(tip):
+    m, f = tip
+    f.setup(0.1)
+    f.assemble(True, False)
+    rc, st = f.solve(precision=0, rel_tol=1e-14, max_iter=5)
+    assert rc < 0 and st["status"] != 1
