@@ -36,18 +36,20 @@ sys.path.insert(0, ROOT)
 E0 = -0.1          # V/A, i.e. 1 GV/m; the Neumann value on the top is -E0
 REL_TOL = 1e-9
 RANK = 1           # interpolation_rank default of the reference (src/Config.cpp:29)
-N_POINTS = {"config2": 1_000_000, "config1": 100_000}
+N_POINTS = {"config2": 1_000_000, "config1": 100_000, "probe": 200_000}
 # SSOR(1.2)-PCG iterations to a 1e-9 relative residual on these exact systems, measured by
 # running the oracle's restatement of the reference solve (oracle/femocs_oracle.c) to
 # convergence; the CPU baseline times iterations live and multiplies by this count.
-SSOR_ITERS = {"config1": 268, "config2": 540}
-# DRAM bytes per launch of the FP32 CG SpMV kernel from an ncu capture (profiles/), or None
-SPMV_TRAFFIC = {"config2": None, "config1": None}
+SSOR_ITERS = {"config1": 268, "config2": 617, "probe": 0}
+# DRAM bytes per iteration of the persistent CG kernel from an ncu capture (profiles/), or None
+KERNEL_TRAFFIC = {"config2": None, "config1": None, "probe": None}
 FALLBACK_HBM_GBS = 6800.0
 
 
 def spec_of(workload):
     import femocs_gb300 as fg
+    if workload == "probe":  # config-2 geometry on a coarser grid, small enough for full ncu captures
+        return dict(fg.CONFIG2, h=13.0, growth=1.22)
     return dict(fg.CONFIG2 if workload == "config2" else fg.CONFIG1)
 
 
@@ -260,12 +262,21 @@ def run_ours(args, world, rank):
             raise RuntimeError(fg.last_error())
     e2e_s = reduce_max(world, statistics.median(e2e_t))
 
-    # roofline of the dominant kernel: FP32 SpMV+dot of the inner CG
-    spmv_ms = field.time_spmv(1, 50)
+    # roofline of the dominant kernel: the persistent mixed-precision CG kernel. Algorithmic
+    # bytes: per FP32 iteration the SELL matrix (4 B value + 4 B column per nonzero) and 12
+    # FP32 row streams (phase A: z, p_old read, p, q written; phase B: d, p, r, q, D^-1 read,
+    # d, r, z written); per FP64 refinement the FP64 matrix (8+4 B per nonzero) and 52 B/row
+    # (x, d update; b, x, D^-1 read; r, z written).
     nnz = field.nnz
-    alg_bytes = nnz * (4 + 4) + (n + 1) * 4 + 2 * n * 4
+    last = solve_stats[-1]
+    it_bytes = nnz * 8 + 48 * n
+    up_bytes = nnz * 12 + 52 * n
+    alg_bytes = last["iterations"] * it_bytes + last["outer"] * up_bytes
+    kms = statistics.median([s["kernel_ms"] for s in solve_stats])
     peak, peak_kind = measured_hbm_peak()
-    achieved = alg_bytes / (spmv_ms * 1e-3) / 1e9
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
+    traffic_it = KERNEL_TRAFFIC.get(args.workload)
+    spmv32_ms = field.time_spmv(1, 50)
     spmv64_ms = field.time_spmv(0, 20)
 
     line = {
@@ -299,13 +310,15 @@ def run_ours(args, world, rank):
                 "d2h_bytes_per_step": 36 * n_points,
                 "note": "femocs_run + femocs_interpolate_elfield through the C ABI, host arrays"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": SPMV_TRAFFIC.get(args.workload), "kernel": "k_cg_spmv_pq<float>",
-                     "algorithmic_bytes": alg_bytes, "launch_ms": spmv_ms, "peak_kind": peak_kind,
-                     "fp64_launch_ms": spmv64_ms},
+                     "traffic": (traffic_it * last["iterations"]) if traffic_it else None,
+                     "kernel": "k_mixed_cg (persistent, cooperative)", "algorithmic_bytes": alg_bytes,
+                     "launch_ms": kms, "bytes_per_iteration": it_bytes, "bytes_per_refinement": up_bytes,
+                     "peak_kind": peak_kind, "spmv_fp32_launch_ms": spmv32_ms, "spmv_fp64_launch_ms": spmv64_ms,
+                     "spmv_fp32_gbs": (nnz * 8 + 12 * n) / (spmv32_ms * 1e-3) / 1e9},
         "clocks": clocks,
         "gpu_launches": launches,
     }
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and SSOR_ITERS.get(args.workload):
         line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -377,7 +390,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config2", "config1"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "config1", "probe"])
     ap.add_argument("--points", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()

@@ -133,13 +133,14 @@ class Field:
     def assemble(self, full_run=True, anode_dirichlet=False):
         self._ok(load().fgb_field_assemble(self.h, int(full_run), int(anode_dirichlet)))
 
-    def solve(self, precision=1, rel_tol=1e-9, abs_tol=0.0, max_iter=10000, inner_tol=1e-4):
-        st = np.zeros(6)
+    def solve(self, precision=1, rel_tol=1e-9, abs_tol=0.0, max_iter=10000, inner_tol=0.1):
+        st = np.zeros(7)
+        st[6] = -1.0  # ask for the kernel-only time as well
         rc = load().fgb_field_solve(self.h, precision, rel_tol, abs_tol, max_iter, inner_tol, ptr(st))
         if rc == -(2 ** 31):
             raise RuntimeError(last_error())
         return rc, dict(iterations=int(st[0]), outer=int(st[1]), status=int(st[2]), rel_residual=st[3],
-                        bnorm=st[4], ms=st[5])
+                        bnorm=st[4], ms=st[5], kernel_ms=st[6] if st[6] != -1.0 else 0.0)
 
     def extract(self, smoothen=True):
         self._ok(load().fgb_field_extract(self.h, int(smoothen)))

@@ -320,6 +320,7 @@ int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol,
             stats6[3] = f->last.rel_residual;
             stats6[4] = f->last.bnorm;
             stats6[5] = f->last.ms;
+            if (stats6[6] == -1.0) stats6[6] = f->last.kernel_ms;  // optional 7th slot on request
         }
         return 0;
     });

@@ -1,0 +1,243 @@
+// Mixed-precision Jacobi-PCG as one persistent cooperative kernel (sm_103a).
+//
+// The whole solve is a single launch: every CTA stays resident, phases are separated by
+// grid-wide barriers, and the scalars of the recurrence are reduced redundantly (and
+// identically) by every CTA from per-CTA partial sums, so no host round trip and no kernel
+// launch happens per iteration.
+//
+// Precision scheme (FP32 inner iterations inside FP64 refinement): the CG recurrence runs
+// in FP32 on the FP32 copy of the matrix and accumulates the correction d in FP32; every
+// time the recursive residual has dropped by `ru_factor` since the last refinement (and when
+// it claims convergence), the correction is folded into the FP64 solution x and the
+// residual is replaced by the true FP64 residual b - A x computed with the FP64 matrix
+// ("reliable updates"). The search direction is kept across refinements, so the Krylov
+// convergence of the FP64 iteration is preserved. Convergence is declared on the FP64 true
+// residual only.
+//
+// One iteration = 2 grid barriers:
+//   phase A: p = z + beta p_old (row owner, double-buffered), q = A p (gathering z and
+//            p_old of the neighbours), partial p.q
+//   phase B: d += alpha p, r -= alpha q, z = D^-1 r, partials r.z and r.r
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "fem_device.h"
+
+namespace cg = cooperative_groups;
+
+namespace fgb {
+
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename T>
+__device__ __forceinline__ T sell_dot(int i, const MixedArgs& a, const T* __restrict__ vals, const T* __restrict__ x) {
+    const int s = i >> 5;
+    const int64_t base = a.sptr[s] + (i & 31);
+    const int len = a.slen[s];
+    T acc0 = 0, acc1 = 0;
+    int j = 0;
+    for (; j + 1 < len; j += 2) {
+        const int64_t o0 = base + (int64_t)j * 32, o1 = o0 + 32;
+        acc0 += __ldg(vals + o0) * x[__ldg(a.scol + o0)];
+        acc1 += __ldg(vals + o1) * x[__ldg(a.scol + o1)];
+    }
+    if (j < len) {
+        const int64_t o0 = base + (int64_t)j * 32;
+        acc0 += __ldg(vals + o0) * x[__ldg(a.scol + o0)];
+    }
+    return acc0 + acc1;
+}
+
+// q_i = sum_j a_ij (z_j + beta * pold_j): the new direction is formed on the fly
+__device__ __forceinline__ float sell_dir_dot(int i, const MixedArgs& a, const float* __restrict__ z,
+                                              const float* __restrict__ pold, float beta) {
+    const int s = i >> 5;
+    const int64_t base = a.sptr[s] + (i & 31);
+    const int len = a.slen[s];
+    float acc0 = 0.f, acc1 = 0.f;
+    int j = 0;
+    for (; j + 1 < len; j += 2) {
+        const int64_t o0 = base + (int64_t)j * 32, o1 = o0 + 32;
+        const int c0 = __ldg(a.scol + o0), c1 = __ldg(a.scol + o1);
+        acc0 += __ldg(a.s32 + o0) * (z[c0] + beta * pold[c0]);
+        acc1 += __ldg(a.s32 + o1) * (z[c1] + beta * pold[c1]);
+    }
+    if (j < len) {
+        const int64_t o0 = base + (int64_t)j * 32;
+        const int c0 = __ldg(a.scol + o0);
+        acc0 += __ldg(a.s32 + o0) * (z[c0] + beta * pold[c0]);
+    }
+    return acc0 + acc1;
+}
+
+// Grid-wide sum of NV values: per-CTA partials into buffer `buf`, barrier, then every CTA
+// sums all partials in the same order (identical result in every CTA, deterministic).
+template <int NV>
+__device__ __forceinline__ void grid_sum(cg::grid_group& grid, double (&v)[NV], double* partial, int buf) {
+    __shared__ double sh[NV][kThreads / 32];
+    __shared__ double tot[NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double t = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[k][wid] = t;
+    }
+    __syncthreads();
+    double* P = partial + (size_t)buf * 2 * gridDim.x;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = 0.0;
+            for (int w = 0; w < kThreads / 32; ++w) t += sh[k][w];
+            P[(size_t)NV * blockIdx.x + k] = t;
+        }
+    }
+    grid.sync();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = 0.0;
+            for (int b = lane; b < (int)gridDim.x; b += 32) t += __ldcg(P + (size_t)NV * b + k);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            if (lane == 0) tot[k] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = tot[k];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads) k_mixed_cg(MixedArgs a) {
+    cg::grid_group grid = cg::this_grid();
+    const int G = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int buf = 0;
+
+    // ---- true residual of the initial guess, z = D^-1 r, d = 0, p_old = 0
+    double v2[2] = {0.0, 0.0};
+    for (int i = t0; i < a.n; i += G) {
+        const double ri = a.b[i] - sell_dot<double>(i, a, a.s64, a.x);
+        const float r32 = (float)ri;
+        const float z32 = a.dinv32[i] * r32;
+        a.r[i] = r32;
+        a.z[i] = z32;
+        a.d[i] = 0.f;
+        a.pa[i] = 0.f;
+        v2[0] += (double)r32 * (double)z32;
+        v2[1] += ri * ri;
+    }
+    grid_sum<2>(grid, v2, a.partial, buf);
+    buf ^= 1;
+    double gamma = v2[0], rr = v2[1];
+    double rr_ref = rr;  // residual at the last refinement
+    int it = 0, updates = 0, status = 0;
+    float beta = 0.f;
+    float* pold = a.pa;
+    float* pnew = a.pb;
+    if (rr <= a.tol2) status = 1;
+
+    while (status == 0) {
+        // ---- phase A
+        double v1[1] = {0.0};
+        for (int i = t0; i < a.n; i += G) {
+            const float qi = sell_dir_dot(i, a, a.z, pold, beta);
+            const float pi = a.z[i] + beta * pold[i];
+            pnew[i] = pi;
+            a.q[i] = qi;
+            v1[0] += (double)pi * (double)qi;
+        }
+        grid_sum<1>(grid, v1, a.partial, buf);
+        buf ^= 1;
+        const float alpha = (float)(gamma / v1[0]);
+        // ---- phase B
+        double w2[2] = {0.0, 0.0};
+        for (int i = t0; i < a.n; i += G) {
+            a.d[i] += alpha * pnew[i];
+            const float ri = a.r[i] - alpha * a.q[i];
+            const float zi = a.dinv32[i] * ri;
+            a.r[i] = ri;
+            a.z[i] = zi;
+            w2[0] += (double)ri * (double)zi;
+            w2[1] += (double)ri * (double)ri;
+        }
+        grid_sum<2>(grid, w2, a.partial, buf);
+        buf ^= 1;
+        ++it;
+        float* tmp = pold;
+        pold = pnew;
+        pnew = tmp;
+        double gamma_new = w2[0];
+        rr = w2[1];
+        if (!(rr == rr) || !(gamma_new == gamma_new)) { status = -2; break; }
+        if (rr <= a.tol2 || rr <= a.ru2 * rr_ref || it >= a.max_iter) {
+            // ---- refinement: fold d into x (FP64), true residual with the FP64 matrix
+            for (int i = t0; i < a.n; i += G) {
+                a.x[i] += (double)a.d[i];
+                a.d[i] = 0.f;
+            }
+            grid.sync();
+            double u2[2] = {0.0, 0.0};
+            for (int i = t0; i < a.n; i += G) {
+                const double ri = a.b[i] - sell_dot<double>(i, a, a.s64, a.x);
+                const float r32 = (float)ri;
+                const float z32 = a.dinv32[i] * r32;
+                a.r[i] = r32;
+                a.z[i] = z32;
+                u2[0] += (double)r32 * (double)z32;
+                u2[1] += ri * ri;
+            }
+            grid_sum<2>(grid, u2, a.partial, buf);
+            buf ^= 1;
+            ++updates;
+            gamma_new = u2[0];
+            rr = u2[1];
+            rr_ref = rr;
+            if (rr <= a.tol2) { status = 1; break; }
+            if (it >= a.max_iter) { status = -1; break; }
+            if (!(rr == rr)) { status = -2; break; }
+        }
+        beta = (float)(gamma_new / gamma);
+        gamma = gamma_new;
+    }
+    if (t0 == 0) {
+        a.out->iterations = it;
+        a.out->updates = updates;
+        a.out->status = status;
+        a.out->rr = rr;
+    }
+}
+
+}  // namespace
+
+int mixed_cg_grid(int n) {
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0, sms = 0, per_sm = 0, coop = 0;
+        FGB_CUDA(cudaGetDevice(&dev));
+        FGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FGB_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        FGB_REQUIRE(coop, "device does not support cooperative launches");
+        FGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_cg, kThreads, 0));
+        FGB_REQUIRE(per_sm > 0, "persistent CG kernel cannot be resident");
+        cached = sms * std::min(per_sm, 4);
+    }
+    return std::max(1, std::min(cached, (n + kThreads - 1) / kThreads));
+}
+
+void launch_mixed_cg(const MixedArgs& args, cudaStream_t stream) {
+    const int grid = mixed_cg_grid(args.n);
+    MixedArgs a = args;
+    void* params[] = {&a};
+    FGB_LAUNCH(FGB_CUDA(cudaLaunchCooperativeKernel((void*)k_mixed_cg, dim3(grid), dim3(kThreads), params, 0, stream)));
+}
+
+}  // namespace fgb

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(128) k_cell_stiffness(int nc, const int32_t* _
         const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
         const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
         const double id = 1.0 / det;
-        // inverse(J)[b][a]; grad_x N = inv^T grad_xi N
+        // inv = J^-1 (inv[i][j] = (J^-1)_ij); grad_x N = J^-T grad_xi N
         double inv[3][3];
         inv[0][0] = c00 * id;
         inv[1][0] = c01 * id;
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(128) k_cell_stiffness(int nc, const int32_t* _
         for (int k = 0; k < 8; ++k)
 #pragma unroll
             for (int a = 0; a < 3; ++a)
-                G[k][a] = inv[a][0] * dN[k][0] + inv[a][1] * dN[k][1] + inv[a][2] * dN[k][2];
+                G[k][a] = inv[0][a] * dN[k][0] + inv[1][a] * dN[k][1] + inv[2][a] * dN[k][2];
         const double w = fabs(det);
         int t = 0;
 #pragma unroll
@@ -450,13 +450,17 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
     x_.resize(n_);
     x_.zero(s);
     r64_.resize(n_); p64_.resize(n_); q64_.resize(n_); z64_.resize(n_);
-    r32_.resize(n_); p32_.resize(n_); q32_.resize(n_); z32_.resize(n_); d32_.resize(n_);
-    partial_.resize(2 * (size_t)grid_for(n_, kBlock) + 64);
+    r32_.resize(n_); p32_.resize(n_); p32b_.resize(n_); q32_.resize(n_); z32_.resize(n_); d32_.resize(n_);
+    partial_.resize(std::max<size_t>(2 * (size_t)grid_for(n_, kBlock), 4 * (size_t)mixed_cg_grid(n_)) + 64);
+    mixed_.resize(1);
+    FGB_CUDA(cudaMallocHost(&h_mixed_, sizeof(MixedResult)));
     state_.resize(2);
     state_.zero(s);
     FGB_CUDA(cudaMallocHost(&h_state_, 2 * sizeof(CgState)));
     FGB_CUDA(cudaEventCreate(&ev0_));
     FGB_CUDA(cudaEventCreate(&ev1_));
+    FGB_CUDA(cudaEventCreate(&kev0_));
+    FGB_CUDA(cudaEventCreate(&kev1_));
     FGB_CUDA(cudaStreamSynchronize(s));
     // the host copies of the structure that only the device needs are dropped
     fs_.r2c_item.clear(); fs_.r2c_item.shrink_to_fit();
@@ -466,8 +470,11 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
 
 FemDevice::~FemDevice() {
     if (h_state_) cudaFreeHost(h_state_);
+    if (h_mixed_) cudaFreeHost(h_mixed_);
     cudaEventDestroy(ev0_);
     cudaEventDestroy(ev1_);
+    cudaEventDestroy(kev0_);
+    cudaEventDestroy(kev1_);
 }
 
 void FemDevice::setup(double applied_field, double applied_potential) {
@@ -633,41 +640,46 @@ int FemDevice::solve_plain(const SolveOptions& opt, SolveStats* st) {
 
 int FemDevice::solve_mixed(const SolveOptions& opt, SolveStats* st) {
     const int gb = grid_for(n_, kBlock);
-    CgState* ds = state_.get();       // outer scalars
-    CgState* di = state_.get() + 1;   // inner CG scalars
+    CgState* ds = state_.get();
     FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
     FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
     FGB_CUDA(cudaStreamSynchronize(stream_));
     const double bnorm = std::sqrt(h_state_->rr);
     st->bnorm = bnorm;
-    const double tol2 = tol2_of(opt, bnorm);
-    int total = 0;
-    st->status = -1;
-    for (int outer = 0; outer <= opt.max_outer; ++outer) {
-        FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(),
-                                                 x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
-        FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
-        FGB_CUDA(cudaStreamSynchronize(stream_));
-        const double rr = h_state_->rr;
-        st->rel_residual = bnorm > 0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
-        st->outer = outer;
-        if (rr <= tol2 || bnorm == 0) { st->status = 1; break; }
-        if (!(rr == rr)) { st->status = -2; break; }
-        if (total >= opt.max_iter || outer == opt.max_outer) break;
-        FGB_LAUNCH(k_scale_to32<<<gb, kBlock, 0, stream_>>>(n_, r64_.get(), ds, r32_.get(), d32_.get()));
-        CgState init{};
-        init.tol2 = opt.inner_tol * opt.inner_tol;
-        init.max_iter = std::max(1, opt.max_iter - total);
-        FGB_CUDA(cudaMemcpyAsync(di, &init, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
-        FGB_LAUNCH(k_cg_init<float><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
-                                                     nullptr, r32_.get(), dinv32_.get(), r32_.get(), z32_.get(), p32_.get(),
-                                                     partial_.get(), di));
-        run_cg(true, di, init.max_iter, std::max(1, opt.chunk));
-        total += h_state_[1].iter;
-        FGB_LAUNCH(k_refine<<<gb, kBlock, 0, stream_>>>(n_, x_.get(), d32_.get(), ds));
-    }
-    st->iterations = total;
-    return st->status == 1 ? total : -total;
+    MixedArgs a;
+    a.n = n_;
+    a.sptr = slice_ptr_.get();
+    a.slen = slice_len_.get();
+    a.scol = sell_col_.get();
+    a.s32 = sell32_.get();
+    a.s64 = sell64_.get();
+    a.dinv32 = dinv32_.get();
+    a.b = rhs_.get();
+    a.x = x_.get();
+    a.d = d32_.get();
+    a.r = r32_.get();
+    a.z = z32_.get();
+    a.pa = p32_.get();
+    a.pb = p32b_.get();
+    a.q = q32_.get();
+    a.partial = partial_.get();
+    a.out = mixed_.get();
+    a.tol2 = tol2_of(opt, bnorm);
+    a.ru2 = opt.inner_tol * opt.inner_tol;
+    a.max_iter = opt.max_iter;
+    FGB_CUDA(cudaEventRecord(kev0_, stream_));
+    launch_mixed_cg(a, stream_);
+    FGB_CUDA(cudaEventRecord(kev1_, stream_));
+    FGB_CUDA(cudaMemcpyAsync(h_mixed_, mixed_.get(), sizeof(MixedResult), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    float kms = 0;
+    FGB_CUDA(cudaEventElapsedTime(&kms, kev0_, kev1_));
+    st->kernel_ms = kms;
+    st->iterations = h_mixed_->iterations;
+    st->outer = h_mixed_->updates;
+    st->status = bnorm == 0 ? 1 : h_mixed_->status;
+    st->rel_residual = bnorm > 0 ? std::sqrt(h_mixed_->rr) / bnorm : std::sqrt(h_mixed_->rr);
+    return st->status == 1 ? st->iterations : -st->iterations;
 }
 
 }  // namespace fgb

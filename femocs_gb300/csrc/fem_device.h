@@ -17,12 +17,44 @@ struct CgState {
     int pad;
 };
 
+// Result block written by the persistent mixed-precision CG kernel.
+struct MixedResult {
+    int iterations, updates, status, pad;
+    double rr;
+};
+
+// Arguments of the persistent mixed-precision CG kernel (cg_persistent.cu).
+struct MixedArgs {
+    int n;
+    const int64_t* sptr;
+    const int32_t* slen;
+    const int32_t* scol;
+    const float* s32;
+    const double* s64;
+    const float* dinv32;
+    const double* b;
+    double* x;
+    float* d;
+    float* r;
+    float* z;
+    float* pa;
+    float* pb;
+    float* q;
+    double* partial;  // 2 buffers x 2 values x grid CTAs
+    MixedResult* out;
+    double tol2;
+    double ru2;       // squared reliable-update factor
+    int max_iter;
+};
+void launch_mixed_cg(const MixedArgs& args, cudaStream_t stream);
+int mixed_cg_grid(int n);
+
 struct SolveOptions {
     int precision = 1;        // 0: plain FP64 Jacobi-PCG; 1: FP32 inner PCG + FP64 refinement
     double rel_tol = 1e-9;    // on ||b - A x||_2 / ||b||_2 (FP64 true residual)
     double abs_tol = 0.0;     // optional absolute floor (reference field_cgtol semantics)
     int max_iter = 10000;     // total CG iterations (inner + plain)
-    double inner_tol = 1e-4;  // relative reduction per refinement sweep
+    double inner_tol = 0.1;   // residual reduction between FP64 refinements (reliable updates)
     int max_outer = 50;
     int chunk = 16;           // iterations per graph launch
 };
@@ -34,6 +66,7 @@ struct SolveStats {
     double rel_residual = 0;  // final ||b-Ax||/||b|| in FP64
     double bnorm = 0;
     double ms = 0;            // device time of the solve (CUDA events)
+    double kernel_ms = 0;     // device time of the persistent CG kernel alone (mixed path)
 };
 
 class FemDevice {
@@ -90,12 +123,14 @@ private:
     bool has_extra_ = false;
     // work vectors
     DBuf<double> r64_, p64_, q64_, z64_;
-    DBuf<float> r32_, p32_, q32_, z32_, d32_;
+    DBuf<float> r32_, p32_, p32b_, q32_, z32_, d32_;
     DBuf<double> partial_;
     DBuf<CgState> state_;
+    DBuf<MixedResult> mixed_;
+    MixedResult* h_mixed_ = nullptr;
     CgState* h_state_ = nullptr;  // pinned mirror
     double spmv64_ms_ = 0, spmv32_ms_ = 0;
-    cudaEvent_t ev0_, ev1_;
+    cudaEvent_t ev0_, ev1_, kev0_, kev1_;
 };
 
 }  // namespace fgb

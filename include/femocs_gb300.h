@@ -114,7 +114,9 @@ int fgb_field_setup(FGB_FIELD* f, double applied_field, double applied_potential
 /* PoissonSolver::assemble(full_run); anode_dirichlet selects anode_bc = dirichlet */
 int fgb_field_assemble(FGB_FIELD* f, int full_run, int anode_dirichlet);
 /* CG solve; precision 0 = plain FP64 Jacobi-PCG, 1 = FP32 inner + FP64 refinement.
- * stats (may be NULL): iterations, outer, status, rel_residual, bnorm, ms.
+ * inner_tol: residual reduction between FP64 refinements (<= 0: default 0.1).
+ * stats (may be NULL): iterations, refinements, status, rel_residual, bnorm, ms; a 7th slot
+ * preset to -1 receives the device time of the solver kernel alone.
  * Returns #iterations (>0) or -#iterations when not converged. */
 int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol, int max_iter, double inner_tol,
                     double* stats6);
