@@ -41,8 +41,11 @@ N_POINTS = {"config2": 1_000_000, "config1": 100_000, "probe": 200_000}
 # running the oracle's restatement of the reference solve (oracle/femocs_oracle.c) to
 # convergence; the CPU baseline times iterations live and multiplies by this count.
 SSOR_ITERS = {"config1": 268, "config2": 617, "probe": 0}
-# DRAM bytes per iteration of the persistent CG kernel from an ncu capture (profiles/), or None
-KERNEL_TRAFFIC = {"config2": None, "config1": None, "probe": None}
+# DRAM bytes (read + write) per row per iteration of the persistent CG kernel, from the ncu
+# capture of the probe workload (profiles/k_mixed_cg_probe_1.08M_dofs.md: 496.5 GB over
+# 1665 iterations x 1,081,693 rows, refinements included); traffic of a launch scales with
+# rows x iterations.
+KERNEL_TRAFFIC_PER_ROW_ITER = 275.7
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -275,7 +278,7 @@ def run_ours(args, world, rank):
     kms = statistics.median([s["kernel_ms"] for s in solve_stats])
     peak, peak_kind = measured_hbm_peak()
     achieved = alg_bytes / (kms * 1e-3) / 1e9
-    traffic_it = KERNEL_TRAFFIC.get(args.workload)
+    traffic = KERNEL_TRAFFIC_PER_ROW_ITER * n * last["iterations"]
     spmv32_ms = field.time_spmv(1, 50)
     spmv64_ms = field.time_spmv(0, 20)
 
@@ -310,7 +313,8 @@ def run_ours(args, world, rank):
                 "d2h_bytes_per_step": 36 * n_points,
                 "note": "femocs_run + femocs_interpolate_elfield through the C ABI, host arrays"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": (traffic_it * last["iterations"]) if traffic_it else None,
+                     "traffic": traffic,
+                     "traffic_note": "ncu dram bytes of the probe capture scaled by rows x iterations",
                      "kernel": "k_mixed_cg (persistent, cooperative)", "algorithmic_bytes": alg_bytes,
                      "launch_ms": kms, "bytes_per_iteration": it_bytes, "bytes_per_refinement": up_bytes,
                      "peak_kind": peak_kind, "spmv_fp32_launch_ms": spmv32_ms, "spmv_fp64_launch_ms": spmv64_ms,
