@@ -68,6 +68,7 @@ _PROTOS = {
     "fgb_field_set_nodal": (C.c_int, [vp, dp]),
     "fgb_field_interpolate": (C.c_int, [vp, C.c_int, dp, C.c_int, ip, dp, i64p]),
     "fgb_field_interpolate_device": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp]),
+    "fgb_field_interpolate_device_noalloc": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp]),
     "fgb_field_export_system": (C.c_int, [vp, i64p, ip, dp, dp, ip]),
     "fgb_field_time_spmv": (C.c_double, [vp, C.c_int, C.c_int]),
     "fgb_field_stream": (vp, [vp]),

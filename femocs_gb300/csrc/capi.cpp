@@ -386,6 +386,13 @@ int fgb_field_interpolate_device(FGB_FIELD* f, int n, const double* d_xyz, int r
         return 0;
     });
 }
+int fgb_field_interpolate_device_noalloc(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells,
+                                        double* d_out5) {
+    return guarded([&] {
+        f->f->interp().locate_interpolate_noalloc(n, d_xyz, rank, d_cells, d_out5);
+        return 0;
+    });
+}
 int fgb_field_export_system(FGB_FIELD* f, int64_t* rowptr, int* col, double* val, double* rhs, int* dof2node) {
     return guarded([&] {
         FemDevice& fem = f->f->fem();

@@ -45,6 +45,11 @@ public:
     // 2 quad-tet, 3 lin-hex; cells and out (5 per point) on the device.
     void locate_interpolate(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out,
                             LocateStats* stats = nullptr);
+    // Same result as locate_interpolate, for callers that cannot allocate device memory: no
+    // cudaMalloc/cudaFree, the per-point scratch is a file-scope device array (at most
+    // 262144 points per call, shared by all calls; overlapping calls race). Asynchronous on
+    // stream(). The first call on a device looks up the array's device address.
+    void locate_interpolate_noalloc(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out);
     // Interpolate with cells already known (SolutionReader::calc_interpolation with mapped atoms)
     void interpolate_known(int n, const double* d_pts, int rank, const int32_t* d_cells, double* d_out);
 

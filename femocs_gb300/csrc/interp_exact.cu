@@ -24,6 +24,8 @@
 #include <algorithm>
 #include <deque>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "interp.h"
 
@@ -468,6 +470,38 @@ __global__ void k_max_norm2(int n, const double* __restrict__ sol, unsigned long
 
 }  // namespace
 
+// ==================================================================== allocation-free variant
+// Scratch of DeviceMesh::locate_interpolate_noalloc: five int32 per query point (walk result,
+// containing-tet count, nearest-centroid tet, resolved cell, dependency flag) plus eight
+// counters, for at most kNoAllocMaxPoints points. It is a file-scope device array: every
+// GPU that loads this library holds these ~5.2 MB until the process exits, and every call
+// shares it, so calls that overlap on the GPU (two streams, or two host threads) race.
+constexpr int kNoAllocMaxPoints = 262144;
+static __device__ __align__(256) int32_t g_noalloc_scratch[5 * kNoAllocMaxPoints + 8];
+
+namespace {
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[256] = {};  // device address of g_noalloc_scratch, per device ordinal
+}  // namespace
+
+// Device address of the scratch array on the current device. The host-side symbol
+// g_noalloc_scratch is only a stand-in and must never be passed to a kernel; the address is
+// looked up once per device (with that device current) by the first call on that device.
+static int32_t* noalloc_scratch() {
+    int dev = 0;
+    FGB_CUDA(cudaGetDevice(&dev));
+    FGB_REQUIRE(dev >= 0 && dev < 256, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        FGB_REQUIRE(e == cudaSuccess && p, std::string("cudaGetSymbolAddress of the location scratch failed: ") +
+                                               cudaGetErrorString(e));
+        g_noalloc_addr[dev] = p;
+    }
+    return static_cast<int32_t*>(g_noalloc_addr[dev]);
+}
+
 // ==================================================================== host side
 SeedGrid build_seed_grid(const PreparedMesh& pm) {
     SeedGrid g;
@@ -642,6 +676,42 @@ void DeviceMesh::locate_interpolate(int n, const double* d_pts, int rank, int32_
         stats->n_dependent = h[2];
         stats->longest_run = h[3];
     }
+}
+
+void DeviceMesh::locate_interpolate_noalloc(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out) {
+    if (n <= 0) return;
+    FGB_REQUIRE(rank >= 1 && rank <= 3, "interpolation rank must be 1, 2 or 3");
+    FGB_REQUIRE(n <= kNoAllocMaxPoints, "the allocation-free interpolation takes at most " +
+                                            std::to_string(kNoAllocMaxPoints) + " points per call, got " +
+                                            std::to_string(n));
+    int32_t* base = noalloc_scratch();
+    int32_t* V = base;
+    int32_t* nin = base + kNoAllocMaxPoints;
+    int32_t* F = base + 2 * kNoAllocMaxPoints;
+    int32_t* res = base + 3 * kNoAllocMaxPoints;
+    int32_t* dep = base + 4 * kNoAllocMaxPoints;
+    int32_t* counters = base + 5 * kNoAllocMaxPoints;
+    // the per-point slots are fully rewritten before they are read; only the counters must
+    // start at zero (the array keeps the previous call's contents)
+    FGB_CUDA(cudaMemsetAsync(counters, 0, 8 * sizeof(int32_t), stream_));
+    const int B = 256;
+    Pts P{d_pts};
+    GridView G{grid_.dim[0], grid_.dim[1], grid_.dim[2], grid_.origin[0], grid_.origin[1], grid_.origin[2],
+               grid_.step[0], grid_.step[1], grid_.step[2]};
+    FGB_LAUNCH(k_locate_walk<<<grid_for(n, B), B, 0, stream_>>>(n, P, G, seed_.get(), det_.get(), face_nbr_.get(), nbr_ptr_.get(),
+                                                     nbr_idx_.get(), search_.get(), bb_lo_[0], bb_lo_[1], bb_lo_[2], bb_hi_[0],
+                                                     bb_hi_[1], bb_hi_[2], V, nin, counters));
+    FGB_LAUNCH(k_locate_scan<<<std::min(n, 1024), B, 0, stream_>>>(n, P, n_tets_, det_.get(), search_.get(), V, nin));
+    FGB_LAUNCH(k_nearest_ctr<<<grid_for(n, 128), 128, 0, stream_>>>(n, P, G, gptr_.get(), gtets_.get(), gcxyz_.get(), V, F,
+                                                                    counters));
+    FGB_LAUNCH(k_resolve<<<grid_for(n, B), B, 0, stream_>>>(n, V, nin, F, res, dep, counters));
+    const int g0 = rank == 3 ? 0 : std::min(1, n_tets_ - 1);
+    FGB_LAUNCH(k_chain_runs<<<grid_for(n, B), B, 0, stream_>>>(n, P, g0, det_.get(), nbr_ptr_.get(), nbr_idx_.get(), V, F, dep,
+                                                              res, counters));
+    FGB_LAUNCH(k_interpolate<<<grid_for(n, 128), 128, 0, stream_>>>(n, P, rank, 1, res, det_.get(), tet_nodes_.get(),
+                                                                    quad_.get(), hexs_.get(), hexf_.get(), sol_.get(), d_cells,
+                                                                    d_out));
+    FGB_CUDA(cudaGetLastError());
 }
 
 void DeviceMesh::interpolate_known(int n, const double* d_pts, int rank, const int32_t* d_cells, double* d_out) {

@@ -133,6 +133,25 @@ int fgb_field_interpolate(FGB_FIELD* f, int n, const double* xyz, int rank, int*
                           int64_t* stats5);
 /* same with device pointers (no copies) */
 int fgb_field_interpolate_device(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells, double* d_out5);
+/* Allocation-free variant of fgb_field_interpolate_device (no counterpart in the reference).
+ * Some callers cannot let a library allocate device memory during their timestep loop: MD
+ * engines that hand the whole device memory to their own pool allocator, or run with a
+ * device-memory footprint fixed at start-up, and pipelines that cannot afford the device
+ * synchronisation a cudaMalloc implies. This entry point calls no cudaMalloc, cudaFree or
+ * other allocating routine: its per-point scratch is a fixed file-scope device array that
+ * every GPU loading the library keeps (about 5.2 MB) until the process exits.
+ *   - at most 262144 points per call; larger n returns 1 with a message, nothing launched;
+ *   - the caller passes device pointers for the points (3n doubles), the cells (n ints, or
+ *     NULL) and the results (5n doubles); results are identical to fgb_field_interpolate_device;
+ *   - asynchronous on the field's stream (fgb_field_stream); results are ready when that
+ *     stream has completed the call;
+ *   - all calls share the scratch array, so calls that overlap on the GPU (from different
+ *     streams, threads or fields) race: serialise them;
+ *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress,
+ *     with that device current); make that first call before any stream capture.
+ * Returns 0 on success, 1 on error (femocs_last_error). */
+int fgb_field_interpolate_device_noalloc(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells,
+                                         double* d_out5);
 /* matrix after Dirichlet elimination in CSR (sorted columns) with the rhs, by dof;
  * dof2node maps dofs to mesh nodes */
 int fgb_field_export_system(FGB_FIELD* f, int64_t* rowptr, int* col, double* val, double* rhs, int* dof2node);
