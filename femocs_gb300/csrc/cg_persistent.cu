@@ -34,43 +34,50 @@ namespace {
 
 constexpr int kThreads = 256;
 
-template <typename T>
-__device__ __forceinline__ T sell_dot(int i, const MixedArgs& a, const T* __restrict__ vals, const T* __restrict__ x) {
+// SELL-32 with 4-wide row chunks (layout in fem_setup.cpp). Matrix values and columns are
+// read-only for the whole kernel (non-coherent loads); vectors written by other CTAs during
+// the kernel are read with plain loads after the grid barrier.
+__device__ __forceinline__ double sell_dot64(int i, const MixedArgs& a, const double* x) {
     const int s = i >> 5;
-    const int64_t base = a.sptr[s] + (i & 31);
-    const int len = a.slen[s];
-    T acc0 = 0, acc1 = 0;
-    int j = 0;
-    for (; j + 1 < len; j += 2) {
-        const int64_t o0 = base + (int64_t)j * 32, o1 = o0 + 32;
-        acc0 += __ldg(vals + o0) * x[__ldg(a.scol + o0)];
-        acc1 += __ldg(vals + o1) * x[__ldg(a.scol + o1)];
-    }
-    if (j < len) {
-        const int64_t o0 = base + (int64_t)j * 32;
-        acc0 += __ldg(vals + o0) * x[__ldg(a.scol + o0)];
+    const int64_t base = a.sptr[s] + (int64_t)(i & 31) * 4;
+    const int nch = a.slen[s] >> 2;
+    double acc0 = 0, acc1 = 0;
+    for (int c = 0; c < nch; ++c) {
+        const int64_t o = base + (int64_t)c * 128;
+        const int4 ci = __ldg(reinterpret_cast<const int4*>(a.scol + o));
+        const double2 v01 = __ldg(reinterpret_cast<const double2*>(a.s64 + o));
+        const double2 v23 = __ldg(reinterpret_cast<const double2*>(a.s64 + o) + 1);
+        acc0 += v01.x * x[ci.x] + v01.y * x[ci.y];
+        acc1 += v23.x * x[ci.z] + v23.y * x[ci.w];
     }
     return acc0 + acc1;
 }
 
 // q_i = sum_j a_ij (z_j + beta * pold_j): the new direction is formed on the fly
-__device__ __forceinline__ float sell_dir_dot(int i, const MixedArgs& a, const float* __restrict__ z,
-                                              const float* __restrict__ pold, float beta) {
+__device__ __forceinline__ float sell_dir_dot(int i, const MixedArgs& a, const float* z, const float* pold,
+                                              float beta) {
     const int s = i >> 5;
-    const int64_t base = a.sptr[s] + (i & 31);
-    const int len = a.slen[s];
+    const int64_t base = a.sptr[s] + (int64_t)(i & 31) * 4;
+    const int nch = a.slen[s] >> 2;
     float acc0 = 0.f, acc1 = 0.f;
-    int j = 0;
-    for (; j + 1 < len; j += 2) {
-        const int64_t o0 = base + (int64_t)j * 32, o1 = o0 + 32;
-        const int c0 = __ldg(a.scol + o0), c1 = __ldg(a.scol + o1);
-        acc0 += __ldg(a.s32 + o0) * (z[c0] + beta * pold[c0]);
-        acc1 += __ldg(a.s32 + o1) * (z[c1] + beta * pold[c1]);
+    int c = 0;
+    for (; c + 1 < nch; c += 2) {
+        const int64_t o0 = base + (int64_t)c * 128, o1 = o0 + 128;
+        const int4 i0 = __ldg(reinterpret_cast<const int4*>(a.scol + o0));
+        const int4 i1 = __ldg(reinterpret_cast<const int4*>(a.scol + o1));
+        const float4 v0 = __ldg(reinterpret_cast<const float4*>(a.s32 + o0));
+        const float4 v1 = __ldg(reinterpret_cast<const float4*>(a.s32 + o1));
+        acc0 += v0.x * (z[i0.x] + beta * pold[i0.x]) + v0.y * (z[i0.y] + beta * pold[i0.y]) +
+                v0.z * (z[i0.z] + beta * pold[i0.z]) + v0.w * (z[i0.w] + beta * pold[i0.w]);
+        acc1 += v1.x * (z[i1.x] + beta * pold[i1.x]) + v1.y * (z[i1.y] + beta * pold[i1.y]) +
+                v1.z * (z[i1.z] + beta * pold[i1.z]) + v1.w * (z[i1.w] + beta * pold[i1.w]);
     }
-    if (j < len) {
-        const int64_t o0 = base + (int64_t)j * 32;
-        const int c0 = __ldg(a.scol + o0);
-        acc0 += __ldg(a.s32 + o0) * (z[c0] + beta * pold[c0]);
+    if (c < nch) {
+        const int64_t o0 = base + (int64_t)c * 128;
+        const int4 i0 = __ldg(reinterpret_cast<const int4*>(a.scol + o0));
+        const float4 v0 = __ldg(reinterpret_cast<const float4*>(a.s32 + o0));
+        acc0 += v0.x * (z[i0.x] + beta * pold[i0.x]) + v0.y * (z[i0.y] + beta * pold[i0.y]) +
+                v0.z * (z[i0.z] + beta * pold[i0.z]) + v0.w * (z[i0.w] + beta * pold[i0.w]);
     }
     return acc0 + acc1;
 }
@@ -125,7 +132,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_cg(MixedArgs a) {
     // ---- true residual of the initial guess, z = D^-1 r, d = 0, p_old = 0
     double v2[2] = {0.0, 0.0};
     for (int i = t0; i < a.n; i += G) {
-        const double ri = a.b[i] - sell_dot<double>(i, a, a.s64, a.x);
+        const double ri = a.b[i] - sell_dot64(i, a, a.x);
         const float r32 = (float)ri;
         const float z32 = a.dinv32[i] * r32;
         a.r[i] = r32;
@@ -187,7 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_cg(MixedArgs a) {
             grid.sync();
             double u2[2] = {0.0, 0.0};
             for (int i = t0; i < a.n; i += G) {
-                const double ri = a.b[i] - sell_dot<double>(i, a, a.s64, a.x);
+                const double ri = a.b[i] - sell_dot64(i, a, a.x);
                 const float r32 = (float)ri;
                 const float z32 = a.dinv32[i] * r32;
                 a.r[i] = r32;
@@ -228,9 +235,12 @@ int mixed_cg_grid(int n) {
         FGB_REQUIRE(coop, "device does not support cooperative launches");
         FGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_cg, kThreads, 0));
         FGB_REQUIRE(per_sm > 0, "persistent CG kernel cannot be resident");
-        cached = sms * std::min(per_sm, 4);
+        cached = sms * std::min(per_sm, 8);
     }
-    return std::max(1, std::min(cached, (n + kThreads - 1) / kThreads));
+    // at least four rows per thread: fewer CTAs make the two grid barriers and the partial
+    // sums of an iteration cheaper when the system is small
+    const int want = (n + 4 * kThreads - 1) / (4 * kThreads);
+    return std::max(1, std::min(cached, want));
 }
 
 void launch_mixed_cg(const MixedArgs& args, cudaStream_t stream) {

@@ -200,24 +200,51 @@ __global__ void k_dirichlet_rows(int n, const int64_t* __restrict__ rowptr, cons
 }
 
 // ---------------------------------------------------------------- SpMV / CG
+// y_r of a SELL-32 matrix with 4-wide row chunks (see fem_setup.cpp): per chunk one 16-byte
+// column load, one 16/32-byte value load and four gathers; two chunks in flight.
+template <typename T>
+struct Vec4Of;
+template <>
+struct Vec4Of<float> {
+    __device__ __forceinline__ static void load(const float* p, float (&v)[4]) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    }
+};
+template <>
+struct Vec4Of<double> {
+    __device__ __forceinline__ static void load(const double* p, double (&v)[4]) {
+        const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+        const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    }
+};
+
 template <typename T>
 __device__ __forceinline__ T sell_row(int r, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
                                       const int32_t* __restrict__ scol, const T* __restrict__ sval,
                                       const T* __restrict__ x) {
     const int s = r >> 5;
-    const int64_t base = sptr[s] + (r & 31);
-    const int len = slen[s];
+    const int64_t base = sptr[s] + (int64_t)(r & 31) * 4;
+    const int nch = slen[s] >> 2;
     T a0 = 0, a1 = 0;
-    int j = 0;
-    for (; j + 1 < len; j += 2) {
-        const int64_t o0 = base + (int64_t)j * 32, o1 = o0 + 32;
-        const int c0 = __ldg(scol + o0), c1 = __ldg(scol + o1);
-        a0 += __ldg(sval + o0) * __ldg(x + c0);
-        a1 += __ldg(sval + o1) * __ldg(x + c1);
+    int c = 0;
+    for (; c + 1 < nch; c += 2) {
+        const int64_t o0 = base + (int64_t)c * 128, o1 = o0 + 128;
+        const int4 i0 = __ldg(reinterpret_cast<const int4*>(scol + o0));
+        const int4 i1 = __ldg(reinterpret_cast<const int4*>(scol + o1));
+        T v0[4], v1[4];
+        Vec4Of<T>::load(sval + o0, v0);
+        Vec4Of<T>::load(sval + o1, v1);
+        a0 += v0[0] * __ldg(x + i0.x) + v0[1] * __ldg(x + i0.y) + v0[2] * __ldg(x + i0.z) + v0[3] * __ldg(x + i0.w);
+        a1 += v1[0] * __ldg(x + i1.x) + v1[1] * __ldg(x + i1.y) + v1[2] * __ldg(x + i1.z) + v1[3] * __ldg(x + i1.w);
     }
-    if (j < len) {
-        const int64_t o0 = base + (int64_t)j * 32;
-        a0 += __ldg(sval + o0) * __ldg(x + __ldg(scol + o0));
+    if (c < nch) {
+        const int64_t o0 = base + (int64_t)c * 128;
+        const int4 i0 = __ldg(reinterpret_cast<const int4*>(scol + o0));
+        T v0[4];
+        Vec4Of<T>::load(sval + o0, v0);
+        a0 += v0[0] * __ldg(x + i0.x) + v0[1] * __ldg(x + i0.y) + v0[2] * __ldg(x + i0.z) + v0[3] * __ldg(x + i0.w);
     }
     return a0 + a1;
 }
@@ -549,8 +576,10 @@ void FemDevice::download_matrix(std::vector<double>& vals, std::vector<double>& 
     // rebuild the CSR->SELL map on the host (kept only on the device after upload)
     for (int r = 0; r < n_; ++r) {
         const int sl = r / 32, lane = r % 32;
-        for (int64_t k = fs_.rowptr[r]; k < fs_.rowptr[r + 1]; ++k)
-            c2s[k] = fs_.slice_ptr[sl] + (k - fs_.rowptr[r]) * 32 + lane;
+        for (int64_t k = fs_.rowptr[r]; k < fs_.rowptr[r + 1]; ++k) {
+            const int64_t j = k - fs_.rowptr[r];
+            c2s[k] = fs_.slice_ptr[sl] + ((j / 4) * 32 + lane) * 4 + j % 4;
+        }
     }
     vals.resize(fs_.nnz());
     for (int64_t k = 0; k < fs_.nnz(); ++k) vals[k] = s[c2s[k]];

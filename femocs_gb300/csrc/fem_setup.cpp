@@ -215,14 +215,17 @@ FemStructure build_fem_structure(const PreparedMesh& pm) {
             for (int q = 0; q < 4; ++q) fs.r2f_item[pos[top[4 * (size_t)f + q]]++] = 4 * f + q;
     }
 
-    // ---- SELL-32
-    const int C = 32;
+    // ---- SELL-32 with 4-wide row chunks: slice s holds rows 32s..32s+31, padded to a length
+    // that is a multiple of 4; entry j of lane l sits at ptr[s] + ((j/4)*32 + l)*4 + j%4, so a
+    // warp reads 32 x 16 contiguous bytes of values (and of columns) per chunk
+    const int C = 32, W4 = 4;
     const int ns = (nv + C - 1) / C;
     fs.slice_ptr.assign(ns + 1, 0);
     fs.slice_len.assign(ns, 0);
     for (int s = 0; s < ns; ++s) {
         int m = 0;
         for (int r = s * C; r < std::min(nv, (s + 1) * C); ++r) m = std::max(m, fs.row_len[r]);
+        m = (m + W4 - 1) / W4 * W4;
         fs.slice_len[s] = m;
         fs.slice_ptr[s + 1] = fs.slice_ptr[s] + (int64_t)m * C;
     }
@@ -232,7 +235,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm) {
         for (int lane = 0; lane < C; ++lane) {
             const int r = s * C + lane;
             for (int j = 0; j < fs.slice_len[s]; ++j) {
-                const int64_t pos = fs.slice_ptr[s] + (int64_t)j * C + lane;
+                const int64_t pos = fs.slice_ptr[s] + ((int64_t)(j / W4) * C + lane) * W4 + j % W4;
                 if (r < nv && j < fs.row_len[r]) {
                     fs.sell_col[pos] = fs.col[fs.rowptr[r] + j];
                     fs.csr2sell[fs.rowptr[r] + j] = pos;
