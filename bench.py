@@ -11,8 +11,11 @@ stand in for the configuration's Q2 elements (not provided).
 
 One step = the reference's Femocs::run field path on resident data: full assembly (element
 matrices, CSR scatter, Neumann rhs, Dirichlet elimination), CG solve to a 1e-9 relative
-FP64 residual (FP32 inner PCG + FP64 refinement), nodal field recovery + smoothing, location
-+ interpolation (rank 1) of all query points. Metric: solved DOF/s = DoFs / step time.
+FP64 residual (FP64 CG preconditioned by an FP32 multigrid V-cycle; the hierarchy is built
+once per mesh, in the warm-up, and its setup time is reported), nodal field recovery +
+smoothing, location + interpolation (rank 1) of all query points. Metric: solved DOF/s =
+DoFs / step time. The plain FP64 Jacobi-PCG and the FP32-Jacobi/FP64-refinement solvers are
+timed on the same system for comparison.
 `e2e` runs the same step through the reference-facing C ABI (femocs_run +
 femocs_interpolate_elfield) with host arrays in and out.
 
@@ -41,11 +44,9 @@ N_POINTS = {"config2": 1_000_000, "config1": 100_000, "probe": 200_000}
 # running the oracle's restatement of the reference solve (oracle/femocs_oracle.c) to
 # convergence; the CPU baseline times iterations live and multiplies by this count.
 SSOR_ITERS = {"config1": 268, "config2": 617, "probe": 0}
-# DRAM bytes (read + write) per row per iteration of the persistent CG kernel, from the ncu
-# capture of the probe workload (profiles/k_mixed_cg_probe_1.08M_dofs.md: 496.5 GB over
-# 1665 iterations x 1,081,693 rows, refinements included); traffic of a launch scales with
-# rows x iterations.
-KERNEL_TRAFFIC_PER_ROW_ITER = 275.7
+# DRAM bytes (read + write) per row of one launch of the hot multigrid kernels, from ncu
+# captures of the probe workload (profiles/); a launch's traffic scales with its rows.
+KERNEL_TRAFFIC_PER_ROW = {}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -66,7 +67,7 @@ def make_points(spec, n_points):
     return np.ascontiguousarray(np.r_[surf, probes][:n_points]), len(surf)
 
 
-def write_conf(path, spec, precision="mixed"):
+def write_conf(path, spec, precision="amg"):
     with open(path, "w") as f:
         f.write(f"""mesh_file synthetic
 radius {spec['radius']}
@@ -227,30 +228,36 @@ def run_ours(args, world, rank):
         field.interpolate_device(n_points, d_pts.ptr, RANK, d_cells.ptr, d_out.ptr)
         return st
 
+    # femocs_run above already built the multigrid hierarchy of this mesh (its setup time)
+    setup_ms = fem.last_stats()["setup_ms"]
     for _ in range(args.warmup):
-        step(1)
+        step(2)
     lib = load()
+    field.set_profiling(True)
     sampler = ClockSampler()
     sampler.start()
     barrier(world)
     launches0 = lib.fgb_kernel_launches()
     field.mark(0)
     for _ in range(args.steps):
-        solve_stats.append(step(1))
+        solve_stats.append(step(2))
     field.mark(1)
     dev_ms = field.elapsed(0, 1)
     launches = lib.fgb_kernel_launches() - launches0
     clocks = sampler.stop(0)
+    field.set_profiling(False)
     dev_ms = reduce_max(world, dev_ms)
     ms_per_step = dev_ms / args.steps
     value = n * args.steps * world / (dev_ms * 1e-3)
     solve_ms = [s["ms"] for s in solve_stats]
+    last = solve_stats[-1]
+    levels = field.amg_levels().split()
 
-    # plain FP64 Jacobi-PCG on the same system, same step otherwise
-    plain = []
-    for _ in range(min(3, args.steps)):
-        plain.append(step(0))
+    # the same step with the plain FP64 Jacobi-PCG, and with FP32 Jacobi-PCG + FP64 refinement
+    plain = [step(0) for _ in range(min(2, args.steps))]
     plain_ms = [s["ms"] for s in plain]
+    mixed = [step(1) for _ in range(min(2, args.steps))]
+    mixed_ms = [s["ms"] for s in mixed]
 
     # end to end through the reference-facing C ABI with host buffers
     x, y, z = (np.ascontiguousarray(pts[:, k]) for k in range(3))
@@ -265,20 +272,26 @@ def run_ours(args, world, rank):
             raise RuntimeError(fg.last_error())
     e2e_s = reduce_max(world, statistics.median(e2e_t))
 
-    # roofline of the dominant kernel: the persistent mixed-precision CG kernel. Algorithmic
-    # bytes: per FP32 iteration the SELL matrix (4 B value + 4 B column per nonzero) and 12
-    # FP32 row streams (phase A: z, p_old read, p, q written; phase B: d, p, r, q, D^-1 read,
-    # d, r, z written); per FP64 refinement the FP64 matrix (8+4 B per nonzero) and 52 B/row
-    # (x, d update; b, x, D^-1 read; r, z written).
+    # roofline of the dominant kernel of the solve, timed live by event pairs around each of
+    # its launches in the timed steps. Algorithmic bytes per launch:
+    #   level-0 Chebyshev step (k_cheb_step): FP32 SELL matrix, 4 B value + 4 B column per
+    #     nonzero, and 24 B per row (b, x gathered once, D^-1 read; d read + written; x written)
+    #   outer FP64 SpMV (k_cg_spmv_pq<double>): 8 B value + 4 B column per nonzero, 16 B per
+    #     row (p gathered once, q written)
     nnz = field.nnz
-    last = solve_stats[-1]
-    it_bytes = nnz * 8 + 48 * n
-    up_bytes = nnz * 12 + 52 * n
-    alg_bytes = last["iterations"] * it_bytes + last["outer"] * up_bytes
-    kms = statistics.median([s["kernel_ms"] for s in solve_stats])
+    kern = {
+        "k_cheb_step (level-0 Chebyshev smoothing, FP32)": (
+            sum(s["smoother_ms"] for s in solve_stats), sum(s["smoother_launches"] for s in solve_stats),
+            nnz * 8 + 24 * n, "smoother"),
+        "k_cg_spmv_pq<double> (outer FP64 SpMV + p.q)": (
+            sum(s["spmv_ms"] for s in solve_stats), sum(s["spmv_launches"] for s in solve_stats),
+            nnz * 12 + 16 * n, "spmv64"),
+    }
+    name, (tot_ms, cnt, bytes_per_launch, key) = max(kern.items(), key=lambda kv: kv[1][0])
+    launch_ms = tot_ms / max(cnt, 1)
     peak, peak_kind = measured_hbm_peak()
-    achieved = alg_bytes / (kms * 1e-3) / 1e9
-    traffic = KERNEL_TRAFFIC_PER_ROW_ITER * n * last["iterations"]
+    achieved = bytes_per_launch / (launch_ms * 1e-3) / 1e9
+    traffic = KERNEL_TRAFFIC_PER_ROW[key] * n if key in KERNEL_TRAFFIC_PER_ROW else None
     spmv32_ms = field.time_spmv(1, 50)
     spmv64_ms = field.time_spmv(0, 20)
 
@@ -293,34 +306,42 @@ def run_ours(args, world, rank):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 inner / f64 refinement",
+        "dtype": "f64 CG / f32 multigrid preconditioner",
         "data": "synthetic (seeded nanotip mesh, FCC surface atoms, random vacuum probes)",
         "config": {"workload": f"{args.workload}: nanotip R={spec['radius'] / 10:g} nm H={spec['height'] / 10:g} nm, "
                                f"box {2 * spec['box_half'] / 10:g} nm, top {spec['top'] / 10:g} nm, Q1",
                    "n_dofs": n, "nnz": nnz, "n_points": n_points, "n_surface_atoms": n_surf,
-                   "interpolation_rank": RANK, "rel_tol": REL_TOL, "precision": "fp32 inner PCG + fp64 refinement",
+                   "interpolation_rank": RANK, "rel_tol": REL_TOL,
+                   "precision": "FP64 CG, FP32 multigrid V-cycle preconditioner",
                    "l2": "inputs larger than L2 (FP64 matrix %.0f MB)" % (nnz * 12 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "solve": {"p50_ms": statistics.median(solve_ms), "p99_ms": float(np.percentile(solve_ms, 99)),
-                  "iterations": solve_stats[-1]["iterations"], "outer": solve_stats[-1]["outer"],
-                  "rel_residual": solve_stats[-1]["rel_residual"],
-                  "solved_dof_per_s": n / (statistics.median(solve_ms) * 1e-3)},
+                  "iterations": last["iterations"], "rel_residual": last["rel_residual"],
+                  "solved_dof_per_s": n / (statistics.median(solve_ms) * 1e-3),
+                  "multigrid_levels": levels, "multigrid_setup_ms": setup_ms},
         "plain_fp64_cg": {"p50_ms": statistics.median(plain_ms), "iterations": plain[-1]["iterations"],
                           "rel_residual": plain[-1]["rel_residual"],
                           "solved_dof_per_s": n / (statistics.median(plain_ms) * 1e-3),
-                          "speedup_mixed_vs_plain": statistics.median(plain_ms) / statistics.median(solve_ms)},
+                          "speedup_vs_plain": statistics.median(plain_ms) / statistics.median(solve_ms)},
+        "mixed_jacobi_cg": {"p50_ms": statistics.median(mixed_ms), "iterations": mixed[-1]["iterations"],
+                            "refinements": mixed[-1]["outer"], "kernel_ms": mixed[-1]["kernel_ms"],
+                            "rel_residual": mixed[-1]["rel_residual"]},
         "e2e": {"value": n * world / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": 24 * n_points,
                 "d2h_bytes_per_step": 36 * n_points,
                 "note": "femocs_run + femocs_interpolate_elfield through the C ABI, host arrays"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic,
-                     "traffic_note": "ncu dram bytes of the probe capture scaled by rows x iterations",
-                     "kernel": "k_mixed_cg (persistent, cooperative)", "algorithmic_bytes": alg_bytes,
-                     "launch_ms": kms, "bytes_per_iteration": it_bytes, "bytes_per_refinement": up_bytes,
+                     "traffic": traffic, "traffic_note": "ncu dram bytes per row of a probe capture x rows",
+                     "kernel": name, "bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
+                     "launches": cnt, "share_of_solve": tot_ms / sum(solve_ms),
+                     "other": {k: {"ms": v[0], "launches": v[1], "gbs": v[2] / (v[0] / max(v[1], 1) * 1e-3) / 1e9}
+                               for k, v in kern.items() if k != name},
                      "peak_kind": peak_kind, "spmv_fp32_launch_ms": spmv32_ms, "spmv_fp64_launch_ms": spmv64_ms,
                      "spmv_fp32_gbs": (nnz * 8 + 12 * n) / (spmv32_ms * 1e-3) / 1e9},
         "clocks": clocks,
         "gpu_launches": launches,
+        # index of the first timed launch among all of this process's kernel launches, and the
+        # count (ncu -s/-c for a launch list of exactly the timed region)
+        "timed_launch_range": [launches0, launches],
     }
     if rank == 0 and world == 1 and not args.no_cpu and SSOR_ITERS.get(args.workload):
         line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec)

@@ -12,6 +12,12 @@ import numpy as np
 
 from ._lib import FgbNanotip, dp, i64p, ip, last_error, load, ptr
 
+
+def _stats_dict(st):
+    return dict(iterations=int(st[0]), outer=int(st[1]), status=int(st[2]), rel_residual=st[3], bnorm=st[4],
+                ms=st[5], kernel_ms=st[6], setup_ms=st[7], levels=int(st[8]), smoother_ms=st[9],
+                smoother_launches=int(st[10]), spmv_ms=st[11], spmv_launches=int(st[12]))
+
 __all__ = ["Mesh", "Field", "Femocs", "nanotip", "synth_atoms", "synth_probes", "load", "last_error",
            "CONFIG1", "CONFIG2", "FgbNanotip", "DeviceBuffer"]
 
@@ -80,7 +86,7 @@ class Mesh:
             "quad_nodes": (np.int32, 10 * s["n_tets"]), "voro_ptr": (np.int32, s["n_tetnodes"] + 1),
             "voro_idx": (np.int32, s["n_voro_idx"]), "vac_node2vertex": (np.int32, s["n_nodes"]),
             "vac_cells": (np.int32, s["n_vac_cells"]), "tet_search": (np.int32, s["n_tets"]),
-            "edgemax": (np.float64, 1),
+            "edgemax": (np.float64, 1), "node_parents": (np.int32, 4 * s["n_nodes"]),
         }
         dt, n = shapes[name]
         out = np.zeros(max(n, 1), dtype=dt)
@@ -133,14 +139,24 @@ class Field:
     def assemble(self, full_run=True, anode_dirichlet=False):
         self._ok(load().fgb_field_assemble(self.h, int(full_run), int(anode_dirichlet)))
 
-    def solve(self, precision=1, rel_tol=1e-9, abs_tol=0.0, max_iter=10000, inner_tol=0.1):
-        st = np.zeros(7)
-        st[6] = -1.0  # ask for the kernel-only time as well
-        rc = load().fgb_field_solve(self.h, precision, rel_tol, abs_tol, max_iter, inner_tol, ptr(st))
+    def solve(self, precision=2, rel_tol=1e-9, abs_tol=0.0, max_iter=10000, inner_tol=0.1):
+        """precision 0: FP64 Jacobi-PCG; 1: FP32 Jacobi-PCG with FP64 refinement;
+        2: FP64 CG with an FP32 multigrid V-cycle as preconditioner."""
+        rc = load().fgb_field_solve(self.h, precision, rel_tol, abs_tol, max_iter, inner_tol, None)
         if rc == -(2 ** 31):
             raise RuntimeError(last_error())
-        return rc, dict(iterations=int(st[0]), outer=int(st[1]), status=int(st[2]), rel_residual=st[3],
-                        bnorm=st[4], ms=st[5], kernel_ms=st[6] if st[6] != -1.0 else 0.0)
+        st = np.zeros(13)
+        self._ok(load().fgb_field_last_stats(self.h, ptr(st)))
+        return rc, _stats_dict(st)
+
+    def set_profiling(self, on=True):
+        """Record CUDA event pairs around the multigrid path's hot launches."""
+        self._ok(load().fgb_field_set_profiling(self.h, int(on)))
+
+    def amg_levels(self):
+        buf = C.create_string_buffer(4096)
+        self._ok(load().fgb_field_amg_levels(self.h, buf, 4096))
+        return buf.value.decode()
 
     def extract(self, smoothen=True):
         self._ok(load().fgb_field_extract(self.h, int(smoothen)))
@@ -269,7 +285,14 @@ class Femocs:
         rv = C.c_int(0)
         self.lib.femocs_last_solve(self.h, C.byref(rv), ptr(out))
         return dict(iterations=int(out[0]), outer=int(out[1]), status=int(out[2]), rel_residual=out[3], ms=out[4],
-                    n_dofs=int(out[5]))
+                    n_dofs=int(out[5]), levels=int(out[7]))
+
+    def last_stats(self):
+        """All solver statistics of the last run (see Field.solve)."""
+        st = np.zeros(13)
+        if self.lib.fgb_femocs_last_stats(self.h, ptr(st)) != 0:
+            raise RuntimeError(last_error())
+        return _stats_dict(st)
 
     def parse_double(self, cmd):
         v = C.c_double(0)

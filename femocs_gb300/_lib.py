@@ -44,6 +44,7 @@ _PROTOS = {
     "femocs_parse_double": (None, [vp, ip, C.c_char_p, dp]),
     "femocs_parse_string": (None, [vp, ip, C.c_char_p, C.c_char_p]),
     "femocs_last_solve": (None, [vp, ip, dp]),
+    "fgb_femocs_last_stats": (C.c_int, [vp, dp]),
     "femocs_last_error": (C.c_char_p, []),
     "fgb_kernel_launches": (C.c_longlong, []),
     # Part 2
@@ -61,6 +62,9 @@ _PROTOS = {
     "fgb_field_setup": (C.c_int, [vp, C.c_double, C.c_double]),
     "fgb_field_assemble": (C.c_int, [vp, C.c_int, C.c_int]),
     "fgb_field_solve": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, dp]),
+    "fgb_field_last_stats": (C.c_int, [vp, dp]),
+    "fgb_field_set_profiling": (C.c_int, [vp, C.c_int]),
+    "fgb_field_amg_levels": (C.c_int, [vp, C.c_char_p, C.c_int]),
     "fgb_field_export_phi_nodes": (C.c_int, [vp, dp]),
     "fgb_field_import_phi_nodes": (C.c_int, [vp, dp]),
     "fgb_field_extract": (C.c_int, [vp, C.c_int]),

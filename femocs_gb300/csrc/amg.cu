@@ -1,0 +1,350 @@
+// FP32 multigrid V-cycle on the device (sm_103a); host hierarchy from amg_setup.cpp.
+//
+//   k_cheb_zero      first Chebyshev step from a zero guess: d = D^-1 b / theta, x = d
+//   k_cheb_step      d = c1 d + c2 D^-1 (b - A x_in), x_out = x_in + d   (x_in gathered, so
+//                    x is ping-ponged between two buffers)
+//   k_residual       r = b - A x
+//   k_csr_apply      b_c = R r  (restriction, R = P^T stored explicitly: gather, no atomics)
+//                    and x += P x_c (prolongation)
+//   k_dense_solve    x = A_c^-1 b on the coarsest level (one warp per row)
+// Chebyshev smoothing of D^-1 A on [0.1, 1.1] x lambda_max, degree 2 before and after the
+// coarse correction (the same polynomial, so the cycle is a symmetric preconditioner).
+// Level 0 runs on the solver's SELL-32 matrix, one thread per row; coarser levels and the
+// transfer operators are CSR with 1..32 threads per row, chosen from the average row length
+// (the aggregated levels get denser, up to hundreds of entries per row).
+#include <cmath>
+#include <sstream>
+
+#include "amg.h"
+
+namespace fgb {
+
+struct AmgDevLevel {
+    int n = 0, n_coarse = 0;
+    double lambda = 1.0;
+    const int64_t* sptr = nullptr;
+    const int32_t* slen = nullptr;
+    const int32_t* scol = nullptr;
+    const float* val = nullptr;
+    const float* dinv = nullptr;
+    // levels >= 1: CSR with `tpr` threads per row (level 0 uses the solver's SELL arrays)
+    DBuf<int64_t> a_ptr;
+    DBuf<int32_t> a_col;
+    DBuf<float> a_val, own_dinv;
+    int tpr = 1, p_tpr = 1, r_tpr = 1;
+    DBuf<int64_t> p_ptr, r_ptr;
+    DBuf<int32_t> p_col, r_col;
+    DBuf<float> p_val, r_val;
+    DBuf<float> b, xa, xb, d, r;
+    const float* bin = nullptr;  // right-hand side of this level (level 0: the caller's vector)
+    float* x = nullptr;          // result of the last cycle on this level
+};
+
+namespace {
+
+constexpr int kB = 256;
+
+__device__ __forceinline__ float sell4_row(int r, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                           const int32_t* __restrict__ scol, const float* __restrict__ val,
+                                           const float* __restrict__ x) {
+    const int s = r >> 5;
+    const int64_t base = sptr[s] + (int64_t)(r & 31) * 4;
+    const int nch = slen[s] >> 2;
+    float a0 = 0.f, a1 = 0.f;
+    int c = 0;
+    for (; c + 1 < nch; c += 2) {
+        const int64_t o0 = base + (int64_t)c * 128, o1 = o0 + 128;
+        const int4 i0 = __ldg(reinterpret_cast<const int4*>(scol + o0));
+        const int4 i1 = __ldg(reinterpret_cast<const int4*>(scol + o1));
+        const float4 v0 = __ldg(reinterpret_cast<const float4*>(val + o0));
+        const float4 v1 = __ldg(reinterpret_cast<const float4*>(val + o1));
+        a0 += v0.x * __ldg(x + i0.x) + v0.y * __ldg(x + i0.y) + v0.z * __ldg(x + i0.z) + v0.w * __ldg(x + i0.w);
+        a1 += v1.x * __ldg(x + i1.x) + v1.y * __ldg(x + i1.y) + v1.z * __ldg(x + i1.z) + v1.w * __ldg(x + i1.w);
+    }
+    if (c < nch) {
+        const int64_t o0 = base + (int64_t)c * 128;
+        const int4 i0 = __ldg(reinterpret_cast<const int4*>(scol + o0));
+        const float4 v0 = __ldg(reinterpret_cast<const float4*>(val + o0));
+        a0 += v0.x * __ldg(x + i0.x) + v0.y * __ldg(x + i0.y) + v0.z * __ldg(x + i0.z) + v0.w * __ldg(x + i0.w);
+    }
+    return a0 + a1;
+}
+
+// Level operator: SELL (level 0, one thread per row) or CSR with TPR threads per row.
+struct Op {
+    int n;
+    const int64_t* sptr;  // SELL slice offsets, or CSR row pointers
+    const int32_t* slen;  // SELL slice lengths (unused for CSR)
+    const int32_t* scol;
+    const float* val;
+    const float* dinv;
+};
+
+// Row `row` of A x, summed over the TPR lanes of the row's group (valid in every lane of the
+// group). All 32 lanes of the warp must call it: rows beyond n contribute nothing.
+template <int TPR>
+__device__ __forceinline__ float op_row(const Op& A, int row, const float* __restrict__ x) {
+    if constexpr (TPR == 0) {
+        return sell4_row(row, A.sptr, A.slen, A.scol, A.val, x);
+    } else {
+        const int sub = threadIdx.x & (TPR - 1);
+        float acc = 0.f;
+        if (row < A.n) {
+            const int64_t end = A.sptr[row + 1];
+            int64_t k = A.sptr[row] + sub;
+            // four independent chains keep more gathers in flight on the long coarse rows
+            float a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            for (; k + 3 * TPR < end; k += 4 * TPR) {
+                acc += __ldg(A.val + k) * __ldg(x + A.scol[k]);
+                a1 += __ldg(A.val + k + TPR) * __ldg(x + A.scol[k + TPR]);
+                a2 += __ldg(A.val + k + 2 * TPR) * __ldg(x + A.scol[k + 2 * TPR]);
+                a3 += __ldg(A.val + k + 3 * TPR) * __ldg(x + A.scol[k + 3 * TPR]);
+            }
+            for (; k < end; k += TPR) acc += __ldg(A.val + k) * __ldg(x + A.scol[k]);
+            acc += (a1 + a2) + a3;
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        return acc;
+    }
+}
+
+// TPR = 0: SELL, one thread per row; TPR = 1..32: CSR, TPR threads per row
+template <int TPR>
+__device__ __forceinline__ int row_of() {
+    constexpr int t = TPR == 0 ? 1 : TPR;
+    return (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) / t);
+}
+template <int TPR>
+__device__ __forceinline__ bool row_leader() {
+    return TPR <= 1 || (threadIdx.x & (TPR - 1)) == 0;
+}
+
+__global__ void __launch_bounds__(kB) k_cheb_zero(int n, const float* __restrict__ dinv, const float* __restrict__ b,
+                                                  float* __restrict__ x, float* __restrict__ d, float inv_theta) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float di = dinv[i] * b[i] * inv_theta;
+    d[i] = di;
+    x[i] = di;
+}
+
+// c1 < 0 marks the first step from a nonzero guess: d = D^-1 r / theta (c2 = 1/theta)
+template <int TPR>
+__global__ void __launch_bounds__(kB) k_cheb_step(Op A, const float* __restrict__ b, const float* __restrict__ xin,
+                                                  float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
+    const int i = row_of<TPR>();
+    if (TPR <= 1 && i >= A.n) return;
+    const float ax = op_row<TPR>(A, i, xin);
+    if (i >= A.n || !row_leader<TPR>()) return;
+    const float ri = b[i] - ax;
+    const float di = (c1 < 0.f ? 0.f : c1 * d[i]) + c2 * A.dinv[i] * ri;
+    d[i] = di;
+    xout[i] = xin[i] + di;
+}
+
+template <int TPR>
+__global__ void __launch_bounds__(kB) k_residual(Op A, const float* __restrict__ b, const float* __restrict__ x,
+                                                 float* __restrict__ r) {
+    const int i = row_of<TPR>();
+    if (TPR <= 1 && i >= A.n) return;
+    const float ax = op_row<TPR>(A, i, x);
+    if (i >= A.n || !row_leader<TPR>()) return;
+    r[i] = b[i] - ax;
+}
+
+// y = M x (accumulate: y += M x) for a CSR transfer operator
+template <int TPR>
+__global__ void __launch_bounds__(kB) k_csr_apply(int n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                                  const float* __restrict__ val, const float* __restrict__ x,
+                                                  float* __restrict__ y, int accumulate) {
+    const int i = row_of<TPR>();
+    if (TPR <= 1 && i >= n) return;
+    const Op M{n, ptr, nullptr, col, val, nullptr};
+    const float acc = op_row<TPR>(M, i, x);
+    if (i >= n || !row_leader<TPR>()) return;
+    y[i] = accumulate ? y[i] + acc : acc;
+}
+
+// threads per row for a CSR operator of average row length `avg`
+int tpr_for(double avg) {
+    if (avg <= 3.0) return 1;
+    if (avg <= 8.0) return 4;
+    if (avg <= 20.0) return 8;
+    if (avg <= 48.0) return 16;
+    return 32;
+}
+
+#define FGB_TPR_DISPATCH(KERNEL, tpr, n, stream, ...)                                                         \
+    do {                                                                                                      \
+        const int t_ = (tpr);                                                                                 \
+        const int g_ = grid_for((long long)(n) * (t_ == 0 ? 1 : t_), kB);                                     \
+        switch (t_) {                                                                                         \
+            case 0: FGB_LAUNCH(KERNEL<0><<<g_, kB, 0, stream>>>(__VA_ARGS__)); break;                         \
+            case 1: FGB_LAUNCH(KERNEL<1><<<g_, kB, 0, stream>>>(__VA_ARGS__)); break;                         \
+            case 4: FGB_LAUNCH(KERNEL<4><<<g_, kB, 0, stream>>>(__VA_ARGS__)); break;                         \
+            case 8: FGB_LAUNCH(KERNEL<8><<<g_, kB, 0, stream>>>(__VA_ARGS__)); break;                         \
+            case 16: FGB_LAUNCH(KERNEL<16><<<g_, kB, 0, stream>>>(__VA_ARGS__)); break;                       \
+            default: FGB_LAUNCH(KERNEL<32><<<g_, kB, 0, stream>>>(__VA_ARGS__)); break;                       \
+        }                                                                                                     \
+    } while (0)
+
+__global__ void k_dense_solve(int n, const float* __restrict__ inv, const float* __restrict__ b, float* __restrict__ x) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const float* row = inv + (size_t)warp * n;
+    float acc = 0.f;
+    for (int j = lane; j < n; j += 32) acc += row[j] * b[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[warp] = acc;
+}
+
+void upload_csr32(const CsrD& M, DBuf<int64_t>& ptr, DBuf<int32_t>& col, DBuf<float>& val, cudaStream_t s) {
+    ptr.upload(M.ptr, s);
+    if (M.nnz() > 0) {
+        col.upload(M.col, s);
+        std::vector<float> v(M.val.begin(), M.val.end());
+        val.upload(v, s);
+    } else {
+        col.resize(1);
+        val.resize(1);
+    }
+}
+
+}  // namespace
+
+AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sptr, const int32_t* l0_slen,
+                     const int32_t* l0_scol, const float* l0_val, const float* l0_dinv)
+    : stream_(stream), n_coarse_(h.n_coarse) {
+    std::ostringstream ds;
+    const int L = (int)h.levels.size();
+    for (int l = 0; l < L; ++l) {
+        const AmgHostLevel& hl = h.levels[l];
+        auto lv = std::make_unique<AmgDevLevel>();
+        lv->n = hl.A.n_rows;
+        lv->lambda = hl.lambda;
+        if (l == 0) {
+            lv->sptr = l0_sptr;
+            lv->slen = l0_slen;
+            lv->scol = l0_scol;
+            lv->val = l0_val;
+            lv->dinv = l0_dinv;
+        } else if (l < L - 1) {
+            upload_csr32(hl.A, lv->a_ptr, lv->a_col, lv->a_val, stream);
+            std::vector<float> di(lv->n, 1.f);
+            for (int i = 0; i < lv->n; ++i)
+                for (int64_t k = hl.A.ptr[i]; k < hl.A.ptr[i + 1]; ++k)
+                    if (hl.A.col[k] == i) di[i] = (float)(1.0 / hl.A.val[k]);
+            lv->own_dinv.upload(di, stream);
+            lv->sptr = lv->a_ptr.get();
+            lv->slen = nullptr;
+            lv->scol = lv->a_col.get();
+            lv->val = lv->a_val.get();
+            lv->dinv = lv->own_dinv.get();
+            lv->tpr = tpr_for((double)hl.A.nnz() / std::max(1, lv->n));
+        }
+        if (l == 0) lv->tpr = 0;
+        if (l < L - 1) {
+            lv->n_coarse = hl.P.n_cols;
+            upload_csr32(hl.P, lv->p_ptr, lv->p_col, lv->p_val, stream);
+            upload_csr32(hl.R, lv->r_ptr, lv->r_col, lv->r_val, stream);
+            lv->p_tpr = tpr_for((double)hl.P.nnz() / std::max(1, hl.P.n_rows));
+            lv->r_tpr = tpr_for((double)hl.R.nnz() / std::max(1, hl.R.n_rows));
+        }
+        lv->b.resize(lv->n);
+        lv->xa.resize(lv->n);
+        lv->xb.resize(lv->n);
+        lv->d.resize(lv->n);
+        lv->r.resize(lv->n);
+        lv->bin = lv->b.get();
+        ds << (l ? " " : "") << lv->n << ":" << (l == L - 1 ? (long long)lv->n * lv->n : hl.A.nnz())
+           << (l == L - 1 ? ":dense" : "");
+        lv_.push_back(std::move(lv));
+    }
+    std::vector<float> inv(h.coarse_inv.begin(), h.coarse_inv.end());
+    coarse_inv_.upload(inv, stream);
+    desc_ = ds.str();
+    FGB_CUDA(cudaStreamSynchronize(stream));
+}
+
+AmgDevice::~AmgDevice() = default;
+
+int AmgDevice::n_levels() const { return (int)lv_.size(); }
+std::string AmgDevice::describe() const { return desc_; }
+
+void AmgDevice::cycle(int l) {
+    AmgDevLevel& L = *lv_[l];
+    const int g = grid_for(L.n, kB);
+    if (l == (int)lv_.size() - 1) {
+        FGB_LAUNCH(k_dense_solve<<<grid_for((long long)L.n * 32, kB), kB, 0, stream_>>>(L.n, coarse_inv_.get(), L.bin,
+                                                                                       L.xb.get()));
+        L.x = L.xb.get();
+        return;
+    }
+    const double lmax = 1.1 * L.lambda, lmin = 0.1 * L.lambda;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+    const double rho0 = 1.0 / sigma, rho1 = 1.0 / (2.0 * sigma - rho0);
+    const float c1 = (float)(rho1 * rho0), c2 = (float)(2.0 * rho1 / delta), inv_theta = (float)(1.0 / theta);
+    const Op A{L.n, L.sptr, L.slen, L.scol, L.val, L.dinv};
+    LaunchTimer* tm = l == 0 ? &smoother_timer : nullptr;
+    // pre-smoothing from zero
+    FGB_LAUNCH(k_cheb_zero<<<g, kB, 0, stream_>>>(L.n, L.dinv, L.bin, L.xa.get(), L.d.get(), inv_theta));
+    if (tm) tm->begin(stream_);
+    FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, L.xa.get(), L.xb.get(), L.d.get(), c1, c2);
+    if (tm) tm->end(stream_);
+    // coarse-grid correction
+    FGB_TPR_DISPATCH(k_residual, L.tpr, L.n, stream_, A, L.bin, L.xb.get(), L.r.get());
+    AmgDevLevel& C = *lv_[l + 1];
+    FGB_TPR_DISPATCH(k_csr_apply, L.r_tpr, C.n, stream_, C.n, L.r_ptr.get(), L.r_col.get(), L.r_val.get(), L.r.get(),
+                     C.b.get(), 0);
+    cycle(l + 1);
+    FGB_TPR_DISPATCH(k_csr_apply, L.p_tpr, L.n, stream_, L.n, L.p_ptr.get(), L.p_col.get(), L.p_val.get(), C.x,
+                     L.xb.get(), 1);
+    // post-smoothing (same polynomial)
+    if (tm) tm->begin(stream_);
+    FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, L.xb.get(), L.xa.get(), L.d.get(), -1.f, inv_theta);
+    if (tm) tm->end(stream_);
+    if (tm) tm->begin(stream_);
+    FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, L.xa.get(), L.xb.get(), L.d.get(), c1, c2);
+    if (tm) tm->end(stream_);
+    L.x = L.xb.get();
+}
+
+double AmgDevice::time_smoother(int reps) {
+    AmgDevLevel& L = *lv_[0];
+    const int g = grid_for(L.n, kB);
+    Op A{L.n, L.sptr, L.slen, L.scol, L.val, L.dinv};
+    // right-hand side: the level's own buffer, zeroed, so nothing of the caller is read
+    FGB_CUDA(cudaMemsetAsync(L.b.get(), 0, sizeof(float) * L.n, stream_));
+    FGB_CUDA(cudaMemsetAsync(L.xa.get(), 0, sizeof(float) * L.n, stream_));
+    FGB_CUDA(cudaMemsetAsync(L.d.get(), 0, sizeof(float) * L.n, stream_));
+    cudaEvent_t e0, e1;
+    FGB_CUDA(cudaEventCreate(&e0));
+    FGB_CUDA(cudaEventCreate(&e1));
+    auto launch = [&](int i) {
+        float* xi = (i & 1) ? L.xb.get() : L.xa.get();
+        float* xo = (i & 1) ? L.xa.get() : L.xb.get();
+        FGB_LAUNCH(k_cheb_step<0><<<g, kB, 0, stream_>>>(A, L.b.get(), xi, xo, L.d.get(), 0.5f, 0.5f));
+    };
+    for (int i = 0; i < 3; ++i) launch(i);
+    FGB_CUDA(cudaEventRecord(e0, stream_));
+    for (int i = 0; i < reps; ++i) launch(i + 1);
+    FGB_CUDA(cudaEventRecord(e1, stream_));
+    FGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    FGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / reps;
+}
+
+const float* AmgDevice::vcycle(const float* r) {
+    AmgDevLevel& L0 = *lv_[0];
+    L0.bin = r;
+    cycle(0);
+    FGB_CUDA(cudaGetLastError());
+    return L0.x;
+}
+
+}  // namespace fgb

@@ -1,0 +1,80 @@
+// Multigrid preconditioner for the vacuum Poisson system.
+//
+// Level 0 is the Q1 system on the hex mesh. Level 1 lives on the free vacuum tet vertices:
+// its prolongation is the exact linear (P1) interpolation the tet->hex split used to create
+// the hex nodes (edge midpoints 1/2, face centroids 1/3, tet centroids 1/4), so the first
+// coarsening is geometric. Deeper levels use smoothed aggregation; the coarsest level is
+// solved with a dense inverse. Galerkin coarse operators (R A P) throughout; Chebyshev
+// smoothing on D^-1 A. The V-cycle runs in FP32 on the device as the preconditioner of an
+// FP64 CG, whose SpMV, residual and solution update stay FP64.
+#pragma once
+
+#include <memory>
+
+#include "device.h"
+#include "fem.h"
+
+namespace fgb {
+
+struct CsrD {
+    int n_rows = 0, n_cols = 0;
+    std::vector<int64_t> ptr;
+    std::vector<int32_t> col;
+    std::vector<double> val;
+    int64_t nnz() const { return ptr.empty() ? 0 : ptr.back(); }
+};
+
+struct AmgHostLevel {
+    CsrD A;        // operator on this level
+    CsrD P, R;     // prolongation to this level from the next coarser one, and its transpose
+    double lambda = 1.0;  // estimate of the largest eigenvalue of D^-1 A
+};
+
+struct AmgHost {
+    std::vector<AmgHostLevel> levels;  // levels[0] = fine; last level has no P/R
+    std::vector<double> coarse_inv;    // dense inverse of the coarsest operator (row major)
+    int n_coarse = 0;
+    double setup_ms = 0;
+};
+
+struct AmgOptions {
+    double strength = 0.08;  // aggregation strength threshold
+    int max_coarse = 1500;   // dense solve below this size
+    int max_dense = 4096;    // largest dense coarsest level accepted
+    int max_levels = 10;
+};
+
+// fixed: 1 for Dirichlet rows (copper, and the anode when it is a Dirichlet boundary)
+AmgHost build_amg(const PreparedMesh& pm, const FemStructure& fs, const std::vector<double>& a0_val,
+                  const std::vector<int8_t>& fixed, const AmgOptions& opt = AmgOptions());
+
+struct AmgDevLevel;
+
+// Device side of the hierarchy and the V-cycle (amg.cu).
+class AmgDevice {
+public:
+    AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sptr, const int32_t* l0_slen,
+              const int32_t* l0_scol, const float* l0_val, const float* l0_dinv);
+    ~AmgDevice();
+    // z = V(r) on level 0 (FP32, length n0); z is the hierarchy's own buffer, valid until the
+    // next cycle
+    const float* vcycle(const float* r);
+    int n_levels() const;
+    // "rows:nnz" per level, coarsest marked dense
+    std::string describe() const;
+    // average device time [ms] of one level-0 Chebyshev smoothing step (one FP32 SpMV plus
+    // the vector update), timed back to back on the solver stream with the current buffers
+    double time_smoother(int reps);
+    // event pairs around every level-0 Chebyshev step of the V-cycles (when enabled)
+    LaunchTimer smoother_timer;
+
+private:
+    void cycle(int l);
+    cudaStream_t stream_;
+    std::vector<std::unique_ptr<AmgDevLevel>> lv_;
+    DBuf<float> coarse_inv_;
+    int n_coarse_ = 0;
+    std::string desc_;
+};
+
+}  // namespace fgb

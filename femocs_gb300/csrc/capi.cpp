@@ -150,9 +150,19 @@ void femocs_last_solve(FEMOCS* h, int* retval, double* out8) {
         out8[4] = s.ms;
         out8[5] = h->f->n_dofs();
         out8[6] = s.bnorm;
-        out8[7] = 0;
+        out8[7] = s.levels;
         return 0;
     });
+}
+
+static void stats13(const SolveStats& s, double* out) {
+    const double v[13] = {(double)s.iterations, (double)s.outer, (double)s.status, s.rel_residual, s.bnorm,
+                          s.ms, s.kernel_ms, s.setup_ms, (double)s.levels, s.smoother_ms,
+                          (double)s.smoother_launches, s.spmv_ms, (double)s.spmv_launches};
+    std::copy(v, v + 13, out);
+}
+int fgb_femocs_last_stats(FEMOCS* h, double* out13) {
+    return guarded([&] { stats13(h->f->last_stats(), out13); return 0; });
 }
 
 // ---------------------------------------------------------------- Part 2: meshes
@@ -222,6 +232,7 @@ int fgb_mesh_export(const FGB_MESH* m, const char* name, void* out) {
             return cp(v);
         }
         if (n == "hex_nodes") return cp(p.hex.hexs);
+        if (n == "node_parents") return cp(p.hex.parents);
         if (n == "hex_marker") return cp(p.hex.hex_marker);
         if (n == "tet_det") return cp(p.tt.det);
         if (n == "tet_centroid") return cp(p.tt.centroid);
@@ -325,6 +336,23 @@ int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol,
         return 0;
     });
     return g ? INT32_MIN : rc;
+}
+int fgb_field_last_stats(const FGB_FIELD* f, double* out13) {
+    return guarded([&] { stats13(f->last, out13); return 0; });
+}
+int fgb_field_set_profiling(FGB_FIELD* f, int on) {
+    return guarded([&] { f->f->fem().set_profiling(on != 0); return 0; });
+}
+int fgb_field_amg_levels(FGB_FIELD* f, char* buf, int cap) {
+    return guarded([&] {
+        const std::string d = f->f->fem().amg_levels();
+        if (cap > 0) {
+            const size_t n = std::min(d.size(), (size_t)cap - 1);
+            d.copy(buf, n);
+            buf[n] = 0;
+        }
+        return 0;
+    });
 }
 int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi) {
     return guarded([&] {

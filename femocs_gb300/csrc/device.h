@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <vector>
 
 #include "common.h"
 
@@ -78,5 +79,49 @@ private:
 };
 
 inline int grid_for(long long n, int block) { return (int)((n + block - 1) / block); }
+
+// Device time of one kernel inside a sequence of launches on one stream: an event pair is
+// recorded around each timed launch while enabled; collect() sums the pairs after the
+// stream has been synchronised. Events are pooled and reused across solves.
+class LaunchTimer {
+public:
+    LaunchTimer() = default;
+    LaunchTimer(const LaunchTimer&) = delete;
+    LaunchTimer& operator=(const LaunchTimer&) = delete;
+    ~LaunchTimer() {
+        for (cudaEvent_t e : ev_) cudaEventDestroy(e);
+    }
+    bool enabled = false;
+    void begin(cudaStream_t s) {
+        if (enabled) FGB_CUDA(cudaEventRecord(next(), s));
+    }
+    void end(cudaStream_t s) {
+        if (enabled) FGB_CUDA(cudaEventRecord(next(), s));
+    }
+    // sum of the recorded pairs [ms] and their count; resets the pool
+    double collect(int* count) {
+        double ms = 0;
+        for (int k = 0; k + 1 < used_; k += 2) {
+            float t = 0;
+            FGB_CUDA(cudaEventElapsedTime(&t, ev_[k], ev_[k + 1]));
+            ms += t;
+        }
+        if (count) *count = used_ / 2;
+        used_ = 0;
+        return ms;
+    }
+
+private:
+    cudaEvent_t next() {
+        if (used_ == (int)ev_.size()) {
+            cudaEvent_t e;
+            FGB_CUDA(cudaEventCreate(&e));
+            ev_.push_back(e);
+        }
+        return ev_[used_++];
+    }
+    std::vector<cudaEvent_t> ev_;
+    int used_ = 0;
+};
 
 }  // namespace fgb

@@ -119,9 +119,9 @@ void FemocsFacade::read_params() {
     // GPU-specific keys
     conf_.get("gpu_rel_tol", rel_tol_);
     conf_.get("gpu_inner_tol", inner_tol_);
-    std::string prec = "mixed";
+    std::string prec = "amg";
     conf_.get("gpu_precision", prec);
-    precision_ = prec == "fp64" ? 0 : 1;
+    precision_ = prec == "fp64" ? 0 : (prec == "mixed" ? 1 : 2);
     conf_.get("gpu_use_abs_tol", use_abs_tol_);
     double lim[2];
     if (conf_.get("field_limit_min", lim[0])) field_min_ = lim[0];

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "amg.h"
 #include "fem_device.h"
 
 namespace fgb {
@@ -403,8 +404,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_direction(int n, const T* __restr
     p[i] = z[i] + (T)st->beta * p[i];
 }
 
-// FP64 residual r = b - A x with its squared norm; also writes the FP32 scaled copy
-// r32 = r / ||r|| used as the right-hand side of the inner solve.
+// FP64 residual r = b - A x with its squared norm.
 __global__ void __launch_bounds__(kBlock) k_residual64(int n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
                                                        const int32_t* __restrict__ scol, const double* __restrict__ sval,
                                                        const double* __restrict__ x, const double* __restrict__ b,
@@ -441,11 +441,73 @@ __global__ void k_refine(int n, double* __restrict__ x, const float* __restrict_
     x[i] += sqrt(st->rr) * (double)d[i];
 }
 
+// ---- FP64 CG preconditioned by the FP32 multigrid V-cycle
+__global__ void k_to32(int n, const double* __restrict__ a, float* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+// p = z (the V-cycle result, FP32), rz = r.z
+__global__ void __launch_bounds__(kBlock) k_pcg_start(int n, const float* __restrict__ z32, const double* __restrict__ r,
+                                                      double* __restrict__ p, double* partial, CgState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n) {
+        const double zi = (double)z32[i];
+        p[i] = zi;
+        v[0] = r[i] * zi;
+    }
+    if (grid_reduce<1>(v, partial, &st->ticket)) st->rz = v[0];
+}
+
+// x += alpha p, r -= alpha q, FP32 copy of r for the V-cycle, rr and the stop test
+__global__ void __launch_bounds__(kBlock) k_pcg_update(int n, double* __restrict__ x, double* __restrict__ r,
+                                                       const double* __restrict__ p, const double* __restrict__ q,
+                                                       float* __restrict__ r32, double* partial, CgState* st) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double alpha = st->alpha;
+    double v[1] = {0.0};
+    if (i < n) {
+        x[i] += alpha * p[i];
+        const double ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        r32[i] = (float)ri;
+        v[0] = ri * ri;
+    }
+    if (grid_reduce<1>(v, partial, &st->ticket)) {
+        st->iter += 1;
+        cg_check(st, v[0]);
+    }
+}
+
+// beta = r.z / r.z_old with z the V-cycle result (FP32)
+__global__ void __launch_bounds__(kBlock) k_pcg_rz(int n, const float* __restrict__ z32, const double* __restrict__ r,
+                                                   double* partial, CgState* st) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n) v[0] = r[i] * (double)z32[i];
+    if (grid_reduce<1>(v, partial, &st->ticket)) {
+        st->beta = v[0] / st->rz;
+        st->rz = v[0];
+    }
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(kBlock) k_pcg_direction(int n, const float* __restrict__ z32, double* __restrict__ p,
+                                                          const CgState* st) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    p[i] = (double)z32[i] + st->beta * p[i];
+}
+
 }  // namespace
 
 // ==================================================================== FemDevice
 FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t stream)
-    : fs_(std::move(fs)), stream_(stream), n_(fs_.n_dofs), nc_(fs_.n_cells) {
+    : fs_(std::move(fs)), pm_(&pm), stream_(stream), n_(fs_.n_dofs), nc_(fs_.n_cells) {
     cudaStream_t s = stream_;
     cell_dofs_.upload(fs_.cell_dofs, s);
     r2c_ptr_.upload(fs_.r2c_ptr, s);
@@ -496,6 +558,7 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
 }
 
 FemDevice::~FemDevice() {
+    amg_.reset();
     if (h_state_) cudaFreeHost(h_state_);
     if (h_mixed_) cudaFreeHost(h_mixed_);
     cudaEventDestroy(ev0_);
@@ -542,6 +605,10 @@ void FemDevice::spmv64(const double* x, double* y) {
 }
 
 double FemDevice::time_spmv(int precision, int reps) {
+    if (precision == 2) {
+        ensure_amg(nullptr);
+        return amg_->time_smoother(reps);
+    }
     // times the SpMV+dot kernel of the CG iteration on a scratch state (done = 0, rz = 1)
     const int gb = grid_for(n_, kBlock);
     CgState* ds = state_.get() + 1;
@@ -621,7 +688,7 @@ int FemDevice::solve(const SolveOptions& opt, SolveStats* st) {
     if (!st) st = &local;
     *st = SolveStats();
     FGB_CUDA(cudaEventRecord(ev0_, stream_));
-    int rc = opt.precision == 0 ? solve_plain(opt, st) : solve_mixed(opt, st);
+    int rc = opt.precision == 0 ? solve_plain(opt, st) : (opt.precision == 1 ? solve_mixed(opt, st) : solve_amg(opt, st));
     FGB_CUDA(cudaEventRecord(ev1_, stream_));
     FGB_CUDA(cudaEventSynchronize(ev1_));
     float ms = 0;
@@ -709,6 +776,88 @@ int FemDevice::solve_mixed(const SolveOptions& opt, SolveStats* st) {
     st->status = bnorm == 0 ? 1 : h_mixed_->status;
     st->rel_residual = bnorm > 0 ? std::sqrt(h_mixed_->rr) / bnorm : std::sqrt(h_mixed_->rr);
     return st->status == 1 ? st->iterations : -st->iterations;
+}
+
+void FemDevice::ensure_amg(SolveStats* st) {
+    const int anode = anode_dirichlet_ ? 1 : 0;
+    if (amg_ && amg_anode_ == anode) return;
+    std::vector<double> vals, rhs;
+    download_matrix(vals, rhs);
+    std::vector<int8_t> fixed(n_, 0);
+    for (int d = 0; d < n_; ++d) fixed[d] = fs_.bc_kind[d] == 1 || (anode && fs_.bc_kind[d] == 2);
+    AmgHost h = build_amg(*pm_, fs_, vals, fixed);
+    amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
+                             dinv32_.get()));
+    amg_->smoother_timer.enabled = profiling_;
+    amg_anode_ = anode;
+    if (st) st->setup_ms = h.setup_ms;
+}
+
+std::string FemDevice::amg_levels() const { return amg_ ? amg_->describe() : std::string(); }
+
+void FemDevice::set_profiling(bool on) {
+    profiling_ = on;
+    spmv_timer_.enabled = on;
+    if (amg_) amg_->smoother_timer.enabled = on;
+}
+
+int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
+    ensure_amg(st);
+    st->levels = amg_->n_levels();
+    const int gb = grid_for(n_, kBlock);
+    CgState* ds = state_.get();
+    FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
+    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    const double bnorm = std::sqrt(h_state_->rr);
+    st->bnorm = bnorm;
+    CgState init{};
+    init.tol2 = tol2_of(opt, bnorm);
+    init.max_iter = opt.max_iter;
+    FGB_CUDA(cudaMemcpyAsync(ds, &init, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
+    // r = b - A x (FP64), stop if already converged
+    FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(),
+                                                       x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
+    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    int status = 0, it = 0;
+    if (h_state_->rr <= init.tol2 || bnorm == 0) status = 1;
+    if (status == 0) {
+        FGB_LAUNCH(k_to32<<<gb, kBlock, 0, stream_>>>(n_, r64_.get(), r32_.get()));
+        const float* z = amg_->vcycle(r32_.get());
+        FGB_LAUNCH(k_pcg_start<<<gb, kBlock, 0, stream_>>>(n_, z, r64_.get(), p64_.get(), partial_.get(), ds));
+        while (true) {
+            spmv_timer_.begin(stream_);
+            FGB_LAUNCH(k_cg_spmv_pq<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                                        sell64_.get(), p64_.get(), q64_.get(), partial_.get(), ds));
+            spmv_timer_.end(stream_);
+            FGB_LAUNCH(k_pcg_update<<<gb, kBlock, 0, stream_>>>(n_, x_.get(), r64_.get(), p64_.get(), q64_.get(), r32_.get(),
+                                                               partial_.get(), ds));
+            FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+            FGB_CUDA(cudaStreamSynchronize(stream_));
+            it = h_state_->iter;
+            if (h_state_->done) {
+                status = h_state_->status;
+                break;
+            }
+            const float* zi = amg_->vcycle(r32_.get());
+            FGB_LAUNCH(k_pcg_rz<<<gb, kBlock, 0, stream_>>>(n_, zi, r64_.get(), partial_.get(), ds));
+            FGB_LAUNCH(k_pcg_direction<<<gb, kBlock, 0, stream_>>>(n_, zi, p64_.get(), ds));
+        }
+    }
+    st->iterations = it;
+    st->outer = 0;
+    // report the true FP64 residual
+    FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(),
+                                                       x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
+    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    const double rn = std::sqrt(h_state_->rr);
+    st->rel_residual = bnorm > 0 ? rn / bnorm : rn;
+    st->status = bnorm == 0 ? 1 : status;
+    st->smoother_ms = amg_->smoother_timer.collect(&st->smoother_launches);
+    st->spmv_ms = spmv_timer_.collect(&st->spmv_launches);
+    return st->status == 1 ? it : -it;
 }
 
 }  // namespace fgb

@@ -6,6 +6,8 @@
 #include "device.h"
 #include "fem.h"
 
+#include <memory>
+
 namespace fgb {
 
 // Scalars of one CG run, kept in device memory so that a whole chunk of iterations can be
@@ -49,8 +51,12 @@ struct MixedArgs {
 void launch_mixed_cg(const MixedArgs& args, cudaStream_t stream);
 int mixed_cg_grid(int n);
 
+class AmgDevice;
+
 struct SolveOptions {
-    int precision = 1;        // 0: plain FP64 Jacobi-PCG; 1: FP32 inner PCG + FP64 refinement
+    // 0: plain FP64 Jacobi-PCG; 1: FP32 Jacobi-PCG with FP64 reliable refinement (persistent
+    // kernel); 2: FP64 CG preconditioned by an FP32 multigrid V-cycle
+    int precision = 2;
     double rel_tol = 1e-9;    // on ||b - A x||_2 / ||b||_2 (FP64 true residual)
     double abs_tol = 0.0;     // optional absolute floor (reference field_cgtol semantics)
     int max_iter = 10000;     // total CG iterations (inner + plain)
@@ -67,11 +73,23 @@ struct SolveStats {
     double bnorm = 0;
     double ms = 0;            // device time of the solve (CUDA events)
     double kernel_ms = 0;     // device time of the persistent CG kernel alone (mixed path)
+    double setup_ms = 0;      // multigrid hierarchy construction in this call (0 when reused)
+    int levels = 0;           // multigrid levels
+    // with profiling on (multigrid path): summed device time and count of the level-0
+    // Chebyshev smoothing launches and of the outer FP64 SpMV launches
+    int smoother_launches = 0, spmv_launches = 0;
+    double smoother_ms = 0, spmv_ms = 0;
 };
 
 class FemDevice {
 public:
     FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t stream);
+    // multigrid hierarchy of the current matrix (built on first use, rebuilt when the anode
+    // boundary condition changes the eliminated matrix)
+    void ensure_amg(SolveStats* st);
+    std::string amg_levels() const;
+    // event pairs around the multigrid path's hot launches (see SolveStats)
+    void set_profiling(bool on);
     ~FemDevice();
 
     // PoissonSolver::setup + assemble verbs (src/PoissonSolver.cpp:162-210)
@@ -99,10 +117,16 @@ private:
     void spmv64(const double* x, double* y);
     int solve_plain(const SolveOptions& opt, SolveStats* st);
     int solve_mixed(const SolveOptions& opt, SolveStats* st);
+    int solve_amg(const SolveOptions& opt, SolveStats* st);
     void run_cg(bool fp32, CgState* d_state, int max_iter, int chunk);
 
     FemStructure fs_;
+    const PreparedMesh* pm_;
     cudaStream_t stream_;
+    std::unique_ptr<AmgDevice> amg_;
+    int amg_anode_ = -1;
+    bool profiling_ = false;
+    LaunchTimer spmv_timer_;
     int n_, nc_;
     double applied_field_ = 0, applied_potential_ = 0;
     bool anode_dirichlet_ = false;

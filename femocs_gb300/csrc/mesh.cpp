@@ -215,10 +215,12 @@ HexMesh tethex_split(const TetMesh& tm) {
     const size_t n_nodes = (size_t)n_old + n_edges + n_faces + n_tets;
     hm.xyz.resize(3 * n_nodes);
     hm.node_marker.resize(n_nodes);
+    hm.parents.assign(4 * n_nodes, -1);
     const double* X = tm.xyz.data();
     for (int i = 0; i < n_old; ++i) {
         for (int c = 0; c < 3; ++c) hm.xyz[3 * i + c] = X[3 * i + c];
         hm.node_marker[i] = kTetNode;
+        hm.parents[4 * (size_t)i] = i;
     }
     for (int e = 0; e < n_edges; ++e) {
         const int32_t hi = (int32_t)(ekeys[e] >> 32), lo = (int32_t)(ekeys[e] & 0xffffffffu);
@@ -230,6 +232,8 @@ HexMesh tethex_split(const TetMesh& tm) {
             hm.xyz[3 * o + c] = s / 2;
         }
         hm.node_marker[o] = kEdgeCentroid;
+        hm.parents[4 * o] = lo;
+        hm.parents[4 * o + 1] = hi;
     }
     for (int f = 0; f < n_faces; ++f) {
         const size_t o = (size_t)n_old + n_edges + f;
@@ -239,6 +243,7 @@ HexMesh tethex_split(const TetMesh& tm) {
             hm.xyz[3 * o + c] = s / 3;
         }
         hm.node_marker[o] = kFaceCentroid;
+        for (int k = 0; k < 3; ++k) hm.parents[4 * o + k] = face_verts[f][k];
     }
     for (int t = 0; t < n_tets; ++t) {
         const size_t o = (size_t)n_old + n_edges + n_faces + t;
@@ -248,6 +253,7 @@ HexMesh tethex_split(const TetMesh& tm) {
             hm.xyz[3 * o + c] = s / 4;
         }
         hm.node_marker[o] = kTetCentroid;
+        for (int k = 0; k < 4; ++k) hm.parents[4 * o + k] = T[4 * t + k];
     }
 
     // ---- hexahedra, four per tet, in the reference's vertex order

@@ -31,6 +31,9 @@ struct HexMesh {
     std::vector<int8_t> node_marker;  // kTetNode .. kTetCentroid
     std::vector<int32_t> hexs;        // 8 * n_hexs (= 4 * n_tets)
     std::vector<int32_t> hex_marker;  // +(1+v) vacuum, -(1+v) bulk
+    // tet vertices a node was made from (itself; edge ends; face corners; tet corners),
+    // 4 slots per node, unused slots -1 -- the linear interpolation from the tet mesh
+    std::vector<int32_t> parents;
     int n_nodes() const { return (int)(xyz.size() / 3); }
     int n_hexs() const { return (int)(hexs.size() / 8); }
 };

@@ -71,8 +71,10 @@ void femocs_parse_string(FEMOCS* femocs, int* retval, const char* command, char*
 void femocs_import_mesh(FEMOCS* femocs, int* retval, int n_nodes, const double* xyz, int n_tets, const int* tets,
                         const int* markers);
 /* Statistics of the last femocs_run: iterations, refinement sweeps, status, relative
- * residual, solve milliseconds, #dofs (as doubles). */
+ * residual, solve milliseconds, #dofs, |b|, multigrid levels (as doubles). */
 void femocs_last_solve(FEMOCS* femocs, int* retval, double* out8);
+/* the 13 statistics of fgb_field_last_stats for the last femocs_run */
+int fgb_femocs_last_stats(FEMOCS* femocs, double* out13);
 const char* femocs_last_error(void);
 /* number of CUDA kernels the library has launched so far (all handles) */
 long long fgb_kernel_launches(void);
@@ -96,7 +98,7 @@ int fgb_mesh_sizes(const FGB_MESH* m, int64_t* out12);
 /* copy a named host table into `out` (caller sized from fgb_mesh_sizes):
  * tet_nodes tet_marker tet_nbor node_xyz node_marker hex_nodes hex_marker tet_det
  * tet_centroid hex_coeffs nbr_ptr nbr_idx quad_nodes voro_ptr voro_idx vac_node2vertex
- * vac_cells edgemax(double) */
+ * vac_cells node_parents (4 per node, -1 = unused) edgemax(double) */
 int fgb_mesh_export(const FGB_MESH* m, const char* name, void* out);
 
 /* synthetic atoms/probes for a nanotip spec; two-call pattern: pass out=NULL to get the count */
@@ -113,7 +115,8 @@ int fgb_field_sizes(const FGB_FIELD* f, int64_t* out4); /* n_dofs, nnz, n_top_fa
 int fgb_field_setup(FGB_FIELD* f, double applied_field, double applied_potential);
 /* PoissonSolver::assemble(full_run); anode_dirichlet selects anode_bc = dirichlet */
 int fgb_field_assemble(FGB_FIELD* f, int full_run, int anode_dirichlet);
-/* CG solve; precision 0 = plain FP64 Jacobi-PCG, 1 = FP32 inner + FP64 refinement.
+/* CG solve; precision 0 = plain FP64 Jacobi-PCG, 1 = FP32 inner + FP64 refinement,
+ * 2 = FP64 CG preconditioned by an FP32 multigrid V-cycle (hierarchy built on first use).
  * inner_tol: residual reduction between FP64 refinements (<= 0: default 0.1).
  * stats (may be NULL): iterations, refinements, status, rel_residual, bnorm, ms; a 7th slot
  * preset to -1 receives the device time of the solver kernel alone.
@@ -121,6 +124,16 @@ int fgb_field_assemble(FGB_FIELD* f, int full_run, int anode_dirichlet);
 int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol, int max_iter, double inner_tol,
                     double* stats6);
 /* phi per vacuum dof order is internal; these export per hex-mesh node (n_nodes values) */
+/* statistics of the last solve (13 doubles): iterations, refinements, status, rel_residual,
+ * bnorm, ms, solver-kernel ms (persistent mixed path), multigrid setup ms in that call,
+ * levels, and with profiling on (multigrid path): level-0 smoother ms, smoother launches,
+ * outer FP64 SpMV ms, SpMV launches */
+int fgb_field_last_stats(const FGB_FIELD* f, double* out13);
+/* record CUDA event pairs around the multigrid path's hot launches (off by default) */
+int fgb_field_set_profiling(FGB_FIELD* f, int on);
+/* multigrid levels as "rows:nnz" separated by spaces, the coarsest "rows:rows^2:dense";
+ * NUL-terminated, truncated to cap bytes; empty before the first multigrid solve */
+int fgb_field_amg_levels(FGB_FIELD* f, char* buf, int cap);
 int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi_nodes);
 int fgb_field_import_phi_nodes(FGB_FIELD* f, const double* phi_nodes);
 /* Interpolator::extract_solution: nodal E from phi, optional smoothing */
@@ -155,7 +168,8 @@ int fgb_field_interpolate_device_noalloc(FGB_FIELD* f, int n, const double* d_xy
 /* matrix after Dirichlet elimination in CSR (sorted columns) with the rhs, by dof;
  * dof2node maps dofs to mesh nodes */
 int fgb_field_export_system(FGB_FIELD* f, int64_t* rowptr, int* col, double* val, double* rhs, int* dof2node);
-/* average device time [ms] of one SpMV with FP64 (precision 0) or FP32 (1) values */
+/* average device time [ms] of one SpMV with FP64 (precision 0) or FP32 (1) values, or of
+ * one level-0 multigrid Chebyshev smoothing step (2; builds the hierarchy if needed) */
 double fgb_field_time_spmv(FGB_FIELD* f, int precision, int reps);
 /* device stream the field works on (cudaStream_t) */
 void* fgb_field_stream(FGB_FIELD* f);

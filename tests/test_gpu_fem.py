@@ -45,7 +45,7 @@ def test_assembled_system_matches_oracle(tip, anode):
     np.testing.assert_allclose(b, s.rhs, rtol=0, atol=1e-12 * np.abs(s.rhs).max())
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 @pytest.mark.parametrize("tol", [1e-9, 1e-12])
 def test_solve_matches_oracle(tip, precision, tol):
     m, f = tip
@@ -53,7 +53,9 @@ def test_solve_matches_oracle(tip, precision, tol):
     f.assemble(True, False)
     rc, st = f.solve(precision=precision, rel_tol=tol, max_iter=20000)
     assert rc > 0 and st["status"] == 1
-    assert st["rel_residual"] <= tol * (1.05 if precision else 2.0)
+    # the mixed solver stops on the true FP64 residual; the FP64 recursions on the
+    # recursive one, which drifts from the true residual by rounding
+    assert st["rel_residual"] <= tol * (1.05 if precision == 1 else 2.0)
     xyz, cells, v2n = vacuum_system_inputs(m)
     s = orc.System(xyz, cells, 0.1)
     it, x = s.ssor_cg(1.2, 1e-13 * np.linalg.norm(s.rhs), 50000)
@@ -76,6 +78,51 @@ def test_mixed_beats_plain_iteration_economy(tip):
     assert s1["iterations"] <= 2 * s0["iterations"] + 50
 
 
+def test_multigrid_iteration_economy():
+    m = fg.Mesh.synthetic(**TIP)
+    f = fg.Field(m)
+    f.setup(0.1)
+    f.assemble(True, False)
+    rc0, s0 = f.solve(precision=0, rel_tol=1e-9)
+    f.setup(0.1)
+    f.assemble(False, False)
+    rc2, s2 = f.solve(precision=2, rel_tol=1e-9)
+    assert s0["status"] == 1 and s2["status"] == 1
+    # first use builds the hierarchy: a geometric level on the tet vertices, then aggregates
+    assert s2["levels"] >= 2 and s2["setup_ms"] > 0
+    assert s2["iterations"] <= 60 and 5 * s2["iterations"] < s0["iterations"]
+    levels = [lv.split(":") for lv in f.amg_levels().split()]
+    assert len(levels) == s2["levels"] and int(levels[0][0]) == f.n_dofs and int(levels[0][1]) == f.nnz
+    assert levels[-1][2] == "dense" and all(int(a[0]) > int(b[0]) for a, b in zip(levels, levels[1:]))
+    # the hierarchy is reused while the matrix is unchanged; profiling times the hot launches
+    f.set_profiling(True)
+    f.setup(0.1)
+    f.assemble(True, False)
+    rc3, s3 = f.solve(precision=2, rel_tol=1e-9)
+    f.set_profiling(False)
+    assert s3["setup_ms"] == 0 and s3["iterations"] == s2["iterations"]
+    it = s3["iterations"]
+    assert s3["smoother_launches"] == 3 * it and s3["spmv_launches"] == it
+    assert 0 < s3["smoother_ms"] < s3["ms"] and 0 < s3["spmv_ms"] < s3["ms"]
+    assert f.time_spmv(2, 5) > 0
+
+
+def test_multigrid_follows_anode_boundary(tip):
+    """Switching the anode to a Dirichlet boundary changes the eliminated matrix; the
+    hierarchy is rebuilt and the solution still matches the oracle."""
+    m, f = tip
+    xyz, cells, v2n = vacuum_system_inputs(m)
+    for anode in (False, True, False):
+        f.setup(0.1, 3.0)
+        f.assemble(True, anode)
+        rc, st = f.solve(precision=2, rel_tol=1e-11)
+        assert rc > 0 and st["status"] == 1 and st["rel_residual"] <= 2e-11
+        s = orc.System(xyz, cells, 0.1, anode, 3.0)
+        it, x = s.ssor_cg(1.2, 1e-13 * np.linalg.norm(s.rhs), 50000)
+        phi = f.phi_nodes()[v2n]
+        assert np.abs(phi - x).max() <= 2e3 * 1e-11 * np.abs(x).max()
+
+
 def test_warm_start_and_reassembly(tip):
     m, f = tip
     f.setup(0.1)
@@ -87,12 +134,13 @@ def test_warm_start_and_reassembly(tip):
     assert st2["iterations"] == 0 and st2["status"] == 1
 
 
-def test_flat_known_answer():
+@pytest.mark.parametrize("precision", [1, 2])
+def test_flat_known_answer(precision):
     m = fg.Mesh.synthetic(**FLAT)
     f = fg.Field(m)
     f.setup(0.1)
     f.assemble(True, False)
-    rc, st = f.solve(precision=1, rel_tol=1e-12)
+    rc, st = f.solve(precision=precision, rel_tol=1e-12)
     assert rc > 0
     xyz = m.export("node_xyz").reshape(-1, 3)
     n2v = m.export("vac_node2vertex")
