@@ -346,3 +346,150 @@ def synth_probes(spec_kw, n, seed=777):
     if load().fgb_synth_probes(C.byref(spec), n, seed, ptr(xyz)) < 0:
         raise RuntimeError(last_error())
     return xyz.reshape(-1, 3)
+
+
+class Batch:
+    """Many meshes resident on the device, solved together (block-diagonal multigrid PCG,
+    one CUDA graph launch per step). Solves: admit(slot, E0, ...) then step()/collect(), or
+    solve_all(). Each slot keeps its last solution as the warm start of its next solve."""
+
+    def __init__(self, use_graph=True, autotune=True, grid_ctas=0):
+        self.h = load().fgb_batch_create(int(use_graph), int(autotune), int(grid_ctas))
+        if not self.h:
+            raise RuntimeError("batch creation failed: " + last_error())
+        self._meshes = {}
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().fgb_batch_free(self.h)
+            self.h = None
+
+    def _ok(self, rc):
+        if rc != 0:
+            raise RuntimeError(last_error())
+
+    def add_mesh(self, mesh: Mesh, hbm_reserve=0.0):
+        """Slot of the placed mesh, or -1 when free device memory does not admit it."""
+        slot = load().fgb_batch_add_mesh(self.h, mesh.h, float(hbm_reserve))
+        if slot == -(2 ** 31):
+            raise RuntimeError(last_error())
+        if slot >= 0:
+            self._meshes[slot] = mesh
+        return slot
+
+    def add_synthetic(self, specs, n_threads=0, hbm_reserve=0.0):
+        """Build and add nanotip meshes from spec dicts on host threads; returns the slots."""
+        arr = (FgbNanotip * len(specs))(*[nanotip(**s) for s in specs])
+        slots = np.full(len(specs), -1, dtype=np.int32)
+        self._ok(load().fgb_batch_add_synthetic(self.h, len(specs), arr, int(n_threads), float(hbm_reserve),
+                                                ptr(slots, ip)))
+        return slots
+
+    def remove_mesh(self, slot):
+        self._ok(load().fgb_batch_remove_mesh(self.h, slot))
+        self._meshes.pop(slot, None)
+
+    def admit(self, slot, E0, rel_tol=1e-9, max_iter=1000):
+        self._ok(load().fgb_batch_admit(self.h, slot, float(E0), float(rel_tol), int(max_iter)))
+
+    def step(self, max_iters=1000):
+        still = load().fgb_batch_step(self.h, int(max_iters))
+        if still == -(2 ** 31):
+            raise RuntimeError(last_error())
+        return still
+
+    def collect(self, cap=4096):
+        slots = np.zeros(cap, dtype=np.int32)
+        res = np.zeros(4 * cap)
+        n = load().fgb_batch_collect(self.h, cap, ptr(slots, ip), ptr(res))
+        if n == -(2 ** 31):
+            raise RuntimeError(last_error())
+        return {int(slots[k]): dict(iterations=int(res[4 * k]), status=int(res[4 * k + 1]),
+                                    rel_residual=res[4 * k + 2], bnorm=res[4 * k + 3]) for k in range(n)}
+
+    def solve_all(self, fields, rel_tol=1e-9, max_iter=1000):
+        """fields: {slot: E0}. Admits all, steps until all finish; returns {slot: result}."""
+        for slot, E0 in fields.items():
+            self.admit(slot, E0, rel_tol, max_iter)
+        out = {}
+        while True:
+            still = self.step(max_iter + 1)
+            out.update(self.collect())
+            if still == 0:
+                break
+        return out
+
+    def extract(self, slot, smoothen=True):
+        self._ok(load().fgb_batch_extract(self.h, slot, int(smoothen)))
+
+    def interpolate_device(self, slot, n, d_xyz, rank, d_cells, d_out5):
+        self._ok(load().fgb_batch_interpolate(self.h, slot, int(n), C.c_void_p(d_xyz), int(rank), C.c_void_p(d_cells),
+                                              C.c_void_p(d_out5)))
+
+    def sync(self, slot):
+        self._ok(load().fgb_batch_sync_slot(self.h, slot))
+
+    def info(self, slot):
+        o = np.zeros(4, dtype=np.int64)
+        self._ok(load().fgb_batch_info(self.h, slot, ptr(o, i64p)))
+        return dict(n_dofs=int(o[0]), n_nodes=int(o[1]), levels=int(o[2]))
+
+    def phi_nodes(self, slot):
+        out = np.zeros(self.info(slot)["n_nodes"])
+        self._ok(load().fgb_batch_export_phi_nodes(self.h, slot, ptr(out)))
+        return out
+
+    def nodal(self, slot):
+        out = np.zeros(5 * self.info(slot)["n_nodes"])
+        self._ok(load().fgb_batch_export_nodal(self.h, slot, ptr(out)))
+        return out.reshape(-1, 5)
+
+    def reset_solution(self, slot):
+        self._ok(load().fgb_batch_reset_solution(self.h, slot))
+
+    def true_residual(self, slot):
+        v = C.c_double(0)
+        self._ok(load().fgb_batch_true_residual(self.h, slot, C.byref(v)))
+        return v.value
+
+    def stats(self):
+        o = np.zeros(6)
+        self._ok(load().fgb_batch_stats(self.h, ptr(o)))
+        return dict(total_dofs=int(o[0]), device_bytes=int(o[1]), last_iterations=int(o[2]),
+                    kernels_per_iteration=int(o[3]), graph_launches=int(o[4]), slots=int(o[5]))
+
+    def tuning(self):
+        buf = C.create_string_buffer(1024)
+        self._ok(load().fgb_batch_tuning(self.h, buf, 1024))
+        return buf.value.decode()
+
+
+def nanotip_vacuum_hexes(spec_kw):
+    """Vacuum hexahedra of the synthetic nanotip mesh of this spec (no mesh is built)."""
+    n = load().fgb_nanotip_vacuum_hexes(C.byref(nanotip(**spec_kw)))
+    if n < 0:
+        raise RuntimeError(last_error())
+    return int(n)
+
+
+def batch_specs(n, seed=2024, lo_hexes=2e4, hi_hexes=8e5, n_threads=0):
+    """Nanotip specs of a batch of independent tips: tip radius uniform 1-6 nm, aspect ratio
+    (height / radius) uniform 2-8, applied field uniform 0.5-3 GV/m, vacuum hex count
+    log-uniform in [lo_hexes, hi_hexes] (the core spacing is fitted to it). Slab half width
+    6 radii, slab thickness max(2 nm, radius), vacuum top 6 tip heights above the slab.
+    Returns (specs, fields in V/A)."""
+    rng = np.random.default_rng(seed)
+    specs, fields = [], []
+    for _ in range(n):
+        r = rng.uniform(10.0, 60.0)
+        hgt = r * rng.uniform(2.0, 8.0)
+        target = float(np.exp(rng.uniform(np.log(lo_hexes), np.log(hi_hexes))))
+        s = dict(radius=r, height=hgt, box_half=6.0 * r, slab=max(20.0, r), top=6.0 * hgt + 2.0 * r,
+                 h=r / 4, growth=1.25, margin=0.5 * r)
+        h = load().fgb_nanotip_fit_spacing(C.byref(nanotip(**s)), target)
+        if h <= 0:
+            raise RuntimeError(last_error())
+        s["h"] = h
+        specs.append(s)
+        fields.append(rng.uniform(0.05, 0.3))
+    return specs, np.array(fields)

@@ -83,6 +83,27 @@ _PROTOS = {
     "fgb_device_free": (None, [vp]),
     "fgb_memcpy_htod": (C.c_int, [vp, vp, C.c_size_t]),
     "fgb_memcpy_dtoh": (C.c_int, [vp, vp, C.c_size_t]),
+    "fgb_nanotip_vacuum_hexes": (C.c_longlong, [C.POINTER(FgbNanotip)]),
+    "fgb_nanotip_fit_spacing": (C.c_double, [C.POINTER(FgbNanotip), C.c_double]),
+    # Part 3: batches
+    "fgb_batch_create": (vp, [C.c_int, C.c_int, C.c_int]),
+    "fgb_batch_free": (None, [vp]),
+    "fgb_batch_add_mesh": (C.c_int, [vp, vp, C.c_double]),
+    "fgb_batch_add_synthetic": (C.c_int, [vp, C.c_int, C.POINTER(FgbNanotip), C.c_int, C.c_double, ip]),
+    "fgb_batch_remove_mesh": (C.c_int, [vp, C.c_int]),
+    "fgb_batch_admit": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_int]),
+    "fgb_batch_step": (C.c_int, [vp, C.c_int]),
+    "fgb_batch_collect": (C.c_int, [vp, C.c_int, ip, dp]),
+    "fgb_batch_extract": (C.c_int, [vp, C.c_int, C.c_int]),
+    "fgb_batch_interpolate": (C.c_int, [vp, C.c_int, C.c_int, vp, C.c_int, vp, vp]),
+    "fgb_batch_sync_slot": (C.c_int, [vp, C.c_int]),
+    "fgb_batch_export_phi_nodes": (C.c_int, [vp, C.c_int, dp]),
+    "fgb_batch_export_nodal": (C.c_int, [vp, C.c_int, dp]),
+    "fgb_batch_reset_solution": (C.c_int, [vp, C.c_int]),
+    "fgb_batch_true_residual": (C.c_int, [vp, C.c_int, dp]),
+    "fgb_batch_info": (C.c_int, [vp, C.c_int, i64p]),
+    "fgb_batch_stats": (C.c_int, [vp, dp]),
+    "fgb_batch_tuning": (C.c_int, [vp, C.c_char_p, C.c_int]),
 }
 
 

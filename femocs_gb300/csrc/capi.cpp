@@ -4,6 +4,9 @@
 #include <cstring>
 #include <memory>
 
+#include <thread>
+
+#include "batch.h"
 #include "facade.h"
 #include "femocs_gb300.h"
 #include "synth.h"
@@ -15,6 +18,9 @@ struct FEMOCS {
 };
 struct FGB_MESH {
     std::shared_ptr<PreparedMesh> pm;
+};
+struct FGB_BATCH {
+    std::unique_ptr<BatchSolver> b;
 };
 struct FGB_FIELD {
     ~FGB_FIELD() {
@@ -492,3 +498,152 @@ FGB_FIELD* femocs_field(FEMOCS* h) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- Part 3: batches
+FGB_BATCH* fgb_batch_create(int use_graph, int autotune, int grid_ctas) {
+    FGB_BATCH* b = new FGB_BATCH;
+    const int rc = guarded([&] {
+        BatchOptions o;
+        o.use_graph = use_graph != 0;
+        o.autotune = autotune != 0;
+        o.grid_ctas = grid_ctas;
+        b->b.reset(new BatchSolver(o));
+        return 0;
+    });
+    if (rc) { delete b; return nullptr; }
+    return b;
+}
+void fgb_batch_free(FGB_BATCH* b) { delete b; }
+
+int fgb_batch_add_mesh(FGB_BATCH* b, const FGB_MESH* m, double hbm_reserve) {
+    int slot = INT32_MIN;
+    const int rc = guarded([&] {
+        slot = b->b->add_mesh(m->pm, (size_t)std::max(0.0, hbm_reserve));
+        return 0;
+    });
+    return rc ? INT32_MIN : slot;
+}
+
+int fgb_batch_add_synthetic(FGB_BATCH* b, int n, const FgbNanotip* specs, int n_threads, double hbm_reserve,
+                            int* slots) {
+    return guarded([&] {
+        const int nt = std::max(1, std::min(n_threads > 0 ? n_threads : (int)std::thread::hardware_concurrency(), n));
+        std::vector<std::string> errors(nt);
+        std::atomic<int> next{0};
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back([&, t] {
+                try {
+                    for (int i = next++; i < n; i = next++) {
+                        auto pm = std::make_shared<PreparedMesh>(prepare_mesh(make_nanotip_mesh(to_spec(&specs[i]))));
+                        slots[i] = b->b->add_mesh(pm, (size_t)std::max(0.0, hbm_reserve));
+                    }
+                } catch (const std::exception& e) {
+                    errors[t] = e.what();
+                }
+            });
+        for (auto& th : pool) th.join();
+        for (auto& e : errors)
+            if (!e.empty()) throw Error(e);
+        return 0;
+    });
+}
+
+int fgb_batch_remove_mesh(FGB_BATCH* b, int slot) {
+    return guarded([&] { b->b->remove_mesh(slot); return 0; });
+}
+int fgb_batch_admit(FGB_BATCH* b, int slot, double E0, double rel_tol, int max_iter) {
+    return guarded([&] { b->b->admit(slot, E0, rel_tol, max_iter); return 0; });
+}
+int fgb_batch_step(FGB_BATCH* b, int max_iters) {
+    int still = 0;
+    const int rc = guarded([&] { still = b->b->step(max_iters); return 0; });
+    return rc ? INT32_MIN : still;
+}
+int fgb_batch_collect(FGB_BATCH* b, int cap, int* slots, double* res4) {
+    int n = 0;
+    const int rc = guarded([&] {
+        auto fin = b->b->collect_finished();
+        FGB_REQUIRE((int)fin.size() <= cap, "result arrays too small for the finished solves");
+        for (auto& f : fin) {
+            slots[n] = f.first;
+            res4[4 * n] = f.second.iterations;
+            res4[4 * n + 1] = f.second.status;
+            res4[4 * n + 2] = f.second.rel_residual;
+            res4[4 * n + 3] = f.second.bnorm;
+            ++n;
+        }
+        return 0;
+    });
+    return rc ? INT32_MIN : n;
+}
+int fgb_batch_extract(FGB_BATCH* b, int slot, int smoothen) {
+    return guarded([&] { b->b->extract(slot, smoothen != 0); return 0; });
+}
+int fgb_batch_interpolate(FGB_BATCH* b, int slot, int n, const double* d_xyz, int rank, int* d_cells, double* d_out5) {
+    return guarded([&] {
+        b->b->interp(slot).locate_interpolate(n, d_xyz, rank, d_cells, d_out5, nullptr);
+        return 0;
+    });
+}
+int fgb_batch_sync_slot(FGB_BATCH* b, int slot) {
+    return guarded([&] { FGB_CUDA(cudaStreamSynchronize(b->b->slot_stream(slot))); return 0; });
+}
+int fgb_batch_export_phi_nodes(FGB_BATCH* b, int slot, double* phi) {
+    return guarded([&] { b->b->export_phi_nodes(slot, phi); return 0; });
+}
+int fgb_batch_export_nodal(FGB_BATCH* b, int slot, double* sol5) {
+    return guarded([&] {
+        FGB_CUDA(cudaStreamSynchronize(b->b->slot_stream(slot)));
+        b->b->interp(slot).get_solution(sol5);
+        return 0;
+    });
+}
+int fgb_batch_reset_solution(FGB_BATCH* b, int slot) {
+    return guarded([&] { b->b->reset_solution(slot); return 0; });
+}
+int fgb_batch_true_residual(FGB_BATCH* b, int slot, double* out) {
+    return guarded([&] { *out = b->b->true_residual(slot); return 0; });
+}
+int fgb_batch_info(FGB_BATCH* b, int slot, int64_t* out4) {
+    return guarded([&] {
+        out4[0] = b->b->n_dofs(slot);
+        out4[1] = b->b->n_nodes(slot);
+        out4[2] = b->b->levels(slot);
+        out4[3] = 0;
+        return 0;
+    });
+}
+int fgb_batch_stats(FGB_BATCH* b, double* out6) {
+    return guarded([&] {
+        out6[0] = (double)b->b->total_rows();
+        out6[1] = (double)b->b->device_bytes();
+        out6[2] = b->b->last_iterations();
+        out6[3] = b->b->body_kernels();
+        out6[4] = (double)b->b->launches();
+        out6[5] = b->b->n_slots();
+        return 0;
+    });
+}
+int fgb_batch_tuning(FGB_BATCH* b, char* buf, int cap) {
+    return guarded([&] {
+        const std::string d = b->b->tuning();
+        if (cap > 0) {
+            const size_t n = std::min(d.size(), (size_t)cap - 1);
+            d.copy(buf, n);
+            buf[n] = 0;
+        }
+        return 0;
+    });
+}
+
+long long fgb_nanotip_vacuum_hexes(const FgbNanotip* spec) {
+    long long n = -1;
+    guarded([&] { n = nanotip_vacuum_hexes(to_spec(spec)); return 0; });
+    return n;
+}
+double fgb_nanotip_fit_spacing(const FgbNanotip* spec, double target_hexes) {
+    double h = -1;
+    guarded([&] { h = fit_nanotip_spacing(to_spec(spec), (long long)target_hexes); return 0; });
+    return h;
+}

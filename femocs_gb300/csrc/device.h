@@ -46,6 +46,18 @@ public:
         if (n) FGB_CUDA(cudaMalloc(&p_, n * sizeof(T)));
         n_ = n;
     }
+    // enlarge to n elements keeping the first size() elements (new tail zeroed); stream-ordered
+    void grow(size_t n, cudaStream_t s = 0) {
+        if (n <= n_) return;
+        T* q = nullptr;
+        FGB_CUDA(cudaMalloc(&q, n * sizeof(T)));
+        if (n_) FGB_CUDA(cudaMemcpyAsync(q, p_, n_ * sizeof(T), cudaMemcpyDeviceToDevice, s));
+        FGB_CUDA(cudaMemsetAsync(q + n_, 0, (n - n_) * sizeof(T), s));
+        FGB_CUDA(cudaStreamSynchronize(s));
+        release();
+        p_ = q;
+        n_ = n;
+    }
     void release() {
         if (p_) cudaFree(p_);
         p_ = nullptr;

@@ -112,6 +112,13 @@ public:
     double time_spmv(int precision, int reps);
     void download_matrix(std::vector<double>& vals, std::vector<double>& rhs);
     cudaStream_t stream() const { return stream_; }
+    // device arrays of the assembled system (SELL-32 layout of the structure), for placing
+    // the system into a multi-mesh batch
+    const double* d_sell64() const { return sell64_.get(); }
+    const float* d_sell32() const { return sell32_.get(); }
+    const int32_t* d_sell_col() const { return sell_col_.get(); }
+    const float* d_dinv32() const { return dinv32_.get(); }
+    const double* d_rhs() const { return rhs_.get(); }
 
 private:
     void spmv64(const double* x, double* y);

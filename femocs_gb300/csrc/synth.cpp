@@ -77,6 +77,56 @@ bool inside_metal(const NanotipSpec& s, double x, double y, double z) {
     return r2 + dz * dz <= R2;
 }
 
+namespace {
+void nanotip_axes(const NanotipSpec& s, std::vector<double>& ax, std::vector<double>& az) {
+    const double cx = s.radius + s.margin;
+    ax = graded_axis(-s.box_half, -cx, cx, s.box_half, s.h, s.growth);
+    az.clear();
+    std::vector<double> up = graded_axis(0.0, 0.0, s.height + s.margin, s.top, s.h, s.growth);
+    std::vector<double> down = graded_axis(-s.slab, 0.0, 0.0 + s.h, s.h, s.h, s.growth);
+    for (double z : down)
+        if (z < 0.0) az.push_back(z);
+    az.insert(az.end(), up.begin(), up.end());
+}
+const int kKuhn[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {2, 1, 0}, {1, 0, 2}};
+}  // namespace
+
+long long nanotip_vacuum_hexes(const NanotipSpec& s) {
+    std::vector<double> ax, az;
+    nanotip_axes(s, ax, az);
+    const int nx = (int)ax.size(), nz = (int)az.size();
+    long long n = 0;
+    for (int k = 0; k + 1 < nz; ++k)
+        for (int j = 0; j + 1 < nx; ++j)
+            for (int i = 0; i + 1 < nx; ++i)
+                for (int p = 0; p < 6; ++p) {
+                    // centroid of the Kuhn tet: corner 000, +e_p0, +e_p0+e_p1, corner 111
+                    int c[3] = {0, 0, 0};
+                    double sx = ax[i] + ax[i + 1], sy = ax[j] + ax[j + 1], sz = az[k] + az[k + 1];
+                    for (int s2 = 0; s2 < 2; ++s2) {
+                        c[kKuhn[p][s2]] = 1;
+                        sx += ax[i + c[0]];
+                        sy += ax[j + c[1]];
+                        sz += az[k + c[2]];
+                    }
+                    if (!inside_metal(s, sx * 0.25, sy * 0.25, sz * 0.25)) n += 4;
+                }
+    return n;
+}
+
+double fit_nanotip_spacing(NanotipSpec s, long long target_hexes) {
+    FGB_REQUIRE(target_hexes > 0, "target hex count must be positive");
+    double lo = 0.05 * std::max(1.0, s.radius), hi = std::max(s.box_half, s.top);
+    for (int it = 0; it < 50; ++it) {
+        const double mid = std::sqrt(lo * hi);
+        s.h = mid;
+        if (nanotip_vacuum_hexes(s) > target_hexes) lo = mid;
+        else hi = mid;
+        if (hi / lo < 1.002) break;
+    }
+    return std::sqrt(lo * hi);
+}
+
 TetMesh make_nanotip_mesh(const NanotipSpec& s) {
     const double cx = s.radius + s.margin;
     std::vector<double> ax = graded_axis(-s.box_half, -cx, cx, s.box_half, s.h, s.growth);

@@ -27,6 +27,10 @@ bool inside_metal(const NanotipSpec& s, double x, double y, double z);
 // Graded tensor grid, each cell split into six tets along the main diagonal; tet marker
 // kVacuum if its centroid lies outside the metal, kBulk otherwise.
 TetMesh make_nanotip_mesh(const NanotipSpec& s);
+// vacuum hexahedra of the mesh make_nanotip_mesh would build (4 per vacuum tet)
+long long nanotip_vacuum_hexes(const NanotipSpec& s);
+// core spacing h for which the mesh has about target_hexes vacuum hexahedra
+double fit_nanotip_spacing(NanotipSpec s, long long target_hexes);
 
 struct AtomSet {
     std::vector<double> xyz;        // 3 * n

@@ -185,6 +185,50 @@ void fgb_device_free(void* p);
 int fgb_memcpy_htod(void* dst, const void* src, size_t bytes);
 int fgb_memcpy_dtoh(void* dst, const void* src, size_t bytes);
 
+/* vacuum hexahedra of the synthetic nanotip mesh of `spec`; the core spacing h that gives
+ * about target_hexes of them (spec's own h ignored); -1 on error */
+long long fgb_nanotip_vacuum_hexes(const FgbNanotip* spec);
+double fgb_nanotip_fit_spacing(const FgbNanotip* spec, double target_hexes);
+
+/* ============================================================ Part 3: batched solves
+ * Many meshes resident on one device in block-diagonal arrays, each solved by
+ * multigrid-preconditioned FP64 CG with its own scalars; one CUDA graph launch advances
+ * every admitted mesh. Meshes are added (admission by free device memory), solves are
+ * admitted with an applied field (Neumann value -E0 on the top, phi = 0 on the metal, warm
+ * start from the mesh's previous solution), stepped and collected. */
+typedef struct FGB_BATCH FGB_BATCH;
+/* use_graph: capture the iteration in a CUDA graph with a WHILE node (0: host loop);
+ * autotune: time threads-per-row variants per level; grid_ctas: 0 = 8 per SM */
+FGB_BATCH* fgb_batch_create(int use_graph, int autotune, int grid_ctas);
+void fgb_batch_free(FGB_BATCH* b);
+/* slot >= 0; -1 when the free device memory minus hbm_reserve bytes does not admit the
+ * mesh; INT32_MIN on error */
+int fgb_batch_add_mesh(FGB_BATCH* b, const FGB_MESH* m, double hbm_reserve);
+/* build n synthetic nanotip meshes on n_threads host threads (0: all cores) and add them;
+ * slots[i] as fgb_batch_add_mesh */
+int fgb_batch_add_synthetic(FGB_BATCH* b, int n, const FgbNanotip* specs, int n_threads, double hbm_reserve, int* slots);
+int fgb_batch_remove_mesh(FGB_BATCH* b, int slot);
+int fgb_batch_admit(FGB_BATCH* b, int slot, double E0, double rel_tol, int max_iter);
+/* at most max_iters iterations of every admitted mesh; returns how many are still running */
+int fgb_batch_step(FGB_BATCH* b, int max_iters);
+/* finished solves since the last call: slots[k], res4 = iterations, status (1 converged,
+ * -1 iteration cap, -2 breakdown), relative residual, |b|; returns the count */
+int fgb_batch_collect(FGB_BATCH* b, int cap, int* slots, double* res4);
+/* nodal phi/E recovery (+ smoothing) and device-pointer interpolation on the slot's stream */
+int fgb_batch_extract(FGB_BATCH* b, int slot, int smoothen);
+int fgb_batch_interpolate(FGB_BATCH* b, int slot, int n, const double* d_xyz, int rank, int* d_cells, double* d_out5);
+int fgb_batch_sync_slot(FGB_BATCH* b, int slot);
+int fgb_batch_export_phi_nodes(FGB_BATCH* b, int slot, double* phi_nodes);
+int fgb_batch_export_nodal(FGB_BATCH* b, int slot, double* sol5_nodes);
+int fgb_batch_reset_solution(FGB_BATCH* b, int slot);
+/* ||b - A x|| / ||b|| in FP64 for the slot's current solution */
+int fgb_batch_true_residual(FGB_BATCH* b, int slot, double* out);
+int fgb_batch_info(FGB_BATCH* b, int slot, int64_t* out4); /* n_dofs, n_nodes, levels, 0 */
+/* total dofs, device bytes, iterations of the last step, kernels per iteration, graph
+ * launches, slots */
+int fgb_batch_stats(FGB_BATCH* b, double* out6);
+int fgb_batch_tuning(FGB_BATCH* b, char* buf, int cap);
+
 #ifdef __cplusplus
 }
 #endif
