@@ -493,3 +493,99 @@ def batch_specs(n, seed=2024, lo_hexes=2e4, hi_hexes=8e5, n_threads=0):
         specs.append(s)
         fields.append(rng.uniform(0.05, 0.3))
     return specs, np.array(fields)
+
+
+class Server:
+    """Serving loop over a Batch: MD runs with resident meshes and atoms submit field solves
+    (Gaussian atom step on the device, warm-started solve, nodal field, interpolation at the
+    atoms); a scheduler thread batches them continuously."""
+
+    def __init__(self, batch: Batch, rel_tol=1e-9, max_iter=500, iters_per_launch=4, rank=1, smoothen=True,
+                 hbm_reserve=2e9):
+        self.batch = batch
+        self.h = load().fgb_server_create(batch.h, float(rel_tol), int(max_iter), int(iters_per_launch), int(rank),
+                                          int(smoothen), float(hbm_reserve))
+        if not self.h:
+            raise RuntimeError("server creation failed: " + last_error())
+        self._meshes = []
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().fgb_server_free(self.h)
+            self.h = None
+
+    def _ok(self, rc):
+        if rc != 0:
+            raise RuntimeError(last_error())
+
+    def add_run(self, mesh: Mesh, xyz, seed=1):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        rid = load().fgb_server_add_run(self.h, mesh.h, ptr(xyz), len(xyz) // 3, int(seed))
+        if rid == -(2 ** 31):
+            raise RuntimeError(last_error())
+        self._meshes.append(mesh)
+        return rid
+
+    def add_synthetic_runs(self, specs, n_atoms, seed=1, n_threads=0):
+        arr = (FgbNanotip * len(specs))(*[nanotip(**s) for s in specs])
+        self._ok(load().fgb_server_add_synthetic_runs(self.h, len(specs), arr, int(n_atoms), int(seed), int(n_threads)))
+
+    def place_pending(self, n_threads=0):
+        n = load().fgb_server_place_pending(self.h, int(n_threads))
+        if n == -(2 ** 31):
+            raise RuntimeError(last_error())
+        return n
+
+    def submit(self, run, E0, sigma=0.02):
+        rid = load().fgb_server_submit(self.h, int(run), float(E0), float(sigma))
+        if rid < 0:
+            raise RuntimeError(last_error())
+        return rid
+
+    def start(self):
+        self._ok(load().fgb_server_start(self.h))
+
+    def stop(self):
+        self._ok(load().fgb_server_stop(self.h))
+
+    def drain(self, timeout=600.0):
+        rc = load().fgb_server_drain(self.h, float(timeout))
+        if rc < 0:
+            raise RuntimeError(last_error())
+        return rc == 0
+
+    def run_poisson(self, rate, n, base_fields, sigma=0.02, seed=7):
+        bf = np.ascontiguousarray(base_fields, dtype=np.float64)
+        self._ok(load().fgb_server_run_poisson(self.h, float(rate), int(n), float(sigma), int(seed), ptr(bf)))
+
+    def records(self, cap=1 << 20):
+        out = np.zeros(10 * cap)
+        n = load().fgb_server_records(self.h, cap, ptr(out))
+        if n == -(2 ** 31):
+            raise RuntimeError(last_error())
+        a = out[:10 * n].reshape(-1, 10)
+        keys = ["id", "run", "E0", "iterations", "status", "rel_residual", "t_submit", "t_admit", "t_solved", "t_done"]
+        return {k: a[:, i] for i, k in enumerate(keys)}
+
+    def clear_records(self):
+        self._ok(load().fgb_server_clear_records(self.h))
+
+    def run_info(self, run):
+        o = np.zeros(2, dtype=np.int64)
+        self._ok(load().fgb_server_run_info(self.h, int(run), ptr(o, i64p)))
+        return dict(slot=int(o[0]), n_atoms=int(o[1]))
+
+    def last_result(self, run):
+        n = self.run_info(run)["n_atoms"]
+        out = np.zeros(5 * n)
+        cells = np.zeros(n, dtype=np.int32)
+        self._ok(load().fgb_server_last_result(self.h, int(run), ptr(out), ptr(cells, ip)))
+        return cells, out.reshape(-1, 5)
+
+    def reset_run(self, run):
+        self._ok(load().fgb_server_reset_run(self.h, int(run)))
+
+    def info(self):
+        o = np.zeros(4)
+        self._ok(load().fgb_server_info(self.h, ptr(o)))
+        return dict(runs=int(o[0]), solver_launches=int(o[1]), max_in_flight=int(o[2]))

@@ -104,6 +104,23 @@ _PROTOS = {
     "fgb_batch_info": (C.c_int, [vp, C.c_int, i64p]),
     "fgb_batch_stats": (C.c_int, [vp, dp]),
     "fgb_batch_tuning": (C.c_int, [vp, C.c_char_p, C.c_int]),
+    # Part 4: serving
+    "fgb_server_create": (vp, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]),
+    "fgb_server_free": (None, [vp]),
+    "fgb_server_add_run": (C.c_int, [vp, vp, dp, C.c_int, C.c_ulonglong]),
+    "fgb_server_add_synthetic_runs": (C.c_int, [vp, C.c_int, C.POINTER(FgbNanotip), C.c_int, C.c_ulonglong, C.c_int]),
+    "fgb_server_place_pending": (C.c_int, [vp, C.c_int]),
+    "fgb_server_submit": (C.c_longlong, [vp, C.c_int, C.c_double, C.c_double]),
+    "fgb_server_start": (C.c_int, [vp]),
+    "fgb_server_stop": (C.c_int, [vp]),
+    "fgb_server_drain": (C.c_int, [vp, C.c_double]),
+    "fgb_server_run_poisson": (C.c_int, [vp, C.c_double, C.c_int, C.c_double, C.c_ulonglong, dp]),
+    "fgb_server_records": (C.c_int, [vp, C.c_int, dp]),
+    "fgb_server_clear_records": (C.c_int, [vp]),
+    "fgb_server_last_result": (C.c_int, [vp, C.c_int, dp, ip]),
+    "fgb_server_reset_run": (C.c_int, [vp, C.c_int]),
+    "fgb_server_info": (C.c_int, [vp, dp]),
+    "fgb_server_run_info": (C.c_int, [vp, C.c_int, i64p]),
 }
 
 

@@ -8,6 +8,7 @@
 
 #include "batch.h"
 #include "facade.h"
+#include "server.h"
 #include "femocs_gb300.h"
 #include "synth.h"
 
@@ -21,6 +22,9 @@ struct FGB_MESH {
 };
 struct FGB_BATCH {
     std::unique_ptr<BatchSolver> b;
+};
+struct FGB_SERVER {
+    std::unique_ptr<FieldServer> s;
 };
 struct FGB_FIELD {
     ~FGB_FIELD() {
@@ -646,4 +650,148 @@ double fgb_nanotip_fit_spacing(const FgbNanotip* spec, double target_hexes) {
     double h = -1;
     guarded([&] { h = fit_nanotip_spacing(to_spec(spec), (long long)target_hexes); return 0; });
     return h;
+}
+
+// ---------------------------------------------------------------- Part 4: serving
+FGB_SERVER* fgb_server_create(FGB_BATCH* b, double rel_tol, int max_iter, int iters_per_launch, int rank, int smoothen,
+                              double hbm_reserve) {
+    FGB_SERVER* s = new FGB_SERVER;
+    const int rc = guarded([&] {
+        ServerOptions o;
+        o.rel_tol = rel_tol;
+        o.max_iter = max_iter;
+        o.iters_per_launch = std::max(1, iters_per_launch);
+        o.rank = rank;
+        o.smoothen = smoothen != 0;
+        o.hbm_reserve = std::max(0.0, hbm_reserve);
+        s->s.reset(new FieldServer(*b->b, o));
+        return 0;
+    });
+    if (rc) { delete s; return nullptr; }
+    return s;
+}
+void fgb_server_free(FGB_SERVER* s) { delete s; }
+
+int fgb_server_add_run(FGB_SERVER* s, const FGB_MESH* m, const double* xyz, int n_atoms, unsigned long long seed) {
+    int id = INT32_MIN;
+    const int rc = guarded([&] { id = s->s->add_run(m->pm, xyz, n_atoms, seed); return 0; });
+    return rc ? INT32_MIN : id;
+}
+
+int fgb_server_add_synthetic_runs(FGB_SERVER* s, int n, const FgbNanotip* specs, int n_atoms, unsigned long long seed,
+                                  int n_threads) {
+    return guarded([&] {
+        // meshes and atoms on host threads; atoms = the tip's surface atoms (every k-th when
+        // there are more than n_atoms) topped up with random vacuum probes
+        const int nt = std::max(1, std::min(n_threads > 0 ? n_threads : (int)std::thread::hardware_concurrency(), n));
+        std::vector<std::shared_ptr<PreparedMesh>> pms(n);
+        std::vector<std::vector<double>> pts(n);
+        std::vector<std::string> err(nt);
+        std::atomic<int> next{0};
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back([&, t] {
+                try {
+                    for (int i = next++; i < n; i = next++) {
+                        const NanotipSpec sp = to_spec(&specs[i]);
+                        pms[i] = std::make_shared<PreparedMesh>(prepare_mesh(make_nanotip_mesh(sp)));
+                        AtomSet at = make_nanotip_atoms(sp, 3.615, 0.05, 3.1, seed + 7919ull * i);
+                        std::vector<double> surf;
+                        for (size_t a = 0; a < at.type.size(); ++a)
+                            if (at.type[a] == kSurface)
+                                surf.insert(surf.end(), &at.xyz[3 * a], &at.xyz[3 * a] + 3);
+                        const size_t ns = surf.size() / 3;
+                        std::vector<double>& p = pts[i];
+                        if (ns >= (size_t)n_atoms) {
+                            for (int k = 0; k < n_atoms; ++k) {
+                                const size_t a = (size_t)k * ns / n_atoms;
+                                p.insert(p.end(), &surf[3 * a], &surf[3 * a] + 3);
+                            }
+                        } else {
+                            p = surf;
+                            std::vector<double> pr = make_vacuum_probes(sp, n_atoms - (int)ns, seed + 104729ull * i);
+                            p.insert(p.end(), pr.begin(), pr.end());
+                        }
+                    }
+                } catch (const std::exception& e) {
+                    err[t] = e.what();
+                }
+            });
+        for (auto& th : pool) th.join();
+        for (auto& e : err)
+            if (!e.empty()) throw Error(e);
+        for (int i = 0; i < n; ++i) s->s->add_run(pms[i], pts[i].data(), (int)(pts[i].size() / 3), seed + 31ull * i);
+        s->s->place_pending(n_threads);
+        return 0;
+    });
+}
+
+int fgb_server_place_pending(FGB_SERVER* s, int n_threads) {
+    int placed = INT32_MIN;
+    const int rc = guarded([&] { placed = s->s->place_pending(n_threads); return 0; });
+    return rc ? INT32_MIN : placed;
+}
+long long fgb_server_submit(FGB_SERVER* s, int run, double E0, double sigma) {
+    long long id = -1;
+    const int rc = guarded([&] { id = s->s->submit(run, E0, sigma); return 0; });
+    return rc ? -1 : id;
+}
+int fgb_server_start(FGB_SERVER* s) {
+    return guarded([&] { s->s->start(); return 0; });
+}
+int fgb_server_stop(FGB_SERVER* s) {
+    return guarded([&] { s->s->stop(); return 0; });
+}
+int fgb_server_drain(FGB_SERVER* s, double timeout_s) {
+    int ok = 0;
+    const int rc = guarded([&] { ok = s->s->drain(timeout_s) ? 1 : 0; return 0; });
+    return rc ? -1 : (ok ? 0 : 2);
+}
+int fgb_server_run_poisson(FGB_SERVER* s, double rate, int n, double sigma, unsigned long long seed,
+                           const double* base_fields) {
+    return guarded([&] {
+        std::vector<double> bf(base_fields, base_fields + s->s->n_runs());
+        s->s->run_poisson(rate, n, sigma, seed, bf);
+        return 0;
+    });
+}
+int fgb_server_records(FGB_SERVER* s, int cap, double* out10) {
+    int n = 0;
+    const int rc = guarded([&] {
+        auto rec = s->s->records();
+        for (auto& r : rec) {
+            if (n >= cap) break;
+            double* o = out10 + 10 * (size_t)n;
+            o[0] = (double)r.id; o[1] = r.run; o[2] = r.E0; o[3] = r.iterations; o[4] = r.status;
+            o[5] = r.rel_residual; o[6] = r.t_submit; o[7] = r.t_admit; o[8] = r.t_solved; o[9] = r.t_done;
+            ++n;
+        }
+        return 0;
+    });
+    return rc ? INT32_MIN : n;
+}
+int fgb_server_clear_records(FGB_SERVER* s) {
+    return guarded([&] { s->s->clear_records(); return 0; });
+}
+int fgb_server_last_result(FGB_SERVER* s, int run, double* out5, int* cells) {
+    return guarded([&] { s->s->last_result(run, out5, cells); return 0; });
+}
+int fgb_server_reset_run(FGB_SERVER* s, int run) {
+    return guarded([&] { s->s->reset_run(run); return 0; });
+}
+int fgb_server_info(FGB_SERVER* s, double* out4) {
+    return guarded([&] {
+        out4[0] = s->s->n_runs();
+        out4[1] = (double)s->s->admitted_launches();
+        out4[2] = s->s->max_in_flight();
+        out4[3] = 0;
+        return 0;
+    });
+}
+int fgb_server_run_info(FGB_SERVER* s, int run, int64_t* out2) {
+    return guarded([&] {
+        out2[0] = s->s->run_slot(run);
+        out2[1] = s->s->n_atoms(run);
+        return 0;
+    });
 }

@@ -229,6 +229,41 @@ int fgb_batch_info(FGB_BATCH* b, int slot, int64_t* out4); /* n_dofs, n_nodes, l
 int fgb_batch_stats(FGB_BATCH* b, double* out6);
 int fgb_batch_tuning(FGB_BATCH* b, char* buf, int cap);
 
+/* ============================================================ Part 4: serving
+ * Field solves requested by concurrent MD runs, each with a resident mesh (a batch slot),
+ * resident atoms and a result buffer. A request displaces the run's atoms by a Gaussian
+ * step on the device, re-solves warm-started from the run's previous phi with the given
+ * applied field, recovers the nodal field and interpolates E and phi at the atoms. One
+ * scheduler thread batches continuously: requests arriving while others are on the device
+ * join the next bounded solver launch; runs are admitted by free device memory. */
+typedef struct FGB_SERVER FGB_SERVER;
+FGB_SERVER* fgb_server_create(FGB_BATCH* b, double rel_tol, int max_iter, int iters_per_launch, int rank, int smoothen,
+                              double hbm_reserve);
+void fgb_server_free(FGB_SERVER* s);
+/* register a run (mesh placed by fgb_server_place_pending or later by the scheduler) */
+int fgb_server_add_run(FGB_SERVER* s, const FGB_MESH* m, const double* xyz, int n_atoms, unsigned long long seed);
+/* n synthetic runs: nanotip meshes of specs[i], n_atoms points each (surface atoms, topped
+ * up with vacuum probes), built on host threads and placed */
+int fgb_server_add_synthetic_runs(FGB_SERVER* s, int n, const FgbNanotip* specs, int n_atoms, unsigned long long seed,
+                                  int n_threads);
+int fgb_server_place_pending(FGB_SERVER* s, int n_threads); /* runs placed so far */
+long long fgb_server_submit(FGB_SERVER* s, int run, double E0, double sigma); /* request id, -1 on error */
+int fgb_server_start(FGB_SERVER* s);
+int fgb_server_stop(FGB_SERVER* s);
+int fgb_server_drain(FGB_SERVER* s, double timeout_s); /* 0 drained, 2 timed out */
+/* Poisson arrivals: n requests at `rate` per second on uniformly chosen runs, applied field
+ * base_fields[run] x (1 + 0.01 N(0,1)); returns when all have completed */
+int fgb_server_run_poisson(FGB_SERVER* s, double rate, int n, double sigma, unsigned long long seed,
+                           const double* base_fields);
+/* completed requests: id, run, E0, iterations, status, rel_residual, t_submit, t_admit,
+ * t_solved, t_done (seconds since the server was created); returns the count */
+int fgb_server_records(FGB_SERVER* s, int cap, double* out10);
+int fgb_server_clear_records(FGB_SERVER* s);
+int fgb_server_last_result(FGB_SERVER* s, int run, double* out5, int* cells);
+int fgb_server_reset_run(FGB_SERVER* s, int run); /* server stopped: zero warm start, initial atoms */
+int fgb_server_info(FGB_SERVER* s, double* out4);  /* runs, solver launches, max requests in flight, 0 */
+int fgb_server_run_info(FGB_SERVER* s, int run, int64_t* out2); /* slot (-1 pending), n_atoms */
+
 #ifdef __cplusplus
 }
 #endif
