@@ -353,6 +353,11 @@ def run_reference(args, world, rank):
     """The reference's CPU path (oracle port; the reference itself needs deal.II): per step,
     SSOR-PCG iterations on the assembled system plus the sequential location/interpolation
     of a sample of the points, scaled to the full solve and point count."""
+    if args.workload in ("batch", "serve"):
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference solves one mesh per process; "
+                              "its CPU arm is timed on the single-mesh workloads (config1, config2)"}), flush=True)
+        return
     if rank != 0:
         return
     import numpy as np
@@ -409,13 +414,187 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank):
+    """256 independent nanotip meshes (tip radius 1-6 nm, aspect 2-8, field 0.5-3 GV/m, Q1
+    meshes of 2e4-8e5 vacuum hexes, log-uniform) resident in one batch. One step = a cold
+    (zero start) solve of every mesh to 1e-9, all meshes in one graph-captured WHILE loop.
+    Plain FP64 Jacobi-CG single-mesh solves of a size-stratified sample give the baseline;
+    the batch solves the same sample alone for the like-for-like ratio."""
+    import numpy as np
+    import femocs_gb300 as fg
+    from femocs_gb300._lib import load
+
+    n_mesh = args.meshes or 256
+    specs, fields = fg.batch_specs(n_mesh, seed=2024)
+    b = fg.Batch()
+    t0 = time.perf_counter()
+    slots = [int(v) for v in b.add_synthetic(specs)]
+    build_s = time.perf_counter() - t0
+    if min(slots) < 0:
+        raise RuntimeError("device memory did not admit every mesh")
+    dofs = np.array([b.info(s)["n_dofs"] for s in slots])
+    total = int(dofs.sum())
+    req = {s: float(e) for s, e in zip(slots, fields)}
+
+    def step(sel):
+        for s_ in sel:
+            b.reset_solution(s_)
+        return b.solve_all({s_: req[s_] for s_ in sel}, rel_tol=REL_TOL, max_iter=1000)
+
+    for _ in range(args.warmup):
+        step(slots)
+    lib = load()
+    sampler = ClockSampler()
+    sampler.start()
+    launches0 = lib.fgb_kernel_launches()
+    b.mark(0)
+    results = [step(slots) for _ in range(args.steps)]
+    b.mark(1)
+    dev_ms = b.elapsed(0, 1)
+    launches = lib.fgb_kernel_launches() - launches0
+    clocks = sampler.stop(0)
+    res = results[-1]
+    its = np.array([res[s_]["iterations"] for s_ in slots])
+    conv = sum(res[s_]["status"] == 1 for s_ in slots)
+    ms_per_step = dev_ms / args.steps
+
+    # like-for-like: a size-stratified sample, plain FP64 Jacobi-CG one mesh at a time vs
+    # the same sample solved as one batch
+    order = np.argsort(dofs)
+    sample = [slots[k] for k in order[np.linspace(0, n_mesh - 1, min(args.sample, n_mesh)).astype(int)]]
+    b.mark(2)
+    step(sample)
+    b.mark(3)
+    batch_sample_ms = b.elapsed(2, 3)
+    plain_ms, plain_its = [], []
+    for s_ in sample:
+        m = fg.Mesh.synthetic(**specs[slots.index(s_)])
+        f = fg.Field(m)
+        f.setup(-req[s_])
+        f.assemble(True, False)
+        rc, st = f.solve(precision=0, rel_tol=REL_TOL, max_iter=100000)
+        plain_ms.append(st["ms"])
+        plain_its.append(st["iterations"])
+        del f, m
+    sample_dofs = int(sum(dofs[slots.index(s_)] for s_ in sample))
+    line = {
+        "metric": "solved DOF/s and p50/p99 solve latency at 1e-9 rel. residual vs plain FP64 CG",
+        "value": total * args.steps / (dev_ms * 1e-3), "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 CG / f32 multigrid preconditioner",
+        "data": "synthetic (seeded random nanotips)",
+        "config": {"workload": f"batch: {n_mesh} nanotips, radius 1-6 nm, aspect 2-8, field 0.5-3 GV/m, "
+                               "Q1 2e4-8e5 vacuum hexes log-uniform, one graph-captured launch",
+                   "n_meshes": n_mesh, "total_dofs": total, "rel_tol": REL_TOL,
+                   "l2": "inputs larger than L2 (level-0 matrices %.1f GB)" % (total * 25 * 12 / 1e9)},
+        "batch": {"solves_per_s": n_mesh * args.steps / (dev_ms * 1e-3), "converged": int(conv),
+                  "iterations_p50": float(np.median(its)), "iterations_max": int(its.max()),
+                  "dofs_min": int(dofs.min()), "dofs_max": int(dofs.max()), "build_s": build_s,
+                  "device_bytes": b.stats()["device_bytes"], "tuning": b.tuning(),
+                  "kernels_per_iteration": b.stats()["kernels_per_iteration"]},
+        "sample_vs_plain_fp64_cg": {"meshes": len(sample), "dofs": sample_dofs,
+                                    "batched_ms": batch_sample_ms, "plain_sequential_ms": float(sum(plain_ms)),
+                                    "plain_iterations_p50": float(np.median(plain_its)),
+                                    "solves_per_s_batched": len(sample) / (batch_sample_ms * 1e-3),
+                                    "solves_per_s_plain": len(sample) / (sum(plain_ms) * 1e-3),
+                                    "speedup": float(sum(plain_ms)) / batch_sample_ms},
+        "clocks": clocks, "gpu_launches": launches,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_serve(args, world, rank):
+    """64 concurrent MD runs (half the config-0 tip, half random batch-style tips), ~5e4
+    atoms each, resident; Poisson arrivals swept over rates; each request displaces its run's
+    atoms by N(0, 0.02 A), re-solves warm-started with an applied field within 1% of the
+    run's base field, recovers the nodal field and interpolates E and phi at the atoms, and
+    copies the result to the host. Latency = submit to result on the host."""
+    import numpy as np
+    import femocs_gb300 as fg
+    from femocs_gb300._lib import load
+
+    n_runs = args.runs or 64
+    rng = np.random.default_rng(99)
+    half = n_runs // 2
+    spec0 = dict(fg.CONFIG1)
+    rspecs, rfields = fg.batch_specs(n_runs - half, seed=4242)
+    specs = [spec0] * half + rspecs
+    base = np.r_[np.full(half, 0.1), rfields]
+    b = fg.Batch()
+    srv = fg.Server(b, rel_tol=REL_TOL, max_iter=1000, iters_per_launch=args.iters_per_launch, rank=RANK)
+    t0 = time.perf_counter()
+    srv.add_synthetic_runs(specs, n_atoms=args.atoms, seed=5)
+    build_s = time.perf_counter() - t0
+    dofs = np.array([b.info(srv.run_info(r)["slot"])["n_dofs"] for r in range(n_runs)])
+    srv.start()
+    # warm-up: every run solved once (cold), so the sweep sees warm-started MD steps
+    for r in range(n_runs):
+        srv.submit(r, float(base[r]), 0.02)
+    srv.drain(600)
+    lib = load()
+    sampler = ClockSampler()
+    sampler.start()
+    launches0 = lib.fgb_kernel_launches()
+    sweep = []
+    for rate in args.rates:
+        srv.clear_records()
+        n_req = int(max(20, rate * args.duration))
+        t_start = time.perf_counter()
+        srv.run_poisson(rate=rate, n=n_req, base_fields=base, sigma=0.02, seed=int(rate))
+        wall = time.perf_counter() - t_start
+        rec = srv.records()
+        lat = (rec["t_done"] - rec["t_submit"]) * 1e3
+        sweep.append({"rate": rate, "requests": n_req, "completed": int(len(lat)),
+                      "converged": int((rec["status"] == 1).sum()),
+                      "solves_per_s": len(lat) / (rec["t_done"].max() - rec["t_submit"].min()),
+                      "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                      "iterations_mean": float(rec["iterations"].mean()), "wall_s": wall})
+    launches = lib.fgb_kernel_launches() - launches0
+    clocks = sampler.stop(0)
+    srv.stop()
+    info = srv.info()
+    # plain FP64 Jacobi-CG: cold single-mesh solve latency of a few runs' meshes
+    plain = []
+    for r in [0, half, n_runs - 1]:
+        m = fg.Mesh.synthetic(**specs[r])
+        f = fg.Field(m)
+        f.setup(-float(base[r]))
+        f.assemble(True, False)
+        rc, st = f.solve(precision=0, rel_tol=REL_TOL, max_iter=100000)
+        plain.append({"run": r, "dofs": f.n_dofs, "ms": st["ms"], "iterations": st["iterations"]})
+        del f, m
+    best = max(sweep, key=lambda d: d["solves_per_s"])
+    line = {
+        "metric": "solves/s and p50/p99 latency at 1e-9 rel. residual (serving, Poisson arrivals)",
+        "value": best["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": len(args.rates),
+        "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 CG / f32 multigrid preconditioner", "data": "synthetic (seeded nanotips, FCC surface atoms)",
+        "config": {"workload": f"serve: {n_runs} MD runs ({half} config-0 tips, {n_runs - half} random tips), "
+                               f"{args.atoms} atoms each, sigma 0.02 A per step, Poisson arrivals",
+                   "total_dofs": int(dofs.sum()), "rates": args.rates, "iters_per_launch": args.iters_per_launch},
+        "sweep": sweep, "build_s": build_s, "max_requests_in_flight": info["max_in_flight"],
+        "solver_launches": info["solver_launches"], "plain_fp64_cg_cold_solves": plain,
+        "clocks": clocks, "gpu_launches": launches,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config2", "config1", "probe"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "config1", "probe", "batch", "serve"])
+    ap.add_argument("--meshes", type=int, default=0, help="batch: number of meshes (default 256)")
+    ap.add_argument("--sample", type=int, default=16, help="batch: meshes solved by plain CG for the ratio")
+    ap.add_argument("--runs", type=int, default=0, help="serve: MD runs (default 64)")
+    ap.add_argument("--atoms", type=int, default=50000, help="serve: atoms per run")
+    ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000])
+    ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
+    ap.add_argument("--iters-per-launch", type=int, default=4)
     ap.add_argument("--points", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
@@ -425,7 +604,12 @@ def main():
     else:
         from femocs_gb300.build import build
         build()
-        run_ours(args, world, rank)
+        if args.workload == "batch":
+            run_batch(args, world, rank)
+        elif args.workload == "serve":
+            run_serve(args, world, rank)
+        else:
+            run_ours(args, world, rank)
 
 
 if __name__ == "__main__":

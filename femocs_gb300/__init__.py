@@ -463,6 +463,15 @@ class Batch:
         self._ok(load().fgb_batch_tuning(self.h, buf, 1024))
         return buf.value.decode()
 
+    def mark(self, k):
+        self._ok(load().fgb_batch_mark(self.h, int(k)))
+
+    def elapsed(self, k0, k1):
+        ms = load().fgb_batch_elapsed(self.h, int(k0), int(k1))
+        if ms < 0:
+            raise RuntimeError(last_error())
+        return ms
+
 
 def nanotip_vacuum_hexes(spec_kw):
     """Vacuum hexahedra of the synthetic nanotip mesh of this spec (no mesh is built)."""

@@ -104,6 +104,8 @@ _PROTOS = {
     "fgb_batch_info": (C.c_int, [vp, C.c_int, i64p]),
     "fgb_batch_stats": (C.c_int, [vp, dp]),
     "fgb_batch_tuning": (C.c_int, [vp, C.c_char_p, C.c_int]),
+    "fgb_batch_mark": (C.c_int, [vp, C.c_int]),
+    "fgb_batch_elapsed": (C.c_double, [vp, C.c_int, C.c_int]),
     # Part 4: serving
     "fgb_server_create": (vp, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]),
     "fgb_server_free": (None, [vp]),

@@ -571,7 +571,23 @@ BatchSolver::BatchSolver(const BatchOptions& opt) : opt_(opt), d_(new Dev) {
     FGB_CUDA(cudaStreamSynchronize(stream_));
 }
 
+void BatchSolver::mark(int k) {
+    FGB_REQUIRE(k >= 0 && k < 8, "event index out of range");
+    if (!marks_[k]) FGB_CUDA(cudaEventCreate(&marks_[k]));
+    FGB_CUDA(cudaEventRecord(marks_[k], stream_));
+}
+
+float BatchSolver::elapsed_ms(int a, int b) {
+    FGB_REQUIRE(a >= 0 && a < 8 && b >= 0 && b < 8 && marks_[a] && marks_[b], "events not recorded");
+    FGB_CUDA(cudaEventSynchronize(marks_[b]));
+    float ms = 0;
+    FGB_CUDA(cudaEventElapsedTime(&ms, marks_[a], marks_[b]));
+    return ms;
+}
+
 BatchSolver::~BatchSolver() {
+    for (cudaEvent_t e : marks_)
+        if (e) cudaEventDestroy(e);
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
     for (auto& m : meshes_)
@@ -1043,7 +1059,13 @@ void BatchSolver::tune() {
     cudaEvent_t e0, e1;
     FGB_CUDA(cudaEventCreate(&e0));
     FGB_CUDA(cudaEventCreate(&e1));
-    BatchMeshState* st = d_->st.get();
+    // the timed kernels skip finished meshes: time them against a copy of the states with
+    // every mesh marked unfinished (the kernels timed here read the states only)
+    std::vector<BatchMeshState> hs(h_state_);
+    for (auto& x : hs) x.done = 0;
+    DBuf<BatchMeshState> tst;
+    tst.upload(hs, stream_);
+    BatchMeshState* st = tst.get();
     const int cands[] = {1, 4, 8, 16, 32};
     auto bucket_key = [](int kind, int l, long long rows, long long nnz) {
         const int lr = rows > 0 ? (int)std::log2((double)rows) : 0;
@@ -1131,6 +1153,7 @@ void BatchSolver::tune() {
             }
         }
     }
+    FGB_CUDA(cudaStreamSynchronize(stream_));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
 }
@@ -1139,13 +1162,21 @@ int BatchSolver::step(int max_iters) {
     std::lock_guard<std::mutex> lk(mu_);
     if (running_.empty()) return 0;
     ensure_capacity();
-    const bool relist = lists_dirty_;
-    if (lists_dirty_) rebuild_lists();
-    if (opt_.autotune && (dirty_ || relist)) {
+    if (opt_.autotune && dirty_) {
+        // the layout changed (meshes placed or levels added): tune the threads-per-row over
+        // every resident mesh, so that later admissions reuse the choice and the graph
         const std::vector<int> t0 = tpr_, p0 = p_tpr_, r0 = r_tpr_;
+        std::vector<int> active;
+        active.swap(running_);
+        for (size_t i = 0; i < meshes_.size(); ++i)
+            if (meshes_[i]) running_.push_back((int)i);
+        rebuild_lists();
         tune();
-        if (t0 != tpr_ || p0 != p_tpr_ || r0 != r_tpr_) dirty_ = true;
+        running_.swap(active);
+        lists_dirty_ = true;
+        (void)t0; (void)p0; (void)r0;
     }
+    if (lists_dirty_) rebuild_lists();
     int iters = 0;
     if (opt_.use_graph) {
         if (dirty_ || !exec_) {

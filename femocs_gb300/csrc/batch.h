@@ -121,6 +121,9 @@ public:
     long long launches() const { return launches_; }       // graph launches (or host loops)
     int last_iterations() const { return last_iters_; }    // iterations run by the last step
     int body_kernels() const { return body_kernels_; }     // kernels per iteration
+    // CUDA events on the solver stream (k < 8) and the device time between two of them
+    void mark(int k);
+    float elapsed_ms(int a, int b);
 
 private:
     struct Mesh;
@@ -156,6 +159,7 @@ private:
     std::map<long long, int> tune_cache_;  // size bucket -> threads per row
     std::vector<BatchMeshState> h_state_;
     int h_nrun_ = 0, body_kernels_ = 0, last_iters_ = 0;
+    cudaEvent_t marks_[8] = {};
 };
 
 }  // namespace fgb

@@ -629,6 +629,14 @@ int fgb_batch_stats(FGB_BATCH* b, double* out6) {
         return 0;
     });
 }
+int fgb_batch_mark(FGB_BATCH* b, int k) {
+    return guarded([&] { b->b->mark(k); return 0; });
+}
+double fgb_batch_elapsed(FGB_BATCH* b, int k0, int k1) {
+    double ms = -1;
+    guarded([&] { ms = b->b->elapsed_ms(k0, k1); return 0; });
+    return ms;
+}
 int fgb_batch_tuning(FGB_BATCH* b, char* buf, int cap) {
     return guarded([&] {
         const std::string d = b->b->tuning();

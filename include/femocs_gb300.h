@@ -228,6 +228,9 @@ int fgb_batch_info(FGB_BATCH* b, int slot, int64_t* out4); /* n_dofs, n_nodes, l
  * launches, slots */
 int fgb_batch_stats(FGB_BATCH* b, double* out6);
 int fgb_batch_tuning(FGB_BATCH* b, char* buf, int cap);
+/* CUDA event k (0..7) on the batch's solver stream; device ms between two events (-1 on error) */
+int fgb_batch_mark(FGB_BATCH* b, int k);
+double fgb_batch_elapsed(FGB_BATCH* b, int k0, int k1);
 
 /* ============================================================ Part 4: serving
  * Field solves requested by concurrent MD runs, each with a resident mesh (a batch slot),
