@@ -74,6 +74,13 @@ class Mesh:
             self._sizes = dict(zip(self.SIZE_NAMES, o[:8].tolist()))
         return self._sizes
 
+    def q2_sizes(self):
+        """Q2 structure built on the host: DoFs, nonzeros, top faces, longest row."""
+        o = np.zeros(4, dtype=np.int64)
+        if load().fgb_mesh_q2_sizes(self.h, ptr(o, i64p)) != 0:
+            raise RuntimeError(last_error())
+        return dict(n_dofs=int(o[0]), nnz=int(o[1]), n_top_faces=int(o[2]), max_row=int(o[3]))
+
     def export(self, name):
         s = self.sizes()
         shapes = {
@@ -98,9 +105,10 @@ class Mesh:
 class Field:
     """Device-resident Poisson system + interpolator of one mesh (PoissonSolver verbs)."""
 
-    def __init__(self, mesh: Mesh):
+    def __init__(self, mesh: Mesh, order=1):
         self.mesh = mesh
-        self.h = load().fgb_field_create(mesh.h)
+        self.order = order
+        self.h = load().fgb_field_create_order(mesh.h, int(order))
         if not self.h:
             raise RuntimeError("field creation failed: " + last_error())
         o = np.zeros(4, dtype=np.int64)
@@ -157,6 +165,13 @@ class Field:
         buf = C.create_string_buffer(4096)
         self._ok(load().fgb_field_amg_levels(self.h, buf, 4096))
         return buf.value.decode()
+
+    def q2_dofs(self):
+        """(cell, lattice index) holding every Q2 DoF."""
+        dc = np.zeros(self.n_dofs, dtype=np.int32)
+        dl = np.zeros(self.n_dofs, dtype=np.int32)
+        self._ok(load().fgb_field_q2_dofs(self.h, ptr(dc, ip), ptr(dl, ip)))
+        return dc, dl
 
     def extract(self, smoothen=True):
         self._ok(load().fgb_field_extract(self.h, int(smoothen)))

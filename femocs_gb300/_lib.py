@@ -57,6 +57,9 @@ _PROTOS = {
     "fgb_synth_atoms": (C.c_int64, [C.POINTER(FgbNanotip), C.c_double, C.c_double, C.c_double, C.c_uint64, dp, ip]),
     "fgb_synth_probes": (C.c_int64, [C.POINTER(FgbNanotip), C.c_int, C.c_uint64, dp]),
     "fgb_field_create": (vp, [vp]),
+    "fgb_field_create_order": (vp, [vp, C.c_int]),
+    "fgb_field_q2_dofs": (C.c_int, [vp, ip, ip]),
+    "fgb_mesh_q2_sizes": (C.c_int, [vp, i64p]),
     "fgb_field_free": (None, [vp]),
     "fgb_field_sizes": (C.c_int, [vp, i64p]),
     "fgb_field_setup": (C.c_int, [vp, C.c_double, C.c_double]),

@@ -1256,7 +1256,8 @@ void BatchSolver::export_phi_nodes(int slot, double* phi) {
                              m.stream));
     FGB_CUDA(cudaStreamSynchronize(m.stream));
     std::fill(phi, phi + m.n_nodes, 0.0);
-    for (int d = 0; d < m.n_dofs; ++d) phi[m.h_dof2node[d]] = x[d];
+    for (int d = 0; d < m.n_dofs; ++d)
+        if (m.h_dof2node[d] >= 0) phi[m.h_dof2node[d]] = x[d];
 }
 
 void BatchSolver::reset_solution(int slot) {

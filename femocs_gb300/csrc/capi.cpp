@@ -293,11 +293,12 @@ int64_t fgb_synth_probes(const FgbNanotip* spec, int n, uint64_t seed, double* x
 }
 
 // ---------------------------------------------------------------- Part 2: device field
-FGB_FIELD* fgb_field_create(const FGB_MESH* m) {
+FGB_FIELD* fgb_field_create(const FGB_MESH* m) { return fgb_field_create_order(m, 1); }
+FGB_FIELD* fgb_field_create_order(const FGB_MESH* m, int order) {
     FGB_FIELD* f = new FGB_FIELD;
     const int rc = guarded([&] {
         f->pm = m->pm;
-        f->owned.reset(new Field(f->pm));
+        f->owned.reset(new Field(f->pm, nullptr, order));
         f->f = f->owned.get();
         f->mesh = f->pm.get();
         return 0;
@@ -372,7 +373,8 @@ int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi) {
         FGB_CUDA(cudaStreamSynchronize(fem.stream()));
         const FemStructure& s = fem.structure();
         std::fill(phi, phi + f->mesh->hex.n_nodes(), 0.0);
-        for (int d = 0; d < s.n_dofs; ++d) phi[s.dof2node[d]] = x[d];
+        for (int d = 0; d < s.n_dofs; ++d)
+            if (s.dof2node[d] >= 0) phi[s.dof2node[d]] = x[d];  // Q2: only vertex DoFs sit on nodes
         return 0;
     });
 }
@@ -381,7 +383,21 @@ int fgb_field_import_phi_nodes(FGB_FIELD* f, const double* phi) {
         FemDevice& fem = f->f->fem();
         const FemStructure& s = fem.structure();
         std::vector<double> x(s.n_dofs);
-        for (int d = 0; d < s.n_dofs; ++d) x[d] = phi[s.dof2node[d]];
+        const PreparedMesh& pm = *f->mesh;
+        for (int d = 0; d < s.n_dofs; ++d) {
+            if (s.dof2node[d] >= 0) {
+                x[d] = phi[s.dof2node[d]];
+            } else {
+                // Q2 edge/face/interior DoF: the trilinear interpolant of the nodal values,
+                // i.e. the mean over the corners of its entity
+                int cr[8];
+                const int nk = q2_entity_corners(s.dof_local[d], cr);
+                const int hex = pm.vac.cells[s.dof_cell[d]];
+                double acc = 0.0;
+                for (int q = 0; q < nk; ++q) acc += phi[pm.hex.hexs[8 * (size_t)hex + cr[q]]];
+                x[d] = acc / nk;
+            }
+        }
         FGB_CUDA(cudaMemcpyAsync(fem.d_solution(), x.data(), sizeof(double) * x.size(), cudaMemcpyHostToDevice, fem.stream()));
         FGB_CUDA(cudaStreamSynchronize(fem.stream()));
         return 0;
@@ -437,11 +453,37 @@ int fgb_field_export_system(FGB_FIELD* f, int64_t* rowptr, int* col, double* val
         const FemStructure& s = fem.structure();
         std::vector<double> v, b;
         fem.download_matrix(v, b);
-        if (rowptr) std::memcpy(rowptr, s.rowptr.data(), sizeof(int64_t) * s.rowptr.size());
-        if (col) std::memcpy(col, s.col.data(), sizeof(int32_t) * s.col.size());
+        std::vector<int64_t> rp;
+        std::vector<int32_t> cl;
+        if (rowptr || col) fem.download_pattern(rp, cl);
+        if (rowptr) std::memcpy(rowptr, rp.data(), sizeof(int64_t) * rp.size());
+        if (col) std::memcpy(col, cl.data(), sizeof(int32_t) * cl.size());
         if (val) std::memcpy(val, v.data(), sizeof(double) * v.size());
         if (rhs) std::memcpy(rhs, b.data(), sizeof(double) * b.size());
         if (dof2node) std::memcpy(dof2node, s.dof2node.data(), sizeof(int32_t) * s.dof2node.size());
+        return 0;
+    });
+}
+int fgb_field_q2_dofs(FGB_FIELD* f, int* dof_cell, int* dof_local) {
+    return guarded([&] {
+        const FemStructure& s = f->f->fem().structure();
+        FGB_REQUIRE(s.order == 2, "not a Q2 field");
+        for (int d = 0; d < s.n_dofs; ++d) {
+            if (dof_cell) dof_cell[d] = s.dof_cell[d];
+            if (dof_local) dof_local[d] = s.dof_local[d];
+        }
+        return 0;
+    });
+}
+int fgb_mesh_q2_sizes(const FGB_MESH* m, int64_t* out4) {
+    return guarded([&] {
+        FemStructure s = build_q2_structure(*m->pm);
+        int mx = 0;
+        for (int v : s.row_len) mx = std::max(mx, v);
+        out4[0] = s.n_dofs;
+        out4[1] = s.nnz();
+        out4[2] = s.n_top_faces();
+        out4[3] = mx;
         return 0;
     });
 }

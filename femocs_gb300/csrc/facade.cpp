@@ -123,6 +123,8 @@ void FemocsFacade::read_params() {
     conf_.get("gpu_precision", prec);
     precision_ = prec == "fp64" ? 0 : (prec == "mixed" ? 1 : 2);
     conf_.get("gpu_use_abs_tol", use_abs_tol_);
+    conf_.get("gpu_element_order", element_order_);
+    FGB_REQUIRE(element_order_ == 1 || element_order_ == 2, "gpu_element_order must be 1 or 2");
     double lim[2];
     if (conf_.get("field_limit_min", lim[0])) field_min_ = lim[0];
     if (conf_.get("field_limit_max", lim[1])) field_max_ = lim[1];
@@ -152,7 +154,7 @@ int FemocsFacade::ensure_mesh() {
             mesh_ = std::make_shared<PreparedMesh>(prepare_mesh(read_gmsh(mf)));
         }
     }
-    field_.reset(new Field(mesh_));
+    field_.reset(new Field(mesh_, nullptr, element_order_));
     return 0;
 }
 

@@ -67,7 +67,7 @@ private:
     SolveStats last_;
     // parameters (reference defaults, src/Config.cpp:17-118)
     double E0_ = 0, V0_ = 0, cg_tol_abs_ = 1e-9, ssor_ = 1.2, rel_tol_ = 1e-9, inner_tol_ = 0.1;
-    int n_cg_ = 10000, rank_ = 1, precision_ = 2;
+    int n_cg_ = 10000, rank_ = 1, precision_ = 2, element_order_ = 1;
     bool smoothen_ = true, anode_dirichlet_ = false, use_abs_tol_ = false;
     double radius_ = 0, tip_height_ = 0, field_min_ = 0.1, field_max_ = 5.0;
 };

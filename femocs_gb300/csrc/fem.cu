@@ -15,10 +15,12 @@
 //   mixed precision    FP32 inner PCG inside FP64 iterative refinement; the true residual,
 //                      the refinement update and the boundary values stay FP64
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 
 #include "amg.h"
 #include "fem_device.h"
+#include "fem_q2.h"
 
 namespace fgb {
 
@@ -494,6 +496,16 @@ __global__ void __launch_bounds__(kBlock) k_pcg_rz(int n, const float* __restric
     }
 }
 
+__global__ void k_scale_mul(int n, double* __restrict__ a, const double* __restrict__ b, double s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] *= s * b[i];
+}
+
+__global__ void k_scale_copy64(int n, const double* __restrict__ a, double s, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = s * a[i];
+}
+
 // p = z + beta p
 __global__ void __launch_bounds__(kBlock) k_pcg_direction(int n, const float* __restrict__ z32, double* __restrict__ p,
                                                           const CgState* st) {
@@ -516,19 +528,31 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
     r2f_item_.upload(fs_.r2f_item, s);
     if (!fs_.top_faces.empty()) top_faces_.upload(fs_.top_faces, s);
     dof2node_.upload(fs_.dof2node, s);
-    rowptr_.upload(fs_.rowptr, s);
-    col_.upload(fs_.col, s);
+    if (fs_.order == 1) {
+        rowptr_.upload(fs_.rowptr, s);
+        col_.upload(fs_.col, s);
+        csr2sell_.upload(fs_.csr2sell, s);
+    } else {
+        row_len_.upload(fs_.row_len, s);
+        for (int v : fs_.row_len) max_row_ = std::max(max_row_, v);
+    }
     slice_ptr_.upload(fs_.slice_ptr, s);
     slice_len_.upload(fs_.slice_len, s);
     sell_col_.upload(fs_.sell_col, s);
-    csr2sell_.upload(fs_.csr2sell, s);
     bc_.upload(fs_.bc_kind, s);
-    std::vector<double> dxyz(3 * (size_t)n_);
-    for (int d = 0; d < n_; ++d)
-        for (int c = 0; c < 3; ++c) dxyz[3 * (size_t)d + c] = pm.hex.xyz[3 * (size_t)fs_.dof2node[d] + c];
-    dof_xyz_.upload(dxyz, s);
-    ke_.resize(64 * (size_t)nc_);
-    kval_.resize(fs_.nnz());
+    if (fs_.order == 1) {
+        std::vector<double> dxyz(3 * (size_t)n_);
+        for (int d = 0; d < n_; ++d)
+            for (int c = 0; c < 3; ++c) dxyz[3 * (size_t)d + c] = pm.hex.xyz[3 * (size_t)fs_.dof2node[d] + c];
+        dof_xyz_.upload(dxyz, s);
+        ke_.resize(64 * (size_t)nc_);
+        kval_.resize(fs_.nnz());
+    } else {
+        dof_xyz_.upload(fs_.dof_xyz, s);
+        ke_.resize(378 * (size_t)nc_);
+        kval_.resize(fs_.slice_ptr.back());  // saved matrix in the SELL layout
+        kval_.zero(s);
+    }
     sell64_.resize(fs_.slice_ptr.back());
     sell32_.resize(fs_.slice_ptr.back());
     sell64_.zero(s);
@@ -555,10 +579,12 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
     fs_.r2c_item.clear(); fs_.r2c_item.shrink_to_fit();
     fs_.csr2sell.clear(); fs_.csr2sell.shrink_to_fit();
     fs_.sell_col.clear(); fs_.sell_col.shrink_to_fit();
+    fs_.dof_xyz.clear(); fs_.dof_xyz.shrink_to_fit();
 }
 
 FemDevice::~FemDevice() {
     amg_.reset();
+    q1_.reset();
     if (h_state_) cudaFreeHost(h_state_);
     if (h_mixed_) cudaFreeHost(h_mixed_);
     cudaEventDestroy(ev0_);
@@ -583,6 +609,21 @@ void FemDevice::set_space_charge(const double* d_extra) {
 void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
     anode_dirichlet_ = anode_dirichlet;
     const int gb = grid_for(n_, kBlock);
+    if (fs_.order == 2) {
+        if (full_run) {
+            q2_cell_stiffness(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), stream_);
+            q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
+                             r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
+        }
+        const double bc = anode_dirichlet ? 0.0 : applied_field_;
+        q2_neumann_rows(n_, r2f_ptr_.get(), r2f_item_.get(), top_faces_.get(), dof_xyz_.get(), bc,
+                        has_extra_ ? rhs_extra_.get() : nullptr, rhs_.get(), stream_);
+        sell_dirichlet(n_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), kval_.get(), bc_.get(),
+                       anode_dirichlet ? 1 : 0, applied_potential_, sell64_.get(), sell32_.get(), dinv64_.get(),
+                       dinv32_.get(), rhs_.get(), x_.get(), stream_);
+        FGB_CUDA(cudaGetLastError());
+        return;
+    }
     if (full_run) {
         FGB_LAUNCH(k_cell_stiffness<<<grid_for(nc_, 128), 128, 0, stream_>>>(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get()));
         FGB_LAUNCH(k_assemble_rows<<<gb, kBlock, 0, stream_>>>(n_, rowptr_.get(), col_.get(), r2c_ptr_.get(), r2c_item_.get(),
@@ -639,6 +680,17 @@ double FemDevice::time_spmv(int precision, int reps) {
 void FemDevice::download_matrix(std::vector<double>& vals, std::vector<double>& rhs) {
     // CSR order values after Dirichlet elimination, gathered back from the SELL layout
     std::vector<double> s = sell64_.to_host(stream_);
+    if (fs_.order == 2) {
+        vals.resize(fs_.nnz());
+        int64_t k = 0;
+        for (int r = 0; r < n_; ++r) {
+            const int sl = r / 32, lane = r % 32;
+            for (int j = 0; j < fs_.row_len[r]; ++j)
+                vals[k++] = s[fs_.slice_ptr[sl] + ((int64_t)(j / 4) * 32 + lane) * 4 + j % 4];
+        }
+        rhs = rhs_.to_host(stream_);
+        return;
+    }
     std::vector<int64_t> c2s(fs_.nnz());
     // rebuild the CSR->SELL map on the host (kept only on the device after upload)
     for (int r = 0; r < n_; ++r) {
@@ -781,6 +833,10 @@ int FemDevice::solve_mixed(const SolveOptions& opt, SolveStats* st) {
 void FemDevice::ensure_amg(SolveStats* st) {
     const int anode = anode_dirichlet_ ? 1 : 0;
     if (amg_ && amg_anode_ == anode) return;
+    if (fs_.order == 2) {
+        build_q2_amg(anode, st);
+        return;
+    }
     std::vector<double> vals, rhs;
     download_matrix(vals, rhs);
     std::vector<int8_t> fixed(n_, 0);
@@ -791,6 +847,125 @@ void FemDevice::ensure_amg(SolveStats* st) {
     amg_->smoother_timer.enabled = profiling_;
     amg_anode_ = anode;
     if (st) st->setup_ms = h.setup_ms;
+}
+
+double FemDevice::estimate_lambda(int iters) {
+    // power iteration on D^-1 A from a fixed pseudo-random start, FP64 on the device
+    std::vector<double> h(n_);
+    uint64_t sd = 0x9e3779b97f4a7c15ull;
+    double nx = 0.0;
+    for (int i = 0; i < n_; ++i) {
+        sd = sd * 6364136223846793005ull + 1442695040888963407ull;
+        h[i] = (double)((sd >> 11) & 0xfffff) / 1048576.0 - 0.5;
+        nx += h[i] * h[i];
+    }
+    FGB_CUDA(cudaMemcpyAsync(p64_.get(), h.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, stream_));
+    nx = std::sqrt(nx);
+    const int gb = grid_for(n_, kBlock);
+    CgState* ds = state_.get() + 1;
+    double lam = 1.0;
+    for (int it = 0; it < iters; ++it) {
+        FGB_LAUNCH(k_sell_spmv<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                                   sell64_.get(), p64_.get(), q64_.get()));
+        FGB_LAUNCH(k_scale_mul<<<gb, kBlock, 0, stream_>>>(n_, q64_.get(), dinv64_.get(), 1.0));
+        FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, q64_.get(), partial_.get(), ds));
+        FGB_CUDA(cudaMemcpyAsync(h_state_ + 1, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        const double ny = std::sqrt(h_state_[1].rr);
+        if (!(ny > 0)) break;
+        lam = ny / nx;
+        FGB_LAUNCH(k_scale_copy64<<<gb, kBlock, 0, stream_>>>(n_, q64_.get(), 1.0 / ny, p64_.get()));
+        nx = 1.0;
+    }
+    return lam;
+}
+
+void FemDevice::build_q2_amg(int anode, SolveStats* st) {
+    const auto t0 = std::chrono::steady_clock::now();
+    // coarse operator: the Q1 system of the same mesh and boundary conditions (the Q2 space
+    // contains the Q1 space, P below is that embedding, so P^T A2 P equals the Q1 matrix up
+    // to the quadrature), with the Q1 hierarchy underneath
+    if (!q1_) q1_.reset(new FemDevice(*pm_, build_fem_structure(*pm_), stream_));
+    q1_->setup(applied_field_, applied_potential_);
+    q1_->assemble(true, anode != 0);
+    std::vector<double> v1, r1;
+    q1_->download_matrix(v1, r1);
+    const FemStructure& f1 = q1_->structure();
+    std::vector<int8_t> fixed1(f1.n_dofs, 0);
+    for (int d = 0; d < f1.n_dofs; ++d) fixed1[d] = f1.bc_kind[d] == 1 || (anode && f1.bc_kind[d] == 2);
+    AmgHost h1 = build_amg(*pm_, f1, v1, fixed1);
+    h1.levels[0].A.col = f1.col;
+    h1.levels[0].A.val = std::move(v1);
+    // embedding: a free Q2 DoF takes the mean of the free Q1 values at its entity's corners
+    CsrD P;
+    P.n_rows = n_;
+    P.n_cols = f1.n_dofs;
+    P.ptr.assign(n_ + 1, 0);
+    for (int d = 0; d < n_; ++d) {
+        const bool fixed = fs_.bc_kind[d] == 1 || (anode && fs_.bc_kind[d] == 2);
+        if (!fixed) {
+            int cr[8];
+            const int nk = q2_entity_corners(fs_.dof_local[d], cr);
+            const int hex = pm_->vac.cells[fs_.dof_cell[d]];
+            for (int q = 0; q < nk; ++q) {
+                const int v = f1.node2dof[pm_->hex.hexs[8 * (size_t)hex + cr[q]]];
+                if (v >= 0 && !fixed1[v]) {
+                    P.col.push_back(v);
+                    P.val.push_back(1.0 / nk);
+                }
+            }
+        }
+        P.ptr[d + 1] = (int64_t)P.col.size();
+    }
+    AmgHost h;
+    AmgHostLevel l0;
+    l0.A.n_rows = l0.A.n_cols = n_;
+    l0.A.ptr.assign(1, fs_.nnz());  // structure lives on the device; nnz for reporting
+    l0.lambda = estimate_lambda(15);
+    l0.R.n_rows = P.n_cols;
+    l0.R.n_cols = P.n_rows;
+    {
+        // R = P^T
+        l0.R.ptr.assign(P.n_cols + 1, 0);
+        for (int32_t c : P.col) l0.R.ptr[c + 1]++;
+        for (int i = 0; i < P.n_cols; ++i) l0.R.ptr[i + 1] += l0.R.ptr[i];
+        l0.R.col.resize(P.nnz());
+        l0.R.val.resize(P.nnz());
+        std::vector<int64_t> pos(l0.R.ptr.begin(), l0.R.ptr.end() - 1);
+        for (int i = 0; i < P.n_rows; ++i)
+            for (int64_t k = P.ptr[i]; k < P.ptr[i + 1]; ++k) {
+                const int64_t q = pos[P.col[k]]++;
+                l0.R.col[q] = i;
+                l0.R.val[q] = P.val[k];
+            }
+    }
+    l0.P = std::move(P);
+    h.levels.push_back(std::move(l0));
+    for (auto& lv : h1.levels) h.levels.push_back(std::move(lv));
+    h.coarse_inv = std::move(h1.coarse_inv);
+    h.n_coarse = h1.n_coarse;
+    amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
+                             dinv32_.get()));
+    amg_->smoother_timer.enabled = profiling_;
+    amg_anode_ = anode;
+    if (st) st->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void FemDevice::download_pattern(std::vector<int64_t>& rowptr, std::vector<int32_t>& col) {
+    if (fs_.order == 1) {
+        rowptr = fs_.rowptr;
+        col = fs_.col;
+        return;
+    }
+    std::vector<int32_t> sc = sell_col_.to_host(stream_);
+    rowptr.assign(n_ + 1, 0);
+    for (int r = 0; r < n_; ++r) rowptr[r + 1] = rowptr[r] + fs_.row_len[r];
+    col.resize(rowptr[n_]);
+    for (int r = 0; r < n_; ++r) {
+        const int sl = r / 32, lane = r % 32;
+        for (int j = 0; j < fs_.row_len[r]; ++j)
+            col[rowptr[r] + j] = sc[fs_.slice_ptr[sl] + ((int64_t)(j / 4) * 32 + lane) * 4 + j % 4];
+    }
 }
 
 std::string FemDevice::amg_levels() const { return amg_ ? amg_->describe() : std::string(); }

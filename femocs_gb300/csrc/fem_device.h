@@ -111,6 +111,9 @@ public:
     // measure: average device time of one SpMV (64 or 32 bit values) over `reps` launches
     double time_spmv(int precision, int reps);
     void download_matrix(std::vector<double>& vals, std::vector<double>& rhs);
+    // CSR pattern of the system (Q1: the host structure; Q2: read back from the SELL layout)
+    void download_pattern(std::vector<int64_t>& rowptr, std::vector<int32_t>& col);
+    int order() const { return fs_.order; }
     cudaStream_t stream() const { return stream_; }
     // device arrays of the assembled system (SELL-32 layout of the structure), for placing
     // the system into a multi-mesh batch
@@ -132,6 +135,9 @@ private:
     cudaStream_t stream_;
     std::unique_ptr<AmgDevice> amg_;
     int amg_anode_ = -1;
+    std::unique_ptr<FemDevice> q1_;   // Q2: the Q1 system of the same mesh, coarse level of the multigrid
+    void build_q2_amg(int anode, SolveStats* st);
+    double estimate_lambda(int iters);  // largest eigenvalue of D^-1 A (FP64 power iteration)
     bool profiling_ = false;
     LaunchTimer spmv_timer_;
     int n_, nc_;
@@ -140,12 +146,13 @@ private:
     // structure
     DBuf<int32_t> cell_dofs_, r2c_ptr_, r2c_item_, r2f_ptr_, r2f_item_, top_faces_, dof2node_;
     DBuf<int64_t> rowptr_, slice_ptr_, csr2sell_;
-    DBuf<int32_t> col_, slice_len_, sell_col_;
+    DBuf<int32_t> col_, slice_len_, sell_col_, row_len_;
+    int max_row_ = 0;
     DBuf<int8_t> bc_;
     DBuf<double> dof_xyz_;
     // values
-    DBuf<double> ke_;        // 64 per cell
-    DBuf<double> kval_;      // CSR values before Dirichlet (saved matrix)
+    DBuf<double> ke_;        // Q1: 64 per cell; Q2: 378 (packed upper triangle)
+    DBuf<double> kval_;      // values before Dirichlet (saved matrix): Q1 CSR order, Q2 SELL layout
     DBuf<double> sell64_;    // SELL values after Dirichlet
     DBuf<float> sell32_;
     DBuf<double> dinv64_;

@@ -1,0 +1,307 @@
+// Q2 (27-node hexahedron) assembly on the device (sm_103a); structure from fem_q2_setup.cpp.
+//
+//   k_q2_cell_stiffness  K_e[i][j] = sum_q w_q |det J_q| grad N_i . grad N_j over 3x3x3 Gauss
+//                        points on the trilinear (Q1) map of the hex, one warp per cell: lanes
+//                        0..26 own the quadrature points for the Jacobians and the nodes for
+//                        the physical gradients, every lane accumulates 11-12 of the 378
+//                        upper-triangle entries (FP64: ~47k FMA per cell, the FP64 pipe bounds it)
+//   k_q2_assemble_rows   row-owned gather of the element matrices into the saved SELL-layout
+//                        matrix, one warp per row: the row's columns in shared memory, one
+//                        cell at a time, lanes 0..26 place the cell's 27 contributions by binary
+//                        search (fixed order: deterministic)
+//   k_q2_neumann_rows    3x3 Gauss on the bilinear top faces, biquadratic face shape functions
+//   k_sell_dirichlet     symmetric elimination on the SELL layout (FP64 + FP32 copies, D^-1)
+// Lattice: node L = a + 3b + 9c at reference coordinates (a-1, b-1, c-1); 1-D quadratic
+// Lagrange l0(t) = t(t-1)/2, l1(t) = 1 - t^2, l2(t) = t(t+1)/2.
+#include <cmath>
+#include <mutex>
+
+#include "fem_q2.h"
+
+namespace fgb {
+
+namespace {
+
+constexpr int kQ2Warps = 4;  // warps (cells or rows) per 128-thread block
+
+__constant__ double c_q2_dN[27 * 27 * 3];   // [qp][node][dir] reference gradients
+__constant__ double c_q1_dN[27 * 8 * 3];    // [qp][corner][dir] trilinear-map gradients
+__constant__ double c_q2_w[27];             // tensor Gauss weights
+__constant__ unsigned char c_q2_ij[378 * 2];
+__constant__ int c_q2_corner[8];            // lattice index of femocs corner k
+
+const double kG3[3] = {-0.77459666924148337704, 0.0, 0.77459666924148337704};  // +-sqrt(3/5)
+const double kW3[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+const int kHx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+const int kHy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+const int kHz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+
+double l1d(int a, double t) { return a == 0 ? 0.5 * t * (t - 1.0) : (a == 1 ? 1.0 - t * t : 0.5 * t * (t + 1.0)); }
+double dl1d(int a, double t) { return a == 0 ? t - 0.5 : (a == 1 ? -2.0 * t : t + 0.5); }
+
+void upload_tables() {
+    static std::once_flag once;
+    static std::string err;
+    std::call_once(once, [] {
+        std::vector<double> dn(27 * 27 * 3), d1(27 * 8 * 3), w(27);
+        for (int q = 0; q < 27; ++q) {
+            const int qa = q % 3, qb = (q / 3) % 3, qc = q / 9;
+            const double x = kG3[qa], y = kG3[qb], z = kG3[qc];
+            w[q] = kW3[qa] * kW3[qb] * kW3[qc];
+            for (int L = 0; L < 27; ++L) {
+                const int a = L % 3, b = (L / 3) % 3, c = L / 9;
+                dn[(q * 27 + L) * 3 + 0] = dl1d(a, x) * l1d(b, y) * l1d(c, z);
+                dn[(q * 27 + L) * 3 + 1] = l1d(a, x) * dl1d(b, y) * l1d(c, z);
+                dn[(q * 27 + L) * 3 + 2] = l1d(a, x) * l1d(b, y) * dl1d(c, z);
+            }
+            for (int k = 0; k < 8; ++k) {
+                d1[(q * 8 + k) * 3 + 0] = 0.125 * kHx[k] * (1 + y * kHy[k]) * (1 + z * kHz[k]);
+                d1[(q * 8 + k) * 3 + 1] = 0.125 * (1 + x * kHx[k]) * kHy[k] * (1 + z * kHz[k]);
+                d1[(q * 8 + k) * 3 + 2] = 0.125 * (1 + x * kHx[k]) * (1 + y * kHy[k]) * kHz[k];
+            }
+        }
+        unsigned char ij[378 * 2];
+        int e = 0;
+        for (int i = 0; i < 27; ++i)
+            for (int j = i; j < 27; ++j, ++e) {
+                ij[2 * e] = (unsigned char)i;
+                ij[2 * e + 1] = (unsigned char)j;
+            }
+        int corner[8];
+        for (int k = 0; k < 8; ++k) corner[k] = (kHx[k] + 1) + 3 * (kHy[k] + 1) + 9 * (kHz[k] + 1);
+        cudaMemcpyToSymbol(c_q2_dN, dn.data(), sizeof(double) * dn.size());
+        cudaMemcpyToSymbol(c_q1_dN, d1.data(), sizeof(double) * d1.size());
+        cudaMemcpyToSymbol(c_q2_w, w.data(), sizeof(double) * w.size());
+        cudaMemcpyToSymbol(c_q2_ij, ij, sizeof(ij));
+        const cudaError_t rc = cudaMemcpyToSymbol(c_q2_corner, corner, sizeof(corner));
+        if (rc != cudaSuccess) err = cudaGetErrorString(rc);
+    });
+    if (!err.empty()) throw Error("Q2 tables: " + err);
+}
+
+// index of (i, j) in the packed upper triangle of a 27x27 symmetric matrix
+__device__ __forceinline__ int sym27(int i, int j) {
+    if (i > j) { const int t = i; i = j; j = t; }
+    return i * 27 - (i * (i - 1)) / 2 + (j - i);
+}
+
+__global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, const int32_t* __restrict__ cd,
+                                                                     const double* __restrict__ dxyz,
+                                                                     double* __restrict__ ke) {
+    __shared__ double sX[kQ2Warps][8][3];
+    __shared__ double sInv[kQ2Warps][27][10];  // J^-1 (row major) and w |det J| per point
+    __shared__ double sG[kQ2Warps][27][3];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kQ2Warps + wid;
+    if (c >= nc) return;  // whole warp leaves together
+    if (lane < 8) {
+        const int d = cd[27 * (size_t)c + c_q2_corner[lane]];
+        sX[wid][lane][0] = dxyz[3 * (size_t)d];
+        sX[wid][lane][1] = dxyz[3 * (size_t)d + 1];
+        sX[wid][lane][2] = dxyz[3 * (size_t)d + 2];
+    }
+    __syncwarp();
+    if (lane < 27) {
+        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int k = 0; k < 8; ++k)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) J[a][b] += sX[wid][k][a] * c_q1_dN[(lane * 8 + k) * 3 + b];
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const double id = 1.0 / det;
+        double* o = sInv[wid][lane];
+        o[0] = c00 * id;
+        o[3] = c01 * id;
+        o[6] = c02 * id;
+        o[1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        o[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        o[7] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        o[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        o[5] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        o[8] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+        o[9] = c_q2_w[lane] * fabs(det);
+    }
+    double acc[12];
+#pragma unroll
+    for (int t = 0; t < 12; ++t) acc[t] = 0.0;
+    for (int q = 0; q < 27; ++q) {
+        __syncwarp();
+        if (lane < 27) {
+            const double* inv = sInv[wid][q];
+            const double* g = c_q2_dN + (q * 27 + lane) * 3;
+            // physical gradient: (J^-T g)_a = sum_k inv[k][a] g_k
+#pragma unroll
+            for (int a = 0; a < 3; ++a) sG[wid][lane][a] = inv[a] * g[0] + inv[3 + a] * g[1] + inv[6 + a] * g[2];
+        }
+        __syncwarp();
+        const double w = sInv[wid][q][9];
+#pragma unroll
+        for (int t = 0; t < 12; ++t) {
+            const int e = lane + 32 * t;
+            if (e < 378) {
+                const int i = c_q2_ij[2 * e], j = c_q2_ij[2 * e + 1];
+                acc[t] += w * (sG[wid][i][0] * sG[wid][j][0] + sG[wid][i][1] * sG[wid][j][1] + sG[wid][i][2] * sG[wid][j][2]);
+            }
+        }
+    }
+    double* o = ke + 378 * (size_t)c;
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+        const int e = lane + 32 * t;
+        if (e < 378) o[e] = acc[t];
+    }
+}
+
+__global__ void __launch_bounds__(32 * kQ2Warps) k_q2_assemble_rows(int n, int max_len, const int64_t* __restrict__ sptr,
+                                                                    const int32_t* __restrict__ scol,
+                                                                    const int32_t* __restrict__ row_len,
+                                                                    const int32_t* __restrict__ r2c_ptr,
+                                                                    const int32_t* __restrict__ r2c_item,
+                                                                    const int32_t* __restrict__ cd,
+                                                                    const double* __restrict__ ke,
+                                                                    double* __restrict__ kval) {
+    extern __shared__ unsigned char q2_smem[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* vals = reinterpret_cast<double*>(q2_smem) + (size_t)wid * max_len;
+    int32_t* cols = reinterpret_cast<int32_t*>(reinterpret_cast<double*>(q2_smem) + (size_t)kQ2Warps * max_len) +
+                    (size_t)wid * max_len;
+    const int r = blockIdx.x * kQ2Warps + wid;
+    if (r >= n) return;  // whole warp leaves together
+    const int len = row_len[r];
+    const int64_t base = sptr[r >> 5] + (int64_t)(r & 31) * 4;
+    for (int j = lane; j < len; j += 32) {
+        cols[j] = scol[base + (int64_t)(j >> 2) * 128 + (j & 3)];
+        vals[j] = 0.0;
+    }
+    __syncwarp();
+    for (int p = r2c_ptr[r]; p < r2c_ptr[r + 1]; ++p) {
+        const int item = r2c_item[p];
+        const int c = item / 27, li = item - 27 * c;
+        if (lane < 27) {
+            const int cj = cd[27 * (size_t)c + lane];
+            int lo = 0, hi = len - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (cols[mid] < cj) lo = mid + 1; else hi = mid;
+            }
+            vals[lo] += ke[378 * (size_t)c + sym27(li, lane)];
+        }
+        __syncwarp();
+    }
+    for (int j = lane; j < len; j += 32) kval[base + (int64_t)(j >> 2) * 128 + (j & 3)] = vals[j];
+}
+
+__global__ void k_q2_neumann_rows(int n, const int32_t* __restrict__ r2f_ptr, const int32_t* __restrict__ r2f_item,
+                                  const int32_t* __restrict__ top, const double* __restrict__ dxyz, double bc,
+                                  const double* __restrict__ extra, double* __restrict__ rhs) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const double g3[3] = {-0.77459666924148337704, 0.0, 0.77459666924148337704};
+    const double w3[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+    double acc = 0.0;
+    for (int p = r2f_ptr[r]; p < r2f_ptr[r + 1]; ++p) {
+        const int f = r2f_item[p] / 9, q = r2f_item[p] - 9 * (r2f_item[p] / 9);
+        const int qu = q % 3, qv = q / 3;
+        // corners (u,v) = (0,0), (2,0), (2,2), (0,2) of the face lattice
+        const int cl[4] = {0, 2, 8, 6};
+        double P[4][3];
+        for (int k = 0; k < 4; ++k)
+            for (int a = 0; a < 3; ++a) P[k][a] = dxyz[3 * (size_t)top[9 * (size_t)f + cl[k]] + a];
+        for (int iv = 0; iv < 3; ++iv)
+            for (int iu = 0; iu < 3; ++iu) {
+                const double s = g3[iu], t = g3[iv];
+                const double lu = qu == 0 ? 0.5 * s * (s - 1.0) : (qu == 1 ? 1.0 - s * s : 0.5 * s * (s + 1.0));
+                const double lv = qv == 0 ? 0.5 * t * (t - 1.0) : (qv == 1 ? 1.0 - t * t : 0.5 * t * (t + 1.0));
+                double ds[3], dt[3];
+                for (int a = 0; a < 3; ++a) {
+                    ds[a] = 0.25 * (-(1 - t) * P[0][a] + (1 - t) * P[1][a] + (1 + t) * P[2][a] - (1 + t) * P[3][a]);
+                    dt[a] = 0.25 * (-(1 - s) * P[0][a] - (1 + s) * P[1][a] + (1 + s) * P[2][a] + (1 - s) * P[3][a]);
+                }
+                const double cx = ds[1] * dt[2] - ds[2] * dt[1], cy = ds[2] * dt[0] - ds[0] * dt[2],
+                             cz = ds[0] * dt[1] - ds[1] * dt[0];
+                acc += w3[iu] * w3[iv] * lu * lv * bc * sqrt(cx * cx + cy * cy + cz * cz);
+            }
+    }
+    if (extra) acc += extra[r];
+    rhs[r] = acc;
+}
+
+__device__ __forceinline__ bool fixed_kind(int8_t k, bool anode) { return k == 1 || (k == 2 && anode); }
+
+__global__ void k_sell_dirichlet(int n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+                                 const int32_t* __restrict__ row_len, const double* __restrict__ kval,
+                                 const int8_t* __restrict__ bc, int anode, double v0, double* __restrict__ s64,
+                                 float* __restrict__ s32, double* __restrict__ dinv64, float* __restrict__ dinv32,
+                                 double* __restrict__ rhs, double* __restrict__ x) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int len = row_len[r];
+    const int64_t base = sptr[r >> 5] + (int64_t)(r & 31) * 4;
+    auto pos = [&](int j) { return base + (int64_t)(j >> 2) * 128 + (j & 3); };
+    double diag = 1.0;
+    for (int j = 0; j < len; ++j)
+        if (scol[pos(j)] == r) diag = kval[pos(j)];
+    if (fixed_kind(bc[r], anode)) {
+        const double gr = bc[r] == 2 ? v0 : 0.0;
+        for (int j = 0; j < len; ++j) {
+            const int64_t q = pos(j);
+            const double a = scol[q] == r ? kval[q] : 0.0;
+            s64[q] = a;
+            s32[q] = (float)a;
+        }
+        rhs[r] = gr * diag;
+        x[r] = gr;
+    } else {
+        double acc = rhs[r];
+        for (int j = 0; j < len; ++j) {
+            const int64_t q = pos(j);
+            const int c = scol[q];
+            double a = kval[q];
+            if (fixed_kind(bc[c], anode)) {
+                acc -= a * (bc[c] == 2 ? v0 : 0.0);
+                a = 0.0;
+            }
+            s64[q] = a;
+            s32[q] = (float)a;
+        }
+        rhs[r] = acc;
+    }
+    dinv64[r] = 1.0 / diag;
+    dinv32[r] = (float)(1.0 / diag);
+}
+
+}  // namespace
+
+void q2_cell_stiffness(int nc, const int32_t* cd, const double* dxyz, double* ke, cudaStream_t s) {
+    upload_tables();
+    FGB_LAUNCH(k_q2_cell_stiffness<<<grid_for(nc, kQ2Warps), 32 * kQ2Warps, 0, s>>>(nc, cd, dxyz, ke));
+}
+
+void q2_assemble_rows(int n, int max_len, const int64_t* sptr, const int32_t* scol, const int32_t* row_len,
+                      const int32_t* r2c_ptr, const int32_t* r2c_item, const int32_t* cd, const double* ke, double* kval,
+                      cudaStream_t s) {
+    const size_t smem = (size_t)kQ2Warps * max_len * (sizeof(double) + sizeof(int32_t));
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(k_q2_assemble_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    FGB_REQUIRE(smem <= 200 * 1024, "Q2 rows too long for the shared-memory assembly");
+    FGB_LAUNCH(k_q2_assemble_rows<<<grid_for(n, kQ2Warps), 32 * kQ2Warps, smem, s>>>(n, max_len, sptr, scol, row_len,
+                                                                                    r2c_ptr, r2c_item, cd, ke, kval));
+}
+
+void q2_neumann_rows(int n, const int32_t* r2f_ptr, const int32_t* r2f_item, const int32_t* top, const double* dxyz,
+                     double bc, const double* extra, double* rhs, cudaStream_t s) {
+    FGB_LAUNCH(k_q2_neumann_rows<<<grid_for(n, 256), 256, 0, s>>>(n, r2f_ptr, r2f_item, top, dxyz, bc, extra, rhs));
+}
+
+void sell_dirichlet(int n, const int64_t* sptr, const int32_t* scol, const int32_t* row_len, const double* kval,
+                    const int8_t* bc, int anode, double v0, double* s64, float* s32, double* dinv64, float* dinv32,
+                    double* rhs, double* x, cudaStream_t s) {
+    FGB_LAUNCH(k_sell_dirichlet<<<grid_for(n, 256), 256, 0, s>>>(n, sptr, scol, row_len, kval, bc, anode, v0, s64, s32,
+                                                                 dinv64, dinv32, rhs, x));
+}
+
+}  // namespace fgb

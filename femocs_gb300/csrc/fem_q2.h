@@ -1,0 +1,23 @@
+// Launchers of the Q2 assembly kernels (fem_q2.cu); the structure is built by
+// build_q2_structure (fem_q2_setup.cpp).
+#pragma once
+
+#include "device.h"
+#include "fem.h"
+
+namespace fgb {
+
+// 378 packed upper-triangle entries per cell
+void q2_cell_stiffness(int nc, const int32_t* cell_dofs, const double* dof_xyz, double* ke, cudaStream_t s);
+// saved (pre-Dirichlet) matrix in the SELL layout of the structure
+void q2_assemble_rows(int n, int max_len, const int64_t* sptr, const int32_t* scol, const int32_t* row_len,
+                      const int32_t* r2c_ptr, const int32_t* r2c_item, const int32_t* cell_dofs, const double* ke,
+                      double* kval, cudaStream_t s);
+void q2_neumann_rows(int n, const int32_t* r2f_ptr, const int32_t* r2f_item, const int32_t* top, const double* dof_xyz,
+                     double bc, const double* extra, double* rhs, cudaStream_t s);
+// symmetric Dirichlet elimination on a SELL-layout matrix (any element order)
+void sell_dirichlet(int n, const int64_t* sptr, const int32_t* scol, const int32_t* row_len, const double* kval,
+                    const int8_t* bc, int anode, double v0, double* s64, float* s32, double* dinv64, float* dinv32,
+                    double* rhs, double* x, cudaStream_t s);
+
+}  // namespace fgb

@@ -1,0 +1,342 @@
+// Host construction of the Q2 (27-node hexahedron) structure on the vacuum hexes.
+//
+// The reference solves with Q1 elements only (DealSolver<3> builds FE_Q<3>(1), its Q2 path
+// is absent: include/DealSolver.h:130); this is the higher-order element of the same mesh,
+// same boundary marking (src/DealSolver.cpp:461-518) and same vertex hand-off to the
+// interpolator: a Q2 DoF sits on every vacuum vertex, hex edge, hex face and hex interior;
+// vertex DoFs carry phi at the mesh nodes. Numbering: Morton order of the DoF positions, then
+// windows of 256 rows by decreasing row length (as the Q1 structure).
+#include "fem.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <numeric>
+#include <parallel/algorithm>
+
+namespace fgb {
+
+namespace {
+
+const int kHx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+const int kHy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+const int kHz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+
+inline uint64_t spread3q(uint64_t v) {
+    v &= 0x1fffff;
+    v = (v | v << 32) & 0x1f00000000ffffull;
+    v = (v | v << 16) & 0x1f0000ff0000ffull;
+    v = (v | v << 8) & 0x100f00f00f00f00full;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+    v = (v | v << 2) & 0x1249249249249249ull;
+    return v;
+}
+
+// lattice corners of the entity that local node L belongs to (1, 2, 4 or 8 corners)
+int corners_of(int L, int out[8]) {
+    int a, b, c;
+    q2_lattice(L, a, b, c);
+    const int ra[2] = {a == 1 ? 0 : a, a == 1 ? 2 : a};
+    const int rb[2] = {b == 1 ? 0 : b, b == 1 ? 2 : b};
+    const int rc[2] = {c == 1 ? 0 : c, c == 1 ? 2 : c};
+    int n = 0;
+    for (int k = 0; k < (c == 1 ? 2 : 1); ++k)
+        for (int j = 0; j < (b == 1 ? 2 : 1); ++j)
+            for (int i = 0; i < (a == 1 ? 2 : 1); ++i) out[n++] = q2_corner_vertex(ra[i], rb[j], rc[k]);
+    return n;
+}
+
+struct EntityKey {
+    std::array<int32_t, 4> k;  // sorted global node ids of the entity's corners (unused: INT32_MAX)
+    int32_t cell;
+    int8_t local;
+    bool operator<(const EntityKey& o) const { return k != o.k ? k < o.k : cell < o.cell; }
+};
+
+}  // namespace
+
+int q2_entity_corners(int L, int out[8]) { return corners_of(L, out); }
+
+int q2_corner_vertex(int a, int b, int c) {
+    for (int k = 0; k < 8; ++k)
+        if (kHx[k] + 1 == a && kHy[k] + 1 == b && kHz[k] + 1 == c) return k;
+    return -1;
+}
+
+FemStructure build_q2_structure(const PreparedMesh& pm) {
+    FemStructure fs;
+    fs.order = 2;
+    fs.npc = 27;
+    fs.nfc = 9;
+    const int nc = (int)pm.vac.cells.size();
+    const int nvx = (int)pm.vac.vertex2node.size();
+    FGB_REQUIRE(nvx > 0 && nc > 0, "mesh has no vacuum hexahedra");
+    fs.n_cells = nc;
+    const std::vector<double>& X = pm.hex.xyz;
+    auto cell_node = [&](int c, int k) { return pm.hex.hexs[8 * (size_t)pm.vac.cells[c] + k]; };
+
+    // ---- entities: vertices by compact vertex index, edges/faces by sorted corner nodes,
+    // interiors by cell
+    std::vector<int32_t> ent(27 * (size_t)nc, -1);  // entity id per (cell, L)
+    std::vector<EntityKey> ek;
+    ek.reserve(18 * (size_t)nc);
+    for (int c = 0; c < nc; ++c)
+        for (int L = 0; L < 27; ++L) {
+            int cr[8];
+            const int n = corners_of(L, cr);
+            if (n == 1) {
+                ent[27 * (size_t)c + L] = pm.vac.node2vertex[cell_node(c, cr[0])];
+            } else if (n == 2 || n == 4) {
+                EntityKey e;
+                e.k = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MAX};
+                for (int q = 0; q < n; ++q) e.k[q] = cell_node(c, cr[q]);
+                std::sort(e.k.begin(), e.k.end());
+                e.cell = c;
+                e.local = (int8_t)L;
+                ek.push_back(e);
+            }
+        }
+    __gnu_parallel::sort(ek.begin(), ek.end());
+    int n_shared = 0;
+    std::vector<int32_t> face_count;  // occurrences of each face entity (boundary faces: 1)
+    std::vector<int32_t> ent_first;   // first (cell, L) of each shared entity
+    for (size_t i = 0; i < ek.size();) {
+        size_t j = i + 1;
+        while (j < ek.size() && ek[j].k == ek[i].k) ++j;
+        const int id = nvx + n_shared++;
+        for (size_t q = i; q < j; ++q) ent[27 * (size_t)ek[q].cell + ek[q].local] = id;
+        face_count.push_back(ek[i].k[2] == INT32_MAX ? 0 : (int32_t)(j - i));
+        ent_first.push_back(27 * ek[i].cell + ek[i].local);
+        i = j;
+    }
+    ek.clear();
+    ek.shrink_to_fit();
+    const int n_ent = nvx + n_shared + nc;
+    for (int c = 0; c < nc; ++c) ent[27 * (size_t)c + 13] = nvx + n_shared + c;
+    fs.n_dofs = n_ent;
+
+    // entity -> one (cell, L) and its position
+    std::vector<int32_t> e_cell(n_ent, -1);
+    std::vector<int8_t> e_loc(n_ent, 0);
+    for (int c = 0; c < nc; ++c)
+        for (int L = 0; L < 27; ++L) {
+            const int32_t e = ent[27 * (size_t)c + L];
+            if (e_cell[e] < 0) {
+                e_cell[e] = c;
+                e_loc[e] = (int8_t)L;
+            }
+        }
+    std::vector<double> exyz(3 * (size_t)n_ent);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < n_ent; ++e) {
+        int cr[8];
+        const int n = corners_of(e_loc[e], cr);
+        for (int d = 0; d < 3; ++d) {
+            double s = 0.0;
+            for (int q = 0; q < n; ++q) s += X[3 * (size_t)cell_node(e_cell[e], cr[q]) + d];
+            exyz[3 * (size_t)e + d] = s / n;
+        }
+    }
+
+    // entity -> cells
+    std::vector<int32_t> e2c_ptr(n_ent + 1, 0);
+    for (int32_t e : ent) e2c_ptr[e + 1]++;
+    for (int i = 0; i < n_ent; ++i) e2c_ptr[i + 1] += e2c_ptr[i];
+    std::vector<int32_t> e2c(e2c_ptr[n_ent]);
+    {
+        std::vector<int32_t> pos(e2c_ptr.begin(), e2c_ptr.end() - 1);
+        for (int c = 0; c < nc; ++c)
+            for (int L = 0; L < 27; ++L) e2c[pos[ent[27 * (size_t)c + L]]++] = 27 * c + L;
+    }
+    // row lengths (union of the DoFs of the incident cells)
+    auto row_set = [&](int e, std::vector<int32_t>& l) {
+        l.clear();
+        for (int p = e2c_ptr[e]; p < e2c_ptr[e + 1]; ++p) {
+            const int c = e2c[p] / 27;
+            for (int L = 0; L < 27; ++L) l.push_back(ent[27 * (size_t)c + L]);
+        }
+        std::sort(l.begin(), l.end());
+        l.erase(std::unique(l.begin(), l.end()), l.end());
+    };
+    std::vector<int32_t> deg(n_ent);
+#pragma omp parallel
+    {
+        std::vector<int32_t> l;
+#pragma omp for schedule(dynamic, 4096)
+        for (int e = 0; e < n_ent; ++e) {
+            row_set(e, l);
+            deg[e] = (int32_t)l.size();
+        }
+    }
+
+    // ---- numbering: Morton order, then windows of 256 by decreasing row length
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int e = 0; e < n_ent; ++e)
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = std::min(mn[d], exyz[3 * (size_t)e + d]);
+            mx[d] = std::max(mx[d], exyz[3 * (size_t)e + d]);
+        }
+    std::vector<std::pair<uint64_t, int32_t>> key(n_ent);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < n_ent; ++e) {
+        uint64_t code = 0;
+        for (int d = 0; d < 3; ++d) {
+            const double span = mx[d] > mn[d] ? mx[d] - mn[d] : 1.0;
+            const double t = (exyz[3 * (size_t)e + d] - mn[d]) / span;
+            const uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, std::floor(t * 2097151.0)));
+            code |= spread3q(q) << d;
+        }
+        key[e] = {code, e};
+    }
+    __gnu_parallel::sort(key.begin(), key.end());
+    std::vector<int32_t> dof2e(n_ent), e2dof(n_ent);
+    for (int i = 0; i < n_ent; ++i) dof2e[i] = key[i].second;
+    key.clear();
+    key.shrink_to_fit();
+    // Q2 rows range from 27 (interiors) to several hundred (tet vertices shared by many
+    // hexes); windows of 4096 keep SELL padding near 5 % (256: 44 %) while the gathers stay
+    // inside a 32 KB stretch of the vector
+    const int kWin = 4096;
+    for (int w0 = 0; w0 < n_ent; w0 += kWin) {
+        const int w1 = std::min(n_ent, w0 + kWin);
+        std::stable_sort(dof2e.begin() + w0, dof2e.begin() + w1, [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+    }
+    for (int d = 0; d < n_ent; ++d) e2dof[dof2e[d]] = d;
+
+    fs.cell_dofs.resize(27 * (size_t)nc);
+    for (size_t i = 0; i < ent.size(); ++i) fs.cell_dofs[i] = e2dof[ent[i]];
+    fs.dof2node.assign(n_ent, -1);
+    fs.node2dof.assign(pm.hex.n_nodes(), -1);
+    for (int v = 0; v < nvx; ++v) {
+        const int d = e2dof[v];
+        fs.dof2node[d] = pm.vac.vertex2node[v];
+        fs.node2dof[pm.vac.vertex2node[v]] = d;
+    }
+    fs.dof_xyz.resize(3 * (size_t)n_ent);
+    fs.dof_cell.resize(n_ent);
+    fs.dof_local.resize(n_ent);
+    fs.row_len.resize(n_ent);
+    for (int d = 0; d < n_ent; ++d) {
+        const int e = dof2e[d];
+        for (int k = 0; k < 3; ++k) fs.dof_xyz[3 * (size_t)d + k] = exyz[3 * (size_t)e + k];
+        fs.dof_cell[d] = e_cell[e];
+        fs.dof_local[d] = e_loc[e];
+        fs.row_len[d] = deg[e];
+    }
+    exyz.clear();
+    exyz.shrink_to_fit();
+
+    // row -> (cell, local), ascending cell
+    fs.r2c_ptr.assign(n_ent + 1, 0);
+    for (int d = 0; d < n_ent; ++d) fs.r2c_ptr[d + 1] = fs.r2c_ptr[d] + (e2c_ptr[dof2e[d] + 1] - e2c_ptr[dof2e[d]]);
+    fs.r2c_item.resize(fs.r2c_ptr[n_ent]);
+    for (int d = 0; d < n_ent; ++d) {
+        const int e = dof2e[d];
+        int32_t* o = &fs.r2c_item[fs.r2c_ptr[d]];
+        std::copy(e2c.begin() + e2c_ptr[e], e2c.begin() + e2c_ptr[e + 1], o);
+        std::sort(o, o + (e2c_ptr[e + 1] - e2c_ptr[e]));
+    }
+
+    // ---- SELL-32 with 4-wide row chunks, filled directly (second pass over the row sets)
+    const int C = 32, W4 = 4;
+    const int ns = (n_ent + C - 1) / C;
+    fs.slice_ptr.assign(ns + 1, 0);
+    fs.slice_len.assign(ns, 0);
+    int64_t nz = 0;
+    for (int s = 0; s < ns; ++s) {
+        int m = 0;
+        for (int r = s * C; r < std::min(n_ent, (s + 1) * C); ++r) {
+            m = std::max(m, fs.row_len[r]);
+            nz += fs.row_len[r];
+        }
+        m = (m + W4 - 1) / W4 * W4;
+        fs.slice_len[s] = m;
+        fs.slice_ptr[s + 1] = fs.slice_ptr[s] + (int64_t)m * C;
+    }
+    fs.n_entries = nz;
+    fs.sell_col.assign(fs.slice_ptr[ns], 0);
+#pragma omp parallel
+    {
+        std::vector<int32_t> l;
+#pragma omp for schedule(dynamic, 256)
+        for (int s = 0; s < ns; ++s)
+            for (int lane = 0; lane < C; ++lane) {
+                const int r = s * C + lane;
+                if (r < n_ent) {
+                    row_set(dof2e[r], l);
+                    for (int32_t& v : l) v = e2dof[v];
+                    std::sort(l.begin(), l.end());
+                }
+                for (int j = 0; j < fs.slice_len[s]; ++j) {
+                    const int64_t pos = fs.slice_ptr[s] + ((int64_t)(j / W4) * C + lane) * W4 + j % W4;
+                    fs.sell_col[pos] = (r < n_ent && j < (int)l.size()) ? l[j] : (r < n_ent ? r : 0);
+                }
+            }
+    }
+
+    // ---- boundary faces: face entities owned by one vacuum cell (src/DealSolver.cpp:461-518)
+    struct BF {
+        int32_t cell;
+        int8_t L;
+        double ctr[3];
+    };
+    std::vector<BF> bnd;
+    for (size_t i = 0; i < face_count.size(); ++i)
+        if (face_count[i] == 1) {
+            BF b;
+            b.cell = ent_first[i] / 27;
+            b.L = (int8_t)(ent_first[i] % 27);
+            const int d = e2dof[nvx + (int)i];
+            for (int k = 0; k < 3; ++k) b.ctr[k] = fs.dof_xyz[3 * (size_t)d + k];
+            bnd.push_back(b);
+        }
+    std::sort(bnd.begin(), bnd.end(), [](const BF& a, const BF& b) { return a.cell != b.cell ? a.cell < b.cell : a.L < b.L; });
+    double bmn[3] = {1e16, 1e16, 1e16}, bmx[3] = {-1e16, -1e16, -1e16};
+    for (const BF& b : bnd)
+        for (int k = 0; k < 3; ++k) {
+            bmn[k] = std::min(bmn[k], b.ctr[k]);
+            bmx[k] = std::max(bmx[k], b.ctr[k]);
+        }
+    const double eps = 1e-6;
+    fs.bc_kind.assign(n_ent, 0);
+    std::vector<int32_t> top;
+    for (const BF& b : bnd) {
+        const double x = b.ctr[0], y = b.ctr[1], z = b.ctr[2];
+        const bool side = std::fabs(x - bmn[0]) <= eps || std::fabs(x - bmx[0]) <= eps ||
+                          std::fabs(y - bmn[1]) <= eps || std::fabs(y - bmx[1]) <= eps;
+        if (side) continue;
+        // the 9 lattice nodes of the face: its fixed axis keeps the face node's value
+        int a0, b0, c0;
+        q2_lattice(b.L, a0, b0, c0);
+        int fd[9];
+        for (int v = 0; v < 3; ++v)
+            for (int u = 0; u < 3; ++u) {
+                int a = a0, bb = b0, c = c0;
+                if (a0 != 1) { bb = u; c = v; }        // face normal along a
+                else if (b0 != 1) { a = u; c = v; }    // normal along b
+                else { a = u; bb = v; }                // normal along c
+                fd[u + 3 * v] = fs.cell_dofs[27 * (size_t)b.cell + a + 3 * bb + 9 * c];
+            }
+        if (std::fabs(z - bmx[2]) <= eps) {
+            top.insert(top.end(), fd, fd + 9);
+        } else {
+            for (int q = 0; q < 9; ++q) fs.bc_kind[fd[q]] = 1;
+        }
+    }
+    fs.top_faces = top;
+    for (int32_t d : top)
+        if (fs.bc_kind[d] == 0) fs.bc_kind[d] = 2;
+    const int nt = fs.n_top_faces();
+    fs.r2f_ptr.assign(n_ent + 1, 0);
+    for (int32_t d : top) fs.r2f_ptr[d + 1]++;
+    for (int i = 0; i < n_ent; ++i) fs.r2f_ptr[i + 1] += fs.r2f_ptr[i];
+    fs.r2f_item.resize(fs.r2f_ptr[n_ent]);
+    {
+        std::vector<int32_t> pos(fs.r2f_ptr.begin(), fs.r2f_ptr.end() - 1);
+        for (int f = 0; f < nt; ++f)
+            for (int q = 0; q < 9; ++q) fs.r2f_item[pos[top[9 * (size_t)f + q]]++] = 9 * f + q;
+    }
+    return fs;
+}
+
+}  // namespace fgb

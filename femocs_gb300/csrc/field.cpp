@@ -2,7 +2,9 @@
 
 namespace fgb {
 
-Field::Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream) : pm_(std::move(pm)), stream_(stream) {
+Field::Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream, int order)
+    : pm_(std::move(pm)), stream_(stream) {
+    FGB_REQUIRE(order == 1 || order == 2, "element order must be 1 or 2");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         throw Error("no CUDA device available: the femocs_gb300 field path runs on the GPU only");
@@ -10,7 +12,7 @@ Field::Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream) : pm_(
         FGB_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
         own_stream_ = true;
     }
-    fem_.reset(new FemDevice(*pm_, build_fem_structure(*pm_), stream_));
+    fem_.reset(new FemDevice(*pm_, order == 2 ? build_q2_structure(*pm_) : build_fem_structure(*pm_), stream_));
     dm_.reset(new DeviceMesh(*pm_, stream_));
 }
 

@@ -12,7 +12,8 @@ namespace fgb {
 
 class Field {
 public:
-    explicit Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream = nullptr);
+    // order: 1 = Q1 elements (the reference's), 2 = Q2 (27-node hexahedra on the same mesh)
+    explicit Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream = nullptr, int order = 1);
     ~Field();
 
     const PreparedMesh& mesh() const { return *pm_; }

@@ -348,7 +348,7 @@ __global__ void k_interpolate(int n, Pts P, int rank, int from_tets, const int32
 __global__ void k_scatter_solution(int n_dofs, const double* __restrict__ phi, const double* __restrict__ charge,
                                    const int32_t* __restrict__ dof2node, double* __restrict__ sol) {
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= n_dofs) return;
+    if (d >= n_dofs || dof2node[d] < 0) return;  // Q2 edge/face/interior DoFs have no mesh node
     double* s = sol + 5 * (size_t)dof2node[d];
     s[0] = 0.0;
     s[1] = 0.0;

@@ -108,6 +108,13 @@ int64_t fgb_synth_probes(const FgbNanotip* spec, int n, uint64_t seed, double* x
 
 /* device field */
 FGB_FIELD* fgb_field_create(const FGB_MESH* m);
+/* element order 1 (Q1, the reference's element) or 2 (Q2: 27-node hexahedra on the same mesh;
+ * phi at the mesh vertices feeds the same interpolator) */
+FGB_FIELD* fgb_field_create_order(const FGB_MESH* m, int order);
+/* Q2 fields: for every DoF one vacuum cell holding it and its lattice index L = a + 3b + 9c */
+int fgb_field_q2_dofs(FGB_FIELD* f, int* dof_cell, int* dof_local);
+/* Q2 structure of a mesh built on the host only: DoFs, nonzeros, top faces, longest row */
+int fgb_mesh_q2_sizes(const FGB_MESH* m, int64_t* out4);
 void fgb_field_free(FGB_FIELD* f);
 int fgb_field_sizes(const FGB_FIELD* f, int64_t* out4); /* n_dofs, nnz, n_top_faces, sell_entries */
 /* PoissonSolver::setup(field, potential): applied_field is the Neumann value on the top

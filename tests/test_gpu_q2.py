@@ -1,0 +1,133 @@
+"""Q2 (27-node hexahedra) assembly and solves on the device against the independent numpy
+restatement (oracle/q2_oracle.py) and the C oracle's SSOR-CG on that system.
+
+Tolerances: matrix and rhs within 1e-12 relative (FP64 summation order differs); solutions
+within 2e3 x tol x max|phi| of the oracle's converged solution at relative residual tol; the
+flat-surface known answer (phi = E z is in the Q2 space) to 1e-8."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import femocs_gb300 as fg
+import oracle as orc
+from oracle.q2_oracle import Q2System, gpu_dof_keys
+
+pytestmark = pytest.mark.gpu
+SMALL = dict(radius=5.0, height=14.0, box_half=18.0, slab=4.0, top=40.0, h=4.0, growth=1.6, margin=3.0)
+FLAT = dict(radius=0.0, height=0.0, box_half=20.0, slab=4.0, top=40.0, h=6.0, growth=1.4, margin=0.0)
+E0 = 0.1
+
+
+@pytest.fixture(scope="module")
+def q2():
+    m = fg.Mesh.synthetic(**SMALL)
+    f = fg.Field(m, order=2)
+    dc, dl = f.q2_dofs()
+    keys = gpu_dof_keys(m, dc, dl)
+    return m, f, keys
+
+
+_cache = {}
+
+
+def oracle_system(m, anode=False, v0=0.0):
+    key = (id(m), anode, v0)
+    if key not in _cache:
+        _cache[key] = Q2System(m.export("node_xyz"), m.export("hex_nodes"), m.export("vac_cells"), -E0, anode, v0)
+    return _cache[key]
+
+
+def gpu_to_oracle(keys, s):
+    return np.array([s.keys[k] for k in keys])
+
+
+def test_q2_structure_sizes(q2):
+    m, f, keys = q2
+    s = oracle_system(m)
+    assert f.n_dofs == s.n and f.nnz == s.nnz_pattern
+    assert len(set(keys)) == f.n_dofs
+    assert m.q2_sizes()["n_dofs"] == f.n_dofs
+
+
+@pytest.mark.parametrize("anode", [False, True])
+def test_q2_system_matches_oracle(q2, anode):
+    m, f, keys = q2
+    f.setup(-E0, 2.0)
+    f.assemble(True, anode)
+    rowptr, col, val, rhs, d2n = f.system()
+    s = oracle_system(m, anode, 2.0)
+    g2o = gpu_to_oracle(keys, s)
+    A = sp.csr_matrix((val, col, rowptr), shape=(f.n_dofs, f.n_dofs)).tocoo()
+    P = sp.csr_matrix((A.data, (g2o[A.row], g2o[A.col])), shape=A.shape)
+    R = s.A.tocsr()
+    assert abs(P - R).max() <= 1e-12 * abs(R).max()
+    b = np.zeros(f.n_dofs)
+    b[g2o] = rhs
+    np.testing.assert_allclose(b, s.rhs, rtol=0, atol=1e-12 * np.abs(s.rhs).max())
+    # vertex DoFs sit on the mesh nodes
+    node_of_vertex = {d: n for d, n in enumerate(d2n) if n >= 0}
+    for d, n in list(node_of_vertex.items())[:200]:
+        assert keys[d] == (n,)
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_q2_solve_matches_oracle(q2, precision):
+    m, f, keys = q2
+    tol = 1e-10
+    f.setup(-E0)
+    f.assemble(True, False)
+    rc, st = f.solve(precision=precision, rel_tol=tol, max_iter=50000)
+    assert rc > 0 and st["status"] == 1
+    assert st["rel_residual"] <= tol * (1.05 if precision == 1 else 2.0)
+    s = oracle_system(m)
+    R = s.A.tocsr()
+    so = orc.System(csr=(R.indptr.astype(np.int64), R.indices.astype(np.int32), R.data, s.rhs))
+    it, x = so.ssor_cg(1.2, 1e-13 * np.linalg.norm(s.rhs), 100000)
+    assert it > 0
+    g2o = gpu_to_oracle(keys, s)
+    rowptr, col, val, rhs, d2n = f.system()
+    phi_dof = np.zeros(f.n_dofs)
+    phi_nodes = f.phi_nodes()
+    vert = d2n >= 0
+    phi_dof[vert] = phi_nodes[d2n[vert]]
+    assert np.abs(phi_dof[vert] - x[g2o[vert]]).max() <= 2e3 * tol * np.abs(x).max()
+    if precision == 2:
+        assert st["iterations"] <= 80 and st["levels"] >= 3
+
+
+def test_q2_flat_known_answer():
+    m = fg.Mesh.synthetic(**FLAT)
+    f = fg.Field(m, order=2)
+    f.setup(0.1)
+    f.assemble(True, False)
+    rc, st = f.solve(precision=2, rel_tol=1e-12)
+    assert rc > 0
+    xyz = m.export("node_xyz").reshape(-1, 3)
+    n2v = m.export("vac_node2vertex")
+    phi = f.phi_nodes()
+    vac = n2v >= 0
+    assert np.abs(phi[vac] - 0.1 * xyz[vac, 2]).max() < 1e-8
+    f.extract(smoothen=True)
+    E = f.nodal()[vac, :3]
+    assert np.abs(E[:, 2] + 0.1).max() < 1e-7 and np.abs(E[:, :2]).max() < 1e-7
+
+
+def test_q2_pipeline_against_q1(q2):
+    """Location does not depend on the element; phi at the vertices differs from the Q1
+    solution only by the discretisation error."""
+    m, f2, _ = q2
+    f1 = fg.Field(m, order=1)
+    for f in (f1, f2):
+        f.setup(-E0)
+        f.assemble(True, False)
+        rc, st = f.solve(precision=2, rel_tol=1e-10)
+        assert rc > 0
+        f.extract(smoothen=True)
+    atoms, types = fg.synth_atoms(SMALL, seed=4)
+    pts = np.ascontiguousarray(np.r_[atoms[types == 2], fg.synth_probes(SMALL, 1000, seed=2)])
+    c1, o1 = f1.interpolate(pts, rank=1)
+    c2, o2 = f2.interpolate(pts, rank=1)
+    np.testing.assert_array_equal(c1, c2)
+    scale = np.abs(o1[:, 4]).max()
+    d = np.abs(o2[:, 4] - o1[:, 4]).max()
+    assert 0 < d < 0.05 * scale

@@ -113,3 +113,15 @@ def test_config_parser_semantics(tmp_path):
     assert f.parse_double("field_ncg") == (0, 77.0)
     assert f.parse_double("hidden")[0] == 1
     assert f.parse_double("radius")[0] == 1  # after femocs_end
+
+
+def test_q2_structure_matches_independent_enumeration():
+    """Host Q2 structure (DoF count, sparsity) against the numpy restatement's own
+    enumeration of vertex/edge/face/interior entities on a small mesh."""
+    from oracle.q2_oracle import Q2System
+    spec = dict(radius=3.0, height=8.0, box_half=10.0, slab=3.0, top=20.0, h=3.0, growth=1.7, margin=2.0)
+    m = fg.Mesh.synthetic(**spec)
+    q = m.q2_sizes()
+    s = Q2System(m.export("node_xyz"), m.export("hex_nodes"), m.export("vac_cells"), -0.1)
+    assert q["n_dofs"] == s.n and q["nnz"] == s.nnz_pattern
+    assert q["n_top_faces"] > 0 and s.fixed.sum() > 0
