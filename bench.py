@@ -1,13 +1,15 @@
 #!/usr/bin/env python
 """Benchmark of the FEMOCS field-solve path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload config2|config1]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload config2|config1|probe|batch|serve] [--order 1|2]
 
 Workload (default `config2`): synthetic FCC-Cu nanotip, tip radius 5 nm, height 40 nm, on an
-80x80x4 nm slab, vacuum box up to 250 nm, graded tet mesh split into ~2.1e6 vacuum Q1
-hexahedra (~2.3e6 DoFs); applied field 1 GV/m (Neumann), phi = 0 on the metal; 1e6 query
-points = all surface atoms (coordination < 12) + uniform random vacuum probes. Q1 elements
-stand in for the configuration's Q2 elements (not provided).
+80x80x4 nm slab, vacuum box up to 250 nm, graded tet mesh split into ~2.1e6 vacuum hexahedra
+with Q2 (27-node) elements (~1.7e7 DoFs; `--order 1` gives the reference's Q1 elements,
+2.3e6 DoFs); applied field 1 GV/m (Neumann), phi = 0 on the metal; 1e6 query points = all
+surface atoms (coordination < 12) + uniform random vacuum probes. `config1` is the R = 2 nm
+tip with Q1 elements.
 
 One step = the reference's Femocs::run field path on resident data: full assembly (element
 matrices, CSR scatter, Neumann rhs, Dirichlet elimination), CG solve to a 1e-9 relative
@@ -44,16 +46,27 @@ N_POINTS = {"config2": 1_000_000, "config1": 100_000, "probe": 200_000}
 # running the oracle's restatement of the reference solve (oracle/femocs_oracle.c) to
 # convergence; the CPU baseline times iterations live and multiplies by this count.
 SSOR_ITERS = {"config1": 268, "config2": 617, "probe": 0}
+# Q2 needs 2.55x the SSOR(1.2)-PCG iterations of Q1 on the same mesh (oracle runs to 1e-9 on
+# two smaller meshes of this family: 151/59 and 270/106); the Q2 CPU baseline of config 2
+# uses 617 x 2.55
+Q2_SSOR_RATIO = 2.55
 # DRAM bytes (read + write) per row of one launch of the hot multigrid kernels, from ncu
 # captures of the probe workload (profiles/); a launch's traffic scales with its rows.
 KERNEL_TRAFFIC_PER_ROW = {}
 FALLBACK_HBM_GBS = 6800.0
 
 
+def element_order(args):
+    """config 2 is quoted with Q2 elements, config 1 with Q1 (the reference's element)"""
+    if args.order:
+        return args.order
+    return 2 if args.workload in ("config2", "probe") else 1
+
+
 def spec_of(workload):
     import femocs_gb300 as fg
     if workload == "probe":  # config-2 geometry on a coarser grid, small enough for full ncu captures
-        return dict(fg.CONFIG2, h=13.0, growth=1.22)
+        return dict(fg.CONFIG2, h=22.0, growth=1.3)
     return dict(fg.CONFIG2 if workload == "config2" else fg.CONFIG1)
 
 
@@ -67,7 +80,7 @@ def make_points(spec, n_points):
     return np.ascontiguousarray(np.r_[surf, probes][:n_points]), len(surf)
 
 
-def write_conf(path, spec, precision="amg"):
+def write_conf(path, spec, precision="amg", order=1):
     with open(path, "w") as f:
         f.write(f"""mesh_file synthetic
 radius {spec['radius']}
@@ -84,6 +97,7 @@ interpolation_rank {RANK}
 smoothen_field true
 gpu_precision {precision}
 gpu_rel_tol {REL_TOL}
+gpu_element_order {order}
 field_ncg 100000
 """)
 
@@ -175,10 +189,10 @@ def measured_hbm_peak():
 
 
 # ----------------------------------------------------------------------------------------
-def cpu_baseline(field, workload, n_points, pts, spec, budget_s=15.0):
+def cpu_baseline(field, workload, n_points, pts, spec, order=1, budget_s=15.0):
     """Oracle restatement of the reference CPU path on the host cores (1 thread, like the
-    reference default n_omp=1): SSOR(1.2)-PCG iterations on the same assembled system, and the
-    reference's sequential location + interpolation on a sample of the points."""
+    reference default n_omp=1): SSOR(1.2)-PCG iterations on the same assembled system (the
+    GPU's own matrix, Q1 or Q2), timed live and multiplied by the iteration count to 1e-9."""
     import numpy as np
     import oracle as orc
     rowptr, col, val, rhs, d2n = field.system()
@@ -187,11 +201,15 @@ def cpu_baseline(field, workload, n_points, pts, spec, budget_s=15.0):
     n_it = max(3, min(200, int(0.7 * budget_s / max(t_it / 2, 1e-6))))
     t = sysm.ssor_cg_fixed(n_it)
     t_iter = t / n_it
-    solve_s = t_iter * SSOR_ITERS[workload]
+    iters = SSOR_ITERS[workload] * (Q2_SSOR_RATIO if order == 2 else 1.0)
+    solve_s = t_iter * iters
+    how = ("count measured by a full oracle solve of the Q1 system" if order == 1 else
+           f"Q1 count {SSOR_ITERS[workload]} measured by a full oracle solve x Q2/Q1 ratio {Q2_SSOR_RATIO} "
+           "measured on two smaller meshes of this family")
     return dict(value=field.n_dofs / solve_s, unit="DOF/s", cores=1, kind="port",
                 sample=f"{n_it} SSOR(1.2)-PCG iterations of the oracle (reference deal.II CG+SSOR restated) on the "
-                       f"full {field.n_dofs}-DoF system, {t_iter * 1e3:.1f} ms/iteration x {SSOR_ITERS[workload]} "
-                       f"iterations to 1e-9 (count measured by a full oracle solve of this system); solve only")
+                       f"full {field.n_dofs}-DoF Q{order} system, {t_iter * 1e3:.1f} ms/iteration x {iters:.0f} "
+                       f"iterations to 1e-9 ({how}); solve only")
 
 
 def run_ours(args, world, rank):
@@ -200,11 +218,12 @@ def run_ours(args, world, rank):
     from femocs_gb300._lib import load
 
     spec = spec_of(args.workload)
+    order = element_order(args)
     n_points = args.points or N_POINTS[args.workload]
     pts, n_surf = make_points(spec, n_points)
     tmp = tempfile.mkdtemp(prefix="fgb_bench_")
     conf = os.path.join(tmp, "bench.in")
-    write_conf(conf, spec)
+    write_conf(conf, spec, order=order)
     fem = fg.Femocs(conf)
     if fem.run() != 0:
         raise RuntimeError("femocs_run failed: " + fg.last_error())
@@ -256,7 +275,9 @@ def run_ours(args, world, rank):
     # the same step with the plain FP64 Jacobi-PCG, and with FP32 Jacobi-PCG + FP64 refinement
     plain = [step(0) for _ in range(min(2, args.steps))]
     plain_ms = [s["ms"] for s in plain]
-    mixed = [step(1) for _ in range(min(2, args.steps))]
+    # the FP32-Jacobi/FP64-refinement solver needs ~1e4 iterations (80+ s) on the Q2 system:
+    # timed on Q1 workloads only
+    mixed = [step(1) for _ in range(min(2, args.steps))] if order == 1 else []
     mixed_ms = [s["ms"] for s in mixed]
 
     # end to end through the reference-facing C ABI with host buffers
@@ -309,7 +330,8 @@ def run_ours(args, world, rank):
         "dtype": "f64 CG / f32 multigrid preconditioner",
         "data": "synthetic (seeded nanotip mesh, FCC surface atoms, random vacuum probes)",
         "config": {"workload": f"{args.workload}: nanotip R={spec['radius'] / 10:g} nm H={spec['height'] / 10:g} nm, "
-                               f"box {2 * spec['box_half'] / 10:g} nm, top {spec['top'] / 10:g} nm, Q1",
+                               f"box {2 * spec['box_half'] / 10:g} nm, top {spec['top'] / 10:g} nm, Q{order}",
+                   "elements": f"Q{order}",
                    "n_dofs": n, "nnz": nnz, "n_points": n_points, "n_surface_atoms": n_surf,
                    "interpolation_rank": RANK, "rel_tol": REL_TOL,
                    "precision": "FP64 CG, FP32 multigrid V-cycle preconditioner",
@@ -323,9 +345,10 @@ def run_ours(args, world, rank):
                           "rel_residual": plain[-1]["rel_residual"],
                           "solved_dof_per_s": n / (statistics.median(plain_ms) * 1e-3),
                           "speedup_vs_plain": statistics.median(plain_ms) / statistics.median(solve_ms)},
-        "mixed_jacobi_cg": {"p50_ms": statistics.median(mixed_ms), "iterations": mixed[-1]["iterations"],
-                            "refinements": mixed[-1]["outer"], "kernel_ms": mixed[-1]["kernel_ms"],
-                            "rel_residual": mixed[-1]["rel_residual"]},
+        "mixed_jacobi_cg": ({"p50_ms": statistics.median(mixed_ms), "iterations": mixed[-1]["iterations"],
+                             "refinements": mixed[-1]["outer"], "kernel_ms": mixed[-1]["kernel_ms"],
+                             "rel_residual": mixed[-1]["rel_residual"]} if mixed else
+                            "not timed on Q2 (~1e4 iterations, 83 s per solve on config 2)"),
         "e2e": {"value": n * world / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": 24 * n_points,
                 "d2h_bytes_per_step": 36 * n_points,
                 "note": "femocs_run + femocs_interpolate_elfield through the C ABI, host arrays"},
@@ -344,7 +367,7 @@ def run_ours(args, world, rank):
         "timed_launch_range": [launches0, launches],
     }
     if rank == 0 and world == 1 and not args.no_cpu and SSOR_ITERS.get(args.workload):
-        line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec)
+        line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec, order)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -404,7 +427,8 @@ def run_reference(args, world, rank):
         "value": v, "unit": "DOF/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": args.workload, "n_dofs": n, "n_points": n_points},
+        "config": {"workload": args.workload, "n_dofs": n, "n_points": n_points,
+                   "elements": "Q1 (the reference's element; it has no Q2 path)"},
         "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": 1, "kind": "port",
                          "sample": f"per step: 10 SSOR(1.2)-PCG iterations x {SSOR_ITERS[args.workload]} to 1e-9, "
                                    f"assembly timed once ({t_assemble:.1f} s), sequential location+interpolation of "
@@ -596,6 +620,8 @@ def main():
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--iters-per-launch", type=int, default=4)
     ap.add_argument("--points", type=int, default=0)
+    ap.add_argument("--order", type=int, default=0, choices=[0, 1, 2],
+                    help="element order (default: 2 for config2/probe, 1 for config1)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
     world, rank, _ = dist_setup()

@@ -157,6 +157,10 @@ class Field:
         self._ok(load().fgb_field_last_stats(self.h, ptr(st)))
         return rc, _stats_dict(st)
 
+    def set_smoothing(self, degree=0, lo=0.0):
+        """Chebyshev degree and interval of the finest multigrid level (0: defaults)."""
+        self._ok(load().fgb_field_set_smoothing(self.h, int(degree), float(lo)))
+
     def set_profiling(self, on=True):
         """Record CUDA event pairs around the multigrid path's hot launches."""
         self._ok(load().fgb_field_set_profiling(self.h, int(on)))

@@ -21,7 +21,8 @@ namespace fgb {
 
 struct AmgDevLevel {
     int n = 0, n_coarse = 0;
-    double lambda = 1.0;
+    double lambda = 1.0, cheb_lo = 0.1;
+    int cheb_degree = 2;
     const int64_t* sptr = nullptr;
     const int32_t* slen = nullptr;
     const int32_t* scol = nullptr;
@@ -29,7 +30,7 @@ struct AmgDevLevel {
     const float* dinv = nullptr;
     // levels >= 1: CSR with `tpr` threads per row (level 0 uses the solver's SELL arrays)
     DBuf<int64_t> a_ptr;
-    DBuf<int32_t> a_col;
+    DBuf<int32_t> a_col, own_slen;
     DBuf<float> a_val, own_dinv;
     int tpr = 1, p_tpr = 1, r_tpr = 1;
     DBuf<int64_t> p_ptr, r_ptr;
@@ -200,6 +201,37 @@ __global__ void k_dense_solve(int n, const float* __restrict__ inv, const float*
     if (lane == 0) x[warp] = acc;
 }
 
+// SELL-32 with 4-wide row chunks (the level-0 layout) of a CSR level
+void sell4_of(const CsrD& A, std::vector<int64_t>& sptr, std::vector<int32_t>& slen, std::vector<int32_t>& scol,
+              std::vector<float>& val) {
+    const int n = A.n_rows, ns = (n + 31) / 32;
+    sptr.assign(ns + 1, 0);
+    slen.assign(ns, 0);
+    for (int s = 0; s < ns; ++s) {
+        int m = 0;
+        for (int r = s * 32; r < std::min(n, s * 32 + 32); ++r) m = std::max<int>(m, (int)(A.ptr[r + 1] - A.ptr[r]));
+        m = (m + 3) / 4 * 4;
+        slen[s] = m;
+        sptr[s + 1] = sptr[s] + (int64_t)m * 32;
+    }
+    scol.assign(sptr[ns], 0);
+    val.assign(sptr[ns], 0.f);
+    for (int s = 0; s < ns; ++s)
+        for (int lane = 0; lane < 32; ++lane) {
+            const int r = s * 32 + lane;
+            const int len = r < n ? (int)(A.ptr[r + 1] - A.ptr[r]) : 0;
+            for (int j = 0; j < slen[s]; ++j) {
+                const int64_t pos = sptr[s] + ((int64_t)(j / 4) * 32 + lane) * 4 + j % 4;
+                if (j < len) {
+                    scol[pos] = A.col[A.ptr[r] + j];
+                    val[pos] = (float)A.val[A.ptr[r] + j];
+                } else {
+                    scol[pos] = r < n ? r : 0;
+                }
+            }
+        }
+}
+
 void upload_csr32(const CsrD& M, DBuf<int64_t>& ptr, DBuf<int32_t>& col, DBuf<float>& val, cudaStream_t s) {
     ptr.upload(M.ptr, s);
     if (M.nnz() > 0) {
@@ -224,6 +256,8 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
         auto lv = std::make_unique<AmgDevLevel>();
         lv->n = hl.A.n_rows;
         lv->lambda = hl.lambda;
+        lv->cheb_degree = std::max(1, hl.cheb_degree);
+        lv->cheb_lo = hl.cheb_lo;
         if (l == 0) {
             lv->sptr = l0_sptr;
             lv->slen = l0_slen;
@@ -231,18 +265,34 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
             lv->val = l0_val;
             lv->dinv = l0_dinv;
         } else if (l < L - 1) {
-            upload_csr32(hl.A, lv->a_ptr, lv->a_col, lv->a_val, stream);
             std::vector<float> di(lv->n, 1.f);
             for (int i = 0; i < lv->n; ++i)
                 for (int64_t k = hl.A.ptr[i]; k < hl.A.ptr[i + 1]; ++k)
                     if (hl.A.col[k] == i) di[i] = (float)(1.0 / hl.A.val[k]);
             lv->own_dinv.upload(di, stream);
-            lv->sptr = lv->a_ptr.get();
-            lv->slen = nullptr;
+            lv->dinv = lv->own_dinv.get();
+            const double avg = (double)hl.A.nnz() / std::max(1, lv->n);
+            if (lv->n >= 32768 && avg <= 48.0) {
+                // large, moderately sparse level: the level-0 SELL layout, one thread per row
+                std::vector<int64_t> sp;
+                std::vector<int32_t> sl, sc;
+                std::vector<float> sv;
+                sell4_of(hl.A, sp, sl, sc, sv);
+                lv->a_ptr.upload(sp, stream);
+                lv->own_slen.upload(sl, stream);
+                lv->a_col.upload(sc, stream);
+                lv->a_val.upload(sv, stream);
+                lv->sptr = lv->a_ptr.get();
+                lv->slen = lv->own_slen.get();
+                lv->tpr = 0;
+            } else {
+                upload_csr32(hl.A, lv->a_ptr, lv->a_col, lv->a_val, stream);
+                lv->sptr = lv->a_ptr.get();
+                lv->slen = nullptr;
+                lv->tpr = tpr_for(avg);
+            }
             lv->scol = lv->a_col.get();
             lv->val = lv->a_val.get();
-            lv->dinv = lv->own_dinv.get();
-            lv->tpr = tpr_for((double)hl.A.nnz() / std::max(1, lv->n));
         }
         if (l == 0) lv->tpr = 0;
         if (l < L - 1) {
@@ -282,17 +332,33 @@ void AmgDevice::cycle(int l) {
         L.x = L.xb.get();
         return;
     }
-    const double lmax = 1.1 * L.lambda, lmin = 0.1 * L.lambda;
+    // Chebyshev on D^-1 A over [lo, 1.1] x lambda: step k uses d_k = c1_k d_{k-1} + c2_k D^-1 r,
+    // rho_0 = 1/sigma, rho_k = 1/(2 sigma - rho_{k-1}), c1_k = rho_k rho_{k-1}, c2_k = 2 rho_k / delta
+    const double lmax = 1.1 * L.lambda, lmin = L.cheb_lo * L.lambda;
     const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
-    const double rho0 = 1.0 / sigma, rho1 = 1.0 / (2.0 * sigma - rho0);
-    const float c1 = (float)(rho1 * rho0), c2 = (float)(2.0 * rho1 / delta), inv_theta = (float)(1.0 / theta);
+    const int deg = L.cheb_degree;
+    float c1[16], c2[16];
+    {
+        double rho = 1.0 / sigma;
+        for (int k = 1; k < deg && k < 16; ++k) {
+            const double rn = 1.0 / (2.0 * sigma - rho);
+            c1[k] = (float)(rn * rho);
+            c2[k] = (float)(2.0 * rn / delta);
+            rho = rn;
+        }
+    }
+    const float inv_theta = (float)(1.0 / theta);
     const Op A{L.n, L.sptr, L.slen, L.scol, L.val, L.dinv};
     LaunchTimer* tm = l == 0 ? &smoother_timer : nullptr;
-    // pre-smoothing from zero
-    FGB_LAUNCH(k_cheb_zero<<<g, kB, 0, stream_>>>(L.n, L.dinv, L.bin, L.xa.get(), L.d.get(), inv_theta));
-    if (tm) tm->begin(stream_);
-    FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, L.xa.get(), L.xb.get(), L.d.get(), c1, c2);
-    if (tm) tm->end(stream_);
+    // pre-smoothing from zero: iterate k writes buffer k; the buffers alternate so that the
+    // last one (k = deg-1) is xb
+    auto pre_buf = [&](int k) { return ((deg - 1 - k) % 2 == 0) ? L.xb.get() : L.xa.get(); };
+    FGB_LAUNCH(k_cheb_zero<<<g, kB, 0, stream_>>>(L.n, L.dinv, L.bin, pre_buf(0), L.d.get(), inv_theta));
+    for (int k = 1; k < deg; ++k) {
+        if (tm) tm->begin(stream_);
+        FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, pre_buf(k - 1), pre_buf(k), L.d.get(), c1[k], c2[k]);
+        if (tm) tm->end(stream_);
+    }
     // coarse-grid correction
     FGB_TPR_DISPATCH(k_residual, L.tpr, L.n, stream_, A, L.bin, L.xb.get(), L.r.get());
     AmgDevLevel& C = *lv_[l + 1];
@@ -301,14 +367,17 @@ void AmgDevice::cycle(int l) {
     cycle(l + 1);
     FGB_TPR_DISPATCH(k_csr_apply, L.p_tpr, L.n, stream_, L.n, L.p_ptr.get(), L.p_col.get(), L.p_val.get(), C.x,
                      L.xb.get(), 1);
-    // post-smoothing (same polynomial)
-    if (tm) tm->begin(stream_);
-    FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, L.xb.get(), L.xa.get(), L.d.get(), -1.f, inv_theta);
-    if (tm) tm->end(stream_);
-    if (tm) tm->begin(stream_);
-    FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, L.xa.get(), L.xb.get(), L.d.get(), c1, c2);
-    if (tm) tm->end(stream_);
-    L.x = L.xb.get();
+    // post-smoothing (same polynomial) from the corrected xb; even steps write xa, odd ones xb
+    float* xin = L.xb.get();
+    for (int k = 0; k < deg; ++k) {
+        float* xout = (k % 2 == 0) ? L.xa.get() : L.xb.get();
+        if (tm) tm->begin(stream_);
+        FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, xin, xout, L.d.get(), k == 0 ? -1.f : c1[k],
+                         k == 0 ? inv_theta : c2[k]);
+        if (tm) tm->end(stream_);
+        xin = xout;
+    }
+    L.x = xin;
 }
 
 double AmgDevice::time_smoother(int reps) {

@@ -28,6 +28,8 @@ struct AmgHostLevel {
     CsrD A;        // operator on this level
     CsrD P, R;     // prolongation to this level from the next coarser one, and its transpose
     double lambda = 1.0;  // estimate of the largest eigenvalue of D^-1 A
+    int cheb_degree = 3;  // Chebyshev smoothing steps before and after the coarse correction
+    double cheb_lo = 0.06; // smoothing interval [cheb_lo, 1.1] x lambda
 };
 
 struct AmgHost {

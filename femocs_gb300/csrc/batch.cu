@@ -5,8 +5,8 @@
 //                  per-mesh p.q -> alpha
 //   kb_update      NEW: r = b - q; RUNNING: x += alpha p, r -= alpha q; FP32 copy of r;
 //                  per-mesh r.r -> stop test
-//   kb_cheb_*      Chebyshev smoothing on D^-1 A scaled by 1/lambda_max of the mesh and level,
-//                  so one coefficient set serves every mesh
+//   kb_cheb_*      degree-3 Chebyshev smoothing on D^-1 A scaled by 1/lambda_max of the mesh
+//                  and level, so one coefficient set serves every mesh
 //   kb_residual, kb_csr_apply (restriction / prolongation), kb_dense (coarsest level)
 //   kb_rz          per-mesh r.z -> beta (0 and phase RUNNING after a NEW pass)
 //   kb_direction   p = z + beta p
@@ -120,15 +120,25 @@ namespace {
 
 constexpr int kB = kBatchRows;
 
-// Chebyshev coefficients on [0.1, 1.1] for D^-1 A scaled to lambda_max = 1
+// Chebyshev smoothing of degree kDeg on [0.06, 1.1] for D^-1 A scaled to lambda_max = 1:
+// step k: d_k = c1[k] d_{k-1} + c2[k] D^-1 r, rho_0 = 1/sigma, rho_k = 1/(2 sigma - rho_{k-1})
+constexpr int kDeg = 3;
 struct Cheb {
-    float c1, c2, inv_theta;
+    float c1[kDeg], c2[kDeg], inv_theta;
 };
 Cheb cheb_coefficients() {
-    const double lmax = 1.1, lmin = 0.1;
+    const double lmax = 1.1, lmin = 0.06;
     const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
-    const double rho0 = 1.0 / sigma, rho1 = 1.0 / (2.0 * sigma - rho0);
-    return {(float)(rho1 * rho0), (float)(2.0 * rho1 / delta), (float)(1.0 / theta)};
+    Cheb c{};
+    double rho = 1.0 / sigma;
+    for (int k = 1; k < kDeg; ++k) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        c.c1[k] = (float)(rn * rho);
+        c.c2[k] = (float)(2.0 * rn / delta);
+        rho = rn;
+    }
+    c.inv_theta = (float)(1.0 / theta);
+    return c;
 }
 
 // --- row kernels
@@ -980,6 +990,10 @@ void BatchSolver::rebuild_lists() {
     lists_dirty_ = false;
 }
 
+// Result of a level's cycle (smoothed or dense): xa for an odd smoothing degree, else xb, so
+// meshes that end at different levels share one buffer per level.
+static float* level_result(BatchLevelDev& L) { return (kDeg % 2 == 1) ? L.xa.get() : L.xb.get(); }
+
 void BatchSolver::vcycle(int l) {
     BatchLevelDev& L = *lv_[l];
     BatchMeshState* st = d_->st.get();
@@ -988,10 +1002,13 @@ void BatchSolver::vcycle(int l) {
     const int tpr = l == 0 ? 0 : tpr_[l];
     const OpB A = l == 0 ? OpB{L.s_begin.get(), L.s_len.get(), L.a_col.get(), L.a_val.get()}
                          : OpB{L.a_begin.get(), L.a_len.get(), L.a_col.get(), L.a_val.get()};
+    // pre-smoothing from zero; step k writes pre_buf(k), the last one xb
+    auto pre_buf = [&](int k) { return ((kDeg - 1 - k) % 2 == 0) ? L.xb.get() : L.xa.get(); };
     FGB_LAUNCH(kb_cheb_zero<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.dinv.get(), L.b.get(),
-                                                       L.xa.get(), L.d.get(), c.inv_theta));
-    FGB_BATCH_TPR(kb_cheb_step, tpr, grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, A, L.dinv.get(), L.b.get(),
-                  L.xa.get(), L.xb.get(), L.d.get(), c.c1, c.c2);
+                                                       pre_buf(0), L.d.get(), c.inv_theta));
+    for (int k = 1; k < kDeg; ++k)
+        FGB_BATCH_TPR(kb_cheb_step, tpr, grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, A, L.dinv.get(),
+                      L.b.get(), pre_buf(k - 1), pre_buf(k), L.d.get(), c.c1[k], c.c2[k]);
     FGB_BATCH_TPR(kb_residual, tpr, grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, A, L.b.get(), L.xb.get(),
                   L.rl.get());
     BatchLevelDev& C = *lv_[l + 1];
@@ -1000,15 +1017,19 @@ void BatchSolver::vcycle(int l) {
     FGB_BATCH_TPR(kb_csr_apply, r_tpr_[l + 1], grid_, stream_, C.T.get(), cC + 2, C.block_mesh.get(), st, R, L.rl.get(),
                   C.b.get(), 0);
     FGB_LAUNCH(kb_dense<<<grid_, kB, 0, stream_>>>(C.D.get(), cC + 1, C.block_mesh.get(), st, d_->dense.get(), C.b.get(),
-                                                   C.xb.get()));
+                                                   level_result(C)));
     if (l + 2 < max_levels_) vcycle(l + 1);
     const OpB P{L.p_begin.get(), L.p_len.get(), L.p_col.get(), L.p_val.get()};
-    FGB_BATCH_TPR(kb_csr_apply, p_tpr_[l], grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, P, C.xb.get(),
+    FGB_BATCH_TPR(kb_csr_apply, p_tpr_[l], grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, P, level_result(C),
                   L.xb.get(), 1);
-    FGB_BATCH_TPR(kb_cheb_step, tpr, grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, A, L.dinv.get(), L.b.get(),
-                  L.xb.get(), L.xa.get(), L.d.get(), -1.f, c.inv_theta);
-    FGB_BATCH_TPR(kb_cheb_step, tpr, grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, A, L.dinv.get(), L.b.get(),
-                  L.xa.get(), L.xb.get(), L.d.get(), c.c1, c.c2);
+    // post-smoothing (same polynomial) from the corrected xb: even steps write xa, odd ones xb
+    float* xin = L.xb.get();
+    for (int k = 0; k < kDeg; ++k) {
+        float* xout = (k % 2 == 0) ? L.xa.get() : L.xb.get();
+        FGB_BATCH_TPR(kb_cheb_step, tpr, grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, A, L.dinv.get(),
+                      L.b.get(), xin, xout, L.d.get(), k == 0 ? -1.f : c.c1[k], k == 0 ? c.inv_theta : c.c2[k]);
+        xin = xout;
+    }
 }
 
 void BatchSolver::launch_iteration() {
@@ -1021,9 +1042,9 @@ void BatchSolver::launch_iteration() {
     FGB_LAUNCH(kb_update<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.x.get(), L.bb.get(), L.r.get(),
                                                     L.p.get(), L.q.get(), L.b.get(), L.partial.get()));
     vcycle(0);
-    FGB_LAUNCH(kb_rz<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.r.get(), L.xb.get(),
+    FGB_LAUNCH(kb_rz<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.r.get(), level_result(L),
                                                 L.partial.get()));
-    FGB_LAUNCH(kb_direction<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.xb.get(), L.p.get()));
+    FGB_LAUNCH(kb_direction<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, level_result(L), L.p.get()));
 }
 
 void BatchSolver::capture() {

@@ -351,6 +351,9 @@ int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol,
 int fgb_field_last_stats(const FGB_FIELD* f, double* out13) {
     return guarded([&] { stats13(f->last, out13); return 0; });
 }
+int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo) {
+    return guarded([&] { f->f->fem().set_smoothing(degree, lo); return 0; });
+}
 int fgb_field_set_profiling(FGB_FIELD* f, int on) {
     return guarded([&] { f->f->fem().set_profiling(on != 0); return 0; });
 }

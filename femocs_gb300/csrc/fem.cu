@@ -16,6 +16,7 @@
 //                      the refinement update and the boundary values stay FP64
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 
 #include "amg.h"
@@ -33,8 +34,11 @@ __constant__ double c_hx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
 __constant__ double c_hy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
 __constant__ double c_hz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
 
+// ng = Gauss points per direction: 2 (the reference's QGauss<3>(2)) or 3 (the Q1 operator of
+// the Q2 coarse level: the exact Galerkin product P^T A_Q2 P, whose integrals use 3 points)
 __global__ void __launch_bounds__(128) k_cell_stiffness(int nc, const int32_t* __restrict__ cd,
-                                                        const double* __restrict__ dxyz, double* __restrict__ ke) {
+                                                        const double* __restrict__ dxyz, double* __restrict__ ke,
+                                                        int ng) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     double X[8][3];
@@ -49,9 +53,22 @@ __global__ void __launch_bounds__(128) k_cell_stiffness(int nc, const int32_t* _
 #pragma unroll
     for (int i = 0; i < 36; ++i) K[i] = 0.0;
     const double g = 0.57735026918962576451;
+    const double g3[3] = {-0.77459666924148337704, 0.0, 0.77459666924148337704};
+    const double w3[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+    const int nq = ng == 3 ? 27 : 8;
 #pragma unroll 1
-    for (int q = 0; q < 8; ++q) {
-        const double xi = (q & 1) ? g : -g, eta = (q & 2) ? g : -g, zeta = (q & 4) ? g : -g;
+    for (int q = 0; q < nq; ++q) {
+        double xi, eta, zeta, wq = 1.0;
+        if (ng == 3) {
+            xi = g3[q % 3];
+            eta = g3[(q / 3) % 3];
+            zeta = g3[q / 9];
+            wq = w3[q % 3] * w3[(q / 3) % 3] * w3[q / 9];
+        } else {
+            xi = (q & 1) ? g : -g;
+            eta = (q & 2) ? g : -g;
+            zeta = (q & 4) ? g : -g;
+        }
         double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         double dN[8][3];
 #pragma unroll
@@ -87,7 +104,7 @@ __global__ void __launch_bounds__(128) k_cell_stiffness(int nc, const int32_t* _
 #pragma unroll
             for (int a = 0; a < 3; ++a)
                 G[k][a] = inv[0][a] * dN[k][0] + inv[1][a] * dN[k][1] + inv[2][a] * dN[k][2];
-        const double w = fabs(det);
+        const double w = wq * fabs(det);
         int t = 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i)
@@ -625,7 +642,8 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
         return;
     }
     if (full_run) {
-        FGB_LAUNCH(k_cell_stiffness<<<grid_for(nc_, 128), 128, 0, stream_>>>(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get()));
+        FGB_LAUNCH(k_cell_stiffness<<<grid_for(nc_, 128), 128, 0, stream_>>>(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(),
+                                                                           q1_gauss_));
         FGB_LAUNCH(k_assemble_rows<<<gb, kBlock, 0, stream_>>>(n_, rowptr_.get(), col_.get(), r2c_ptr_.get(), r2c_item_.get(),
                                                     cell_dofs_.get(), ke_.get(), kval_.get()));
         FGB_CUDA(cudaGetLastError());
@@ -842,6 +860,8 @@ void FemDevice::ensure_amg(SolveStats* st) {
     std::vector<int8_t> fixed(n_, 0);
     for (int d = 0; d < n_; ++d) fixed[d] = fs_.bc_kind[d] == 1 || (anode && fs_.bc_kind[d] == 2);
     AmgHost h = build_amg(*pm_, fs_, vals, fixed);
+    h.levels[0].cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 3;
+    h.levels[0].cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.06;
     amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
                              dinv32_.get()));
     amg_->smoother_timer.enabled = profiling_;
@@ -885,7 +905,10 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     // coarse operator: the Q1 system of the same mesh and boundary conditions (the Q2 space
     // contains the Q1 space, P below is that embedding, so P^T A2 P equals the Q1 matrix up
     // to the quadrature), with the Q1 hierarchy underneath
-    if (!q1_) q1_.reset(new FemDevice(*pm_, build_fem_structure(*pm_), stream_));
+    if (!q1_) {
+        q1_.reset(new FemDevice(*pm_, build_fem_structure(*pm_), stream_));
+        q1_->q1_gauss_ = 3;
+    }
     q1_->setup(applied_field_, applied_potential_);
     q1_->assemble(true, anode != 0);
     std::vector<double> v1, r1;
@@ -894,6 +917,10 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     std::vector<int8_t> fixed1(f1.n_dofs, 0);
     for (int d = 0; d < f1.n_dofs; ++d) fixed1[d] = f1.bc_kind[d] == 1 || (anode && f1.bc_kind[d] == 2);
     AmgHost h1 = build_amg(*pm_, f1, v1, fixed1);
+    // the Q1 level is the coarse solve of the Q2 level: smooth it harder
+    const char* e = std::getenv("FGB_Q2_L1_DEG");
+    h1.levels[0].cheb_degree = e ? std::atoi(e) : 4;
+    h1.levels[0].cheb_lo = 0.04;
     h1.levels[0].A.col = f1.col;
     h1.levels[0].A.val = std::move(v1);
     // embedding: a free Q2 DoF takes the mean of the free Q1 values at its entity's corners
@@ -922,6 +949,8 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     l0.A.n_rows = l0.A.n_cols = n_;
     l0.A.ptr.assign(1, fs_.nnz());  // structure lives on the device; nnz for reporting
     l0.lambda = estimate_lambda(15);
+    l0.cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 3;
+    l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.06;
     l0.R.n_rows = P.n_cols;
     l0.R.n_cols = P.n_rows;
     {
@@ -969,6 +998,13 @@ void FemDevice::download_pattern(std::vector<int64_t>& rowptr, std::vector<int32
 }
 
 std::string FemDevice::amg_levels() const { return amg_ ? amg_->describe() : std::string(); }
+
+void FemDevice::set_smoothing(int degree, double lo) {
+    FGB_REQUIRE(degree >= 0 && degree <= 15 && lo >= 0 && lo < 1, "smoothing degree 1..15 and interval 0..1");
+    smooth_degree_ = degree;
+    smooth_lo_ = lo;
+    amg_.reset();
+}
 
 void FemDevice::set_profiling(bool on) {
     profiling_ = on;

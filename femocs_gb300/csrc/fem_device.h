@@ -90,6 +90,10 @@ public:
     std::string amg_levels() const;
     // event pairs around the multigrid path's hot launches (see SolveStats)
     void set_profiling(bool on);
+    // Chebyshev smoothing of the finest multigrid level: degree (steps before and after the
+    // coarse correction) and the lower end of the interval as a fraction of lambda_max;
+    // 0 keeps the default (3 and 0.06). Drops the current hierarchy.
+    void set_smoothing(int degree, double lo);
     ~FemDevice();
 
     // PoissonSolver::setup + assemble verbs (src/PoissonSolver.cpp:162-210)
@@ -139,6 +143,9 @@ private:
     void build_q2_amg(int anode, SolveStats* st);
     double estimate_lambda(int iters);  // largest eigenvalue of D^-1 A (FP64 power iteration)
     bool profiling_ = false;
+    int smooth_degree_ = 0;
+    double smooth_lo_ = 0;
+    int q1_gauss_ = 2;  // Gauss points per direction of the Q1 element integrals
     LaunchTimer spmv_timer_;
     int n_, nc_;
     double applied_field_ = 0, applied_potential_ = 0;

@@ -91,6 +91,13 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
     __shared__ double sX[kQ2Warps][8][3];
     __shared__ double sInv[kQ2Warps][27][10];  // J^-1 (row major) and w |det J| per point
     __shared__ double sG[kQ2Warps][27][3];
+    // shape-gradient tables in shared memory: lanes read them at different addresses, which
+    // the constant cache would serialise
+    __shared__ double sDN[27 * 27 * 3];
+    __shared__ double sD1[27 * 8 * 3];
+    for (int i = threadIdx.x; i < 27 * 27 * 3; i += blockDim.x) sDN[i] = c_q2_dN[i];
+    for (int i = threadIdx.x; i < 27 * 8 * 3; i += blockDim.x) sD1[i] = c_q1_dN[i];
+    __syncthreads();
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = blockIdx.x * kQ2Warps + wid;
     if (c >= nc) return;  // whole warp leaves together
@@ -105,7 +112,7 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
         double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         for (int k = 0; k < 8; ++k)
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) J[a][b] += sX[wid][k][a] * c_q1_dN[(lane * 8 + k) * 3 + b];
+                for (int b = 0; b < 3; ++b) J[a][b] += sX[wid][k][a] * sD1[(lane * 8 + k) * 3 + b];
         const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
         const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
         const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
@@ -124,13 +131,20 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
         o[9] = c_q2_w[lane] * fabs(det);
     }
     double acc[12];
+    int ei[12], ej[12];  // this lane's packed entries e = lane + 32 t, held in registers (a
+                         // table read per entry would diverge across the warp)
 #pragma unroll
-    for (int t = 0; t < 12; ++t) acc[t] = 0.0;
+    for (int t = 0; t < 12; ++t) {
+        acc[t] = 0.0;
+        const int e = min(lane + 32 * t, 377);
+        ei[t] = c_q2_ij[2 * e];
+        ej[t] = c_q2_ij[2 * e + 1];
+    }
     for (int q = 0; q < 27; ++q) {
         __syncwarp();
         if (lane < 27) {
             const double* inv = sInv[wid][q];
-            const double* g = c_q2_dN + (q * 27 + lane) * 3;
+            const double* g = sDN + (q * 27 + lane) * 3;
             // physical gradient: (J^-T g)_a = sum_k inv[k][a] g_k
 #pragma unroll
             for (int a = 0; a < 3; ++a) sG[wid][lane][a] = inv[a] * g[0] + inv[3 + a] * g[1] + inv[6 + a] * g[2];
@@ -139,11 +153,9 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
         const double w = sInv[wid][q][9];
 #pragma unroll
         for (int t = 0; t < 12; ++t) {
-            const int e = lane + 32 * t;
-            if (e < 378) {
-                const int i = c_q2_ij[2 * e], j = c_q2_ij[2 * e + 1];
-                acc[t] += w * (sG[wid][i][0] * sG[wid][j][0] + sG[wid][i][1] * sG[wid][j][1] + sG[wid][i][2] * sG[wid][j][2]);
-            }
+            const double* gi = sG[wid][ei[t]];
+            const double* gj = sG[wid][ej[t]];
+            acc[t] += w * (gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2]);
         }
     }
     double* o = ke + 378 * (size_t)c;

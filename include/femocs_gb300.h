@@ -136,6 +136,10 @@ int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol,
  * levels, and with profiling on (multigrid path): level-0 smoother ms, smoother launches,
  * outer FP64 SpMV ms, SpMV launches */
 int fgb_field_last_stats(const FGB_FIELD* f, double* out13);
+/* Chebyshev smoothing of the finest multigrid level: steps before and after the coarse
+ * correction (0: default 3) and the interval's lower end as a fraction of lambda_max
+ * (0: default 0.06); the hierarchy is rebuilt at the next solve */
+int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo);
 /* record CUDA event pairs around the multigrid path's hot launches (off by default) */
 int fgb_field_set_profiling(FGB_FIELD* f, int on);
 /* multigrid levels as "rows:nnz" separated by spaces, the coarsest "rows:rows^2:dense";
