@@ -51,8 +51,10 @@ SSOR_ITERS = {"config1": 268, "config2": 617, "probe": 0}
 # uses 617 x 2.55
 Q2_SSOR_RATIO = 2.55
 # DRAM bytes (read + write) per row of one launch of the hot multigrid kernels, from ncu
-# captures of the probe workload (profiles/); a launch's traffic scales with its rows.
-KERNEL_TRAFFIC_PER_ROW = {}
+# captures of the Q2 probe workload (profiles/k_cheb_step_level0_q2_probe.md,
+# profiles/k_cg_spmv_pq_fp64_q2_probe.md: 61.9 nonzeros per row, as config 2's Q2 rows); a
+# launch's traffic scales with its rows
+KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6, ("spmv64", 2): 812.2}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -312,7 +314,7 @@ def run_ours(args, world, rank):
     launch_ms = tot_ms / max(cnt, 1)
     peak, peak_kind = measured_hbm_peak()
     achieved = bytes_per_launch / (launch_ms * 1e-3) / 1e9
-    traffic = KERNEL_TRAFFIC_PER_ROW[key] * n if key in KERNEL_TRAFFIC_PER_ROW else None
+    traffic = KERNEL_TRAFFIC_PER_ROW[(key, order)] * n if (key, order) in KERNEL_TRAFFIC_PER_ROW else None
     spmv32_ms = field.time_spmv(1, 50)
     spmv64_ms = field.time_spmv(0, 20)
 
@@ -353,7 +355,8 @@ def run_ours(args, world, rank):
                 "d2h_bytes_per_step": 36 * n_points,
                 "note": "femocs_run + femocs_interpolate_elfield through the C ABI, host arrays"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "traffic_note": "ncu dram bytes per row of a probe capture x rows",
+                     "traffic": traffic,
+                     "traffic_note": "ncu dram bytes per row of the Q2 probe capture x rows (Q2 only)",
                      "kernel": name, "bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
                      "launches": cnt, "share_of_solve": tot_ms / sum(solve_ms),
                      "other": {k: {"ms": v[0], "launches": v[1], "gbs": v[2] / (v[0] / max(v[1], 1) * 1e-3) / 1e9}
