@@ -170,6 +170,12 @@ class Field:
         self._ok(load().fgb_field_amg_levels(self.h, buf, 4096))
         return buf.value.decode()
 
+    def solution(self):
+        """The solution vector in the field's DoF order."""
+        out = np.zeros(self.n_dofs)
+        self._ok(load().fgb_field_export_solution(self.h, ptr(out)))
+        return out
+
     def q2_dofs(self):
         """(cell, lattice index) holding every Q2 DoF."""
         dc = np.zeros(self.n_dofs, dtype=np.int32)

@@ -59,6 +59,7 @@ _PROTOS = {
     "fgb_field_create": (vp, [vp]),
     "fgb_field_create_order": (vp, [vp, C.c_int]),
     "fgb_field_q2_dofs": (C.c_int, [vp, ip, ip]),
+    "fgb_field_export_solution": (C.c_int, [vp, dp]),
     "fgb_mesh_q2_sizes": (C.c_int, [vp, i64p]),
     "fgb_field_free": (None, [vp]),
     "fgb_field_sizes": (C.c_int, [vp, i64p]),

@@ -381,6 +381,14 @@ int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi) {
         return 0;
     });
 }
+int fgb_field_export_solution(FGB_FIELD* f, double* x) {
+    return guarded([&] {
+        FemDevice& fem = f->f->fem();
+        FGB_CUDA(cudaMemcpyAsync(x, fem.d_solution(), sizeof(double) * fem.n_dofs(), cudaMemcpyDeviceToHost, fem.stream()));
+        FGB_CUDA(cudaStreamSynchronize(fem.stream()));
+        return 0;
+    });
+}
 int fgb_field_import_phi_nodes(FGB_FIELD* f, const double* phi) {
     return guarded([&] {
         FemDevice& fem = f->f->fem();

@@ -146,6 +146,8 @@ int fgb_field_set_profiling(FGB_FIELD* f, int on);
  * NUL-terminated, truncated to cap bytes; empty before the first multigrid solve */
 int fgb_field_amg_levels(FGB_FIELD* f, char* buf, int cap);
 int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi_nodes);
+/* the solution in the field's own DoF order (n_dofs values) */
+int fgb_field_export_solution(FGB_FIELD* f, double* x);
 int fgb_field_import_phi_nodes(FGB_FIELD* f, const double* phi_nodes);
 /* Interpolator::extract_solution: nodal E from phi, optional smoothing */
 int fgb_field_extract(FGB_FIELD* f, int smoothen);
