@@ -170,6 +170,28 @@ class Field:
         self._ok(load().fgb_field_amg_levels(self.h, buf, 4096))
         return buf.value.decode()
 
+    def space_charge(self, xyz, charge_factor, hex_cells=None, accumulate=False):
+        """PIC space charge of particles (host xyz, optional vacuum hex ids) for the next
+        assemble; returns the number of particles outside the vacuum hexes."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = len(xyz)
+        d_pts = DeviceBuffer(max(24 * n, 8))
+        d_pts.upload(xyz)
+        d_hex = None
+        if hex_cells is not None:
+            hc = np.ascontiguousarray(hex_cells, dtype=np.int32)
+            d_hex = DeviceBuffer(max(4 * n, 4))
+            d_hex.upload(hc)
+        sk = C.c_int(0)
+        self._ok(load().fgb_field_space_charge(self.h, n, C.c_void_p(d_pts.ptr),
+                                               C.c_void_p(d_hex.ptr) if d_hex is not None else None,
+                                               float(charge_factor), int(accumulate), C.byref(sk)))
+        self._ok(load().fgb_device_sync())
+        return sk.value
+
+    def clear_space_charge(self):
+        self._ok(load().fgb_field_clear_space_charge(self.h))
+
     def solution(self):
         """The solution vector in the field's DoF order."""
         out = np.zeros(self.n_dofs)

@@ -60,6 +60,9 @@ _PROTOS = {
     "fgb_field_create_order": (vp, [vp, C.c_int]),
     "fgb_field_q2_dofs": (C.c_int, [vp, ip, ip]),
     "fgb_field_export_solution": (C.c_int, [vp, dp]),
+    "fgb_field_space_charge": (C.c_int, [vp, C.c_int, vp, vp, C.c_double, C.c_int, ip]),
+    "fgb_field_clear_space_charge": (C.c_int, [vp]),
+    "fgb_device_sync": (C.c_int, []),
     "fgb_mesh_q2_sizes": (C.c_int, [vp, i64p]),
     "fgb_field_free": (None, [vp]),
     "fgb_field_sizes": (C.c_int, [vp, i64p]),

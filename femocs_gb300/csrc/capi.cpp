@@ -381,6 +381,20 @@ int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi) {
         return 0;
     });
 }
+int fgb_field_space_charge(FGB_FIELD* f, int n, const double* d_xyz, const int* d_hex, double charge_factor,
+                           int accumulate, int* n_skipped) {
+    return guarded([&] {
+        const int sk = f->f->space_charge(n, d_xyz, d_hex, charge_factor, accumulate != 0);
+        if (n_skipped) *n_skipped = sk;
+        return 0;
+    });
+}
+int fgb_device_sync(void) {
+    return guarded([&] { FGB_CUDA(cudaDeviceSynchronize()); return 0; });
+}
+int fgb_field_clear_space_charge(FGB_FIELD* f) {
+    return guarded([&] { f->f->fem().clear_space_charge(); return 0; });
+}
 int fgb_field_export_solution(FGB_FIELD* f, double* x) {
     return guarded([&] {
         FemDevice& fem = f->f->fem();

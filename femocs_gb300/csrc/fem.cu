@@ -616,6 +616,29 @@ void FemDevice::setup(double applied_field, double applied_potential) {
     x_.zero(stream_);  // solution = dirichlet_bc_value (0), src/DealSolver.cpp:384
 }
 
+double* FemDevice::space_charge_buffer(bool accumulate) {
+    if (!has_extra_ || rhs_extra_.size() != (size_t)n_ || !accumulate) {
+        rhs_extra_.resize(n_);
+        rhs_extra_.zero(stream_);
+    }
+    has_extra_ = true;
+    return rhs_extra_.get();
+}
+
+const int32_t* FemDevice::d_node2dof() {
+    if (!node2dof_dev_.size()) node2dof_dev_.upload(fs_.node2dof, stream_);
+    return node2dof_dev_.get();
+}
+
+const int32_t* FemDevice::d_hex2cell() {
+    if (!hex2cell_dev_.size()) {
+        std::vector<int32_t> h(pm_->hex.n_hexs(), -1);
+        for (size_t c = 0; c < pm_->vac.cells.size(); ++c) h[pm_->vac.cells[c]] = (int32_t)c;
+        hex2cell_dev_.upload(h, stream_);
+    }
+    return hex2cell_dev_.get();
+}
+
 void FemDevice::set_space_charge(const double* d_extra) {
     if (!d_extra) { has_extra_ = false; return; }
     rhs_extra_.resize(n_);

@@ -102,6 +102,14 @@ public:
     // adds a space-charge contribution rhs[dof] += w * N(point) to the unconstrained rhs
     // before Dirichlet application; values given per dof (already summed)
     void set_space_charge(const double* d_rhs_extra);
+    // PIC space charge: a zeroed (or kept) per-DoF rhs that particles scatter into; it is
+    // added to the rhs at the next assemble, before the Dirichlet values (as the reference's
+    // assemble_space_charge). clear_space_charge() drops it.
+    double* space_charge_buffer(bool accumulate);
+    void clear_space_charge() { has_extra_ = false; }
+    const int32_t* d_node2dof();   // hex-mesh node -> DoF (Q1) or -1
+    const int32_t* d_hex2cell();   // hex -> vacuum cell index or -1
+    const int32_t* d_cell_dofs() const { return cell_dofs_.get(); }
     int solve(const SolveOptions& opt, SolveStats* st);
 
     // solution by dof / by mesh node
@@ -156,6 +164,7 @@ private:
     DBuf<int32_t> col_, slice_len_, sell_col_, row_len_;
     int max_row_ = 0;
     DBuf<int8_t> bc_;
+    DBuf<int32_t> node2dof_dev_, hex2cell_dev_;
     DBuf<double> dof_xyz_;
     // values
     DBuf<double> ke_;        // Q1: 64 per cell; Q2: 378 (packed upper triangle)

@@ -35,6 +35,22 @@ void Field::extract(bool smoothen) {
     dm_->extract_solution(fem_->d_solution(), fem_->d_dof2node(), fem_->n_dofs(), smoothen);
 }
 
+int Field::space_charge(int n, const double* d_pts, const int32_t* d_hex, double charge_factor, bool accumulate) {
+    double* rhs = fem_->space_charge_buffer(accumulate);
+    if (n <= 0) return 0;
+    const int32_t* hex = d_hex;
+    if (!hex) {
+        if (out_.size() < 5 * (size_t)n) out_.resize(5 * (size_t)n);
+        if (cells_.size() < (size_t)n) cells_.resize(n);
+        dm_->locate_interpolate(n, d_pts, 3, cells_.get(), out_.get(), nullptr);
+        hex = cells_.get();
+    }
+    int skipped = 0;
+    dm_->space_charge(n, d_pts, hex, fem_->order(), fem_->d_node2dof(), fem_->d_hex2cell(), fem_->d_cell_dofs(),
+                      charge_factor, rhs, &skipped);
+    return skipped;
+}
+
 void Field::interpolate_host(int n, const double* xyz, int rank, int32_t* cells, double* out5, LocateStats* ls) {
     if (n <= 0) return;
     if (pts_.size() < 3 * (size_t)n) pts_.resize(3 * (size_t)n);

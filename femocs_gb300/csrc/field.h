@@ -28,6 +28,11 @@ public:
     // host-pointer interpolation through reusable device buffers
     void interpolate_host(int n, const double* xyz, int rank, int32_t* cells, double* out5, LocateStats* ls);
     void extract(bool smoothen);
+    // PIC: scatter n particles (device xyz) with charge factor q/eps0 * W_sp into the space-
+    // charge rhs of the next assemble; d_hex = their vacuum hexes, or null to locate them
+    // first (rank-3 location, as the reference keeps particle.cell). Returns the particles
+    // outside the vacuum hexes.
+    int space_charge(int n, const double* d_pts, const int32_t* d_hex, double charge_factor, bool accumulate);
 
 private:
     std::shared_ptr<const PreparedMesh> pm_;

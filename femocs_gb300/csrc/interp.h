@@ -50,6 +50,12 @@ public:
     // 262144 points per call, shared by all calls; overlapping calls race). Asynchronous on
     // stream(). The first call on a device looks up the array's device address.
     void locate_interpolate_noalloc(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out);
+    // Space charge of n particles in vacuum hexes d_hex (femocs hex ids, < 0: skipped) added to
+    // a per-DoF rhs (order 1: through node -> dof; order 2: through hex -> vacuum cell and its
+    // 27 cell DoFs); n_skipped (may be null) receives the particles outside the vacuum hexes
+    void space_charge(int n, const double* d_pts, const int32_t* d_hex, int order, const int32_t* d_node2dof,
+                      const int32_t* d_hex2cell, const int32_t* d_cell_dofs, double charge_factor, double* d_rhs,
+                      int* n_skipped);
     // Interpolate with cells already known (SolutionReader::calc_interpolation with mapped atoms)
     void interpolate_known(int n, const double* d_pts, int rank, const int32_t* d_cells, double* d_out);
 

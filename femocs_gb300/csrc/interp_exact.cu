@@ -262,6 +262,90 @@ __device__ __forceinline__ void acc5(const double* __restrict__ sol, int node, d
     for (int c = 0; c < 5; ++c) a[c] += s[c] * w;
 }
 
+// LinearHexahedra::project_to_nat_coords (src/InterpolatorCells.cpp:1272-1317): Newton on the
+// trilinear map x = f0 + f1 u + f2 v + f3 w + f4 uv + f5 uw + f6 vw + f7 uvw, Cramer steps,
+// at most 20 iterations, stop when |du|^2 < 1e-15
+__device__ __forceinline__ void hex_natural(const double* __restrict__ F, double x, double y, double z, double& u,
+                                            double& v, double& ww) {
+    const double f0x = x - F[0], f0y = y - F[1], f0z = z - F[2];
+    u = 0;
+    v = 0;
+    ww = 0;
+    for (int it = 0; it < 20; ++it) {
+        const double uv = u * v, uw = u * ww, vw = v * ww, uvw = uv * ww;
+        double f[3], fu[3], fv[3], fw[3];
+        const double f0[3] = {f0x, f0y, f0z};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            f[q] = f0[q] - F[3 + q] * u - F[6 + q] * v - F[9 + q] * ww - F[12 + q] * uv - F[15 + q] * uw -
+                   F[18 + q] * vw - F[21 + q] * uvw;
+            fu[q] = F[3 + q] + F[12 + q] * v + F[15 + q] * ww + F[21 + q] * vw;
+            fv[q] = F[6 + q] + F[12 + q] * u + F[18 + q] * ww + F[21 + q] * uw;
+            fw[q] = F[9 + q] + F[15 + q] * u + F[18 + q] * v + F[21 + q] * uv;
+        }
+        // determinant(v1,v2,v3) of the reference, rows = vectors
+        auto det3 = [](const double* p, const double* q, const double* r) {
+            return p[0] * (q[1] * r[2] - r[1] * q[2]) - q[0] * (p[1] * r[2] - r[1] * p[2]) +
+                   r[0] * (p[1] * q[2] - q[1] * p[2]);
+        };
+        const double D = 1.0 / det3(fu, fv, fw);
+        const double du = det3(f, fv, fw) * D, dv = det3(fu, f, fw) * D, dw = det3(fu, fv, f) * D;
+        u += du;
+        v += dv;
+        ww += dw;
+        if (du * du + dv * dv + dw * dw < kZero) break;
+    }
+}
+
+// PoissonSolver::assemble_space_charge_fast (src/PoissonSolver.cpp:300-319): every particle
+// adds N_k(p) q/eps0 W_sp to the rhs of its hex's nodes, N = the trilinear shape functions
+// at the particle (shape_funs_dealii: the same values in deal.II's vertex order). order 2:
+// the 27 Q2 Lagrange functions of the same natural coordinates on the hex's Q2 DoFs. The sum
+// over particles uses FP64 atomics (order-dependent rounding at the last bit).
+__global__ void k_space_charge(int n, Pts P, const int32_t* __restrict__ hex_of, const double* __restrict__ hexf,
+                               const int32_t* __restrict__ hexs, const int32_t* __restrict__ node2dof, int order,
+                               const int32_t* __restrict__ hex2cell, const int32_t* __restrict__ cell_dofs, double cf,
+                               double* __restrict__ rhs, int32_t* __restrict__ counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int h = hex_of[i];
+    if (h < 0) {  // not inside a vacuum hex: contributes nothing
+        atomicAdd(&counters[0], 1);
+        return;
+    }
+    double x, y, z;
+    P.get(i, x, y, z);
+    double u, v, ww;
+    hex_natural(hexf + 24 * (size_t)h, x, y, z, u, v, ww);
+    if (order == 1) {
+        const double w8[8] = {(1 - u) * (1 - v) * (1 - ww) / 8.0, (1 + u) * (1 - v) * (1 - ww) / 8.0,
+                              (1 + u) * (1 + v) * (1 - ww) / 8.0, (1 - u) * (1 + v) * (1 - ww) / 8.0,
+                              (1 - u) * (1 - v) * (1 + ww) / 8.0, (1 + u) * (1 - v) * (1 + ww) / 8.0,
+                              (1 + u) * (1 + v) * (1 + ww) / 8.0, (1 - u) * (1 + v) * (1 + ww) / 8.0};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int d = node2dof[hexs[8 * (size_t)h + k]];
+            if (d >= 0) atomicAdd(&rhs[d], w8[k] * cf);
+        }
+    } else {
+        const int c = hex2cell[h];
+        if (c < 0) {
+            atomicAdd(&counters[0], 1);
+            return;
+        }
+        const double t[3] = {u, v, ww};
+        double l[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            l[a][0] = 0.5 * t[a] * (t[a] - 1.0);
+            l[a][1] = 1.0 - t[a] * t[a];
+            l[a][2] = 0.5 * t[a] * (t[a] + 1.0);
+        }
+        for (int L = 0; L < 27; ++L)
+            atomicAdd(&rhs[cell_dofs[27 * (size_t)c + L]], l[0][L % 3] * l[1][(L / 3) % 3] * l[2][L / 9] * cf);
+    }
+}
+
 __global__ void k_interpolate(int n, Pts P, int rank, int from_tets, const int32_t* __restrict__ cells_in,
                               const double* __restrict__ det, const int32_t* __restrict__ tets, const int32_t* __restrict__ quad,
                               const int32_t* __restrict__ hexs, const double* __restrict__ hexf, const double* __restrict__ sol,
@@ -304,33 +388,8 @@ __global__ void k_interpolate(int n, Pts P, int rank, int from_tets, const int32
         for (int k = 0; k < 10; ++k) acc5(sol, nd[k], w[k], a);
     } else {
         // LinearHexahedra::project_to_nat_coords + shape_functions, :1272-1353
-        const double* F = hexf + 24 * (size_t)c;
-        const double f0x = x - F[0], f0y = y - F[1], f0z = z - F[2];
-        double u = 0, v = 0, ww = 0;
-        for (int it = 0; it < 20; ++it) {
-            const double uv = u * v, uw = u * ww, vw = v * ww, uvw = uv * ww;
-            double f[3], fu[3], fv[3], fw[3];
-            const double f0[3] = {f0x, f0y, f0z};
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                f[q] = f0[q] - F[3 + q] * u - F[6 + q] * v - F[9 + q] * ww - F[12 + q] * uv - F[15 + q] * uw -
-                       F[18 + q] * vw - F[21 + q] * uvw;
-                fu[q] = F[3 + q] + F[12 + q] * v + F[15 + q] * ww + F[21 + q] * vw;
-                fv[q] = F[6 + q] + F[12 + q] * u + F[18 + q] * ww + F[21 + q] * uw;
-                fw[q] = F[9 + q] + F[15 + q] * u + F[18 + q] * v + F[21 + q] * uv;
-            }
-            // determinant(v1,v2,v3) of the reference, rows = vectors
-            auto det3 = [](const double* p, const double* q, const double* r) {
-                return p[0] * (q[1] * r[2] - r[1] * q[2]) - q[0] * (p[1] * r[2] - r[1] * p[2]) +
-                       r[0] * (p[1] * q[2] - q[1] * p[2]);
-            };
-            const double D = 1.0 / det3(fu, fv, fw);
-            const double du = det3(f, fv, fw) * D, dv = det3(fu, f, fw) * D, dw = det3(fu, fv, f) * D;
-            u += du;
-            v += dv;
-            ww += dw;
-            if (du * du + dv * dv + dw * dw < kZero) break;
-        }
+        double u, v, ww;
+        hex_natural(hexf + 24 * (size_t)c, x, y, z, u, v, ww);
         const double w8[8] = {(1 - u) * (1 - v) * (1 - ww) / 8.0, (1 + u) * (1 - v) * (1 - ww) / 8.0,
                               (1 + u) * (1 + v) * (1 - ww) / 8.0, (1 - u) * (1 + v) * (1 - ww) / 8.0,
                               (1 - u) * (1 - v) * (1 + ww) / 8.0, (1 + u) * (1 - v) * (1 + ww) / 8.0,
@@ -712,6 +771,25 @@ void DeviceMesh::locate_interpolate_noalloc(int n, const double* d_pts, int rank
                                                                     quad_.get(), hexs_.get(), hexf_.get(), sol_.get(), d_cells,
                                                                     d_out));
     FGB_CUDA(cudaGetLastError());
+}
+
+void DeviceMesh::space_charge(int n, const double* d_pts, const int32_t* d_hex, int order, const int32_t* d_node2dof,
+                              const int32_t* d_hex2cell, const int32_t* d_cell_dofs, double charge_factor,
+                              double* d_rhs, int* n_skipped) {
+    if (n <= 0) return;
+    FGB_REQUIRE(order == 1 || order == 2, "element order must be 1 or 2");
+    counters_.zero(stream_);
+    Pts P{d_pts};
+    FGB_LAUNCH(k_space_charge<<<grid_for(n, 256), 256, 0, stream_>>>(n, P, d_hex, hexf_.get(), hexs_.get(), d_node2dof,
+                                                                     order, d_hex2cell, d_cell_dofs, charge_factor,
+                                                                     d_rhs, counters_.get()));
+    FGB_CUDA(cudaGetLastError());
+    if (n_skipped) {
+        int32_t h = 0;
+        FGB_CUDA(cudaMemcpyAsync(&h, counters_.get(), sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        *n_skipped = h;
+    }
 }
 
 void DeviceMesh::interpolate_known(int n, const double* d_pts, int rank, const int32_t* d_cells, double* d_out) {

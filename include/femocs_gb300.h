@@ -146,6 +146,17 @@ int fgb_field_set_profiling(FGB_FIELD* f, int on);
  * NUL-terminated, truncated to cap bytes; empty before the first multigrid solve */
 int fgb_field_amg_levels(FGB_FIELD* f, char* buf, int cap);
 int fgb_field_export_phi_nodes(FGB_FIELD* f, double* phi_nodes);
+/* PIC space charge (PoissonSolver::assemble_space_charge_fast, src/PoissonSolver.cpp:300-319):
+ * n particles at device positions d_xyz in vacuum hexes d_hex (NULL: located here, rank 3)
+ * add N_k(p) * charge_factor (= q/eps0 * W_sp) to the rhs of their hex's DoFs at the next
+ * fgb_field_assemble (before the Dirichlet values; full_run = 0 reuses the matrix, as
+ * ProjectRunaway::make_pic_step). accumulate = 0 starts a new charge distribution.
+ * n_skipped (may be NULL): particles outside the vacuum hexes. */
+int fgb_field_space_charge(FGB_FIELD* f, int n, const double* d_xyz, const int* d_hex, double charge_factor,
+                           int accumulate, int* n_skipped);
+int fgb_field_clear_space_charge(FGB_FIELD* f);
+/* wait for all work of this process on the current device */
+int fgb_device_sync(void);
 /* the solution in the field's own DoF order (n_dofs values) */
 int fgb_field_export_solution(FGB_FIELD* f, double* x);
 int fgb_field_import_phi_nodes(FGB_FIELD* f, const double* phi_nodes);
