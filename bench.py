@@ -298,14 +298,17 @@ def run_ours(args, world, rank):
     # roofline of the dominant kernel of the solve, timed live by event pairs around each of
     # its launches in the timed steps. Algorithmic bytes per launch:
     #   level-0 Chebyshev step (k_cheb_step): FP32 SELL matrix, 4 B value + 4 B column per
-    #     nonzero, and 24 B per row (b, x gathered once, D^-1 read; d read + written; x written)
+    #     nonzero, and 24 B per row (b, x gathered once, D^-1 read; d read + written; x written);
+    #     Q2 element by element: the solver's own count (AmgDevice::smoother_bytes)
     #   outer FP64 SpMV (k_cg_spmv_pq<double>): 8 B value + 4 B column per nonzero, 16 B per
     #     row (p gathered once, q written)
     nnz = field.nnz
+    ebe = order == 2 and last["smoother_bytes"] != nnz * 8 + 24 * n
     kern = {
-        "k_cheb_step (level-0 Chebyshev smoothing, FP32)": (
+        ("k_ebe_apply + k_ebe_cheb (level-0 Chebyshev smoothing, Q2 element by element, FP32)" if ebe else
+         "k_cheb_step (level-0 Chebyshev smoothing, FP32)"): (
             sum(s["smoother_ms"] for s in solve_stats), sum(s["smoother_launches"] for s in solve_stats),
-            nnz * 8 + 24 * n, "smoother"),
+            last["smoother_bytes"], "smoother_ebe" if ebe else "smoother"),
         "k_cg_spmv_pq<double> (outer FP64 SpMV + p.q)": (
             sum(s["spmv_ms"] for s in solve_stats), sum(s["spmv_launches"] for s in solve_stats),
             nnz * 12 + 16 * n, "spmv64"),

@@ -16,7 +16,7 @@ from ._lib import FgbNanotip, dp, i64p, ip, last_error, load, ptr
 def _stats_dict(st):
     return dict(iterations=int(st[0]), outer=int(st[1]), status=int(st[2]), rel_residual=st[3], bnorm=st[4],
                 ms=st[5], kernel_ms=st[6], setup_ms=st[7], levels=int(st[8]), smoother_ms=st[9],
-                smoother_launches=int(st[10]), spmv_ms=st[11], spmv_launches=int(st[12]))
+                smoother_launches=int(st[10]), spmv_ms=st[11], spmv_launches=int(st[12]), smoother_bytes=st[13])
 
 __all__ = ["Mesh", "Field", "Femocs", "nanotip", "synth_atoms", "synth_probes", "load", "last_error",
            "CONFIG1", "CONFIG2", "FgbNanotip", "DeviceBuffer"]
@@ -153,9 +153,14 @@ class Field:
         rc = load().fgb_field_solve(self.h, precision, rel_tol, abs_tol, max_iter, inner_tol, None)
         if rc == -(2 ** 31):
             raise RuntimeError(last_error())
-        st = np.zeros(13)
+        st = np.zeros(14)
         self._ok(load().fgb_field_last_stats(self.h, ptr(st)))
         return rc, _stats_dict(st)
+
+    def set_level0_ebe(self, on=True):
+        """Q2: finest multigrid level element by element (True) or through the SELL matrix
+        (False, the default)."""
+        self._ok(load().fgb_field_set_level0_ebe(self.h, int(on)))
 
     def set_smoothing(self, degree=0, lo=0.0):
         """Chebyshev degree and interval of the finest multigrid level (0: defaults)."""
@@ -336,7 +341,7 @@ class Femocs:
 
     def last_stats(self):
         """All solver statistics of the last run (see Field.solve)."""
-        st = np.zeros(13)
+        st = np.zeros(14)
         if self.lib.fgb_femocs_last_stats(self.h, ptr(st)) != 0:
             raise RuntimeError(last_error())
         return _stats_dict(st)

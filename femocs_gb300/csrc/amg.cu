@@ -167,6 +167,65 @@ __global__ void __launch_bounds__(kB) k_csr_apply(int n, const int64_t* __restri
     y[i] = accumulate ? y[i] + acc : acc;
 }
 
+// ---- element-by-element level-0 operator (Q2)
+__device__ __forceinline__ int sym27f(int i, int j) {
+    if (i > j) { const int t = i; i = j; j = t; }
+    return i * 27 - (i * (i - 1)) / 2 + (j - i);
+}
+
+// ye[27 c + i] = sum_j K_e[i][j] x[cd[27 c + j]], one warp per cell
+__global__ void __launch_bounds__(kB) k_ebe_apply(int nc, const int32_t* __restrict__ cd, const float* __restrict__ ke,
+                                                  const float* __restrict__ x, float* __restrict__ ye) {
+    __shared__ float sK[kB / 32][378];
+    __shared__ float sx[kB / 32][28];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (kB / 32) + wid;
+    if (c >= nc) return;  // whole warp leaves together
+    const float* kc = ke + 378 * (size_t)c;
+    for (int e = lane; e < 378; e += 32) sK[wid][e] = __ldg(kc + e);
+    if (lane < 27) sx[wid][lane] = __ldg(x + cd[27 * (size_t)c + lane]);
+    __syncwarp();
+    if (lane < 27) {
+        float acc = 0.f;
+#pragma unroll 9
+        for (int j = 0; j < 27; ++j) acc += sK[wid][sym27f(lane, j)] * sx[wid][j];
+        ye[27 * (size_t)c + lane] = acc;
+    }
+}
+
+// row gather of the element products (ascending cell: fixed order), Dirichlet rows diag * x
+__device__ __forceinline__ float ebe_row(int i, const int32_t* __restrict__ r2c_ptr, const int32_t* __restrict__ r2c_item,
+                                         const float* __restrict__ ye, const int8_t* __restrict__ fixed,
+                                         const float* __restrict__ dinv, const float* __restrict__ x) {
+    if (fixed[i]) return x[i] / dinv[i];
+    float a = 0.f;
+    for (int p = r2c_ptr[i]; p < r2c_ptr[i + 1]; ++p) a += __ldg(ye + r2c_item[p]);
+    return a;
+}
+
+__global__ void __launch_bounds__(kB) k_ebe_cheb(int n, const int32_t* __restrict__ r2c_ptr,
+                                                 const int32_t* __restrict__ r2c_item, const float* __restrict__ ye,
+                                                 const int8_t* __restrict__ fixed, const float* __restrict__ dinv,
+                                                 const float* __restrict__ b, const float* __restrict__ xin,
+                                                 float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float ax = ebe_row(i, r2c_ptr, r2c_item, ye, fixed, dinv, xin);
+    const float di = (c1 < 0.f ? 0.f : c1 * d[i]) + c2 * dinv[i] * (b[i] - ax);
+    d[i] = di;
+    xout[i] = xin[i] + di;
+}
+
+__global__ void __launch_bounds__(kB) k_ebe_residual(int n, const int32_t* __restrict__ r2c_ptr,
+                                                     const int32_t* __restrict__ r2c_item, const float* __restrict__ ye,
+                                                     const int8_t* __restrict__ fixed, const float* __restrict__ dinv,
+                                                     const float* __restrict__ b, const float* __restrict__ x,
+                                                     float* __restrict__ r) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    r[i] = b[i] - ebe_row(i, r2c_ptr, r2c_item, ye, fixed, dinv, x);
+}
+
 // threads per row for a CSR operator of average row length `avg`
 int tpr_for(double avg) {
     if (avg <= 3.0) return 1;
@@ -308,6 +367,7 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
         lv->d.resize(lv->n);
         lv->r.resize(lv->n);
         lv->bin = lv->b.get();
+        if (l == 0) nnz0_ = hl.A.nnz();
         ds << (l ? " " : "") << lv->n << ":" << (l == L - 1 ? (long long)lv->n * lv->n : hl.A.nnz())
            << (l == L - 1 ? ":dense" : "");
         lv_.push_back(std::move(lv));
@@ -356,11 +416,13 @@ void AmgDevice::cycle(int l) {
     FGB_LAUNCH(k_cheb_zero<<<g, kB, 0, stream_>>>(L.n, L.dinv, L.bin, pre_buf(0), L.d.get(), inv_theta));
     for (int k = 1; k < deg; ++k) {
         if (tm) tm->begin(stream_);
-        FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, pre_buf(k - 1), pre_buf(k), L.d.get(), c1[k], c2[k]);
+        if (l == 0) level0_apply(0, pre_buf(k - 1), pre_buf(k), c1[k], c2[k]);
+        else FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, pre_buf(k - 1), pre_buf(k), L.d.get(), c1[k], c2[k]);
         if (tm) tm->end(stream_);
     }
     // coarse-grid correction
-    FGB_TPR_DISPATCH(k_residual, L.tpr, L.n, stream_, A, L.bin, L.xb.get(), L.r.get());
+    if (l == 0) level0_apply(1, L.xb.get(), L.r.get(), 0.f, 0.f);
+    else FGB_TPR_DISPATCH(k_residual, L.tpr, L.n, stream_, A, L.bin, L.xb.get(), L.r.get());
     AmgDevLevel& C = *lv_[l + 1];
     FGB_TPR_DISPATCH(k_csr_apply, L.r_tpr, C.n, stream_, C.n, L.r_ptr.get(), L.r_col.get(), L.r_val.get(), L.r.get(),
                      C.b.get(), 0);
@@ -372,12 +434,55 @@ void AmgDevice::cycle(int l) {
     for (int k = 0; k < deg; ++k) {
         float* xout = (k % 2 == 0) ? L.xa.get() : L.xb.get();
         if (tm) tm->begin(stream_);
-        FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, xin, xout, L.d.get(), k == 0 ? -1.f : c1[k],
-                         k == 0 ? inv_theta : c2[k]);
+        if (l == 0) level0_apply(0, xin, xout, k == 0 ? -1.f : c1[k], k == 0 ? inv_theta : c2[k]);
+        else FGB_TPR_DISPATCH(k_cheb_step, L.tpr, L.n, stream_, A, L.bin, xin, xout, L.d.get(), k == 0 ? -1.f : c1[k],
+                              k == 0 ? inv_theta : c2[k]);
         if (tm) tm->end(stream_);
         xin = xout;
     }
     L.x = xin;
+}
+
+void AmgDevice::set_level0_ebe(const EbeOperator* op) {
+    if (!op) {
+        ebe_on_ = false;
+        return;
+    }
+    ebe_ = *op;
+    ebe_on_ = true;
+    ye_.resize(27 * (size_t)op->n_cells);
+}
+
+double AmgDevice::smoother_bytes() const {
+    const double n = lv_[0]->n;
+    if (!ebe_on_) return (double)nnz0_ * 8.0 + 24.0 * n;
+    const double nc = ebe_.n_cells;
+    // apply: element matrix, cell DoF list, products written, x gathered once per row;
+    // finish: row pointers, items, products gathered, b, D^-1, d read+written, x in/out, flag
+    return nc * (378.0 * 4 + 27.0 * 4 + 27.0 * 4) + n * 4 + (n + 1) * 4 + nc * 27.0 * 8 + n * 25.0;
+}
+
+// one level-0 operator application fused with the Chebyshev update (kind 0) or the residual
+// (kind 1, c1/c2 unused, result in xout)
+void AmgDevice::level0_apply(int kind, const float* xin, float* xout, float c1, float c2) {
+    AmgDevLevel& L = *lv_[0];
+    const int g = grid_for(L.n, kB);
+    if (ebe_on_) {
+        FGB_LAUNCH(k_ebe_apply<<<grid_for(ebe_.n_cells, kB / 32), kB, 0, stream_>>>(ebe_.n_cells, ebe_.cell_dofs, ebe_.ke,
+                                                                                 xin, ye_.get()));
+        if (kind == 0)
+            FGB_LAUNCH(k_ebe_cheb<<<g, kB, 0, stream_>>>(L.n, ebe_.r2c_ptr, ebe_.r2c_item, ye_.get(), ebe_.fixed, L.dinv,
+                                                         L.bin, xin, xout, L.d.get(), c1, c2));
+        else
+            FGB_LAUNCH(k_ebe_residual<<<g, kB, 0, stream_>>>(L.n, ebe_.r2c_ptr, ebe_.r2c_item, ye_.get(), ebe_.fixed,
+                                                             L.dinv, L.bin, xin, xout));
+        return;
+    }
+    const Op A{L.n, L.sptr, L.slen, L.scol, L.val, L.dinv};
+    if (kind == 0)
+        FGB_LAUNCH(k_cheb_step<0><<<g, kB, 0, stream_>>>(A, L.bin, xin, xout, L.d.get(), c1, c2));
+    else
+        FGB_LAUNCH(k_residual<0><<<g, kB, 0, stream_>>>(A, L.bin, xin, xout));
 }
 
 double AmgDevice::time_smoother(int reps) {
@@ -391,10 +496,12 @@ double AmgDevice::time_smoother(int reps) {
     cudaEvent_t e0, e1;
     FGB_CUDA(cudaEventCreate(&e0));
     FGB_CUDA(cudaEventCreate(&e1));
+    const float* bin = L.bin;
+    L.bin = L.b.get();
     auto launch = [&](int i) {
         float* xi = (i & 1) ? L.xb.get() : L.xa.get();
         float* xo = (i & 1) ? L.xa.get() : L.xb.get();
-        FGB_LAUNCH(k_cheb_step<0><<<g, kB, 0, stream_>>>(A, L.b.get(), xi, xo, L.d.get(), 0.5f, 0.5f));
+        level0_apply(0, xi, xo, 0.5f, 0.5f);
     };
     for (int i = 0; i < 3; ++i) launch(i);
     FGB_CUDA(cudaEventRecord(e0, stream_));
@@ -405,6 +512,9 @@ double AmgDevice::time_smoother(int reps) {
     FGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    L.bin = bin;
+    (void)g;
+    (void)A;
     return ms / reps;
 }
 

@@ -52,6 +52,18 @@ AmgHost build_amg(const PreparedMesh& pm, const FemStructure& fs, const std::vec
 
 struct AmgDevLevel;
 
+// Element-by-element form of a level-0 operator (Q2): y = sum over cells of K_e x_e, rows of
+// Dirichlet DoFs replaced by diag * x -- the eliminated operator on vectors that vanish on the
+// Dirichlet DoFs, which every V-cycle vector does
+struct EbeOperator {
+    int n_cells = 0;
+    const int32_t* cell_dofs = nullptr;  // 27 per cell, lattice order
+    const float* ke = nullptr;           // 378 packed upper-triangle entries per cell
+    const int32_t* r2c_ptr = nullptr;    // row -> items 27*cell+local, ascending cell
+    const int32_t* r2c_item = nullptr;
+    const int8_t* fixed = nullptr;       // 1 on Dirichlet rows
+};
+
 // Device side of the hierarchy and the V-cycle (amg.cu).
 class AmgDevice {
 public:
@@ -69,9 +81,20 @@ public:
     double time_smoother(int reps);
     // event pairs around every level-0 Chebyshev step of the V-cycles (when enabled)
     LaunchTimer smoother_timer;
+    // apply level 0 element by element (null operator: back to the SELL matrix)
+    void set_level0_ebe(const EbeOperator* op);
+    bool level0_ebe() const { return ebe_on_; }
+    // algorithmic bytes of one level-0 smoothing step (SELL: nnz*8 + 24 n; element by element:
+    // the packed element matrices, cell DoF lists, per-(cell, local) products and row gathers)
+    double smoother_bytes() const;
 
 private:
     void cycle(int l);
+    void level0_apply(int kind, const float* xin, float* xout, float c1, float c2);  // 0 cheb, 1 residual
+    EbeOperator ebe_;
+    bool ebe_on_ = false;
+    DBuf<float> ye_;
+    int64_t nnz0_ = 0;
     cudaStream_t stream_;
     std::vector<std::unique_ptr<AmgDevLevel>> lv_;
     DBuf<float> coarse_inv_;

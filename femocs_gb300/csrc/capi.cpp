@@ -166,13 +166,13 @@ void femocs_last_solve(FEMOCS* h, int* retval, double* out8) {
 }
 
 static void stats13(const SolveStats& s, double* out) {
-    const double v[13] = {(double)s.iterations, (double)s.outer, (double)s.status, s.rel_residual, s.bnorm,
+    const double v[14] = {(double)s.iterations, (double)s.outer, (double)s.status, s.rel_residual, s.bnorm,
                           s.ms, s.kernel_ms, s.setup_ms, (double)s.levels, s.smoother_ms,
-                          (double)s.smoother_launches, s.spmv_ms, (double)s.spmv_launches};
-    std::copy(v, v + 13, out);
+                          (double)s.smoother_launches, s.spmv_ms, (double)s.spmv_launches, s.smoother_bytes};
+    std::copy(v, v + 14, out);
 }
-int fgb_femocs_last_stats(FEMOCS* h, double* out13) {
-    return guarded([&] { stats13(h->f->last_stats(), out13); return 0; });
+int fgb_femocs_last_stats(FEMOCS* h, double* out14) {
+    return guarded([&] { stats13(h->f->last_stats(), out14); return 0; });
 }
 
 // ---------------------------------------------------------------- Part 2: meshes
@@ -348,8 +348,11 @@ int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol,
     });
     return g ? INT32_MIN : rc;
 }
-int fgb_field_last_stats(const FGB_FIELD* f, double* out13) {
-    return guarded([&] { stats13(f->last, out13); return 0; });
+int fgb_field_last_stats(const FGB_FIELD* f, double* out14) {
+    return guarded([&] { stats13(f->last, out14); return 0; });
+}
+int fgb_field_set_level0_ebe(FGB_FIELD* f, int on) {
+    return guarded([&] { f->f->fem().set_level0_ebe(on != 0); return 0; });
 }
 int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo) {
     return guarded([&] { f->f->fem().set_smoothing(degree, lo); return 0; });

@@ -513,6 +513,16 @@ __global__ void __launch_bounds__(kBlock) k_pcg_rz(int n, const float* __restric
     }
 }
 
+__global__ void k_to_float(long long n, const double* __restrict__ a, float* __restrict__ b) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+__global__ void k_fixed_flags(int n, const int8_t* __restrict__ bc, int anode, int8_t* __restrict__ fixed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) fixed[i] = (bc[i] == 1 || (anode && bc[i] == 2)) ? 1 : 0;
+}
+
 __global__ void k_scale_mul(int n, double* __restrict__ a, const double* __restrict__ b, double s) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] *= s * b[i];
@@ -654,7 +664,14 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
             q2_cell_stiffness(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), stream_);
             q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
                              r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
+            if (level0_ebe_) {
+                ke32_.resize(378 * (size_t)nc_);
+                FGB_LAUNCH(k_to_float<<<grid_for(378LL * nc_, kBlock), kBlock, 0, stream_>>>(378LL * nc_, ke_.get(),
+                                                                                             ke32_.get()));
+            }
         }
+        fixed_.resize(n_);
+        FGB_LAUNCH(k_fixed_flags<<<gb, kBlock, 0, stream_>>>(n_, bc_.get(), anode_dirichlet ? 1 : 0, fixed_.get()));
         const double bc = anode_dirichlet ? 0.0 : applied_field_;
         q2_neumann_rows(n_, r2f_ptr_.get(), r2f_item_.get(), top_faces_.get(), dof_xyz_.get(), bc,
                         has_extra_ ? rhs_extra_.get() : nullptr, rhs_.get(), stream_);
@@ -941,8 +958,7 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     for (int d = 0; d < f1.n_dofs; ++d) fixed1[d] = f1.bc_kind[d] == 1 || (anode && f1.bc_kind[d] == 2);
     AmgHost h1 = build_amg(*pm_, f1, v1, fixed1);
     // the Q1 level is the coarse solve of the Q2 level: smooth it harder
-    const char* e = std::getenv("FGB_Q2_L1_DEG");
-    h1.levels[0].cheb_degree = e ? std::atoi(e) : 4;
+    h1.levels[0].cheb_degree = 4;
     h1.levels[0].cheb_lo = 0.04;
     h1.levels[0].A.col = f1.col;
     h1.levels[0].A.val = std::move(v1);
@@ -998,6 +1014,17 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     h.n_coarse = h1.n_coarse;
     amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
                              dinv32_.get()));
+    if (level0_ebe_) {
+        FGB_REQUIRE(ke32_.size() == 378 * (size_t)nc_, "element matrices not assembled");
+        EbeOperator op;
+        op.n_cells = nc_;
+        op.cell_dofs = cell_dofs_.get();
+        op.ke = ke32_.get();
+        op.r2c_ptr = r2c_ptr_.get();
+        op.r2c_item = r2c_item_.get();
+        op.fixed = fixed_.get();
+        amg_->set_level0_ebe(&op);
+    }
     amg_->smoother_timer.enabled = profiling_;
     amg_anode_ = anode;
     if (st) st->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -1021,6 +1048,12 @@ void FemDevice::download_pattern(std::vector<int64_t>& rowptr, std::vector<int32
 }
 
 std::string FemDevice::amg_levels() const { return amg_ ? amg_->describe() : std::string(); }
+
+void FemDevice::set_level0_ebe(bool on) {
+    FGB_REQUIRE(!on || fs_.order == 2, "the element-by-element level 0 is for Q2 fields");
+    level0_ebe_ = on;
+    amg_.reset();
+}
 
 void FemDevice::set_smoothing(int degree, double lo) {
     FGB_REQUIRE(degree >= 0 && degree <= 15 && lo >= 0 && lo < 1, "smoothing degree 1..15 and interval 0..1");
@@ -1090,6 +1123,7 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     st->rel_residual = bnorm > 0 ? rn / bnorm : rn;
     st->status = bnorm == 0 ? 1 : status;
     st->smoother_ms = amg_->smoother_timer.collect(&st->smoother_launches);
+    st->smoother_bytes = amg_->smoother_bytes();
     st->spmv_ms = spmv_timer_.collect(&st->spmv_launches);
     return st->status == 1 ? it : -it;
 }

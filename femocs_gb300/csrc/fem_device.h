@@ -79,6 +79,7 @@ struct SolveStats {
     // Chebyshev smoothing launches and of the outer FP64 SpMV launches
     int smoother_launches = 0, spmv_launches = 0;
     double smoother_ms = 0, spmv_ms = 0;
+    double smoother_bytes = 0;  // algorithmic bytes of one level-0 smoothing step
 };
 
 class FemDevice {
@@ -94,6 +95,9 @@ public:
     // coarse correction) and the lower end of the interval as a fraction of lambda_max;
     // 0 keeps the default (3 and 0.06). Drops the current hierarchy.
     void set_smoothing(int degree, double lo);
+    // Q2: apply the finest multigrid level element by element or through the assembled SELL
+    // matrix (default: measured faster, the element products' row gather is scattered)
+    void set_level0_ebe(bool on);
     ~FemDevice();
 
     // PoissonSolver::setup + assemble verbs (src/PoissonSolver.cpp:162-210)
@@ -154,6 +158,9 @@ private:
     int smooth_degree_ = 0;
     double smooth_lo_ = 0;
     int q1_gauss_ = 2;  // Gauss points per direction of the Q1 element integrals
+    bool level0_ebe_ = false;
+    DBuf<float> ke32_;      // Q2: FP32 copy of the packed element matrices (element-by-element level 0)
+    DBuf<int8_t> fixed_;    // 1 on Dirichlet rows of the current anode mode
     LaunchTimer spmv_timer_;
     int n_, nc_;
     double applied_field_ = 0, applied_potential_ = 0;

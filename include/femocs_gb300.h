@@ -73,8 +73,8 @@ void femocs_import_mesh(FEMOCS* femocs, int* retval, int n_nodes, const double* 
 /* Statistics of the last femocs_run: iterations, refinement sweeps, status, relative
  * residual, solve milliseconds, #dofs, |b|, multigrid levels (as doubles). */
 void femocs_last_solve(FEMOCS* femocs, int* retval, double* out8);
-/* the 13 statistics of fgb_field_last_stats for the last femocs_run */
-int fgb_femocs_last_stats(FEMOCS* femocs, double* out13);
+/* the 14 statistics of fgb_field_last_stats for the last femocs_run */
+int fgb_femocs_last_stats(FEMOCS* femocs, double* out14);
 const char* femocs_last_error(void);
 /* number of CUDA kernels the library has launched so far (all handles) */
 long long fgb_kernel_launches(void);
@@ -131,11 +131,14 @@ int fgb_field_assemble(FGB_FIELD* f, int full_run, int anode_dirichlet);
 int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol, int max_iter, double inner_tol,
                     double* stats6);
 /* phi per vacuum dof order is internal; these export per hex-mesh node (n_nodes values) */
-/* statistics of the last solve (13 doubles): iterations, refinements, status, rel_residual,
+/* statistics of the last solve (14 doubles): iterations, refinements, status, rel_residual,
  * bnorm, ms, solver-kernel ms (persistent mixed path), multigrid setup ms in that call,
  * levels, and with profiling on (multigrid path): level-0 smoother ms, smoother launches,
- * outer FP64 SpMV ms, SpMV launches */
-int fgb_field_last_stats(const FGB_FIELD* f, double* out13);
+ * outer FP64 SpMV ms, SpMV launches; algorithmic bytes of one level-0 smoothing step */
+int fgb_field_last_stats(const FGB_FIELD* f, double* out14);
+/* Q2 fields: apply the finest multigrid level element by element (1) or through the
+ * assembled SELL matrix (0, default); the hierarchy is rebuilt at the next solve */
+int fgb_field_set_level0_ebe(FGB_FIELD* f, int on);
 /* Chebyshev smoothing of the finest multigrid level: steps before and after the coarse
  * correction (0: default 3) and the interval's lower end as a fraction of lambda_max
  * (0: default 0.06); the hierarchy is rebuilt at the next solve */

@@ -131,3 +131,21 @@ def test_q2_pipeline_against_q1(q2):
     scale = np.abs(o1[:, 4]).max()
     d = np.abs(o2[:, 4] - o1[:, 4]).max()
     assert 0 < d < 0.05 * scale
+
+
+def test_q2_level0_element_by_element_matches_sell(q2):
+    """The finest multigrid level applied element by element is the same operator as the
+    assembled SELL matrix (FP32 rounding aside): same convergence, same solution."""
+    m, f, keys = q2
+    out = {}
+    for ebe in (True, False):
+        f.set_level0_ebe(ebe)
+        f.setup(-E0)
+        f.assemble(True, False)
+        rc, st = f.solve(precision=2, rel_tol=1e-10)
+        assert rc > 0 and st["status"] == 1
+        out[ebe] = (st["iterations"], f.solution())
+    f.set_level0_ebe(False)
+    assert abs(out[True][0] - out[False][0]) <= 2
+    x = out[False][1]
+    assert np.abs(out[True][1] - x).max() <= 2e3 * 1e-10 * np.abs(x).max()
