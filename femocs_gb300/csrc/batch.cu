@@ -5,7 +5,7 @@
 //                  per-mesh p.q -> alpha
 //   kb_update      NEW: r = b - q; RUNNING: x += alpha p, r -= alpha q; FP32 copy of r;
 //                  per-mesh r.r -> stop test
-//   kb_cheb_*      degree-3 Chebyshev smoothing on D^-1 A scaled by 1/lambda_max of the mesh
+//   kb_cheb_*      degree-4 Chebyshev smoothing on D^-1 A scaled by 1/lambda_max of the mesh
 //                  and level, so one coefficient set serves every mesh
 //   kb_residual, kb_csr_apply (restriction / prolongation), kb_dense (coarsest level)
 //   kb_rz          per-mesh r.z -> beta (0 and phase RUNNING after a NEW pass)
@@ -120,14 +120,14 @@ namespace {
 
 constexpr int kB = kBatchRows;
 
-// Chebyshev smoothing of degree kDeg on [0.06, 1.1] for D^-1 A scaled to lambda_max = 1:
+// Chebyshev smoothing of degree kDeg on [0.04, 1.1] for D^-1 A scaled to lambda_max = 1:
 // step k: d_k = c1[k] d_{k-1} + c2[k] D^-1 r, rho_0 = 1/sigma, rho_k = 1/(2 sigma - rho_{k-1})
-constexpr int kDeg = 3;
+constexpr int kDeg = 4;
 struct Cheb {
     float c1[kDeg], c2[kDeg], inv_theta;
 };
 Cheb cheb_coefficients() {
-    const double lmax = 1.1, lmin = 0.06;
+    const double lmax = 1.1, lmin = 0.04;
     const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
     Cheb c{};
     double rho = 1.0 / sigma;

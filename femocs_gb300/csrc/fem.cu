@@ -900,8 +900,8 @@ void FemDevice::ensure_amg(SolveStats* st) {
     std::vector<int8_t> fixed(n_, 0);
     for (int d = 0; d < n_; ++d) fixed[d] = fs_.bc_kind[d] == 1 || (anode && fs_.bc_kind[d] == 2);
     AmgHost h = build_amg(*pm_, fs_, vals, fixed);
-    h.levels[0].cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 3;
-    h.levels[0].cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.06;
+    h.levels[0].cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 4;
+    h.levels[0].cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.04;
     amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
                              dinv32_.get()));
     amg_->smoother_timer.enabled = profiling_;

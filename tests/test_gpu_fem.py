@@ -102,8 +102,8 @@ def test_multigrid_iteration_economy():
     f.set_profiling(False)
     assert s3["setup_ms"] == 0 and s3["iterations"] == s2["iterations"]
     it = s3["iterations"]
-    # degree-3 Chebyshev: 2 steps after the zero-start step before, 3 after the correction
-    assert s3["smoother_launches"] == 5 * it and s3["spmv_launches"] == it
+    # degree-4 Chebyshev: 3 steps after the zero-start step before, 4 after the correction
+    assert s3["smoother_launches"] == 7 * it and s3["spmv_launches"] == it
     assert 0 < s3["smoother_ms"] < s3["ms"] and 0 < s3["spmv_ms"] < s3["ms"]
     assert f.time_spmv(2, 5) > 0
 
