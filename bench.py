@@ -480,7 +480,7 @@ def run_batch(args, world, rank):
     b.mark(0)
     results = [step(slots) for _ in range(args.steps)]
     b.mark(1)
-    dev_ms = b.elapsed(0, 1)
+    dev_ms = reduce_max(world, b.elapsed(0, 1))
     launches = lib.fgb_kernel_launches() - launches0
     clocks = sampler.stop(0)
     res = results[-1]
@@ -509,7 +509,7 @@ def run_batch(args, world, rank):
     sample_dofs = int(sum(dofs[slots.index(s_)] for s_ in sample))
     line = {
         "metric": "solved DOF/s and p50/p99 solve latency at 1e-9 rel. residual vs plain FP64 CG",
-        "value": total * args.steps / (dev_ms * 1e-3), "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+        "value": world * total * args.steps / (dev_ms * 1e-3), "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64 CG / f32 multigrid preconditioner",
         "data": "synthetic (seeded random nanotips)",
@@ -517,7 +517,7 @@ def run_batch(args, world, rank):
                                "Q1 2e4-8e5 vacuum hexes log-uniform, one graph-captured launch",
                    "n_meshes": n_mesh, "total_dofs": total, "rel_tol": REL_TOL,
                    "l2": "inputs larger than L2 (level-0 matrices %.1f GB)" % (total * 25 * 12 / 1e9)},
-        "batch": {"solves_per_s": n_mesh * args.steps / (dev_ms * 1e-3), "converged": int(conv),
+        "batch": {"solves_per_s": world * n_mesh * args.steps / (dev_ms * 1e-3), "converged": int(conv),
                   "iterations_p50": float(np.median(its)), "iterations_max": int(its.max()),
                   "dofs_min": int(dofs.min()), "dofs_max": int(dofs.max()), "build_s": build_s,
                   "device_bytes": b.stats()["device_bytes"], "tuning": b.tuning(),
@@ -579,6 +579,11 @@ def run_serve(args, world, rank):
                       "converged": int((rec["status"] == 1).sum()),
                       "solves_per_s": len(lat) / (rec["t_done"].max() - rec["t_submit"].min()),
                       "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                      # where a request's time goes (medians): waiting for its run / the
+                      # scheduler, solving in the batch, nodal field + interpolation + copy
+                      "p50_queue_ms": float(np.median(rec["t_admit"] - rec["t_submit"]) * 1e3),
+                      "p50_solve_ms": float(np.median(rec["t_solved"] - rec["t_admit"]) * 1e3),
+                      "p50_post_ms": float(np.median(rec["t_done"] - rec["t_solved"]) * 1e3),
                       "iterations_mean": float(rec["iterations"].mean()), "wall_s": wall})
     launches = lib.fgb_kernel_launches() - launches0
     clocks = sampler.stop(0)
