@@ -988,8 +988,10 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     l0.A.n_rows = l0.A.n_cols = n_;
     l0.A.ptr.assign(1, fs_.nnz());  // structure lives on the device; nnz for reporting
     l0.lambda = estimate_lambda(15);
-    l0.cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 3;
-    l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.06;
+    // degree 2 on [0.1, 1.1]: more iterations than degree 3-4 but fewer passes over the big Q2
+    // matrix per cycle (config 2: 95 iterations / 1.11 s vs 84 / 1.23 s at degree 3)
+    l0.cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 2;
+    l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.1;
     l0.R.n_rows = P.n_cols;
     l0.R.n_cols = P.n_rows;
     {

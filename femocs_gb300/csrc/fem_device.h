@@ -93,7 +93,7 @@ public:
     void set_profiling(bool on);
     // Chebyshev smoothing of the finest multigrid level: degree (steps before and after the
     // coarse correction) and the lower end of the interval as a fraction of lambda_max;
-    // 0 keeps the default (Q1: 4 and 0.04; Q2: 3 and 0.06). Drops the current hierarchy.
+    // 0 keeps the default (Q1: 4 and 0.04; Q2: 2 and 0.1). Drops the current hierarchy.
     void set_smoothing(int degree, double lo);
     // Q2: apply the finest multigrid level element by element or through the assembled SELL
     // matrix (default: measured faster, the element products' row gather is scattered)

@@ -4,7 +4,7 @@
 //                        points on the trilinear (Q1) map of the hex, one warp per cell: lanes
 //                        0..26 own the quadrature points for the Jacobians and the nodes for
 //                        the physical gradients, every lane accumulates 11-12 of the 378
-//                        upper-triangle entries (FP64: ~47k FMA per cell, the FP64 pipe bounds it)
+//                        upper-triangle entries (FP64: ~31k FMA per cell, the FP64 pipe bounds it)
 //   k_q2_assemble_rows   row-owned gather of the element matrices into the saved SELL-layout
 //                        matrix, one warp per row: the row's columns in shared memory, one
 //                        cell at a time, lanes 0..26 place the cell's 27 contributions by binary
@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
     __shared__ double sX[kQ2Warps][8][3];
     __shared__ double sInv[kQ2Warps][27][10];  // J^-1 (row major) and w |det J| per point
     __shared__ double sG[kQ2Warps][27][3];
+    __shared__ double sGw[kQ2Warps][27][3];  // w |det J| times the gradients
     // shape-gradient tables in shared memory: lanes read them at different addresses, which
     // the constant cache would serialise
     __shared__ double sDN[27 * 27 * 3];
@@ -145,17 +146,21 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
         if (lane < 27) {
             const double* inv = sInv[wid][q];
             const double* g = sDN + (q * 27 + lane) * 3;
-            // physical gradient: (J^-T g)_a = sum_k inv[k][a] g_k
+            // physical gradient: (J^-T g)_a = sum_k inv[k][a] g_k; the weight folded into one copy
+            const double w = inv[9];
 #pragma unroll
-            for (int a = 0; a < 3; ++a) sG[wid][lane][a] = inv[a] * g[0] + inv[3 + a] * g[1] + inv[6 + a] * g[2];
+            for (int a = 0; a < 3; ++a) {
+                const double ga = inv[a] * g[0] + inv[3 + a] * g[1] + inv[6 + a] * g[2];
+                sG[wid][lane][a] = ga;
+                sGw[wid][lane][a] = w * ga;
+            }
         }
         __syncwarp();
-        const double w = sInv[wid][q][9];
 #pragma unroll
         for (int t = 0; t < 12; ++t) {
-            const double* gi = sG[wid][ei[t]];
+            const double* gi = sGw[wid][ei[t]];
             const double* gj = sG[wid][ej[t]];
-            acc[t] += w * (gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2]);
+            acc[t] += gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2];
         }
     }
     double* o = ke + 378 * (size_t)c;

@@ -140,8 +140,8 @@ int fgb_field_last_stats(const FGB_FIELD* f, double* out14);
  * assembled SELL matrix (0, default); the hierarchy is rebuilt at the next solve */
 int fgb_field_set_level0_ebe(FGB_FIELD* f, int on);
 /* Chebyshev smoothing of the finest multigrid level: steps before and after the coarse
- * correction (0: default, Q1 4, Q2 3) and the interval's lower end as a fraction of
- * lambda_max (0: default, Q1 0.04, Q2 0.06); the hierarchy is rebuilt at the next solve */
+ * correction (0: default, Q1 4, Q2 2) and the interval's lower end as a fraction of
+ * lambda_max (0: default, Q1 0.04, Q2 0.1); the hierarchy is rebuilt at the next solve */
 int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo);
 /* record CUDA event pairs around the multigrid path's hot launches (off by default) */
 int fgb_field_set_profiling(FGB_FIELD* f, int on);
