@@ -157,6 +157,10 @@ class Field:
         self._ok(load().fgb_field_last_stats(self.h, ptr(st)))
         return rc, _stats_dict(st)
 
+    def set_outer_spmv(self, mode=1):
+        """Outer SpMV of the multigrid PCG: 1 FP32 hi/lo pairs, 0 FP64 matrix (default)."""
+        self._ok(load().fgb_field_set_outer_spmv(self.h, int(mode)))
+
     def set_level0_ebe(self, on=True):
         """Q2: finest multigrid level element by element (True) or through the SELL matrix
         (False, the default)."""

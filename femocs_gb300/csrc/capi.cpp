@@ -351,6 +351,9 @@ int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol,
 int fgb_field_last_stats(const FGB_FIELD* f, double* out14) {
     return guarded([&] { stats13(f->last, out14); return 0; });
 }
+int fgb_field_set_outer_spmv(FGB_FIELD* f, int mode) {
+    return guarded([&] { f->f->fem().set_outer_spmv(mode); return 0; });
+}
 int fgb_field_set_level0_ebe(FGB_FIELD* f, int on) {
     return guarded([&] { f->f->fem().set_level0_ebe(on != 0); return 0; });
 }

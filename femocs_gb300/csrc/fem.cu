@@ -390,6 +390,68 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_pq(int n, const int64_t* __r
     }
 }
 
+// ---- FP64-accurate SpMV from FP32 pairs ("double-float"): GB300 runs FP64 at 1/64 of the FP32
+// rate, so the outer CG's A p reads the matrix as hi + lo FP32 pairs (hi = fl32(a), lo =
+// fl32(a - hi)) and p as hi + lo pairs, forms every product with an error-free FMA split and
+// sums each row with TwoSum (Dekker/Knuth); the FP64 pipe only sees one conversion per row.
+// Accuracy ~2^-48 relative per term (FP64: 2^-53); the bytes per nonzero equal the FP64
+// matrix's (4 + 4 value, 4 column).
+// the _rn intrinsics are never contracted into FMAs, which the error-free steps rely on
+__device__ __forceinline__ void df_add(float& sh, float& sl, float prod, float small) {
+    const float s = __fadd_rn(sh, prod);
+    const float bb = __fsub_rn(s, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(prod, bb));  // TwoSum error
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(e, small));
+}
+
+__device__ __forceinline__ void df_term(float& sh, float& sl, float ah, float al, float ph, float pl) {
+    const float prod = __fmul_rn(ah, ph);
+    const float perr = __fmaf_rn(ah, ph, -prod);  // exact rounding error of ah * ph
+    const float cross = __fadd_rn(__fmaf_rn(ah, pl, __fmul_rn(al, ph)), perr);
+    df_add(sh, sl, prod, cross);
+}
+
+__global__ void __launch_bounds__(kBlock) k_cg_spmv_pq_df(int n, const int64_t* __restrict__ sptr,
+                                                          const int32_t* __restrict__ slen,
+                                                          const int32_t* __restrict__ scol, const float* __restrict__ vhi,
+                                                          const float* __restrict__ vlo, const float* __restrict__ phi,
+                                                          const float* __restrict__ plo, const double* __restrict__ p,
+                                                          double* __restrict__ q, double* partial, CgState* st) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n) {
+        const int s = i >> 5;
+        const int64_t base = sptr[s] + (int64_t)(i & 31) * 4;
+        const int nch = slen[s] >> 2;
+        float sh = 0.f, sl = 0.f;
+        for (int c = 0; c < nch; ++c) {
+            const int64_t o = base + (int64_t)c * 128;
+            const int4 ci = __ldg(reinterpret_cast<const int4*>(scol + o));
+            const float4 hi = __ldg(reinterpret_cast<const float4*>(vhi + o));
+            const float4 lo = __ldg(reinterpret_cast<const float4*>(vlo + o));
+            df_term(sh, sl, hi.x, lo.x, __ldg(phi + ci.x), __ldg(plo + ci.x));
+            df_term(sh, sl, hi.y, lo.y, __ldg(phi + ci.y), __ldg(plo + ci.y));
+            df_term(sh, sl, hi.z, lo.z, __ldg(phi + ci.z), __ldg(plo + ci.z));
+            df_term(sh, sl, hi.w, lo.w, __ldg(phi + ci.w), __ldg(plo + ci.w));
+        }
+        const double qi = (double)sh + (double)sl;
+        q[i] = qi;
+        v[0] = p[i] * qi;
+    }
+    if (grid_reduce<1>(v, partial, &st->ticket)) {
+        st->pq = v[0];
+        st->alpha = st->rz / v[0];
+    }
+}
+
+// lo = fl32(a - fl32(a)) for every stored entry
+__global__ void k_split_lo(long long n, const double* __restrict__ a, const float* __restrict__ hi, float* __restrict__ lo) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) lo[i] = (float)(a[i] - (double)hi[i]);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_update(int n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                                                       const T* __restrict__ q, const T* __restrict__ dinv, T* __restrict__ z,
@@ -466,14 +528,19 @@ __global__ void k_to32(int n, const double* __restrict__ a, float* __restrict__ 
     if (i < n) b[i] = (float)a[i];
 }
 
-// p = z (the V-cycle result, FP32), rz = r.z
+// p = z (the V-cycle result, FP32), rz = r.z; phi/plo: the FP32 pair of p (may be null)
 __global__ void __launch_bounds__(kBlock) k_pcg_start(int n, const float* __restrict__ z32, const double* __restrict__ r,
-                                                      double* __restrict__ p, double* partial, CgState* st) {
+                                                      double* __restrict__ p, float* __restrict__ phi,
+                                                      float* __restrict__ plo, double* partial, CgState* st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (i < n) {
         const double zi = (double)z32[i];
         p[i] = zi;
+        if (phi) {
+            phi[i] = z32[i];
+            plo[i] = 0.f;
+        }
         v[0] = r[i] * zi;
     }
     if (grid_reduce<1>(v, partial, &st->ticket)) st->rz = v[0];
@@ -533,13 +600,20 @@ __global__ void k_scale_copy64(int n, const double* __restrict__ a, double s, do
     if (i < n) out[i] = s * a[i];
 }
 
-// p = z + beta p
+// p = z + beta p (and its FP32 pair when phi is not null)
 __global__ void __launch_bounds__(kBlock) k_pcg_direction(int n, const float* __restrict__ z32, double* __restrict__ p,
+                                                          float* __restrict__ phi, float* __restrict__ plo,
                                                           const CgState* st) {
     if (st->done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    p[i] = (double)z32[i] + st->beta * p[i];
+    const double pi = (double)z32[i] + st->beta * p[i];
+    p[i] = pi;
+    if (phi) {
+        const float h = (float)pi;
+        phi[i] = h;
+        plo[i] = (float)(pi - (double)h);
+    }
 }
 
 }  // namespace
@@ -658,6 +732,7 @@ void FemDevice::set_space_charge(const double* d_extra) {
 
 void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
     anode_dirichlet_ = anode_dirichlet;
+    split_valid_ = false;
     const int gb = grid_for(n_, kBlock);
     if (fs_.order == 2) {
         if (full_run) {
@@ -1051,6 +1126,19 @@ void FemDevice::download_pattern(std::vector<int64_t>& rowptr, std::vector<int32
 
 std::string FemDevice::amg_levels() const { return amg_ ? amg_->describe() : std::string(); }
 
+void FemDevice::ensure_split() {
+    if (split_valid_) return;
+    const long long ne = (long long)fs_.slice_ptr.back();
+    sell_lo_.resize(ne);
+    FGB_LAUNCH(k_split_lo<<<grid_for(ne, kBlock), kBlock, 0, stream_>>>(ne, sell64_.get(), sell32_.get(), sell_lo_.get()));
+    split_valid_ = true;
+}
+
+void FemDevice::set_outer_spmv(int mode) {
+    FGB_REQUIRE(mode == 0 || mode == 1, "outer SpMV mode 0 (FP64) or 1 (FP32 pairs)");
+    outer_df_ = mode == 1;
+}
+
 void FemDevice::set_level0_ebe(bool on) {
     FGB_REQUIRE(!on || fs_.order == 2, "the element-by-element level 0 is for Q2 fields");
     level0_ebe_ = on;
@@ -1089,16 +1177,34 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
                                                        x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
     FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
     FGB_CUDA(cudaStreamSynchronize(stream_));
-    int status = 0, it = 0;
-    if (h_state_->rr <= init.tol2 || bnorm == 0) status = 1;
-    if (status == 0) {
+    int status = 0, it = 0, restarts = 0;
+    double rr_true = h_state_->rr;
+    if (rr_true <= init.tol2 || bnorm == 0) status = 1;
+    const bool df = outer_df_;
+    if (df && status == 0) {
+        ensure_split();
+        phi_.resize(n_);
+        plo_.resize(n_);
+    }
+    float* ph = df ? phi_.get() : nullptr;
+    float* pl = df ? plo_.get() : nullptr;
+    // Convergence is declared on the FP64 true residual b - A x: when the recursion reports
+    // convergence, r is recomputed exactly and CG restarts from it if it is still above the
+    // tolerance (the FP32-pair SpMV lets the recursive residual drift by ~2^-48 per term)
+    while (status == 0) {
         FGB_LAUNCH(k_to32<<<gb, kBlock, 0, stream_>>>(n_, r64_.get(), r32_.get()));
         const float* z = amg_->vcycle(r32_.get());
-        FGB_LAUNCH(k_pcg_start<<<gb, kBlock, 0, stream_>>>(n_, z, r64_.get(), p64_.get(), partial_.get(), ds));
+        FGB_LAUNCH(k_pcg_start<<<gb, kBlock, 0, stream_>>>(n_, z, r64_.get(), p64_.get(), ph, pl, partial_.get(), ds));
         while (true) {
             spmv_timer_.begin(stream_);
-            FGB_LAUNCH(k_cg_spmv_pq<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
-                                                                        sell64_.get(), p64_.get(), q64_.get(), partial_.get(), ds));
+            if (df)
+                FGB_LAUNCH(k_cg_spmv_pq_df<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                                      sell32_.get(), sell_lo_.get(), ph, pl, p64_.get(),
+                                                                      q64_.get(), partial_.get(), ds));
+            else
+                FGB_LAUNCH(k_cg_spmv_pq<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(),
+                                                                            sell_col_.get(), sell64_.get(), p64_.get(),
+                                                                            q64_.get(), partial_.get(), ds));
             spmv_timer_.end(stream_);
             FGB_LAUNCH(k_pcg_update<<<gb, kBlock, 0, stream_>>>(n_, x_.get(), r64_.get(), p64_.get(), q64_.get(), r32_.get(),
                                                                partial_.get(), ds));
@@ -1111,17 +1217,29 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
             }
             const float* zi = amg_->vcycle(r32_.get());
             FGB_LAUNCH(k_pcg_rz<<<gb, kBlock, 0, stream_>>>(n_, zi, r64_.get(), partial_.get(), ds));
-            FGB_LAUNCH(k_pcg_direction<<<gb, kBlock, 0, stream_>>>(n_, zi, p64_.get(), ds));
+            FGB_LAUNCH(k_pcg_direction<<<gb, kBlock, 0, stream_>>>(n_, zi, p64_.get(), ph, pl, ds));
         }
+        // true FP64 residual of the current x (also the restart residual)
+        FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                           sell64_.get(), x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
+        FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        rr_true = h_state_->rr;
+        if (status != 1 || rr_true <= init.tol2 || restarts >= 3 || it >= opt.max_iter) {
+            if (status == 1 && rr_true > init.tol2) status = -1;  // recursion converged, x did not
+            break;
+        }
+        ++restarts;
+        status = 0;
+        CgState again = *h_state_;
+        again.done = 0;
+        again.status = 0;
+        again.ticket = 0;
+        FGB_CUDA(cudaMemcpyAsync(ds, &again, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
     }
     st->iterations = it;
-    st->outer = 0;
-    // report the true FP64 residual
-    FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(),
-                                                       x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
-    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
-    FGB_CUDA(cudaStreamSynchronize(stream_));
-    const double rn = std::sqrt(h_state_->rr);
+    st->outer = restarts;
+    const double rn = std::sqrt(rr_true);
     st->rel_residual = bnorm > 0 ? rn / bnorm : rn;
     st->status = bnorm == 0 ? 1 : status;
     st->smoother_ms = amg_->smoother_timer.collect(&st->smoother_launches);

@@ -159,3 +159,23 @@ def test_nonconvergence_reports_failure(tip):
     f.assemble(True, False)
     rc, st = f.solve(precision=0, rel_tol=1e-14, max_iter=5)
     assert rc < 0 and st["status"] != 1
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_outer_spmv_fp32_pairs_matches_fp64(order):
+    """The outer SpMV from FP32 hi/lo pairs is FP64-accurate: same iterations (within 1), same
+    solution within the solve tolerance, true FP64 residual at the tolerance."""
+    m = fg.Mesh.synthetic(**TIP) if order == 1 else fg.Mesh.synthetic(
+        radius=5.0, height=14.0, box_half=18.0, slab=4.0, top=40.0, h=4.0, growth=1.6, margin=3.0)
+    f = fg.Field(m, order=order)
+    out = {}
+    for mode in (0, 1):
+        f.set_outer_spmv(mode)
+        f.setup(0.1)
+        f.assemble(True, False)
+        rc, st = f.solve(precision=2, rel_tol=1e-11)
+        assert rc > 0 and st["status"] == 1 and st["rel_residual"] <= 2e-11
+        out[mode] = (st["iterations"], f.solution())
+    assert abs(out[0][0] - out[1][0]) <= 1
+    x = out[0][1]
+    assert np.abs(out[1][1] - x).max() <= 2e3 * 1e-11 * np.abs(x).max()
