@@ -214,6 +214,30 @@ def cpu_baseline(field, workload, n_points, pts, spec, order=1, budget_s=15.0):
                        f"iterations to 1e-9 ({how}); solve only")
 
 
+MESH_TABLES = ["tet_nodes", "tet_marker", "tet_nbor", "node_xyz", "node_marker", "hex_nodes", "hex_marker", "tet_det",
+               "tet_centroid", "hex_coeffs", "nbr_ptr", "nbr_idx", "quad_nodes", "voro_ptr", "voro_idx",
+               "vac_node2vertex", "vac_cells", "tet_search", "edgemax", "node_parents"]
+
+
+def mesh_prep_timing(spec):
+    """Tet -> hex split, grouping and interpolation tables of the workload's mesh: host builder
+    against the kernels (second device run; the first warms the allocator), tables compared
+    byte for byte. Outside the timed steps (the bench mesh is prepared once)."""
+    import numpy as np
+    import femocs_gb300 as fg
+    mh = fg.Mesh.synthetic(**spec)
+    fg.Mesh.synthetic(device=True, **spec)
+    md = fg.Mesh.synthetic(device=True, **spec)
+    equal = mh.sizes() == md.sizes() and all(
+        np.array_equal(np.ascontiguousarray(mh.export(t)).view(np.uint8), np.ascontiguousarray(md.export(t)).view(np.uint8))
+        for t in MESH_TABLES)
+    th, td = mh.prep_timing(), md.prep_timing()
+    s = md.sizes()
+    return {"tets": s["n_tets"], "hexes": s["n_hexs"], "nodes": s["n_nodes"], "host_ms": th["total_ms"],
+            "device_ms": td["total_ms"], "device_kernel_ms": td["kernel_ms"], "tables_equal": bool(equal),
+            "note": "device_ms includes the tet upload and the download of every table into host memory"}
+
+
 def run_ours(args, world, rank):
     import numpy as np
     import femocs_gb300 as fg
@@ -374,6 +398,8 @@ def run_ours(args, world, rank):
     }
     if rank == 0 and world == 1 and not args.no_cpu and SSOR_ITERS.get(args.workload):
         line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec, order)
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["mesh_prep"] = mesh_prep_timing(spec)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -46,17 +46,28 @@ class Mesh:
         self._sizes = None
 
     @classmethod
-    def from_arrays(cls, xyz, tets, markers):
+    def from_arrays(cls, xyz, tets, markers, device=False):
+        """Prepare a tet mesh (vertices, 4 vertex ids per tet, one region marker per tet) on
+        the host or, with device=True, by kernels on the current CUDA device (same tables)."""
         lib = load()
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
         tets = np.ascontiguousarray(tets, dtype=np.int32).reshape(-1)
         markers = np.ascontiguousarray(markers, dtype=np.int32).reshape(-1)
-        return cls(lib.fgb_mesh_from_arrays(len(xyz) // 3, ptr(xyz), len(tets) // 4, ptr(tets, ip), ptr(markers, ip)))
+        fn = lib.fgb_mesh_from_arrays_device if device else lib.fgb_mesh_from_arrays
+        return cls(fn(len(xyz) // 3, ptr(xyz), len(tets) // 4, ptr(tets, ip), ptr(markers, ip)))
 
     @classmethod
-    def synthetic(cls, **kw):
+    def synthetic(cls, device=False, **kw):
         spec = nanotip(**kw)
-        return cls(load().fgb_mesh_synthetic(C.byref(spec)))
+        fn = load().fgb_mesh_synthetic_device if device else load().fgb_mesh_synthetic
+        return cls(fn(C.byref(spec)))
+
+    def prep_timing(self):
+        """{"kernel_ms": device time of the preparation kernels (0 on the host),
+        "total_ms": wall time of the preparation}"""
+        o = np.zeros(2)
+        load().fgb_mesh_prep_timing(self.h, ptr(o))
+        return dict(kernel_ms=float(o[0]), total_ms=float(o[1]))
 
     @classmethod
     def read_gmsh(cls, path):

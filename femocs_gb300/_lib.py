@@ -51,6 +51,9 @@ _PROTOS = {
     "fgb_mesh_from_arrays": (vp, [C.c_int, dp, C.c_int, ip, ip]),
     "fgb_mesh_read_gmsh": (vp, [C.c_char_p]),
     "fgb_mesh_synthetic": (vp, [C.POINTER(FgbNanotip)]),
+    "fgb_mesh_from_arrays_device": (vp, [C.c_int, dp, C.c_int, ip, ip]),
+    "fgb_mesh_synthetic_device": (vp, [C.POINTER(FgbNanotip)]),
+    "fgb_mesh_prep_timing": (C.c_int, [vp, dp]),
     "fgb_mesh_free": (None, [vp]),
     "fgb_mesh_sizes": (C.c_int, [vp, i64p]),
     "fgb_mesh_export": (C.c_int, [vp, C.c_char_p, vp]),

@@ -1,6 +1,7 @@
 // extern "C" shims over the C++ classes; no exception crosses this boundary. Failures are
 // reported through retval = 1 (reference convention) or a NULL / negative return, with the
 // message available from femocs_last_error().
+#include <chrono>
 #include <cstring>
 #include <memory>
 
@@ -10,6 +11,7 @@
 #include "facade.h"
 #include "server.h"
 #include "femocs_gb300.h"
+#include "mesh_prep.h"
 #include "synth.h"
 
 using namespace fgb;
@@ -19,6 +21,7 @@ struct FEMOCS {
 };
 struct FGB_MESH {
     std::shared_ptr<PreparedMesh> pm;
+    MeshPrepTiming timing;  // device: kernel and total ms; host: total ms
 };
 struct FGB_BATCH {
     std::unique_ptr<BatchSolver> b;
@@ -176,18 +179,63 @@ int fgb_femocs_last_stats(FEMOCS* h, double* out14) {
 }
 
 // ---------------------------------------------------------------- Part 2: meshes
+namespace {
+TetMesh tet_mesh_of(int n_nodes, const double* xyz, int n_tets, const int* tets, const int* markers) {
+    FGB_REQUIRE(n_nodes >= 0 && n_tets >= 0 && (xyz || !n_nodes) && ((tets && markers) || !n_tets),
+                "invalid mesh arrays");
+    TetMesh tm;
+    tm.xyz.assign(xyz, xyz + 3 * (size_t)n_nodes);
+    tm.tets.assign(tets, tets + 4 * (size_t)n_tets);
+    tm.marker.assign(markers, markers + n_tets);
+    return tm;
+}
+// host (prepare_mesh) or device (prepare_mesh_device) preparation, timed
+void prepare_into(FGB_MESH* m, TetMesh&& tm, bool device) {
+    if (device) {
+        cudaStream_t s;
+        FGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        try {
+            m->pm = std::make_shared<PreparedMesh>(prepare_mesh_device(std::move(tm), s, &m->timing));
+        } catch (...) {
+            cudaStreamDestroy(s);
+            throw;
+        }
+        cudaStreamDestroy(s);
+    } else {
+        const auto t0 = std::chrono::steady_clock::now();
+        m->pm = std::make_shared<PreparedMesh>(prepare_mesh(std::move(tm)));
+        m->timing.kernel_ms = 0;
+        m->timing.total_ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+}
+}  // namespace
+
 FGB_MESH* fgb_mesh_from_arrays(int n_nodes, const double* xyz, int n_tets, const int* tets, const int* markers) {
     FGB_MESH* m = new FGB_MESH;
     const int rc = guarded([&] {
-        TetMesh tm;
-        tm.xyz.assign(xyz, xyz + 3 * (size_t)n_nodes);
-        tm.tets.assign(tets, tets + 4 * (size_t)n_tets);
-        tm.marker.assign(markers, markers + n_tets);
-        m->pm = std::make_shared<PreparedMesh>(prepare_mesh(std::move(tm)));
+        prepare_into(m, tet_mesh_of(n_nodes, xyz, n_tets, tets, markers), false);
         return 0;
     });
     if (rc) { delete m; return nullptr; }
     return m;
+}
+FGB_MESH* fgb_mesh_from_arrays_device(int n_nodes, const double* xyz, int n_tets, const int* tets,
+                                      const int* markers) {
+    FGB_MESH* m = new FGB_MESH;
+    const int rc = guarded([&] {
+        prepare_into(m, tet_mesh_of(n_nodes, xyz, n_tets, tets, markers), true);
+        return 0;
+    });
+    if (rc) { delete m; return nullptr; }
+    return m;
+}
+int fgb_mesh_prep_timing(const FGB_MESH* m, double* out2) {
+    return guarded([&] {
+        out2[0] = m->timing.kernel_ms;
+        out2[1] = m->timing.total_ms;
+        return 0;
+    });
 }
 FGB_MESH* fgb_mesh_read_gmsh(const char* path) {
     FGB_MESH* m = new FGB_MESH;
@@ -201,7 +249,16 @@ FGB_MESH* fgb_mesh_read_gmsh(const char* path) {
 FGB_MESH* fgb_mesh_synthetic(const FgbNanotip* spec) {
     FGB_MESH* m = new FGB_MESH;
     const int rc = guarded([&] {
-        m->pm = std::make_shared<PreparedMesh>(prepare_mesh(make_nanotip_mesh(to_spec(spec))));
+        prepare_into(m, make_nanotip_mesh(to_spec(spec)), false);
+        return 0;
+    });
+    if (rc) { delete m; return nullptr; }
+    return m;
+}
+FGB_MESH* fgb_mesh_synthetic_device(const FgbNanotip* spec) {
+    FGB_MESH* m = new FGB_MESH;
+    const int rc = guarded([&] {
+        prepare_into(m, make_nanotip_mesh(to_spec(spec)), true);
         return 0;
     });
     if (rc) { delete m; return nullptr; }

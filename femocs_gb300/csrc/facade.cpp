@@ -1,4 +1,5 @@
 #include "facade.h"
+#include "mesh_prep.h"
 
 #include <algorithm>
 #include <cctype>
@@ -124,10 +125,19 @@ void FemocsFacade::read_params() {
     precision_ = prec == "fp64" ? 0 : (prec == "mixed" ? 1 : 2);
     conf_.get("gpu_use_abs_tol", use_abs_tol_);
     conf_.get("gpu_element_order", element_order_);
+    std::string prep = "device";
+    conf_.get("gpu_mesh_prep", prep);
+    FGB_REQUIRE(prep == "device" || prep == "host", "gpu_mesh_prep must be device or host");
+    mesh_prep_device_ = prep == "device";
     FGB_REQUIRE(element_order_ == 1 || element_order_ == 2, "gpu_element_order must be 1 or 2");
     double lim[2];
     if (conf_.get("field_limit_min", lim[0])) field_min_ = lim[0];
     if (conf_.get("field_limit_max", lim[1])) field_max_ = lim[1];
+}
+
+std::shared_ptr<const PreparedMesh> FemocsFacade::prepare(TetMesh&& tm) {
+    if (mesh_prep_device_) return std::make_shared<PreparedMesh>(prepare_mesh_device(std::move(tm), 0));
+    return std::make_shared<PreparedMesh>(prepare_mesh(std::move(tm)));
 }
 
 int FemocsFacade::ensure_mesh() {
@@ -149,9 +159,9 @@ int FemocsFacade::ensure_mesh() {
             conf_.get("gpu_h", s.h);
             conf_.get("gpu_growth", s.growth);
             conf_.get("gpu_margin", s.margin);
-            mesh_ = std::make_shared<PreparedMesh>(prepare_mesh(make_nanotip_mesh(s)));
+            mesh_ = prepare(make_nanotip_mesh(s));
         } else {
-            mesh_ = std::make_shared<PreparedMesh>(prepare_mesh(read_gmsh(mf)));
+            mesh_ = prepare(read_gmsh(mf));
         }
     }
     field_.reset(new Field(mesh_, nullptr, element_order_));
@@ -163,7 +173,7 @@ int FemocsFacade::import_mesh(int n_nodes, const double* xyz, int n_tets, const 
     tm.xyz.assign(xyz, xyz + 3 * (size_t)n_nodes);
     tm.tets.assign(tets, tets + 4 * (size_t)n_tets);
     tm.marker.assign(markers, markers + n_tets);
-    mesh_ = std::make_shared<PreparedMesh>(prepare_mesh(std::move(tm)));
+    mesh_ = prepare(std::move(tm));
     field_.reset();
     solved_ = false;
     return 0;

@@ -50,6 +50,8 @@ public:
 
 private:
     int ensure_mesh();
+    // tet mesh -> prepared tables, by kernels (gpu_mesh_prep = device, default) or on the host
+    std::shared_ptr<const PreparedMesh> prepare(TetMesh&& tm);
     void read_params();
     int interp_points(int n, const double* x, const double* y, const double* z, std::vector<int32_t>& cells,
                       std::vector<double>& out);
@@ -57,6 +59,7 @@ private:
     ConfigScript conf_;
     std::shared_ptr<const PreparedMesh> mesh_;
     std::unique_ptr<Field> field_;
+    bool mesh_prep_device_ = true;
     bool solved_ = false;
     // atoms and the surface (dense) subset that run() interpolates onto
     std::vector<double> atoms_;

@@ -1,6 +1,7 @@
 // Host-side mesh preparation (see mesh.h). Compiled with -ffp-contract=off so that every
 // coordinate and table entry is produced by the same IEEE operation sequence on x86 and Arm.
 #include "mesh.h"
+#include "mesh_math.h"
 
 #include <algorithm>
 #include <array>
@@ -79,23 +80,8 @@ TetMesh read_gmsh(const std::string& path) {
 // ------------------------------------------------------------------------------------
 namespace {
 
-// Local edges of a tet in the order the reference enumerates them (src/Tethex.cpp:1244-1262):
-// all ordered pairs (i, j) of local vertices with v[i] > v[j], i outer, j inner.
-struct LocalEdges {
-    int n = 0;
-    int a[6], b[6];  // local vertex indices, v[a] > v[b]
-};
-inline LocalEdges local_edges(const int32_t* v) {
-    LocalEdges le;
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j)
-            if (v[i] > v[j]) {
-                le.a[le.n] = i;
-                le.b[le.n] = j;
-                ++le.n;
-            }
-    return le;
-}
+using mm::LocalEdges;
+using mm::local_edges;
 
 inline uint64_t edge_key(int32_t hi, int32_t lo) { return ((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo; }
 
@@ -105,22 +91,6 @@ struct FaceRec {
     int32_t tet;
     int32_t opp;         // local index of the vertex opposite to this face in `tet`
 };
-
-// sign of the trilinear-hex volume for vertices given in deal.II lexicographic order,
-// from the Jacobian at the cell centre (sufficient for the convex tet corners produced here)
-inline double hex_orientation(const double* d) {
-    double ex[3], ey[3], ez[3];
-    for (int c = 0; c < 3; ++c) {
-        ex[c] = (d[3 * 1 + c] - d[3 * 0 + c]) + (d[3 * 3 + c] - d[3 * 2 + c]) +
-                (d[3 * 5 + c] - d[3 * 4 + c]) + (d[3 * 7 + c] - d[3 * 6 + c]);
-        ey[c] = (d[3 * 2 + c] - d[3 * 0 + c]) + (d[3 * 3 + c] - d[3 * 1 + c]) +
-                (d[3 * 6 + c] - d[3 * 4 + c]) + (d[3 * 7 + c] - d[3 * 5 + c]);
-        ez[c] = (d[3 * 4 + c] - d[3 * 0 + c]) + (d[3 * 5 + c] - d[3 * 1 + c]) +
-                (d[3 * 6 + c] - d[3 * 2 + c]) + (d[3 * 7 + c] - d[3 * 3 + c]);
-    }
-    return ex[0] * (ey[1] * ez[2] - ey[2] * ez[1]) - ex[1] * (ey[0] * ez[2] - ey[2] * ez[0]) +
-           ex[2] * (ey[0] * ez[1] - ey[1] * ez[0]);
-}
 
 }  // namespace
 
@@ -259,7 +229,6 @@ HexMesh tethex_split(const TetMesh& tm) {
     // ---- hexahedra, four per tet, in the reference's vertex order
     hm.hexs.resize(32 * (size_t)n_tets);
     hm.hex_marker.resize(4 * (size_t)n_tets);
-    static const int to_deal[8] = {0, 1, 5, 4, 2, 3, 7, 6};
     for (int t = 0; t < n_tets; ++t) {
         const int32_t* v = T + 4 * t;
         LocalEdges le = local_edges(v);
@@ -288,8 +257,8 @@ HexMesh tethex_split(const TetMesh& tm) {
             h[7] = face_node(1, 2);
             double d[24];
             for (int i = 0; i < 8; ++i)
-                for (int c = 0; c < 3; ++c) d[3 * to_deal[i] + c] = hm.xyz[3 * (size_t)h[i] + c];
-            if (hex_orientation(d) < 0)
+                for (int c = 0; c < 3; ++c) d[3 * mm::to_deal(i) + c] = hm.xyz[3 * (size_t)h[i] + c];
+            if (mm::hex_orientation(d) < 0)
                 for (int i = 0; i < 4; ++i) std::swap(h[i], h[i + 4]);
             const size_t hx = 4 * (size_t)t + ver;
             for (int i = 0; i < 8; ++i) hm.hexs[8 * hx + i] = h[i];
@@ -353,38 +322,7 @@ double tet_edgemax(const TetMesh& tm) {
 }
 
 // ------------------------------------------------------------------------------------
-namespace {
-struct V3 { double x, y, z; };
-
-// 2x3 "determinant" helper of the barycentric minors: a.x*(b.y-b.z) - a.y*(b.x-b.z) + a.z*(b.x-b.y)
-inline double minor2(const V3& a, const V3& b) {
-    return a.x * (b.y - b.z) - a.y * (b.x - b.z) + a.z * (b.x - b.y);
-}
-inline double minor3(const V3& a, const V3& b, const V3& c) {
-    return a.x * (b.y * c.z - c.y * b.z) - b.x * (a.y * c.z - c.y * a.z) + c.x * (a.y * b.z - b.y * a.z);
-}
-// |x y z 1| determinant of four points, expanded along the column of ones
-inline double det4(const V3& p1, const V3& p2, const V3& p3, const V3& p4) {
-    const double a = minor3(p2, p3, p4);
-    const double b = minor3(p1, p3, p4);
-    const double c = minor3(p1, p2, p4);
-    const double d = minor3(p1, p2, p3);
-    return d - c + b - a;
-}
-// Minor vector of the barycentric coordinate that replaces point `skip` by (x,y,z,1);
-// `sgn` = +1 for coordinates 1 and 3, -1 for 2 and 4.
-// The 3x3 minor of the last coordinate is evaluated on the transposed vectors for the first
-// three coordinates and on the points themselves for the fourth, as the reference does
-// (src/InterpolatorCells.cpp:586-626); both are the same determinant but round differently.
-inline void bary_minor(const V3& p, const V3& q, const V3& r, int sgn, bool rows, double* out) {
-    const double m1 = minor2({p.y, q.y, r.y}, {p.z, q.z, r.z});
-    const double m2 = minor2({p.x, q.x, r.x}, {p.z, q.z, r.z});
-    const double m3 = minor2({p.x, q.x, r.x}, {p.y, q.y, r.y});
-    const double m4 = rows ? minor3(p, q, r) : minor3({p.x, q.x, r.x}, {p.y, q.y, r.y}, {p.z, q.z, r.z});
-    if (sgn > 0) { out[0] = m1; out[1] = -m2; out[2] = m3; out[3] = -m4; }
-    else { out[0] = -m1; out[1] = m2; out[2] = -m3; out[3] = m4; }
-}
-}  // namespace
+using mm::V3;
 
 TetTables build_tet_tables(const TetMesh& tm, const HexMesh& hm, const std::vector<int32_t>& face_nbr) {
     const int n_tets = tm.n_tets();
@@ -435,12 +373,7 @@ TetTables build_tet_tables(const TetMesh& tm, const HexMesh& hm, const std::vect
         V3 p2{X[3 * v[1]], X[3 * v[1] + 1], X[3 * v[1] + 2]};
         V3 p3{X[3 * v[2]], X[3 * v[2] + 1], X[3 * v[2] + 2]};
         V3 p4{X[3 * v[3]], X[3 * v[3] + 1], X[3 * v[3] + 2]};
-        double* d = &tt.det[(size_t)kTetDetStride * t];
-        d[0] = 1.0 / det4(p1, p2, p3, p4);
-        bary_minor(p2, p3, p4, +1, false, d + 1);
-        bary_minor(p1, p3, p4, -1, false, d + 5);
-        bary_minor(p1, p2, p4, +1, false, d + 9);
-        bary_minor(p1, p2, p3, -1, true, d + 13);
+        mm::tet_det_table(p1, p2, p3, p4, &tt.det[(size_t)kTetDetStride * t]);
 
         double cx = 0.0, cy = 0.0, cz = 0.0;
         for (int k = 0; k < 4; ++k) {
@@ -478,24 +411,10 @@ TetTables build_tet_tables(const TetMesh& tm, const HexMesh& hm, const std::vect
 std::vector<double> build_hex_coeffs(const HexMesh& hm) {
     const int n = hm.n_hexs();
     std::vector<double> f(24 * (size_t)n);
-    // sign table of the trilinear expansion, rows f0..f7, columns hex nodes 0..7
-    static const int S[8][8] = {
-        {+1, +1, +1, +1, +1, +1, +1, +1}, {-1, +1, +1, -1, -1, +1, +1, -1},
-        {-1, -1, +1, +1, -1, -1, +1, +1}, {-1, -1, -1, -1, +1, +1, +1, +1},
-        {+1, -1, +1, -1, +1, -1, +1, -1}, {+1, -1, -1, +1, -1, +1, +1, -1},
-        {+1, +1, -1, -1, -1, -1, +1, +1}, {-1, +1, -1, +1, +1, -1, +1, -1}};
     for (int h = 0; h < n; ++h) {
-        const int32_t* nd = &hm.hexs[8 * (size_t)h];
-        for (int r = 0; r < 8; ++r)
-            for (int c = 0; c < 3; ++c) {
-                // left-to-right signed sum starting from the first node (negated if its sign is -1)
-                double s = hm.xyz[3 * (size_t)nd[0] + c] * (double)S[r][0];
-                for (int k = 1; k < 8; ++k) {
-                    const double x = hm.xyz[3 * (size_t)nd[k] + c];
-                    s = S[r][k] > 0 ? s + x : s - x;
-                }
-                f[24 * (size_t)h + 3 * r + c] = s / 8.0;
-            }
+        const double* nodes[8];
+        for (int k = 0; k < 8; ++k) nodes[k] = &hm.xyz[3 * (size_t)hm.hexs[8 * (size_t)h + k]];
+        mm::hex_coefficients(nodes, &f[24 * (size_t)h]);
     }
     return f;
 }

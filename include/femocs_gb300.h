@@ -91,6 +91,14 @@ typedef struct {
 FGB_MESH* fgb_mesh_from_arrays(int n_nodes, const double* xyz, int n_tets, const int* tets, const int* markers);
 FGB_MESH* fgb_mesh_read_gmsh(const char* path);
 FGB_MESH* fgb_mesh_synthetic(const FgbNanotip* spec);
+/* the same meshes prepared by kernels on the current CUDA device (tet -> hex split, grouping,
+ * interpolation tables: src/Tethex.cpp:1037-1102, src/TetgenMesh.cpp:353-385,
+ * src/InterpolatorCells.cpp:523-629, 1205-1267); tables equal bit for bit to the host
+ * builder's; up to 2^21 tet vertices */
+FGB_MESH* fgb_mesh_from_arrays_device(int n_nodes, const double* xyz, int n_tets, const int* tets, const int* markers);
+FGB_MESH* fgb_mesh_synthetic_device(const FgbNanotip* spec);
+/* preparation time of a mesh: [device kernel ms (0 for the host builder), total ms] */
+int fgb_mesh_prep_timing(const FGB_MESH* m, double* out2);
 void fgb_mesh_free(FGB_MESH* m);
 /* sizes: [n_tetnodes, n_tets, n_nodes, n_hexs, n_vac_vertices, n_vac_cells, n_nbr_idx, n_voro_idx,
  *         n_dofs, nnz, n_top_faces, n_sell] (n_dofs.. are 0 until a field is created) */
