@@ -62,6 +62,24 @@ class Mesh:
         fn = load().fgb_mesh_synthetic_device if device else load().fgb_mesh_synthetic
         return cls(fn(C.byref(spec)))
 
+    def set_surface(self, tris, tri2tet):
+        """Replace the surface triangles (3 tet-mesh node ids and 2 tets per triangle)."""
+        tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1)
+        tri2tet = np.ascontiguousarray(tri2tet, dtype=np.int32).reshape(-1)
+        if load().fgb_mesh_set_surface(self.h, len(tris) // 3, ptr(tris, ip), ptr(tri2tet, ip)) != 0:
+            raise RuntimeError(last_error())
+
+    def surface(self):
+        """(tris (n,3), tri2tet (n,2), geo (n,19)) of the surface triangles"""
+        n = int(load().fgb_mesh_surface_tris(self.h))
+        out = []
+        for name, dt, k in (("surf_tris", np.int32, 3), ("surf_tri2tet", np.int32, 2), ("surf_geo", np.float64, 19)):
+            a = np.zeros(max(k * n, 1), dtype=dt)
+            if load().fgb_mesh_export(self.h, name.encode(), a.ctypes.data_as(C.c_void_p)) != 0:
+                raise RuntimeError(last_error())
+            out.append(a[: k * n].reshape(n, k))
+        return tuple(out)
+
     def prep_timing(self):
         """{"kernel_ms": device time of the preparation kernels (0 on the host),
         "total_ms": wall time of the preparation}"""
@@ -106,6 +124,12 @@ class Mesh:
             "vac_cells": (np.int32, s["n_vac_cells"]), "tet_search": (np.int32, s["n_tets"]),
             "edgemax": (np.float64, 1), "node_parents": (np.int32, 4 * s["n_nodes"]),
         }
+        if name.startswith("surf_"):
+            nt = int(load().fgb_mesh_surface_tris(self.h))
+            n_nbr = int(self.export("surf_nbr_ptr")[-1]) if name == "surf_nbr_idx" and nt > 0 else 0
+            shapes.update({"surf_tris": (np.int32, 3 * nt), "surf_tri2tet": (np.int32, 2 * nt),
+                           "surf_geo": (np.float64, 19 * nt), "surf_nbr_ptr": (np.int32, nt + 1 if nt else 0),
+                           "surf_nbr_idx": (np.int32, n_nbr)})
         dt, n = shapes[name]
         out = np.zeros(max(n, 1), dtype=dt)
         if load().fgb_mesh_export(self.h, name.encode(), out.ctypes.data_as(C.c_void_p)) != 0:
@@ -258,6 +282,16 @@ class Field:
             return res + (dict(zip(["n", "walk_failed", "fallback", "dependent", "longest_run"], st.tolist())),)
         return res
 
+    def interpolate_surface(self, xyz, rank=1):
+        """Surface (2-D) location + interpolation (rank 1 linear, 2 quadratic): (triangle per
+        point, negative when no triangle holds it; 5 values per point)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        n = len(xyz) // 3
+        cells = np.zeros(max(n, 1), dtype=np.int32)
+        out = np.zeros(max(5 * n, 1))
+        self._ok(load().fgb_field_interpolate_surface(self.h, n, ptr(xyz), rank, ptr(cells, ip), ptr(out)))
+        return cells[:n], out[:5 * n].reshape(-1, 5)
+
     def mark(self, slot):
         """Record CUDA event `slot` (0..7) on the field's stream."""
         self._ok(load().fgb_field_mark(self.h, slot))
@@ -326,6 +360,16 @@ class Femocs:
         rv = C.c_int(0)
         self.lib.femocs_interpolate_elfield(self.h, C.byref(rv), n, ptr(x), ptr(y), ptr(z), ptr(Ex), ptr(Ey), ptr(Ez),
                                             ptr(En), ptr(flag, ip))
+        return rv.value, Ex, Ey, Ez, En, flag
+
+    def interpolate_surface_elfield(self, x, y, z):
+        x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+        n = len(x)
+        Ex, Ey, Ez, En = (np.zeros(n) for _ in range(4))
+        flag = np.zeros(n, dtype=np.int32)
+        rv = C.c_int(0)
+        self.lib.femocs_interpolate_surface_elfield(self.h, C.byref(rv), n, ptr(x), ptr(y), ptr(z), ptr(Ex), ptr(Ey),
+                                                    ptr(Ez), ptr(En), ptr(flag, ip))
         return rv.value, Ex, Ey, Ez, En, flag
 
     def interpolate_phi(self, x, y, z):

@@ -54,6 +54,8 @@ _PROTOS = {
     "fgb_mesh_from_arrays_device": (vp, [C.c_int, dp, C.c_int, ip, ip]),
     "fgb_mesh_synthetic_device": (vp, [C.POINTER(FgbNanotip)]),
     "fgb_mesh_prep_timing": (C.c_int, [vp, dp]),
+    "fgb_mesh_set_surface": (C.c_int, [vp, C.c_int, ip, ip]),
+    "fgb_mesh_surface_tris": (C.c_int64, [vp]),
     "fgb_mesh_free": (None, [vp]),
     "fgb_mesh_sizes": (C.c_int, [vp, i64p]),
     "fgb_mesh_export": (C.c_int, [vp, C.c_char_p, vp]),
@@ -85,6 +87,8 @@ _PROTOS = {
     "fgb_field_set_nodal": (C.c_int, [vp, dp]),
     "fgb_field_interpolate": (C.c_int, [vp, C.c_int, dp, C.c_int, ip, dp, i64p]),
     "fgb_field_interpolate_device": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp]),
+    "fgb_field_interpolate_surface": (C.c_int, [vp, C.c_int, dp, C.c_int, ip, dp]),
+    "fgb_field_interpolate_surface_device": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp]),
     "fgb_field_interpolate_device_noalloc": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp]),
     "fgb_field_export_system": (C.c_int, [vp, i64p, ip, dp, dp, ip]),
     "fgb_field_time_spmv": (C.c_double, [vp, C.c_int, C.c_int]),

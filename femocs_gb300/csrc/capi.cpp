@@ -119,11 +119,7 @@ void femocs_interpolate_elfield(FEMOCS* h, int* retval, int n, const double* x, 
 }
 void femocs_interpolate_surface_elfield(FEMOCS* h, int* retval, int n, const double* x, const double* y,
                                         const double* z, double* Ex, double* Ey, double* Ez, double* En, int* flag) {
-    (void)Ex; (void)Ey; (void)Ez; (void)En;
-    guarded_rv(retval, [&] {
-        std::vector<double> d(3 * (size_t)std::max(n, 0));
-        return h->f->interpolate(d.data(), flag, n, "Elfield", true, x, y, z);
-    });
+    guarded_rv(retval, [&] { return h->f->interpolate_surface_elfield(n, x, y, z, Ex, Ey, Ez, En, flag); });
 }
 void femocs_interpolate_phi(FEMOCS* h, int* retval, int n, const double* x, const double* y, const double* z,
                             double* phi, int* flag) {
@@ -230,6 +226,21 @@ FGB_MESH* fgb_mesh_from_arrays_device(int n_nodes, const double* xyz, int n_tets
     if (rc) { delete m; return nullptr; }
     return m;
 }
+int fgb_mesh_set_surface(FGB_MESH* m, int n_tris, const int* tris, const int* tri2tet) {
+    return guarded([&] {
+        FGB_REQUIRE(n_tris >= 0 && (n_tris == 0 || (tris && tri2tet)), "invalid surface arrays");
+        const PreparedMesh& p = *m->pm;
+        SurfaceTables st = build_surface_tables(p.tet.xyz.data(), p.tet.n_nodes(), p.tet.n_tets(),
+                                                std::vector<int32_t>(tris, tris + 3 * (size_t)n_tris),
+                                                std::vector<int32_t>(tri2tet, tri2tet + 2 * (size_t)n_tris));
+        // fields created before keep the tables they were built with
+        auto pm = std::make_shared<PreparedMesh>(p);
+        pm->surf = std::move(st);
+        m->pm = std::move(pm);
+        return 0;
+    });
+}
+int64_t fgb_mesh_surface_tris(const FGB_MESH* m) { return m && m->pm ? m->pm->surf.n_tris() : -1; }
 int fgb_mesh_prep_timing(const FGB_MESH* m, double* out2) {
     return guarded([&] {
         out2[0] = m->timing.kernel_ms;
@@ -311,6 +322,11 @@ int fgb_mesh_export(const FGB_MESH* m, const char* name, void* out) {
         if (n == "voro_idx") return cp(p.voro_idx);
         if (n == "vac_node2vertex") return cp(p.vac.node2vertex);
         if (n == "vac_cells") return cp(p.vac.cells);
+        if (n == "surf_tris") return cp(p.surf.tris);
+        if (n == "surf_tri2tet") return cp(p.surf.tri2tet);
+        if (n == "surf_geo") return cp(p.surf.geo);
+        if (n == "surf_nbr_ptr") return cp(p.surf.nbr_ptr);
+        if (n == "surf_nbr_idx") return cp(p.surf.nbr_idx);
         if (n == "tet_search") {
             std::vector<int32_t> v(p.tt.search.begin(), p.tt.search.end());
             return cp(v);
@@ -519,6 +535,19 @@ int fgb_field_interpolate(FGB_FIELD* f, int n, const double* xyz, int rank, int*
             st5[3] = ls.n_dependent;
             st5[4] = ls.longest_run;
         }
+        return 0;
+    });
+}
+int fgb_field_interpolate_surface(FGB_FIELD* f, int n, const double* xyz, int rank, int* cells, double* out5) {
+    return guarded([&] {
+        f->f->interpolate_surface_host(n, xyz, rank, cells, out5);
+        return 0;
+    });
+}
+int fgb_field_interpolate_surface_device(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells,
+                                         double* d_out5) {
+    return guarded([&] {
+        f->f->interp().surface_interpolate(n, d_xyz, rank, d_cells, d_out5);
         return 0;
     });
 }

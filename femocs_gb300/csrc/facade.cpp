@@ -267,8 +267,12 @@ int FemocsFacade::run(int timestep, double time) {
 }
 
 int FemocsFacade::interp_points(int n, const double* x, const double* y, const double* z, std::vector<int32_t>& cells,
-                                std::vector<double>& out) {
+                                std::vector<double>& out, bool surface) {
     if (!field_ || !solved_) { set_last_error("no solution to interpolate"); return 1; }
+    if (surface && rank_ == 3) {
+        set_last_error("surface interpolation of rank 3 (quadrangles) is not provided; use interpolation_rank 1 or 2");
+        return 1;
+    }
     std::vector<double> p(3 * (size_t)n);
     for (int i = 0; i < n; ++i) {
         p[3 * (size_t)i] = x[i];
@@ -277,7 +281,25 @@ int FemocsFacade::interp_points(int n, const double* x, const double* y, const d
     }
     cells.resize(n);
     out.resize(5 * (size_t)n);
-    field_->interpolate_host(n, p.data(), rank_, cells.data(), out.data(), nullptr);
+    if (surface) field_->interpolate_surface_host(n, p.data(), rank_, cells.data(), out.data());
+    else field_->interpolate_host(n, p.data(), rank_, cells.data(), out.data(), nullptr);
+    return 0;
+}
+
+int FemocsFacade::interpolate_surface_elfield(int n, const double* x, const double* y, const double* z, double* Ex,
+                                              double* Ey, double* Ez, double* En, int* flag) {
+    if (n <= 0) return 0;
+    std::vector<int32_t> cells;
+    std::vector<double> out;
+    if (interp_points(n, x, y, z, cells, out, true)) return 1;
+    for (int i = 0; i < n; ++i) {
+        const double* o = &out[5 * (size_t)i];
+        Ex[i] = o[0];
+        Ey[i] = o[1];
+        Ez[i] = o[2];
+        En[i] = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+        flag[i] = cells[i] < 0 ? 1 : 0;
+    }
     return 0;
 }
 
@@ -343,15 +365,11 @@ void export_by_label(int kind, int n, const std::vector<int32_t>& ids, const std
 int FemocsFacade::interpolate(double* data, int* flag, int n, const std::string& label, bool near_surface,
                               const double* x, const double* y, const double* z) {
     if (n <= 0) return 0;
-    if (near_surface) {
-        set_last_error("surface (2-D) interpolation is not provided by this library");
-        return 1;
-    }
     const int kind = label_kind(label);
     if (!kind) { set_last_error("unimplemented type of interpolation data: " + label); return 1; }
     std::vector<int32_t> cells;
     std::vector<double> out;
-    if (interp_points(n, x, y, z, cells, out)) return 1;
+    if (interp_points(n, x, y, z, cells, out, near_surface)) return 1;
     std::vector<int32_t> ids(n);
     for (int i = 0; i < n; ++i) ids[i] = i;
     export_by_label(kind, n, ids, out, data);

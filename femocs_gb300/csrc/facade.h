@@ -37,6 +37,9 @@ public:
     int interpolate_elfield(int n, const double* x, const double* y, const double* z, double* Ex, double* Ey, double* Ez,
                             double* En, int* flag);
     int interpolate_phi(int n, const double* x, const double* y, const double* z, double* phi, int* flag);
+    // Femocs::interpolate_surface_elfield (src/Femocs.cpp:198-214): E on the surface triangles
+    int interpolate_surface_elfield(int n, const double* x, const double* y, const double* z, double* Ex, double* Ey,
+                                    double* Ez, double* En, int* flag);
     int interpolate(double* data, int* flag, int n, const std::string& label, bool near_surface, const double* x,
                     const double* y, const double* z);
     int export_data(double* data, int n, const std::string& label);
@@ -54,7 +57,7 @@ private:
     std::shared_ptr<const PreparedMesh> prepare(TetMesh&& tm);
     void read_params();
     int interp_points(int n, const double* x, const double* y, const double* z, std::vector<int32_t>& cells,
-                      std::vector<double>& out);
+                      std::vector<double>& out, bool surface = false);
 
     ConfigScript conf_;
     std::shared_ptr<const PreparedMesh> mesh_;

@@ -63,4 +63,16 @@ void Field::interpolate_host(int n, const double* xyz, int rank, int32_t* cells,
     FGB_CUDA(cudaStreamSynchronize(stream_));
 }
 
+void Field::interpolate_surface_host(int n, const double* xyz, int rank, int32_t* cells, double* out5) {
+    if (n <= 0) return;
+    if (pts_.size() < 3 * (size_t)n) pts_.resize(3 * (size_t)n);
+    if (out_.size() < 5 * (size_t)n) out_.resize(5 * (size_t)n);
+    if (cells_.size() < (size_t)n) cells_.resize(n);
+    FGB_CUDA(cudaMemcpyAsync(pts_.get(), xyz, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, stream_));
+    dm_->surface_interpolate(n, pts_.get(), rank, cells_.get(), out_.get());
+    if (cells) FGB_CUDA(cudaMemcpyAsync(cells, cells_.get(), sizeof(int32_t) * n, cudaMemcpyDeviceToHost, stream_));
+    if (out5) FGB_CUDA(cudaMemcpyAsync(out5, out_.get(), 5 * sizeof(double) * n, cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+}
+
 }  // namespace fgb

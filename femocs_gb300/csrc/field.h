@@ -27,6 +27,8 @@ public:
 
     // host-pointer interpolation through reusable device buffers
     void interpolate_host(int n, const double* xyz, int rank, int32_t* cells, double* out5, LocateStats* ls);
+    // surface (2-D) variant: cells are surface triangles (DeviceMesh::surface_interpolate)
+    void interpolate_surface_host(int n, const double* xyz, int rank, int32_t* cells, double* out5);
     void extract(bool smoothen);
     // PIC: scatter n particles (device xyz) with charge factor q/eps0 * W_sp into the space-
     // charge rhs of the next assemble; d_hex = their vacuum hexes, or null to locate them

@@ -56,6 +56,13 @@ public:
     void space_charge(int n, const double* d_pts, const int32_t* d_hex, int order, const int32_t* d_node2dof,
                       const int32_t* d_hex2cell, const int32_t* d_cell_dofs, double charge_factor, double* d_rhs,
                       int* n_skipped);
+    // Surface (2-D) location + interpolation on the mesh's surface triangles: the chained
+    // triangle search of InterpolatorCells<3>::locate_cell, then the tet reached through the
+    // triangle's two tets (LinearTriangles / QuadraticTriangles::interp_solution,
+    // src/InterpolatorCells.cpp:1639-1686, 1834-1856), rank 1 linear or 2 quadratic in that tet.
+    // d_cells: triangle per point (negative = nearest-centroid fallback); d_out: 5 per point.
+    void surface_interpolate(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out);
+    int n_surface_tris() const { return n_stris_; }
     // Interpolate with cells already known (SolutionReader::calc_interpolation with mapped atoms)
     void interpolate_known(int n, const double* d_pts, int rank, const int32_t* d_cells, double* d_out);
 
@@ -69,6 +76,7 @@ public:
 
 private:
     void ensure_scratch(int n);
+    void set_surface(const PreparedMesh& pm);
     cudaStream_t stream_;
     int n_nodes_, n_tets_, n_tetnodes_;
     double decay_;
@@ -85,6 +93,16 @@ private:
     // per-point scratch
     DBuf<int32_t> v_, nin_, f_, res_, dep_, counters_;
     int scratch_n_ = 0;
+    // surface triangles: tables, candidate grid (triangles whose acceptance region meets a
+    // cell), centroid buckets for the nearest-centroid fallback, per-point scratch
+    int n_stris_ = 0;
+    DBuf<int32_t> stri2tet_, snbr_ptr_, snbr_idx_, scand_ptr_, scand_idx_, sgptr_, sgtris_;
+    DBuf<double> sgeo_, sgcxyz_;
+    int scand_dim_[3] = {1, 1, 1}, sg_dim_[3] = {1, 1, 1};
+    double scand_org_[3] = {0, 0, 0}, scand_step_[3] = {1, 1, 1}, scand_lo_[3] = {0, 0, 0}, scand_hi_[3] = {0, 0, 0};
+    double sg_org_[3] = {0, 0, 0}, sg_step_[3] = {1, 1, 1};
+    DBuf<int32_t> s_tv_, s_nin_, s_tf_, s_res_, s_dep_, s_counters_;
+    int s_scratch_n_ = 0;
 };
 
 }  // namespace fgb

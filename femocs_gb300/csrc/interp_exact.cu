@@ -256,6 +256,117 @@ __global__ void k_chain_runs(int n, Pts P, int g0, const double* __restrict__ de
     atomicMax(&counters[3], j - i);
 }
 
+// ---------------------------------------------------------------- surface triangles
+// LinearTriangles::point_in_cell (src/InterpolatorCells.cpp:1639-1650) on the 19-double rows
+// of SurfaceTables::geo: vert0, edge1/D, edge2, pvec/D, normal, |edge2|, centroid
+__device__ __forceinline__ bool tri_pic(const double* __restrict__ geo, int f, double x, double y, double z) {
+    const double* g = geo + 19 * (size_t)f;
+    const double tx = x - g[0], ty = y - g[1], tz = z - g[2];
+    const double u = tx * g[9] + ty * g[10] + tz * g[11];
+    if (u < -kZero || u > 1 + kZero) return false;
+    const double qx = ty * g[5] - tz * g[4], qy = tz * g[3] - tx * g[5], qz = tx * g[4] - ty * g[3];
+    const double v = qx * g[12] + qy * g[13] + qz * g[14];
+    if (v < -kZero || u + v > 1 + kZero) return false;
+    return fabs(qx * g[6] + qy * g[7] + qz * g[8]) < g[15];
+}
+
+// LinearTriangles::fast_distance, :1743-1747
+__device__ __forceinline__ double tri_fast_distance(const double* __restrict__ geo, int f, double x, double y, double z) {
+    const double* g = geo + 19 * (size_t)f;
+    const double tx = x - g[0], ty = y - g[1], tz = z - g[2];
+    const double qx = ty * g[5] - tz * g[4], qy = tz * g[3] - tx * g[5], qz = tx * g[4] - ty * g[3];
+    return g[6] * qx + g[7] * qy + g[8] * qz;
+}
+
+// per point: the triangles whose acceptance region meets the point's candidate cell ->
+// #containing triangles and the lowest containing one (the result of the reference's scan)
+__global__ void k_tri_locate(int n, Pts P, GridView C, double lo0, double lo1, double lo2, double hi0, double hi1,
+                             double hi2, const int32_t* __restrict__ cptr, const int32_t* __restrict__ cidx,
+                             const double* __restrict__ geo, int32_t* __restrict__ V, int32_t* __restrict__ nin) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x, y, z;
+    P.get(i, x, y, z);
+    if (!(x >= lo0 && x <= hi0 && y >= lo1 && y <= hi1 && z >= lo2 && z <= hi2)) {
+        V[i] = -1;
+        nin[i] = 0;
+        return;
+    }
+    int ci, cj, ck;
+    C.cell(x, y, z, ci, cj, ck);
+    const size_t c = ((size_t)ck * C.dy + cj) * C.dx + ci;
+    int cnt = 0, v = INT_MAX;
+    for (int q = cptr[c]; q < cptr[c + 1]; ++q) {
+        const int f = cidx[q];
+        if (tri_pic(geo, f, x, y, z)) {
+            ++cnt;
+            if (f < v) v = f;
+        }
+    }
+    V[i] = cnt ? v : -1;
+    nin[i] = cnt;
+}
+
+// runs of guess-dependent points replay the chained triangle search from the last
+// independent point: guess, the triangles sharing its nodes, then the scan result
+__global__ void k_tri_chain_runs(int n, Pts P, int g0, int n_tris, const double* __restrict__ geo,
+                                 const int32_t* __restrict__ nptr, const int32_t* __restrict__ nidx,
+                                 const int32_t* __restrict__ V, const int32_t* __restrict__ F,
+                                 const int32_t* __restrict__ dep, int32_t* __restrict__ res, int32_t* __restrict__ counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!dep[i] || (i > 0 && dep[i - 1])) return;
+    int g = i == 0 ? g0 : abs(res[i - 1]);
+    int j = i;
+    for (; j < n && dep[j]; ++j) {
+        double x, y, z;
+        P.get(j, x, y, z);
+        int r = INT_MIN;
+        if (g < n_tris) {
+            if (tri_pic(geo, g, x, y, z)) {
+                r = g;
+            } else {
+                for (int k = nptr[g]; k < nptr[g + 1]; ++k) {
+                    const int u = nidx[k];
+                    if (tri_pic(geo, u, x, y, z)) { r = u; break; }
+                }
+            }
+        }
+        if (r == INT_MIN) r = V[j] >= 0 ? V[j] : -F[j];
+        res[j] = r;
+        g = abs(r);
+    }
+    atomicMax(&counters[3], j - i);
+}
+
+// the tet of each located point: the triangle's first tet if the point lies on the triangle
+// or inside that tet, otherwise the chained tet search from the second tet
+__global__ void k_surface_tet(int n, Pts P, const int32_t* __restrict__ tres, const int32_t* __restrict__ t2t,
+                              const double* __restrict__ geo, const double* __restrict__ det,
+                              const int32_t* __restrict__ nptr, const int32_t* __restrict__ nidx,
+                              const int32_t* __restrict__ V, const int32_t* __restrict__ F, int32_t* __restrict__ tcell) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x, y, z;
+    P.get(i, x, y, z);
+    const int tri = abs(tres[i]);
+    const int t0 = t2t[2 * (size_t)tri], t1 = t2t[2 * (size_t)tri + 1];
+    int tet;
+    if (fabs(tri_fast_distance(geo, tri, x, y, z)) <= 100.0 * kZero || pic(det, t0, x, y, z)) {
+        tet = t0;
+    } else if (pic(det, t1, x, y, z)) {
+        tet = t1;
+    } else {
+        tet = INT_MIN;
+        for (int k = nptr[t1]; k < nptr[t1 + 1]; ++k) {
+            const int u = nidx[k];
+            if (pic(det, u, x, y, z)) { tet = u; break; }
+        }
+        if (tet == INT_MIN) tet = V[i] >= 0 ? V[i] : -F[i];
+    }
+    tcell[i] = tet;
+}
+
 __device__ __forceinline__ void acc5(const double* __restrict__ sol, int node, double w, double* a) {
     const double* s = sol + 5 * (size_t)node;
 #pragma unroll
@@ -657,9 +768,187 @@ DeviceMesh::DeviceMesh(const PreparedMesh& pm, cudaStream_t stream)
     sol_.resize(5 * (size_t)n_nodes_);
     sol_.zero(s);
     counters_.resize(8);
+    set_surface(pm);
     FGB_CUDA(cudaStreamSynchronize(s));
     // host copies of the search tables are no longer needed
     grid_.seed.clear(); grid_.ptr.clear(); grid_.tets.clear(); grid_.cxyz.clear();
+}
+
+namespace {
+// uniform grid over [lo, hi] with about `per_cell` items per cell (at most 1024 per axis)
+void grid_dims(const double* lo, const double* hi, double n_items, double per_cell, int* dim, double* org, double* step) {
+    double ext[3];
+    for (int c = 0; c < 3; ++c) ext[c] = std::max(1e-9, hi[c] - lo[c]);
+    const double cells = std::max(1.0, n_items / per_cell);
+    const double h = std::cbrt(ext[0] * ext[1] * ext[2] / cells);
+    for (int c = 0; c < 3; ++c) {
+        dim[c] = std::max(1, std::min(1024, (int)std::ceil(ext[c] / h)));
+        org[c] = lo[c];
+        step[c] = ext[c] / dim[c];
+    }
+}
+inline int grid_index(double v, double org, double step, int dim) {
+    const int k = (int)std::floor((v - org) / step);
+    return std::min(std::max(k, 0), dim - 1);
+}
+}  // namespace
+
+void DeviceMesh::set_surface(const PreparedMesh& pm) {
+    const SurfaceTables& st = pm.surf;
+    n_stris_ = st.n_tris();
+    if (n_stris_ == 0) return;
+    cudaStream_t s = stream_;
+    const int nf = n_stris_;
+    const double* X = pm.tet.xyz.data();
+    // acceptance region of a triangle: inside the prism over it, |distance| < |edge2|; its box
+    // is that of the vertices moved by +-|edge2| along the unit normal
+    std::vector<double> rlo(3 * (size_t)nf), rhi(3 * (size_t)nf);
+    double glo[3] = {1e300, 1e300, 1e300}, ghi[3] = {-1e300, -1e300, -1e300};
+    for (int f = 0; f < nf; ++f) {
+        const double* g = &st.geo[(size_t)kTriGeoStride * f];
+        for (int c = 0; c < 3; ++c) {
+            double a = 1e300, b = -1e300;
+            for (int k = 0; k < 3; ++k) {
+                const double p = X[3 * (size_t)st.tris[3 * (size_t)f + k] + c];
+                const double d = std::fabs(g[12 + c]) * g[15];
+                a = std::min(a, p - d);
+                b = std::max(b, p + d);
+            }
+            rlo[3 * (size_t)f + c] = a;
+            rhi[3 * (size_t)f + c] = b;
+            glo[c] = std::min(glo[c], a);
+            ghi[c] = std::max(ghi[c], b);
+        }
+    }
+    // margin far above the rounding of the point-in-triangle test
+    for (int c = 0; c < 3; ++c) {
+        const double m = 1e-9 * std::max(1.0, ghi[c] - glo[c]);
+        glo[c] -= m;
+        ghi[c] += m;
+        scand_lo_[c] = glo[c];
+        scand_hi_[c] = ghi[c];
+    }
+    for (size_t q = 0; q < rlo.size(); ++q) {
+        const int c = (int)(q % 3);
+        const double m = 1e-9 * std::max(1.0, ghi[c] - glo[c]);
+        rlo[q] -= m;
+        rhi[q] += m;
+    }
+    grid_dims(glo, ghi, nf, 0.5, scand_dim_, scand_org_, scand_step_);
+    const size_t ncell = (size_t)scand_dim_[0] * scand_dim_[1] * scand_dim_[2];
+    std::vector<int32_t> cptr(ncell + 1, 0), cidx;
+    for (int pass = 0; pass < 2; ++pass) {
+        std::vector<int32_t> pos;
+        if (pass == 1) {
+            for (size_t c = 0; c < ncell; ++c) cptr[c + 1] += cptr[c];
+            cidx.resize(cptr[ncell]);
+            pos.assign(cptr.begin(), cptr.end() - 1);
+        }
+        for (int f = 0; f < nf; ++f) {
+            int a[3], b[3];
+            for (int c = 0; c < 3; ++c) {
+                a[c] = grid_index(rlo[3 * (size_t)f + c], scand_org_[c], scand_step_[c], scand_dim_[c]);
+                b[c] = grid_index(rhi[3 * (size_t)f + c], scand_org_[c], scand_step_[c], scand_dim_[c]);
+            }
+            for (int k = a[2]; k <= b[2]; ++k)
+                for (int j = a[1]; j <= b[1]; ++j)
+                    for (int i = a[0]; i <= b[0]; ++i) {
+                        const size_t c = ((size_t)k * scand_dim_[1] + j) * scand_dim_[0] + i;
+                        if (pass == 0) cptr[c + 1]++;
+                        else cidx[pos[c]++] = f;
+                    }
+        }
+    }
+    // centroid buckets (ascending triangle within a bucket) for the exact nearest centroid
+    double clo[3] = {1e300, 1e300, 1e300}, chi[3] = {-1e300, -1e300, -1e300};
+    for (int f = 0; f < nf; ++f)
+        for (int c = 0; c < 3; ++c) {
+            clo[c] = std::min(clo[c], st.geo[(size_t)kTriGeoStride * f + 16 + c]);
+            chi[c] = std::max(chi[c], st.geo[(size_t)kTriGeoStride * f + 16 + c]);
+        }
+    grid_dims(clo, chi, nf, 4.0, sg_dim_, sg_org_, sg_step_);
+    const size_t nb = (size_t)sg_dim_[0] * sg_dim_[1] * sg_dim_[2];
+    std::vector<int32_t> gptr(nb + 1, 0), gtris(nf);
+    std::vector<double> gc(3 * (size_t)nf);
+    std::vector<size_t> bc(nf);
+    for (int f = 0; f < nf; ++f) {
+        const double* cc = &st.geo[(size_t)kTriGeoStride * f + 16];
+        bc[f] = ((size_t)grid_index(cc[2], sg_org_[2], sg_step_[2], sg_dim_[2]) * sg_dim_[1] +
+                 grid_index(cc[1], sg_org_[1], sg_step_[1], sg_dim_[1])) * sg_dim_[0] +
+                grid_index(cc[0], sg_org_[0], sg_step_[0], sg_dim_[0]);
+        gptr[bc[f] + 1]++;
+    }
+    for (size_t c = 0; c < nb; ++c) gptr[c + 1] += gptr[c];
+    {
+        std::vector<int32_t> pos(gptr.begin(), gptr.end() - 1);
+        for (int f = 0; f < nf; ++f) {
+            const int32_t q = pos[bc[f]]++;
+            gtris[q] = f;
+            for (int c = 0; c < 3; ++c) gc[3 * (size_t)q + c] = st.geo[(size_t)kTriGeoStride * f + 16 + c];
+        }
+    }
+    stri2tet_.upload(st.tri2tet, s);
+    snbr_ptr_.upload(st.nbr_ptr, s);
+    snbr_idx_.upload(st.nbr_idx.empty() ? std::vector<int32_t>(1, 0) : st.nbr_idx, s);
+    sgeo_.upload(st.geo, s);
+    scand_ptr_.upload(cptr, s);
+    scand_idx_.upload(cidx.empty() ? std::vector<int32_t>(1, 0) : cidx, s);
+    sgptr_.upload(gptr, s);
+    sgtris_.upload(gtris, s);
+    sgcxyz_.upload(gc, s);
+    s_counters_.resize(8);
+    FGB_CUDA(cudaStreamSynchronize(s));
+}
+
+void DeviceMesh::surface_interpolate(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out) {
+    if (n <= 0) return;
+    FGB_REQUIRE(rank == 1 || rank == 2, "surface interpolation rank must be 1 or 2");
+    FGB_REQUIRE(n_stris_ > 0, "the mesh has no surface triangles");
+    ensure_scratch(n);
+    if (s_scratch_n_ < n) {
+        s_tv_.resize(n); s_nin_.resize(n); s_tf_.resize(n); s_res_.resize(n); s_dep_.resize(n);
+        s_scratch_n_ = n;
+    }
+    const int B = 256;
+    Pts P{d_pts};
+    // tets: the guess-independent results of the chained tet search
+    GridView G{grid_.dim[0], grid_.dim[1], grid_.dim[2], grid_.origin[0], grid_.origin[1], grid_.origin[2],
+               grid_.step[0], grid_.step[1], grid_.step[2]};
+    counters_.zero(stream_);
+    s_counters_.zero(stream_);
+    FGB_LAUNCH(k_locate_walk<<<grid_for(n, B), B, 0, stream_>>>(n, P, G, seed_.get(), det_.get(), face_nbr_.get(),
+                                                                nbr_ptr_.get(), nbr_idx_.get(), search_.get(), bb_lo_[0],
+                                                                bb_lo_[1], bb_lo_[2], bb_hi_[0], bb_hi_[1], bb_hi_[2],
+                                                                v_.get(), nin_.get(), counters_.get()));
+    FGB_LAUNCH(k_locate_scan<<<std::min(n, 1024), B, 0, stream_>>>(n, P, n_tets_, det_.get(), search_.get(), v_.get(),
+                                                                   nin_.get()));
+    FGB_LAUNCH(k_nearest_ctr<<<grid_for(n, 128), 128, 0, stream_>>>(n, P, G, gptr_.get(), gtets_.get(), gcxyz_.get(),
+                                                                    v_.get(), f_.get(), counters_.get()));
+    // triangles: scan result, nearest centroid, then the chained search of a fresh reader
+    // (first guess abs(-1) = 1)
+    GridView C{scand_dim_[0], scand_dim_[1], scand_dim_[2], scand_org_[0], scand_org_[1], scand_org_[2],
+               scand_step_[0], scand_step_[1], scand_step_[2]};
+    GridView S{sg_dim_[0], sg_dim_[1], sg_dim_[2], sg_org_[0], sg_org_[1], sg_org_[2], sg_step_[0], sg_step_[1],
+               sg_step_[2]};
+    FGB_LAUNCH(k_tri_locate<<<grid_for(n, B), B, 0, stream_>>>(n, P, C, scand_lo_[0], scand_lo_[1], scand_lo_[2],
+                                                               scand_hi_[0], scand_hi_[1], scand_hi_[2], scand_ptr_.get(),
+                                                               scand_idx_.get(), sgeo_.get(), s_tv_.get(), s_nin_.get()));
+    FGB_LAUNCH(k_nearest_ctr<<<grid_for(n, 128), 128, 0, stream_>>>(n, P, S, sgptr_.get(), sgtris_.get(), sgcxyz_.get(),
+                                                                    s_tv_.get(), s_tf_.get(), s_counters_.get()));
+    FGB_LAUNCH(k_resolve<<<grid_for(n, B), B, 0, stream_>>>(n, s_tv_.get(), s_nin_.get(), s_tf_.get(), s_res_.get(),
+                                                            s_dep_.get(), s_counters_.get()));
+    FGB_LAUNCH(k_tri_chain_runs<<<grid_for(n, B), B, 0, stream_>>>(n, P, 1, n_stris_, sgeo_.get(), snbr_ptr_.get(),
+                                                                   snbr_idx_.get(), s_tv_.get(), s_tf_.get(), s_dep_.get(),
+                                                                   s_res_.get(), s_counters_.get()));
+    FGB_LAUNCH(k_surface_tet<<<grid_for(n, B), B, 0, stream_>>>(n, P, s_res_.get(), stri2tet_.get(), sgeo_.get(), det_.get(),
+                                                                nbr_ptr_.get(), nbr_idx_.get(), v_.get(), f_.get(),
+                                                                res_.get()));
+    FGB_LAUNCH(k_interpolate<<<grid_for(n, 128), 128, 0, stream_>>>(n, P, rank, 0, res_.get(), det_.get(), tet_nodes_.get(),
+                                                                    quad_.get(), hexs_.get(), hexf_.get(), sol_.get(),
+                                                                    nullptr, d_out));
+    if (d_cells)
+        FGB_CUDA(cudaMemcpyAsync(d_cells, s_res_.get(), sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, stream_));
+    FGB_CUDA(cudaGetLastError());
 }
 
 void DeviceMesh::ensure_scratch(int n) {

@@ -709,6 +709,7 @@ PreparedMesh prepare_mesh_device(TetMesh&& tm, cudaStream_t s, MeshPrepTiming* t
             pm.bbox_max[c] = std::max(pm.bbox_max[c], tm.xyz[3 * (size_t)i + c]);
         }
     pm.tet = std::move(tm);
+    attach_interface_surface(pm);
     if (timing) {
         timing->kernel_ms = kms;
         timing->total_ms =

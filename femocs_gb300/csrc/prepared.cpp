@@ -39,7 +39,15 @@ PreparedMesh prepare_mesh(TetMesh&& tm) {
             pm.bbox_min[c] = std::min(pm.bbox_min[c], pm.tet.xyz[3 * (size_t)i + c]);
             pm.bbox_max[c] = std::max(pm.bbox_max[c], pm.tet.xyz[3 * (size_t)i + c]);
         }
+    attach_interface_surface(pm);
     return pm;
+}
+
+void attach_interface_surface(PreparedMesh& pm) {
+    std::vector<int32_t> tris, tri2tet;
+    interface_triangles(pm.tet.tets, pm.tet.marker, pm.face_nbr, pm.tet.xyz, tris, tri2tet);
+    pm.surf = build_surface_tables(pm.tet.xyz.data(), pm.tet.n_nodes(), pm.tet.n_tets(), std::move(tris),
+                                   std::move(tri2tet));
 }
 
 }  // namespace fgb

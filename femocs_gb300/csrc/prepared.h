@@ -2,6 +2,7 @@
 #pragma once
 
 #include "mesh.h"
+#include "surface.h"
 
 namespace fgb {
 
@@ -18,7 +19,12 @@ struct PreparedMesh {
     double edgemax = 0.0;
     double decay_factor = 0.0;
     double bbox_min[3] = {0, 0, 0}, bbox_max[3] = {0, 0, 0};
+    // surface triangles for 2-D location (default: the vacuum/metal interface faces)
+    SurfaceTables surf;
 };
+
+// the default surface of a prepared mesh: its vacuum/metal interface triangles
+void attach_interface_surface(PreparedMesh& pm);
 
 PreparedMesh prepare_mesh(TetMesh&& tm);
 

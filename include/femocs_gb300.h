@@ -97,6 +97,14 @@ FGB_MESH* fgb_mesh_synthetic(const FgbNanotip* spec);
  * builder's; up to 2^21 tet vertices */
 FGB_MESH* fgb_mesh_from_arrays_device(int n_nodes, const double* xyz, int n_tets, const int* tets, const int* markers);
 FGB_MESH* fgb_mesh_synthetic_device(const FgbNanotip* spec);
+/* Surface triangles for surface (2-D) location and interpolation. A prepared mesh starts with
+ * its vacuum/metal interface faces (per vacuum tet ascending, faces opposite vertex 0..3 whose
+ * neighbour is not vacuum; normal into the vacuum; tri2tet = {vacuum tet, metal tet}).
+ * fgb_mesh_set_surface replaces them, e.g. by TetGen's surface triangles and their tet
+ * pairs (TetgenMesh tris / tris.to_tets, src/TetgenMesh.cpp:592-612): 3 tet-mesh node ids and
+ * 2 tets per triangle, the first tet tried first. Fields created afterwards use the new set. */
+int fgb_mesh_set_surface(FGB_MESH* m, int n_tris, const int* tris, const int* tri2tet);
+int64_t fgb_mesh_surface_tris(const FGB_MESH* m);
 /* preparation time of a mesh: [device kernel ms (0 for the host builder), total ms] */
 int fgb_mesh_prep_timing(const FGB_MESH* m, double* out2);
 void fgb_mesh_free(FGB_MESH* m);
@@ -106,7 +114,9 @@ int fgb_mesh_sizes(const FGB_MESH* m, int64_t* out12);
 /* copy a named host table into `out` (caller sized from fgb_mesh_sizes):
  * tet_nodes tet_marker tet_nbor node_xyz node_marker hex_nodes hex_marker tet_det
  * tet_centroid hex_coeffs nbr_ptr nbr_idx quad_nodes voro_ptr voro_idx vac_node2vertex
- * vac_cells node_parents (4 per node, -1 = unused) edgemax(double) */
+ * vac_cells node_parents (4 per node, -1 = unused) edgemax(double);
+ * surface: surf_tris (3 per triangle) surf_tri2tet (2) surf_geo (19 doubles: vertex 0, edge1/D,
+ * edge2, pvec/D, unit normal, |edge2|, centroid) surf_nbr_ptr surf_nbr_idx */
 int fgb_mesh_export(const FGB_MESH* m, const char* name, void* out);
 
 /* synthetic atoms/probes for a nanotip spec; two-call pattern: pass out=NULL to get the count */
@@ -185,6 +195,13 @@ int fgb_field_interpolate(FGB_FIELD* f, int n, const double* xyz, int rank, int*
                           int64_t* stats5);
 /* same with device pointers (no copies) */
 int fgb_field_interpolate_device(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells, double* d_out5);
+/* surface (2-D) location + interpolation on the mesh's surface triangles (LinearTriangles rank 1,
+ * QuadraticTriangles rank 2: src/InterpolatorCells.cpp:1639-1686, 1834-1856, driven as
+ * SolutionReader::calc_full_interpolation with dim = 2, src/SolutionReader.cpp:43-55);
+ * cells = triangle per point (negative: no triangle holds the point, nearest centroid) */
+int fgb_field_interpolate_surface(FGB_FIELD* f, int n, const double* xyz, int rank, int* cells, double* out5);
+int fgb_field_interpolate_surface_device(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells,
+                                         double* d_out5);
 /* Allocation-free variant of fgb_field_interpolate_device (no counterpart in the reference).
  * Some callers cannot let a library allocate device memory during their timestep loop: MD
  * engines that hand the whole device memory to their own pool allocator, or run with a

@@ -4,6 +4,7 @@
 #define _POSIX_C_SOURCE 199309L
 #include "femocs_oracle.h"
 
+#include <limits.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -623,6 +624,125 @@ void orc_locate_interpolate(const OrcInterp* m, int rank, int n_pts, const doubl
             weighted(m, m->hexs + 8 * (size_t)c, w, 8, out + 5 * (size_t)i);
         }
     }
+}
+
+/* ------------------------------------------------------------------ surface */
+typedef struct {
+    V3 v0, e1d, e2, pvd, n, c;
+    double maxd;
+} TriRow;
+
+static V3 vsub(V3 a, V3 b) { V3 r = {a.x - b.x, a.y - b.y, a.z - b.z}; return r; }
+static V3 vmul(V3 a, double s) { V3 r = {a.x * s, a.y * s, a.z * s}; return r; }
+/* Vec3::crossProduct / dotProduct, include/Primitives.h:307-313 */
+static V3 vcross(V3 a, V3 v) {
+    V3 r = {a.y * v.z - a.z * v.y, a.z * v.x - a.x * v.z, a.x * v.y - a.y * v.x};
+    return r;
+}
+static double vdot(V3 a, V3 v) { return a.x * v.x + a.y * v.y + a.z * v.z; }
+
+/* TetgenFaces::calc_appendices (src/TetgenCells.cpp:387-412) + LinearTriangles::precompute
+ * (src/InterpolatorCells.cpp:1585-1637) */
+static void tri_rows(const OrcSurface* s, TriRow* r) {
+    for (int f = 0; f < s->n_tris; ++f) {
+        const V3 v0 = ld3(s->xyz, s->tris[3 * (size_t)f]);
+        const V3 v1 = ld3(s->xyz, s->tris[3 * (size_t)f + 1]);
+        const V3 v2 = ld3(s->xyz, s->tris[3 * (size_t)f + 2]);
+        const V3 e1 = vsub(v1, v0), e2 = vsub(v2, v0);
+        V3 n = vcross(e1, e2);
+        const double nn = sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+        if (nn > 0) n = vmul(n, 1 / nn);
+        V3 c = {v0.x + v1.x, v0.y + v1.y, v0.z + v1.z};
+        c.x = (c.x + v2.x) / 3.0; c.y = (c.y + v2.y) / 3.0; c.z = (c.z + v2.z) / 3.0;
+        const V3 pv = vcross(n, e2);
+        const double i_det = 1.0 / vdot(e1, pv);
+        r[f].v0 = v0; r[f].e1d = vmul(e1, i_det); r[f].e2 = e2; r[f].pvd = vmul(pv, i_det);
+        r[f].n = n; r[f].c = c; r[f].maxd = sqrt(e2.x * e2.x + e2.y * e2.y + e2.z * e2.z);
+    }
+}
+/* LinearTriangles::point_in_cell, src/InterpolatorCells.cpp:1639-1650 */
+static int tri_pic(const TriRow* r, const double* p) {
+    const V3 pt = {p[0], p[1], p[2]};
+    const V3 tv = vsub(pt, r->v0);
+    const double u = vdot(tv, r->pvd);
+    if (u < -ZERO || u > 1 + ZERO) return 0;
+    const V3 q = vcross(tv, r->e1d);
+    const double v = vdot(q, r->n);
+    if (v < -ZERO || u + v > 1 + ZERO) return 0;
+    return fabs(vdot(q, r->e2)) < r->maxd;
+}
+/* LinearTriangles::fast_distance, :1743-1747 */
+static double tri_fast_distance(const TriRow* r, const double* p) {
+    const V3 pt = {p[0], p[1], p[2]};
+    const V3 q = vcross(vsub(pt, r->v0), r->e1d);
+    return vdot(r->e2, q);
+}
+
+void orc_surface_interpolate(const OrcInterp* m, const OrcSurface* s, int rank, int n_pts, const double* pts,
+                             int32_t* cells, double* out) {
+    const int nf = s->n_tris;
+    TriRow* rows = (TriRow*)malloc(sizeof(TriRow) * (size_t)(nf ? nf : 1));
+    tri_rows(s, rows);
+    /* neighbours: for each node of the triangle, the other triangles of that node (ascending) */
+    int* cnt = (int*)calloc((size_t)s->n_nodes + 1, sizeof(int));
+    for (int f = 0; f < 3 * nf; ++f) cnt[s->tris[f] + 1]++;
+    for (int i = 0; i < s->n_nodes; ++i) cnt[i + 1] += cnt[i];
+    int* n2f = (int*)malloc(sizeof(int) * (size_t)(cnt[s->n_nodes] ? cnt[s->n_nodes] : 1));
+    int* pos = (int*)malloc(sizeof(int) * (size_t)(s->n_nodes ? s->n_nodes : 1));
+    memcpy(pos, cnt, sizeof(int) * (size_t)s->n_nodes);
+    for (int f = 0; f < nf; ++f)
+        for (int k = 0; k < 3; ++k) n2f[pos[s->tris[3 * (size_t)f + k]]++] = f;
+
+    int cell = -1;
+    for (int i = 0; i < n_pts; ++i) {
+        const double* p = pts + 3 * (size_t)i;
+        /* InterpolatorCells<3>::locate_cell (src/InterpolatorCells.cpp:269-307), guess abs(cell) */
+        const int guess = abs(cell);
+        int found = INT_MIN;
+        if (guess < nf) {
+            if (tri_pic(rows + guess, p)) found = guess;
+            for (int k = 0; k < 3 && found == INT_MIN; ++k) {
+                const int v = s->tris[3 * (size_t)guess + k];
+                for (int q = cnt[v]; q < cnt[v + 1]; ++q) {
+                    const int g = n2f[q];
+                    if (g != guess && tri_pic(rows + g, p)) { found = g; break; }
+                }
+            }
+        }
+        if (found == INT_MIN) {
+            double best = 1e100;
+            int best_i = 0;
+            for (int f = 0; f < nf; ++f) {
+                if (tri_pic(rows + f, p)) { found = f; break; }
+                const double dx = p[0] - rows[f].c.x, dy = p[1] - rows[f].c.y, dz = p[2] - rows[f].c.z;
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 < best) { best = d2; best_i = f; }
+            }
+            if (found == INT_MIN) found = -best_i;
+        }
+        cell = found;
+        cells[i] = cell;
+        /* LinearTriangles::interp_solution (:1662-1686) / QuadraticTriangles (:1834-1856) */
+        const int tri = abs(cell);
+        const int t0 = s->tri2tet[2 * (size_t)tri], t1 = s->tri2tet[2 * (size_t)tri + 1];
+        int tet;
+        if (fabs(tri_fast_distance(rows + tri, p)) <= 100.0 * ZERO) tet = t0;
+        else if (pic(m, p, t0)) tet = t0;
+        else tet = tet_locate(m, p, t1);
+        const int c = abs(tet);
+        double w[10], b[4];
+        bcc(m, p, c, b);
+        if (rank == 1) {
+            weighted(m, m->tets + 4 * (size_t)c, b, 4, out + 5 * (size_t)i);
+        } else {
+            w[0] = b[0] * (2 * b[0] - 1); w[1] = b[1] * (2 * b[1] - 1);
+            w[2] = b[2] * (2 * b[2] - 1); w[3] = b[3] * (2 * b[3] - 1);
+            w[4] = 4 * b[0] * b[1]; w[5] = 4 * b[1] * b[2]; w[6] = 4 * b[2] * b[0];
+            w[7] = 4 * b[0] * b[3]; w[8] = 4 * b[1] * b[3]; w[9] = 4 * b[2] * b[3];
+            weighted(m, m->quad_nodes + 10 * (size_t)c, w, 10, out + 5 * (size_t)i);
+        }
+    }
+    free(rows); free(cnt); free(n2f); free(pos);
 }
 
 int orc_tet_neighbour_lists(int n_nodes, int n_tets, const int32_t* tets, const int32_t* face_nbr,

@@ -87,6 +87,24 @@ typedef struct {
 void orc_locate_interpolate(const OrcInterp* m, int rank, int n_pts, const double* pts,
                             int32_t* cells, double* out);
 
+/* ---------- surface (2-D) location + interpolation ----------
+ * LinearTriangles / QuadraticTriangles (src/InterpolatorCells.cpp:1585-1686, 1791-1862):
+ * triangle tables from the node coordinates (TetgenFaces::calc_appendices,
+ * src/TetgenCells.cpp:387-412, and LinearTriangles::precompute), the chained triangle
+ * location of a fresh reader (src/SolutionReader.cpp:43-55, 136-165) and the tet chosen
+ * through the triangle's two tets. rank 1 interpolates linearly, rank 2 quadratically in
+ * that tet. cells: triangle per point (negative = nearest-centroid fallback). */
+typedef struct {
+    int n_tris;
+    const int32_t* tris;     /* 3 node ids per triangle */
+    const int32_t* tri2tet;  /* 2 tets per triangle, the first tried first */
+    int n_nodes;
+    const double* xyz;       /* 3 per node */
+} OrcSurface;
+
+void orc_surface_interpolate(const OrcInterp* m, const OrcSurface* s, int rank, int n_pts, const double* pts,
+                             int32_t* cells, double* out);
+
 /* neighbour lists exactly as the reference stores them (face neighbours, then
  * vertex-sharing tets with repeats), src/InterpolatorCells.cpp:537-558 */
 int orc_tet_neighbour_lists(int n_nodes, int n_tets, const int32_t* tets, const int32_t* face_nbr,

@@ -19,7 +19,7 @@ i64p = C.POINTER(C.c_int64)
 i8p = C.POINTER(C.c_int8)
 
 __all__ = ["build_oracle", "lib", "tet_tables", "System", "neighbour_lists", "nodal_field", "smooth_field",
-           "locate_interpolate", "read_records", "write_msh", "test_solution"]
+           "locate_interpolate", "surface_interpolate", "read_records", "write_msh", "test_solution"]
 
 
 def build_oracle(force=False):
@@ -42,6 +42,10 @@ class OrcInterp(C.Structure):
                 ("nbr_ptr", ip), ("nbr_idx", ip), ("hexs", ip), ("hexf", dp), ("quad_nodes", ip), ("sol", dp)]
 
 
+class OrcSurface(C.Structure):
+    _fields_ = [("n_tris", C.c_int), ("tris", ip), ("tri2tet", ip), ("n_nodes", C.c_int), ("xyz", dp)]
+
+
 _lib = None
 
 
@@ -62,6 +66,8 @@ def lib():
         L.orc_nodal_field.argtypes = [C.c_int, dp, C.c_int, ip, ip, i8p, dp, dp]
         L.orc_smooth_field.argtypes = [C.c_int, dp, ip, ip, C.c_double, dp]
         L.orc_locate_interpolate.argtypes = [C.POINTER(OrcInterp), C.c_int, C.c_int, dp, ip, dp]
+        L.orc_surface_interpolate.argtypes = [C.POINTER(OrcInterp), C.POINTER(OrcSurface), C.c_int, C.c_int, dp, ip,
+                                              dp]
         L.orc_tet_neighbour_lists.argtypes = [C.c_int, C.c_int, ip, ip, ip, ip, C.c_int]
         _lib = L
     return _lib
@@ -197,6 +203,45 @@ def locate_interpolate(tables, rank, pts):
     return cells, out.reshape(-1, 5)
 
 
+def surface_interpolate(tables, tris, tri2tet, xyz, rank, pts):
+    """Surface (2-D) location + interpolation of LinearTriangles (rank 1) / QuadraticTriangles
+    (rank 2) over the tet tables of locate_interpolate; tris (n,3), tri2tet (n,2), xyz the node
+    coordinates. Returns (triangle per point, 5 values per point)."""
+    keep = {}
+
+    def a(name, dt, src=None):
+        v = np.ascontiguousarray(tables[name] if src is None else src, dtype=dt).reshape(-1)
+        keep[name] = v
+        return v
+
+    m = OrcInterp()
+    m.n_tets = len(np.asarray(tables["tets"]).reshape(-1)) // 4
+    m.tets = _p(a("tets", np.int32), ip)
+    m.search = _p(a("search", np.int8), i8p)
+    m.det = _p(a("det", np.float64))
+    m.centroid = _p(a("centroid", np.float64))
+    m.nbr_ptr = _p(a("nbr_ptr", np.int32), ip)
+    m.nbr_idx = _p(a("nbr_idx", np.int32), ip)
+    m.hexs = _p(a("hexs", np.int32), ip)
+    m.hexf = _p(a("hexf", np.float64))
+    m.quad_nodes = _p(a("quad_nodes", np.int32), ip)
+    m.sol = _p(a("sol", np.float64))
+    sf = OrcSurface()
+    t = a("tris", np.int32, tris)
+    sf.n_tris = len(t) // 3
+    sf.tris = _p(t, ip)
+    sf.tri2tet = _p(a("tri2tet", np.int32, tri2tet), ip)
+    x = a("xyz", np.float64, xyz)
+    sf.n_nodes = len(x) // 3
+    sf.xyz = _p(x)
+    pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1)
+    n = len(pts) // 3
+    cells = np.zeros(n, dtype=np.int32)
+    out = np.zeros(5 * n)
+    lib().orc_surface_interpolate(C.byref(m), C.byref(sf), rank, n, _p(pts), _p(cells, ip), _p(out))
+    return cells, out.reshape(-1, 5)
+
+
 def test_solution(xyz):
     """Smooth nodal test field (same formula as oracle/ref_driver.cpp test_solution)."""
     p = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
@@ -229,15 +274,20 @@ def read_records(path):
     return out
 
 
-def write_msh(path, xyz, tets, markers):
-    """Gmsh 2.2 ASCII tetrahedral mesh, coordinates printed round-trip exact."""
+def write_msh(path, xyz, tets, markers, tris=None, tri_marker=2):
+    """Gmsh 2.2 ASCII tetrahedral mesh, coordinates printed round-trip exact; optional surface
+    triangles (element type 2) after the tets."""
     xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
     tets = np.asarray(tets).reshape(-1, 4)
+    tris = np.zeros((0, 3), dtype=np.int64) if tris is None else np.asarray(tris).reshape(-1, 3)
     with open(path, "w") as f:
         f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % len(xyz))
         for i, p in enumerate(xyz):
             f.write("%d %r %r %r\n" % (i + 1, float(p[0]), float(p[1]), float(p[2])))
-        f.write("$EndNodes\n$Elements\n%d\n" % len(tets))
+        f.write("$EndNodes\n$Elements\n%d\n" % (len(tets) + len(tris)))
         for i, (t, m) in enumerate(zip(tets, markers)):
             f.write("%d 4 2 %d %d %d %d %d %d\n" % (i + 1, m, m, t[0] + 1, t[1] + 1, t[2] + 1, t[3] + 1))
+        for i, t in enumerate(tris):
+            f.write("%d 2 2 %d %d %d %d %d\n" % (len(tets) + i + 1, tri_marker, tri_marker, t[0] + 1, t[1] + 1,
+                                                  t[2] + 1))
         f.write("$EndElements\n")

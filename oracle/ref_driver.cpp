@@ -177,6 +177,52 @@ int main(int argc, char** argv) {
         put(fo, nm, 'd', sol.size(), sol.data());
     }
 
+    // ---------------- surface (2-D) location and interpolation, when the mesh file carries
+    // surface triangles: TetGen's tri->tet mapping of the read (calc_tri2tet2tri_mapping,
+    // src/TetgenMesh.cpp:592-612), LinearTriangles / QuadraticTriangles set up as in
+    // Interpolator::initialize, and the chained query loop of calc_full_interpolation with
+    // dim = 2 (src/SolutionReader.cpp:43-55)
+    const int n_tris = mesh.tris.size();
+    if (n_tris > 0) {
+        LinearTriangles lintri(&nodes, &lintet);
+        QuadraticTriangles quadtri(&nodes, &lintri, &quadtet);
+        lintri.set_mesh(&mesh);
+        quadtri.set_mesh(&mesh);
+        lintri.precompute();
+        quadtri.precompute();
+        std::vector<int32_t> tv(3 * (size_t)n_tris), t2t(2 * (size_t)n_tris);
+        std::vector<double> tn(3 * (size_t)n_tris);
+        for (int f = 0; f < n_tris; ++f) {
+            SimpleFace sf = mesh.tris[f];
+            for (int k = 0; k < 3; ++k) tv[3 * f + k] = sf[k];
+            std::array<int, 2> tt = mesh.tris.to_tets(f);
+            t2t[2 * f] = tt[0];
+            t2t[2 * f + 1] = tt[1];
+            Vec3 nv = lintri.get_norm(f);
+            tn[3 * f] = nv.x; tn[3 * f + 1] = nv.y; tn[3 * f + 2] = nv.z;
+        }
+        put(fo, "tri_nodes", 'i', tv.size(), tv.data());
+        put(fo, "tri2tet", 'i', t2t.size(), t2t.data());
+        put(fo, "tri_norm", 'd', tn.size(), tn.data());
+        for (int rank = 1; rank <= 2; ++rank) {
+            std::vector<int32_t> cells(n_pts);
+            std::vector<double> sol(5 * (size_t)n_pts);
+            int cell = -1;
+            for (int i = 0; i < n_pts; ++i) {
+                Point3 p(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+                Solution s = rank == 1 ? lintri.locate_interpolate(p, cell) : quadtri.locate_interpolate(p, cell);
+                cells[i] = cell;
+                sol[5 * i] = s.vector.x; sol[5 * i + 1] = s.vector.y; sol[5 * i + 2] = s.vector.z;
+                sol[5 * i + 3] = s.scalar1; sol[5 * i + 4] = s.scalar2;
+            }
+            char nm[16];
+            std::snprintf(nm, sizeof(nm), "cells_s%d", rank);
+            put(fo, nm, 'i', cells.size(), cells.data());
+            std::snprintf(nm, sizeof(nm), "interp_s%d", rank);
+            put(fo, nm, 'd', sol.size(), sol.data());
+        }
+    }
+
     // ---------------- nodal field recovery (vacuum hexes) and smoothing
     {
         std::vector<std::vector<std::pair<int, int>>> node2cells(n_nodes);

@@ -1,6 +1,7 @@
 """Generate the golden vectors in tests/golden/ from the reference's own compiled sources.
 
     python tests/golden/make_golden.py            (needs the mounted FEMOCS sources)
+    python tests/golden/make_golden.py --surface  (only the surface-interpolation fixtures)
 
 The tetrahedral input meshes are synthetic nanotip meshes (femocs_gb300's seeded generator),
 written as Gmsh files and read back by the reference exactly the way it reads `mesh_file`
@@ -100,6 +101,54 @@ def make_case(name: str, spec: dict, seed: int) -> dict:
     return g
 
 
+def surface_points(mesh: fg.Mesh, spec: dict, seed: int) -> np.ndarray:
+    """Queries for surface (2-D) interpolation: surface atoms, points off triangle centroids
+    along the normal, triangle vertices and edge midpoints (held by several triangles, where
+    the chained guess decides), points exactly on triangles, and points far from the surface
+    (nearest-centroid fallback)."""
+    rng = np.random.default_rng(seed)
+    tris, _, geo = mesh.surface()
+    X = mesh.export("node_xyz").reshape(-1, 3)
+    atoms, types = fg.synth_atoms(spec, seed=seed)
+    surf = atoms[types == 2][:1200]
+    pick = rng.integers(0, len(tris), 300)
+    off = geo[pick, 16:19] + geo[pick, 12:15] * (rng.uniform(-0.8, 0.8, 300) * geo[pick, 15])[:, None]
+    on = geo[pick[:100], 16:19]
+    verts = X[tris[rng.integers(0, len(tris), 120)][:, 0]]
+    tt = tris[rng.integers(0, len(tris), 120)]
+    edges = (X[tt[:, 0]] + X[tt[:, 1]]) / 2.0
+    b, top, slab = spec["box_half"], spec["top"], spec["slab"]
+    far = np.c_[rng.uniform(-b, b, 80), rng.uniform(-b, b, 80), rng.uniform(0.5 * top, top, 80)]
+    return np.ascontiguousarray(np.r_[surf, off, on, verts, edges, far], dtype=np.float64)
+
+
+def make_surface_case(name: str, spec: dict, seed: int) -> dict:
+    """The reference reads the mesh together with its vacuum/metal surface triangles (TetGen
+    recomputes their tet pairs) and interpolates on the surface for ranks 1 and 2."""
+    mesh = fg.Mesh.synthetic(**spec)
+    s = mesh.sizes()
+    tris, t2t, _ = mesh.surface()
+    pts = surface_points(mesh, spec, seed)
+    with tempfile.TemporaryDirectory() as td:
+        msh, pbin, obin = (os.path.join(td, f) for f in ("m.msh", "p.bin", "o.bin"))
+        write_msh(msh, mesh.export("node_xyz").reshape(-1, 3)[: s["n_tetnodes"]], mesh.export("tet_nodes"),
+                  mesh.export("tet_marker"), tris)
+        with open(pbin, "wb") as f:
+            f.write(struct.pack("<i", len(pts)) + pts.astype("<f8").tobytes())
+        subprocess.run([DRIVER, msh, pbin, obin], check=True)
+        r = read_records(obin)
+    assert digest(r["hex_nodes"]) == digest(mesh.export("hex_nodes")), "the triangles changed the hex split"
+    g = dict(
+        spec=np.array([spec[k] for k in ("radius", "height", "box_half", "slab", "top", "h", "growth", "margin")]),
+        pts=pts, tri_nodes=r["tri_nodes"].reshape(-1, 3), tri2tet=r["tri2tet"].reshape(-1, 2),
+        tri_norm=r["tri_norm"].reshape(-1, 3),
+    )
+    for rank in (1, 2):
+        g[f"cells_s{rank}"] = r[f"cells_s{rank}"]
+        g[f"interp_s{rank}"] = r[f"interp_s{rank}"].reshape(-1, 5)
+    return g
+
+
 def main():
     if not os.path.exists(DRIVER):
         subprocess.run(["make", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), f"REF={REF}", "-j8"], cwd=ROOT,
@@ -107,12 +156,19 @@ def main():
     fg.load()
     from femocs_gb300.build import build
     build()
+    only_surface = "--surface" in sys.argv
     for i, (name, spec) in enumerate(CASES.items()):
-        g = make_case(name, spec, seed=100 + i)
-        path = os.path.join(HERE, f"golden_{name}.npz")
+        if not only_surface:
+            g = make_case(name, spec, seed=100 + i)
+            path = os.path.join(HERE, f"golden_{name}.npz")
+            np.savez_compressed(path, **g)
+            print(path, os.path.getsize(path), "bytes,", len(g["pts"]), "points, neg cells r3:",
+                  int((g["cells_r3"] < 0).sum()))
+        g = make_surface_case(name, spec, seed=200 + i)
+        path = os.path.join(HERE, f"surface_{name}.npz")
         np.savez_compressed(path, **g)
-        print(path, os.path.getsize(path), "bytes,", len(g["pts"]), "points, neg cells r3:",
-              int((g["cells_r3"] < 0).sum()))
+        print(path, os.path.getsize(path), "bytes,", len(g["pts"]), "points,", len(g["tri_nodes"]),
+              "triangles, neg cells s1:", int((g["cells_s1"] < 0).sum()))
 
 
 if __name__ == "__main__":

@@ -10,7 +10,7 @@ import pytest
 
 import femocs_gb300 as fg
 import oracle as orc
-from util import bits_equal, golden_cases, load_golden, oracle_tables
+from util import bits_equal, golden_cases, load_golden, load_surface, oracle_tables, surface_cases
 
 CASES = golden_cases()
 
@@ -79,3 +79,27 @@ def test_neighbour_lists_cover_reference_lists(case):
                 seen.add(u)
                 dedup.append(u)
         assert list(pidx[pptr[t]:pptr[t + 1]]) == dedup
+
+
+@pytest.mark.parametrize("name", surface_cases())
+def test_surface_fixture_matches_product_surface(name):
+    """The reference (with TetGen recomputing the triangle/tet pairs) keeps the product's
+    interface triangles, their vertex order and their tet pairs."""
+    g = load_surface(name)
+    m = fg.Mesh.synthetic(**g["spec_kw"])
+    tris, t2t, geo = m.surface()
+    np.testing.assert_array_equal(tris, g["tri_nodes"])
+    np.testing.assert_array_equal(t2t, g["tri2tet"])
+    assert bits_equal(geo[:, 12:15], g["tri_norm"])
+
+
+@pytest.mark.parametrize("name", surface_cases())
+@pytest.mark.parametrize("rank", [1, 2])
+def test_oracle_surface_interpolation_bit_exact(name, rank):
+    g = load_surface(name)
+    m = fg.Mesh.synthetic(**g["spec_kw"])
+    xyz = m.export("node_xyz")
+    sol = orc.test_solution(xyz)
+    cells, out = orc.surface_interpolate(oracle_tables(m, sol), g["tri_nodes"], g["tri2tet"], xyz, rank, g["pts"])
+    np.testing.assert_array_equal(cells, g[f"cells_s{rank}"])
+    assert bits_equal(out, g[f"interp_s{rank}"])

@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 
 TABLES = ["tet_nodes", "tet_marker", "tet_nbor", "node_xyz", "node_marker", "hex_nodes", "hex_marker", "tet_det",
           "tet_centroid", "hex_coeffs", "nbr_ptr", "nbr_idx", "quad_nodes", "voro_ptr", "voro_idx", "vac_node2vertex",
-          "vac_cells", "tet_search", "edgemax", "node_parents"]
+          "vac_cells", "tet_search", "edgemax", "node_parents", "surf_tris", "surf_tri2tet", "surf_geo", "surf_nbr_ptr",
+          "surf_nbr_idx"]
 SMALL = dict(radius=5.0, height=14.0, box_half=18.0, slab=4.0, top=40.0, h=4.0, growth=1.6, margin=3.0)
 
 

@@ -20,6 +20,16 @@ def load_golden(name):
     return g
 
 
+def surface_cases():
+    return sorted(f[len("surface_"):-4] for f in os.listdir(GOLDEN_DIR) if f.startswith("surface_") and f.endswith(".npz"))
+
+
+def load_surface(name):
+    g = dict(np.load(os.path.join(GOLDEN_DIR, f"surface_{name}.npz")))
+    g["spec_kw"] = dict(zip(SPEC_KEYS, [float(v) for v in g["spec"]]))
+    return g
+
+
 def oracle_tables(mesh, sol):
     s = mesh.sizes()
     tets = mesh.export("tet_nodes")
