@@ -238,6 +238,24 @@ def mesh_prep_timing(spec):
             "note": "device_ms includes the tet upload and the download of every table into host memory"}
 
 
+def surface_cpu_timing(spec, surf_pts, sample=2000):
+    """The oracle's sequential restatement of the reference's surface interpolation (1 thread)
+    on a sample of the surface atoms (the nodal values do not change the work)."""
+    import numpy as np
+    import femocs_gb300 as fg
+    import oracle as orc
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from util import oracle_tables
+    m = fg.Mesh.synthetic(**spec)
+    tables = oracle_tables(m, np.zeros((m.sizes()["n_nodes"], 5)))
+    tris, t2t, _ = m.surface()
+    pts = np.ascontiguousarray(surf_pts[:sample])
+    t0 = time.perf_counter()
+    orc.surface_interpolate(tables, tris, t2t, m.export("node_xyz"), 1, pts)
+    dt = time.perf_counter() - t0
+    return {"cpu_points_per_s": len(pts) / dt, "cpu_sample": len(pts), "cpu_kind": "port", "cpu_cores": 1}
+
+
 def run_ours(args, world, rank):
     import numpy as np
     import femocs_gb300 as fg
@@ -319,6 +337,15 @@ def run_ours(args, world, rank):
             raise RuntimeError(fg.last_error())
     e2e_s = reduce_max(world, statistics.median(e2e_t))
 
+    # surface (2-D) interpolation of the surface atoms (rank 1, LinearTriangles), points resident
+    surf_reps = 5
+    lib.fgb_field_interpolate_surface_device(field.h, n_surf, d_pts.ptr, 1, d_cells.ptr, d_out.ptr)
+    field.mark(2)
+    for _ in range(surf_reps):
+        lib.fgb_field_interpolate_surface_device(field.h, n_surf, d_pts.ptr, 1, d_cells.ptr, d_out.ptr)
+    field.mark(3)
+    surf_ms = field.elapsed(2, 3) / surf_reps
+
     # roofline of the dominant kernel of the solve, timed live by event pairs around each of
     # its launches in the timed steps. Algorithmic bytes per launch:
     #   level-0 Chebyshev step (k_cheb_step): FP32 SELL matrix, 4 B value + 4 B column per
@@ -398,8 +425,11 @@ def run_ours(args, world, rank):
     }
     if rank == 0 and world == 1 and not args.no_cpu and SSOR_ITERS.get(args.workload):
         line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec, order)
+    line["surface_interp"] = {"points": n_surf, "gpu_ms": surf_ms, "gpu_points_per_s": n_surf / (surf_ms * 1e-3),
+                              "rank": 1, "note": "femocs_interpolate_surface_elfield path, device-resident points"}
     if rank == 0 and world == 1 and not args.no_cpu:
         line["mesh_prep"] = mesh_prep_timing(spec)
+        line["surface_interp"].update(surface_cpu_timing(spec, pts[:n_surf]))
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -18,7 +18,7 @@ def _stats_dict(st):
                 ms=st[5], kernel_ms=st[6], setup_ms=st[7], levels=int(st[8]), smoother_ms=st[9],
                 smoother_launches=int(st[10]), spmv_ms=st[11], spmv_launches=int(st[12]), smoother_bytes=st[13])
 
-__all__ = ["Mesh", "Field", "Femocs", "nanotip", "synth_atoms", "synth_probes", "load", "last_error",
+__all__ = ["Mesh", "Field", "Femocs", "Heat", "nanotip", "synth_atoms", "synth_probes", "load", "last_error",
            "CONFIG1", "CONFIG2", "FgbNanotip", "DeviceBuffer"]
 
 
@@ -315,6 +315,75 @@ class Field:
 
     def time_spmv(self, precision, reps=20):
         return load().fgb_field_time_spmv(self.h, precision, reps)
+
+
+class Heat:
+    """Current and heat on the bulk hexahedra of a mesh (CurrentHeatSolver verbs, Q1 on the GPU).
+
+    Surface values are per copper-surface face, in the order of surface_faces()."""
+
+    def __init__(self, mesh: Mesh):
+        self.mesh = mesh
+        self.h = load().fgb_heat_create(mesh.h)
+        if not self.h:
+            raise RuntimeError("heat solver creation failed: " + last_error())
+        o = np.zeros(3, dtype=np.int64)
+        self._ok(load().fgb_heat_sizes(self.h, ptr(o, i64p)))
+        self.n_dofs, self.nnz, self.n_faces = (int(v) for v in o)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().fgb_heat_free(self.h)
+            self.h = None
+
+    @staticmethod
+    def _ok(rc):
+        if rc != 0:
+            raise RuntimeError(last_error())
+
+    def surface_faces(self):
+        """(centroids (n,3), (hex id, femocs local face) (n,2)) of the copper-surface faces"""
+        c = np.zeros(max(3 * self.n_faces, 1))
+        hf = np.zeros(max(2 * self.n_faces, 1), dtype=np.int32)
+        self._ok(load().fgb_heat_surface_faces(self.h, ptr(c), ptr(hf, ip)))
+        return c[: 3 * self.n_faces].reshape(-1, 3), hf[: 2 * self.n_faces].reshape(-1, 2)
+
+    def set_resistivity(self, T, rho):
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        self._ok(load().fgb_heat_set_resistivity(self.h, len(T), ptr(T), ptr(rho)))
+
+    def setup(self, t_ambient=300.0, lorentz=2.44e-8, rho_cp=3.4496e-24):
+        self._ok(load().fgb_heat_setup(self.h, t_ambient, lorentz, rho_cp))
+
+    def _solve(self, fn, args, precision, rel_tol, max_iter):
+        st = np.zeros(14)
+        rc = fn(self.h, *args, precision, rel_tol, max_iter, ptr(st))
+        if rc == -2 ** 31:
+            raise RuntimeError(last_error())
+        return rc, _stats_dict(st)
+
+    def solve_current(self, face_j, precision=0, rel_tol=1e-9, max_iter=100000):
+        j = np.ascontiguousarray(face_j, dtype=np.float64)
+        assert len(j) == self.n_faces
+        return self._solve(load().fgb_heat_solve_current, (ptr(j),), precision, rel_tol, max_iter)
+
+    def solve_heat(self, delta_time_s, face_q, precision=0, rel_tol=1e-9, max_iter=100000):
+        q = np.ascontiguousarray(face_q, dtype=np.float64)
+        assert len(q) == self.n_faces
+        return self._solve(load().fgb_heat_solve_heat, (float(delta_time_s), ptr(q)), precision, rel_tol, max_iter)
+
+    def nodes(self):
+        """(temperature, current potential) per hex-mesh node; NaN outside the bulk"""
+        n = self.mesh.sizes()["n_nodes"]
+        T, p = np.zeros(n), np.zeros(n)
+        self._ok(load().fgb_heat_export(self.h, ptr(T), ptr(p)))
+        return T, p
+
+    def temperature_range(self):
+        o = np.zeros(2)
+        self._ok(load().fgb_heat_temperature_range(self.h, ptr(o)))
+        return float(o[0]), float(o[1])
 
 
 class Femocs:

@@ -57,6 +57,16 @@ _PROTOS = {
     "fgb_mesh_set_surface": (C.c_int, [vp, C.c_int, ip, ip]),
     "fgb_mesh_surface_tris": (C.c_int64, [vp]),
     "fgb_mesh_free": (None, [vp]),
+    "fgb_heat_create": (vp, [vp]),
+    "fgb_heat_free": (None, [vp]),
+    "fgb_heat_sizes": (C.c_int, [vp, i64p]),
+    "fgb_heat_surface_faces": (C.c_int, [vp, dp, ip]),
+    "fgb_heat_set_resistivity": (C.c_int, [vp, C.c_int, dp, dp]),
+    "fgb_heat_setup": (C.c_int, [vp, C.c_double, C.c_double, C.c_double]),
+    "fgb_heat_solve_current": (C.c_int, [vp, dp, C.c_int, C.c_double, C.c_int, dp]),
+    "fgb_heat_solve_heat": (C.c_int, [vp, C.c_double, dp, C.c_int, C.c_double, C.c_int, dp]),
+    "fgb_heat_export": (C.c_int, [vp, dp, dp]),
+    "fgb_heat_temperature_range": (C.c_int, [vp, dp]),
     "fgb_mesh_sizes": (C.c_int, [vp, i64p]),
     "fgb_mesh_export": (C.c_int, [vp, C.c_char_p, vp]),
     "fgb_synth_atoms": (C.c_int64, [C.POINTER(FgbNanotip), C.c_double, C.c_double, C.c_double, C.c_uint64, dp, ip]),

@@ -8,6 +8,7 @@
 #include <thread>
 
 #include "batch.h"
+#include "bulk.h"
 #include "facade.h"
 #include "server.h"
 #include "femocs_gb300.h"
@@ -22,6 +23,11 @@ struct FEMOCS {
 struct FGB_MESH {
     std::shared_ptr<PreparedMesh> pm;
     MeshPrepTiming timing;  // device: kernel and total ms; host: total ms
+};
+struct FGB_HEAT {
+    std::shared_ptr<const PreparedMesh> pm;
+    std::unique_ptr<BulkSolver> b;
+    SolveStats last;
 };
 struct FGB_BATCH {
     std::unique_ptr<BatchSolver> b;
@@ -658,6 +664,69 @@ FGB_FIELD* femocs_field(FEMOCS* h) {
     });
     if (rc) { delete f; return nullptr; }
     return f;
+}
+
+
+// ---------------------------------------------------------------- Part 5: current and heat
+FGB_HEAT* fgb_heat_create(const FGB_MESH* m) {
+    FGB_HEAT* h = new FGB_HEAT;
+    const int rc = guarded([&] {
+        h->pm = m->pm;
+        h->b.reset(new BulkSolver(h->pm));
+        return 0;
+    });
+    if (rc) { delete h; return nullptr; }
+    return h;
+}
+void fgb_heat_free(FGB_HEAT* h) { delete h; }
+int fgb_heat_sizes(FGB_HEAT* h, int64_t* out3) {
+    return guarded([&] {
+        out3[0] = h->b->n_dofs();
+        out3[1] = h->b->nnz();
+        out3[2] = h->b->n_faces();
+        return 0;
+    });
+}
+int fgb_heat_surface_faces(FGB_HEAT* h, double* centroid3, int* hex_face2) {
+    return guarded([&] { h->b->surface_faces(centroid3, hex_face2); return 0; });
+}
+int fgb_heat_set_resistivity(FGB_HEAT* h, int n, const double* T, const double* rho) {
+    return guarded([&] {
+        FGB_REQUIRE(n >= 2 && T && rho, "resistivity table needs >= 2 points");
+        h->b->set_resistivity(std::vector<double>(T, T + n), std::vector<double>(rho, rho + n));
+        return 0;
+    });
+}
+int fgb_heat_setup(FGB_HEAT* h, double t_ambient, double lorentz, double rho_cp) {
+    return guarded([&] { h->b->setup(t_ambient, lorentz, rho_cp); return 0; });
+}
+static int heat_solve(FGB_HEAT* h, bool heat, double dt, const double* vals, int precision, double rel_tol, int max_iter,
+                      double* stats14) {
+    int rc = 0;
+    const int g = guarded([&] {
+        SolveOptions o;
+        o.precision = precision;
+        o.rel_tol = rel_tol;
+        o.max_iter = max_iter;
+        rc = heat ? h->b->solve_heat(dt, vals, o, &h->last) : h->b->solve_current(vals, o, &h->last);
+        if (stats14) stats13(h->last, stats14);
+        return 0;
+    });
+    return g ? INT32_MIN : rc;
+}
+int fgb_heat_solve_current(FGB_HEAT* h, const double* face_j, int precision, double rel_tol, int max_iter,
+                           double* stats14) {
+    return heat_solve(h, false, 0.0, face_j, precision, rel_tol, max_iter, stats14);
+}
+int fgb_heat_solve_heat(FGB_HEAT* h, double delta_time_s, const double* face_q, int precision, double rel_tol,
+                        int max_iter, double* stats14) {
+    return heat_solve(h, true, delta_time_s, face_q, precision, rel_tol, max_iter, stats14);
+}
+int fgb_heat_export(FGB_HEAT* h, double* T_node, double* phi_node) {
+    return guarded([&] { h->b->export_nodes(T_node, phi_node); return 0; });
+}
+int fgb_heat_temperature_range(FGB_HEAT* h, double* out2) {
+    return guarded([&] { h->b->temperature_range(out2, out2 + 1); return 0; });
 }
 
 }  // extern "C"

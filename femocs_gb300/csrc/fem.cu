@@ -147,9 +147,11 @@ __global__ void k_assemble_rows(int n, const int64_t* __restrict__ rowptr, const
     }
 }
 
+// Neumann rows; the face value is `bc`, or fvals[face] when per-face values are given
 __global__ void k_neumann_rows(int n, const int32_t* __restrict__ r2f_ptr, const int32_t* __restrict__ r2f_item,
                                const int32_t* __restrict__ top, const double* __restrict__ dxyz, double bc,
-                               const double* __restrict__ extra, double* __restrict__ rhs) {
+                               const double* __restrict__ fvals, const double* __restrict__ extra,
+                               double* __restrict__ rhs) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     double acc = 0.0;
@@ -170,7 +172,7 @@ __global__ void k_neumann_rows(int n, const int32_t* __restrict__ r2f_ptr, const
             }
             const double cx = ds[1] * dt[2] - ds[2] * dt[1], cy = ds[2] * dt[0] - ds[0] * dt[2],
                          cz = ds[0] * dt[1] - ds[1] * dt[0];
-            acc += N[q] * bc * sqrt(cx * cx + cy * cy + cz * cz);
+            acc += N[q] * (fvals ? fvals[f] : bc) * sqrt(cx * cx + cy * cy + cz * cz);
         }
     }
     if (extra) acc += extra[r];
@@ -179,8 +181,10 @@ __global__ void k_neumann_rows(int n, const int32_t* __restrict__ r2f_ptr, const
 
 __device__ __forceinline__ bool is_fixed(int8_t k, bool anode) { return k == 1 || (k == 2 && anode); }
 
+// symmetric elimination; rows of kind 1 take the value v1, of kind 2 (anode Dirichlet) v0
 __global__ void k_dirichlet_rows(int n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                  const double* __restrict__ kval, const int8_t* __restrict__ bc, int anode, double v0,
+                                 double v1,
                                  const int64_t* __restrict__ csr2sell, double* __restrict__ s64, float* __restrict__ s32,
                                  double* __restrict__ dinv64, float* __restrict__ dinv32, double* __restrict__ rhs,
                                  double* __restrict__ x) {
@@ -192,7 +196,7 @@ __global__ void k_dirichlet_rows(int n, const int64_t* __restrict__ rowptr, cons
         if (col[k] == r) diag = kval[k];
     const bool fr = is_fixed(bc[r], anode);
     if (fr) {
-        const double gr = bc[r] == 2 ? v0 : 0.0;
+        const double gr = bc[r] == 2 ? v0 : v1;
         for (int64_t k = b; k < e; ++k) {
             const double a = col[k] == r ? kval[k] : 0.0;
             s64[csr2sell[k]] = a;
@@ -206,7 +210,7 @@ __global__ void k_dirichlet_rows(int n, const int64_t* __restrict__ rowptr, cons
             const int c = col[k];
             double a = kval[k];
             if (is_fixed(bc[c], anode)) {
-                const double gc = bc[c] == 2 ? v0 : 0.0;
+                const double gc = bc[c] == 2 ? v0 : v1;
                 acc -= a * gc;
                 a = 0.0;
             }
@@ -756,9 +760,22 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
         FGB_CUDA(cudaGetLastError());
         return;
     }
-    if (full_run) {
+    if (full_run)
         FGB_LAUNCH(k_cell_stiffness<<<grid_for(nc_, 128), 128, 0, stream_>>>(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(),
                                                                            q1_gauss_));
+    assemble_q1_rows(full_run, anode_dirichlet);
+}
+
+void FemDevice::assemble_from_ke(bool anode_dirichlet) {
+    FGB_REQUIRE(fs_.order == 1, "element matrices from the caller: Q1 only");
+    anode_dirichlet_ = anode_dirichlet;
+    split_valid_ = false;
+    assemble_q1_rows(true, anode_dirichlet);
+}
+
+void FemDevice::assemble_q1_rows(bool matrix, bool anode_dirichlet) {
+    const int gb = grid_for(n_, kBlock);
+    if (matrix) {
         FGB_LAUNCH(k_assemble_rows<<<gb, kBlock, 0, stream_>>>(n_, rowptr_.get(), col_.get(), r2c_ptr_.get(), r2c_item_.get(),
                                                     cell_dofs_.get(), ke_.get(), kval_.get()));
         FGB_CUDA(cudaGetLastError());
@@ -766,10 +783,10 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
     // Neumann rhs (or zero when the anode is a Dirichlet boundary)
     const double bc = anode_dirichlet ? 0.0 : applied_field_;
     FGB_LAUNCH(k_neumann_rows<<<gb, kBlock, 0, stream_>>>(n_, r2f_ptr_.get(), r2f_item_.get(), top_faces_.get(), dof_xyz_.get(), bc,
-                                               has_extra_ ? rhs_extra_.get() : nullptr, rhs_.get()));
+                                               face_vals_, has_extra_ ? rhs_extra_.get() : nullptr, rhs_.get()));
     FGB_LAUNCH(k_dirichlet_rows<<<gb, kBlock, 0, stream_>>>(n_, rowptr_.get(), col_.get(), kval_.get(), bc_.get(), anode_dirichlet ? 1 : 0,
-                                                 applied_potential_, csr2sell_.get(), sell64_.get(), sell32_.get(),
-                                                 dinv64_.get(), dinv32_.get(), rhs_.get(), x_.get()));
+                                                 applied_potential_, dirichlet_value_, csr2sell_.get(), sell64_.get(),
+                                                 sell32_.get(), dinv64_.get(), dinv32_.get(), rhs_.get(), x_.get()));
     FGB_CUDA(cudaGetLastError());
 }
 

@@ -28,7 +28,10 @@ struct FemStructure {
     std::vector<int64_t> rowptr;      // CSR, columns ascending, diagonal included
     std::vector<int32_t> col;
     std::vector<int32_t> r2c_ptr, r2c_item;  // row -> npc*cell+local, ascending cell
+    int region = 0;                   // kRegionVacuum or kRegionBulk
     std::vector<int32_t> top_faces;   // nfc dofs per top (Neumann/anode) face (Q1: cyclic order)
+    std::vector<int32_t> top_face_cells;  // Q1: cell of each Neumann face
+    std::vector<int8_t> top_face_local;   // Q1: its local face (femocs face numbering)
     std::vector<int32_t> r2f_ptr, r2f_item;  // row -> nfc*face+local
     std::vector<int8_t> bc_kind;      // 0 free, 1 copper (phi=0), 2 top (phi=V0 if anode Dirichlet)
     // SELL-32 layout of the same matrix
@@ -44,7 +47,17 @@ struct FemStructure {
     int64_t nnz() const { return !rowptr.empty() ? rowptr.back() : n_entries; }
 };
 
-FemStructure build_fem_structure(const PreparedMesh& pm);
+// Region of the hex mesh a structure is built on: the vacuum (field solve) or the bulk
+// (current and heat, src/CurrentHeatSolver.cpp)
+enum : int { kRegionVacuum = 0, kRegionBulk = 1 };
+struct RegionCells {
+    std::vector<int32_t> cells;        // hex ids of the region, ascending
+    std::vector<int32_t> node2vertex;  // hex-mesh node -> compact vertex (ascending node order) or -1
+    std::vector<int32_t> vertex2node;
+};
+RegionCells region_cells(const PreparedMesh& pm, int region);
+
+FemStructure build_fem_structure(const PreparedMesh& pm, int region = kRegionVacuum);
 // Q2 structure of the same vacuum hexahedra (see the order-2 notes above)
 FemStructure build_q2_structure(const PreparedMesh& pm);
 // lattice coordinates (a,b,c) of local Q2 node L, and the femocs vertex of a lattice corner

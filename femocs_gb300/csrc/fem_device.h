@@ -107,6 +107,16 @@ public:
     // PoissonSolver::setup + assemble verbs (src/PoissonSolver.cpp:162-210)
     void setup(double applied_field, double applied_potential);   // zeroes the solution
     void assemble(bool full_run, bool anode_dirichlet);
+    // Q1 hooks of the bulk (current/heat) systems: element matrices written by the caller into
+    // d_ke() (64 per cell, row-major), per-face Neumann values (device, one per Neumann face in
+    // the structure's order; null = the applied field), the value of the kind-1 Dirichlet rows
+    double* d_ke() { return ke_.get(); }
+    void assemble_from_ke(bool anode_dirichlet);
+    void set_face_values(const double* d_vals) { face_vals_ = d_vals; }
+    void set_dirichlet_value(double v) { dirichlet_value_ = v; }
+    const int32_t* d_r2c_ptr() const { return r2c_ptr_.get(); }
+    const int32_t* d_r2c_item() const { return r2c_item_.get(); }
+    const double* d_dof_xyz() const { return dof_xyz_.get(); }
     // adds a space-charge contribution rhs[dof] += w * N(point) to the unconstrained rhs
     // before Dirichlet application; values given per dof (already summed)
     void set_space_charge(const double* d_rhs_extra);
@@ -145,6 +155,7 @@ public:
 
 private:
     void spmv64(const double* x, double* y);
+    void assemble_q1_rows(bool matrix, bool anode_dirichlet);
     int solve_plain(const SolveOptions& opt, SolveStats* st);
     int solve_mixed(const SolveOptions& opt, SolveStats* st);
     int solve_amg(const SolveOptions& opt, SolveStats* st);
@@ -189,6 +200,8 @@ private:
     DBuf<double> dinv64_;
     DBuf<float> dinv32_;
     DBuf<double> rhs_, rhs_extra_, x_;
+    const double* face_vals_ = nullptr;
+    double dirichlet_value_ = 0.0;
     bool has_extra_ = false;
     // work vectors
     DBuf<double> r64_, p64_, q64_, z64_;

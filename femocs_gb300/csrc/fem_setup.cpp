@@ -37,20 +37,40 @@ struct BFace {
 
 }  // namespace
 
-FemStructure build_fem_structure(const PreparedMesh& pm) {
+RegionCells region_cells(const PreparedMesh& pm, int region) {
+    if (region == kRegionVacuum) return {pm.vac.cells, pm.vac.node2vertex, pm.vac.vertex2node};
+    FGB_REQUIRE(region == kRegionBulk, "region must be vacuum or bulk");
+    RegionCells rc;
+    rc.node2vertex.assign(pm.hex.n_nodes(), -1);
+    for (int h = 0; h < pm.hex.n_hexs(); ++h)
+        if (pm.hex.hex_marker[h] < 0) {
+            rc.cells.push_back(h);
+            for (int k = 0; k < 8; ++k) rc.node2vertex[pm.hex.hexs[8 * (size_t)h + k]] = -2;
+        }
+    for (int i = 0; i < pm.hex.n_nodes(); ++i)
+        if (rc.node2vertex[i] == -2) {
+            rc.node2vertex[i] = (int32_t)rc.vertex2node.size();
+            rc.vertex2node.push_back(i);
+        }
+    return rc;
+}
+
+FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     FemStructure fs;
-    const int nv = (int)pm.vac.vertex2node.size();
-    const int nc = (int)pm.vac.cells.size();
-    FGB_REQUIRE(nv > 0 && nc > 0, "mesh has no vacuum hexahedra");
+    const RegionCells rcs = region_cells(pm, region);
+    const int nv = (int)rcs.vertex2node.size();
+    const int nc = (int)rcs.cells.size();
+    FGB_REQUIRE(nv > 0 && nc > 0, region == kRegionBulk ? "mesh has no bulk hexahedra" : "mesh has no vacuum hexahedra");
     fs.n_dofs = nv;
     fs.n_cells = nc;
+    fs.region = region;
     const std::vector<double>& X = pm.hex.xyz;
 
     // cells in vertex numbering
     std::vector<int32_t> cv(8 * (size_t)nc);
     for (int c = 0; c < nc; ++c)
         for (int k = 0; k < 8; ++k)
-            cv[8 * (size_t)c + k] = pm.vac.node2vertex[pm.hex.hexs[8 * (size_t)pm.vac.cells[c] + k]];
+            cv[8 * (size_t)c + k] = rcs.node2vertex[pm.hex.hexs[8 * (size_t)rcs.cells[c] + k]];
 
     // vertex -> cells
     std::vector<int32_t> v2c_ptr(nv + 1, 0);
@@ -83,7 +103,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm) {
     double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
     for (int v = 0; v < nv; ++v)
         for (int c = 0; c < 3; ++c) {
-            const double x = X[3 * (size_t)pm.vac.vertex2node[v] + c];
+            const double x = X[3 * (size_t)rcs.vertex2node[v] + c];
             mn[c] = std::min(mn[c], x);
             mx[c] = std::max(mx[c], x);
         }
@@ -92,7 +112,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm) {
         uint64_t code = 0;
         for (int c = 0; c < 3; ++c) {
             const double span = mx[c] > mn[c] ? mx[c] - mn[c] : 1.0;
-            double t = (X[3 * (size_t)pm.vac.vertex2node[v] + c] - mn[c]) / span;
+            double t = (X[3 * (size_t)rcs.vertex2node[v] + c] - mn[c]) / span;
             uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, std::floor(t * 2097151.0)));
             code |= spread3(q) << c;
         }
@@ -113,7 +133,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm) {
     fs.dof2node.resize(nv);
     fs.node2dof.assign(pm.hex.n_nodes(), -1);
     for (int d = 0; d < nv; ++d) {
-        fs.dof2node[d] = pm.vac.vertex2node[dof2v[d]];
+        fs.dof2node[d] = rcs.vertex2node[dof2v[d]];
         fs.node2dof[fs.dof2node[d]] = d;
     }
     fs.cell_dofs.resize(8 * (size_t)nc);
@@ -170,8 +190,12 @@ FemStructure build_fem_structure(const PreparedMesh& pm) {
     }
     faces.clear();
     faces.shrink_to_fit();
-    std::sort(bnd.begin(), bnd.end(), [](const BFace& a, const BFace& b) {
-        return a.cell != b.cell ? a.cell < b.cell : a.face < b.face;
+    // vacuum: (cell, face) order; bulk: the reference's per-face order of the boundary values,
+    // cells ascending and deal.II faces x-, x+, y-, y+, z-, z+ (kHexFace 2, 3, 0, 1, 4, 5)
+    static const int kDealRank[6] = {2, 3, 0, 1, 4, 5};
+    std::sort(bnd.begin(), bnd.end(), [&](const BFace& a, const BFace& b) {
+        if (a.cell != b.cell) return a.cell < b.cell;
+        return region == kRegionBulk ? kDealRank[a.face] < kDealRank[b.face] : a.face < b.face;
     });
     auto dof_x = [&](int32_t d, int c) { return X[3 * (size_t)fs.dof2node[d] + c]; };
     double bmn[3] = {1e16, 1e16, 1e16}, bmx[3] = {-1e16, -1e16, -1e16};
@@ -195,8 +219,14 @@ FemStructure build_fem_structure(const PreparedMesh& pm) {
         if (side) continue;
         int32_t fd[4];
         for (int q = 0; q < 4; ++q) fd[q] = fs.cell_dofs[8 * (size_t)bnd[i].cell + kHexFace[bnd[i].face][q]];
-        if (std::fabs(z - bmx[2]) <= eps) {
+        // vacuum (PoissonSolver::mark_mesh): z max -> top (Neumann), the rest -> copper (phi = 0);
+        // bulk (CurrentHeatSolver::mark_mesh, src/CurrentHeatSolver.cpp:535-539): z min -> copper
+        // bottom (Dirichlet), z max and the rest -> copper surface (Neumann, per-face values)
+        const bool neumann = region == kRegionBulk ? !(std::fabs(z - bmn[2]) <= eps) : std::fabs(z - bmx[2]) <= eps;
+        if (neumann) {
             top.insert(top.end(), fd, fd + 4);
+            fs.top_face_cells.push_back(bnd[i].cell);
+            fs.top_face_local.push_back(bnd[i].face);
         } else {
             for (int q = 0; q < 4; ++q) fs.bc_kind[fd[q]] = 1;
         }

@@ -323,6 +323,40 @@ int fgb_server_reset_run(FGB_SERVER* s, int run); /* server stopped: zero warm s
 int fgb_server_info(FGB_SERVER* s, double* out4);  /* runs, solver launches, max requests in flight, 0 */
 int fgb_server_run_info(FGB_SERVER* s, int run, int64_t* out2); /* slot (-1 pending), n_atoms */
 
+/* ============================ Part 5: current and heat (bulk) ============================
+ * The GPU counterpart of the reference's CurrentHeatSolver (src/CurrentHeatSolver.cpp) on the
+ * bulk (metal) hexahedra of a mesh: Q1, 2x2x2 Gauss, boundary marking of
+ * CurrentHeatSolver::mark_mesh (:535-539: x/y extremes natural, z min = copper bottom, the rest
+ * = copper surface). Surface values are given per copper-surface face, in the order
+ * fgb_heat_surface_faces lists them (the reference's order: bulk cells ascending, deal.II faces
+ * x-, x+, y-, y+, z-, z+). The emission model that produces them is outside this library. */
+typedef struct FGB_HEAT FGB_HEAT;
+FGB_HEAT* fgb_heat_create(const FGB_MESH* m);
+void fgb_heat_free(FGB_HEAT* h);
+int fgb_heat_sizes(FGB_HEAT* h, int64_t* out3); /* n_dofs, nnz, n_surface_faces */
+/* per surface face: centroid (3 doubles) and (hex id, femocs local face 0..5); either may be NULL */
+int fgb_heat_surface_faces(FGB_HEAT* h, double* centroid3, int* hex_face2);
+/* PhysicalQuantities resistivity table (src/PhysicalQuantities.cpp:31-64, 173-184): T ascending;
+ * rho(T) = 10 * linear interpolation, T clamped to the table; sigma = 1/rho,
+ * kappa = lorentz * T * sigma */
+int fgb_heat_set_resistivity(FGB_HEAT* h, int n, const double* T, const double* rho);
+/* CurrentHeatSolver::setup: T = t_ambient (also the bottom value), phi = 0; lorentz number and
+ * volumetric heat capacity rho_cp [J/(K A^3)] (the reference uses 2.44e-8 and 3.4496e-24) */
+int fgb_heat_setup(FGB_HEAT* h, double t_ambient, double lorentz, double rho_cp);
+/* CurrentSolver::assemble + solve (:421-489): Laplace with sigma = 1, Neumann j per surface face,
+ * phi = 0 at the bottom. Returns #iterations (< 0: not converged; INT32_MIN: error); precision
+ * as fgb_field_solve; stats14 as fgb_field_last_stats (may be NULL) */
+int fgb_heat_solve_current(FGB_HEAT* h, const double* face_j, int precision, double rel_tol, int max_iter,
+                           double* stats14);
+/* HeatSolver::assemble(dt) + solve (:116-153, :347-398): implicit Euler with
+ * gamma = rho_cp / dt [s], kappa(T_prev), Joule source sigma(T_prev) |grad phi|^2, heat flux q per
+ * surface face, T = t_ambient at the bottom */
+int fgb_heat_solve_heat(FGB_HEAT* h, double delta_time_s, const double* face_q, int precision, double rel_tol,
+                        int max_iter, double* stats14);
+/* per hex-mesh node (NaN outside the bulk): temperature and current potential; either may be NULL */
+int fgb_heat_export(FGB_HEAT* h, double* T_node, double* phi_node);
+int fgb_heat_temperature_range(FGB_HEAT* h, double* out2); /* HeatSolver::check_limits extremes */
+
 #ifdef __cplusplus
 }
 #endif
