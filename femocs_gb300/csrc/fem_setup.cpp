@@ -1,4 +1,5 @@
-// Host construction of the vacuum FEM structure.
+// Host construction of the Q1 FEM structure of the vacuum (field) or the bulk (current/heat)
+// hexahedra.
 //
 // DoF numbering: the reference lets deal.II number DoFs (DoFHandler::distribute_dofs) and
 // maps them back to mesh vertices (src/DealSolver.cpp:318-341); only the per-vertex
