@@ -283,8 +283,9 @@ class Field:
         return res
 
     def interpolate_surface(self, xyz, rank=1):
-        """Surface (2-D) location + interpolation (rank 1 linear, 2 quadratic): (triangle per
-        point, negative when no triangle holds it; 5 values per point)."""
+        """Surface (2-D) location + interpolation (rank 1 linear, 2 quadratic in the tet, 3
+        trilinear in the hex of the quadrangle): (triangle, or quadrangle for rank 3, per point,
+        negative when no triangle holds it; 5 values per point)."""
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
         n = len(xyz) // 3
         cells = np.zeros(max(n, 1), dtype=np.int32)

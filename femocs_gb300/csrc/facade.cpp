@@ -269,10 +269,6 @@ int FemocsFacade::run(int timestep, double time) {
 int FemocsFacade::interp_points(int n, const double* x, const double* y, const double* z, std::vector<int32_t>& cells,
                                 std::vector<double>& out, bool surface) {
     if (!field_ || !solved_) { set_last_error("no solution to interpolate"); return 1; }
-    if (surface && rank_ == 3) {
-        set_last_error("surface interpolation of rank 3 (quadrangles) is not provided; use interpolation_rank 1 or 2");
-        return 1;
-    }
     std::vector<double> p(3 * (size_t)n);
     for (int i = 0; i < n; ++i) {
         p[3 * (size_t)i] = x[i];

@@ -59,8 +59,10 @@ public:
     // Surface (2-D) location + interpolation on the mesh's surface triangles: the chained
     // triangle search of InterpolatorCells<3>::locate_cell, then the tet reached through the
     // triangle's two tets (LinearTriangles / QuadraticTriangles::interp_solution,
-    // src/InterpolatorCells.cpp:1639-1686, 1834-1856), rank 1 linear or 2 quadratic in that tet.
-    // d_cells: triangle per point (negative = nearest-centroid fallback); d_out: 5 per point.
+    // src/InterpolatorCells.cpp:1639-1686, 1834-1856), rank 1 linear or 2 quadratic in that tet;
+    // rank 3 (LinearQuadrangles, :1922-1993) trilinear in the hex of the point's quadrangle.
+    // d_cells: triangle (ranks 1, 2) or quadrangle (rank 3) per point (negative = nearest-
+    // centroid fallback); d_out: 5 per point.
     void surface_interpolate(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out);
     int n_surface_tris() const { return n_stris_; }
     // Interpolate with cells already known (SolutionReader::calc_interpolation with mapped atoms)
@@ -96,7 +98,7 @@ private:
     // surface triangles: tables, candidate grid (triangles whose acceptance region meets a
     // cell), centroid buckets for the nearest-centroid fallback, per-point scratch
     int n_stris_ = 0;
-    DBuf<int32_t> stri2tet_, snbr_ptr_, snbr_idx_, scand_ptr_, scand_idx_, sgptr_, sgtris_;
+    DBuf<int32_t> stris_, stri2tet_, snbr_ptr_, snbr_idx_, scand_ptr_, scand_idx_, sgptr_, sgtris_;
     DBuf<double> sgeo_, sgcxyz_;
     int scand_dim_[3] = {1, 1, 1}, sg_dim_[3] = {1, 1, 1};
     double scand_org_[3] = {0, 0, 0}, scand_step_[3] = {1, 1, 1}, scand_lo_[3] = {0, 0, 0}, scand_hi_[3] = {0, 0, 0};

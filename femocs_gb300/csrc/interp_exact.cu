@@ -367,6 +367,90 @@ __global__ void k_surface_tet(int n, Pts P, const int32_t* __restrict__ tres, co
     tcell[i] = tet;
 }
 
+// rank 3 (LinearQuadrangles::locate_cell + interp_solution, src/InterpolatorCells.cpp:1922-1993):
+// quadrangle = 3 * triangle + the vertex with the largest barycentric coordinate (sign of the
+// triangle result), then the hexes of the triangle's two tets around that vertex: the first if
+// the point lies on the triangle or in that hex, else LinearHexahedra::locate_cell from the
+// second (tet search from its tet, hex by the largest barycentric coordinate)
+__global__ void k_surface_hex(int n, Pts P, const int32_t* __restrict__ tres, const int32_t* __restrict__ tris,
+                              const int32_t* __restrict__ t2t, const double* __restrict__ geo,
+                              const double* __restrict__ det, const int32_t* __restrict__ tets,
+                              const int32_t* __restrict__ nptr, const int32_t* __restrict__ nidx,
+                              const int32_t* __restrict__ V, const int32_t* __restrict__ F, int32_t* __restrict__ quad_out,
+                              int32_t* __restrict__ hex_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x, y, z;
+    P.get(i, x, y, z);
+    const int tr = tres[i];
+    const int tf = abs(tr);
+    {
+        // LinearTriangles::shape_functions (:1652-1660)
+        const double* g = geo + 19 * (size_t)tf;
+        const double tx = x - g[0], ty = y - g[1], tz = z - g[2];
+        const double qx = ty * g[5] - tz * g[4], qy = tz * g[3] - tx * g[5], qz = tx * g[4] - ty * g[3];
+        const double v = tx * g[9] + ty * g[10] + tz * g[11];
+        const double w = qx * g[12] + qy * g[13] + qz * g[14];
+        const double u = 1.0 - v - w;
+        const double b0 = kZero + u, b1 = kZero + v, b2 = kZero + w;
+        int k = -1;
+        if (b0 >= b1 && b0 >= b2) k = 0;
+        else if (b1 >= b0 && b1 >= b2) k = 1;
+        else if (b2 >= b0 && b2 >= b1) k = 2;
+        quad_out[i] = k < 0 ? -1 : (tr < 0 ? -1 : 1) * (3 * tf + k);
+    }
+    const int q = abs(quad_out[i]), tq = q / 3;
+    const int vert = tris[3 * (size_t)tq + q % 3];
+    int hx[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int t = t2t[2 * (size_t)tq + r];
+        int loc = 0;
+        while (loc < 4 && tets[4 * (size_t)t + loc] != vert) ++loc;
+        hx[r] = 4 * t + (loc < 4 ? loc : 0);
+    }
+    int hex;
+    bool in0 = fabs(tri_fast_distance(geo, tq, x, y, z)) <= 100.0 * kZero;
+    if (!in0) {
+        // LinearHexahedra::point_in_cell (:1507-1528)
+        double b[4];
+        bcc4(det, hx[0] / 4, x, y, z, b);
+        if (b[0] >= 0 && b[1] >= 0 && b[2] >= 0 && b[3] >= 0) {
+            const int s = hx[0] % 4;
+            in0 = true;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j != s && !(b[s] >= b[j])) in0 = false;
+        }
+    }
+    if (in0) {
+        hex = hx[0];
+    } else {
+        const int t1 = hx[1] / 4;
+        int tet;
+        if (pic(det, t1, x, y, z)) {
+            tet = t1;
+        } else {
+            tet = INT_MIN;
+            for (int k = nptr[t1]; k < nptr[t1 + 1]; ++k) {
+                const int u = nidx[k];
+                if (pic(det, u, x, y, z)) { tet = u; break; }
+            }
+            if (tet == INT_MIN) tet = V[i] >= 0 ? V[i] : -F[i];
+        }
+        const int sign = tet < 0 ? -1 : 1;
+        const int t = abs(tet);
+        double b[4];
+        bcc4(det, t, x, y, z, b);
+        hex = -1;
+        if (b[0] >= b[1] && b[0] >= b[2] && b[0] >= b[3]) hex = sign * (4 * t + 0);
+        else if (b[1] >= b[0] && b[1] >= b[2] && b[1] >= b[3]) hex = sign * (4 * t + 1);
+        else if (b[2] >= b[0] && b[2] >= b[1] && b[2] >= b[3]) hex = sign * (4 * t + 2);
+        else if (b[3] >= b[0] && b[3] >= b[1] && b[3] >= b[2]) hex = sign * (4 * t + 3);
+    }
+    hex_out[i] = hex;
+}
+
 __device__ __forceinline__ void acc5(const double* __restrict__ sol, int node, double w, double* a) {
     const double* s = sol + 5 * (size_t)node;
 #pragma unroll
@@ -887,6 +971,7 @@ void DeviceMesh::set_surface(const PreparedMesh& pm) {
             for (int c = 0; c < 3; ++c) gc[3 * (size_t)q + c] = st.geo[(size_t)kTriGeoStride * f + 16 + c];
         }
     }
+    stris_.upload(st.tris, s);
     stri2tet_.upload(st.tri2tet, s);
     snbr_ptr_.upload(st.nbr_ptr, s);
     snbr_idx_.upload(st.nbr_idx.empty() ? std::vector<int32_t>(1, 0) : st.nbr_idx, s);
@@ -902,7 +987,7 @@ void DeviceMesh::set_surface(const PreparedMesh& pm) {
 
 void DeviceMesh::surface_interpolate(int n, const double* d_pts, int rank, int32_t* d_cells, double* d_out) {
     if (n <= 0) return;
-    FGB_REQUIRE(rank == 1 || rank == 2, "surface interpolation rank must be 1 or 2");
+    FGB_REQUIRE(rank >= 1 && rank <= 3, "surface interpolation rank must be 1, 2 or 3");
     FGB_REQUIRE(n_stris_ > 0, "the mesh has no surface triangles");
     ensure_scratch(n);
     if (s_scratch_n_ < n) {
@@ -937,17 +1022,28 @@ void DeviceMesh::surface_interpolate(int n, const double* d_pts, int rank, int32
                                                                     s_tv_.get(), s_tf_.get(), s_counters_.get()));
     FGB_LAUNCH(k_resolve<<<grid_for(n, B), B, 0, stream_>>>(n, s_tv_.get(), s_nin_.get(), s_tf_.get(), s_res_.get(),
                                                             s_dep_.get(), s_counters_.get()));
-    FGB_LAUNCH(k_tri_chain_runs<<<grid_for(n, B), B, 0, stream_>>>(n, P, 1, n_stris_, sgeo_.get(), snbr_ptr_.get(),
-                                                                   snbr_idx_.get(), s_tv_.get(), s_tf_.get(), s_dep_.get(),
-                                                                   s_res_.get(), s_counters_.get()));
-    FGB_LAUNCH(k_surface_tet<<<grid_for(n, B), B, 0, stream_>>>(n, P, s_res_.get(), stri2tet_.get(), sgeo_.get(), det_.get(),
-                                                                nbr_ptr_.get(), nbr_idx_.get(), v_.get(), f_.get(),
-                                                                res_.get()));
+    // rank 3 keeps quadrangle cells: its first guess is quadrangle 1's triangle, 0
+    FGB_LAUNCH(k_tri_chain_runs<<<grid_for(n, B), B, 0, stream_>>>(n, P, rank == 3 ? 0 : 1, n_stris_, sgeo_.get(),
+                                                                   snbr_ptr_.get(), snbr_idx_.get(), s_tv_.get(),
+                                                                   s_tf_.get(), s_dep_.get(), s_res_.get(),
+                                                                   s_counters_.get()));
+    if (rank == 3) {
+        FGB_LAUNCH(k_surface_hex<<<grid_for(n, B), B, 0, stream_>>>(n, P, s_res_.get(), stris_.get(), stri2tet_.get(),
+                                                                    sgeo_.get(), det_.get(), tet_nodes_.get(),
+                                                                    nbr_ptr_.get(), nbr_idx_.get(), v_.get(), f_.get(),
+                                                                    s_tv_.get(), res_.get()));
+    } else {
+        FGB_LAUNCH(k_surface_tet<<<grid_for(n, B), B, 0, stream_>>>(n, P, s_res_.get(), stri2tet_.get(), sgeo_.get(),
+                                                                    det_.get(), nbr_ptr_.get(), nbr_idx_.get(), v_.get(),
+                                                                    f_.get(), res_.get()));
+    }
     FGB_LAUNCH(k_interpolate<<<grid_for(n, 128), 128, 0, stream_>>>(n, P, rank, 0, res_.get(), det_.get(), tet_nodes_.get(),
                                                                     quad_.get(), hexs_.get(), hexf_.get(), sol_.get(),
                                                                     nullptr, d_out));
+    // cells: triangles (ranks 1, 2) or quadrangles (rank 3, computed into s_tv_)
     if (d_cells)
-        FGB_CUDA(cudaMemcpyAsync(d_cells, s_res_.get(), sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, stream_));
+        FGB_CUDA(cudaMemcpyAsync(d_cells, rank == 3 ? s_tv_.get() : s_res_.get(), sizeof(int32_t) * n,
+                                 cudaMemcpyDeviceToDevice, stream_));
     FGB_CUDA(cudaGetLastError());
 }
 

@@ -196,9 +196,10 @@ int fgb_field_interpolate(FGB_FIELD* f, int n, const double* xyz, int rank, int*
 /* same with device pointers (no copies) */
 int fgb_field_interpolate_device(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells, double* d_out5);
 /* surface (2-D) location + interpolation on the mesh's surface triangles (LinearTriangles rank 1,
- * QuadraticTriangles rank 2: src/InterpolatorCells.cpp:1639-1686, 1834-1856, driven as
- * SolutionReader::calc_full_interpolation with dim = 2, src/SolutionReader.cpp:43-55);
- * cells = triangle per point (negative: no triangle holds the point, nearest centroid) */
+ * QuadraticTriangles rank 2, LinearQuadrangles rank 3: src/InterpolatorCells.cpp:1639-1686,
+ * 1834-1856, 1922-1993, driven as SolutionReader::calc_full_interpolation with dim = 2,
+ * src/SolutionReader.cpp:43-55); cells = triangle (ranks 1, 2) or quadrangle 3*tri+vertex
+ * (rank 3) per point (negative: no triangle holds the point, nearest centroid) */
 int fgb_field_interpolate_surface(FGB_FIELD* f, int n, const double* xyz, int rank, int* cells, double* out5);
 int fgb_field_interpolate_surface_device(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells,
                                          double* d_out5);

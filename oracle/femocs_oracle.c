@@ -678,6 +678,27 @@ static double tri_fast_distance(const TriRow* r, const double* p) {
     return vdot(r->e2, q);
 }
 
+/* LinearTriangles::shape_functions, :1652-1660 */
+static void tri_shape(const TriRow* r, const double* p, double* b) {
+    const V3 pt = {p[0], p[1], p[2]};
+    const V3 tv = vsub(pt, r->v0);
+    const V3 q = vcross(tv, r->e1d);
+    const double v = vdot(tv, r->pvd);
+    const double w = vdot(q, r->n);
+    const double u = 1.0 - v - w;
+    b[0] = ZERO + u; b[1] = ZERO + v; b[2] = ZERO + w;
+}
+/* LinearHexahedra::point_in_cell, :1507-1528 */
+static int hex_pic(const OrcInterp* m, const double* p, int hex) {
+    double b[4];
+    bcc(m, p, hex / 4, b);
+    if (!(b[0] >= 0 && b[1] >= 0 && b[2] >= 0 && b[3] >= 0)) return 0;
+    const int k = hex % 4;
+    for (int j = 0; j < 4; ++j)
+        if (j != k && !(b[k] >= b[j])) return 0;
+    return 1;
+}
+
 void orc_surface_interpolate(const OrcInterp* m, const OrcSurface* s, int rank, int n_pts, const double* pts,
                              int32_t* cells, double* out) {
     const int nf = s->n_tris;
@@ -696,8 +717,10 @@ void orc_surface_interpolate(const OrcInterp* m, const OrcSurface* s, int rank, 
     int cell = -1;
     for (int i = 0; i < n_pts; ++i) {
         const double* p = pts + 3 * (size_t)i;
-        /* InterpolatorCells<3>::locate_cell (src/InterpolatorCells.cpp:269-307), guess abs(cell) */
-        const int guess = abs(cell);
+        /* InterpolatorCells<3>::locate_cell (src/InterpolatorCells.cpp:269-307), guess abs(cell);
+         * rank 3 keeps quadrangle cells and guesses their triangle (LinearQuadrangles::locate_cell,
+         * :1969-1993, quads->to_tri = quad / 3) */
+        const int guess = rank == 3 ? abs(cell) / 3 : abs(cell);
         int found = INT_MIN;
         if (guess < nf) {
             if (tri_pic(rows + guess, p)) found = guess;
@@ -719,6 +742,38 @@ void orc_surface_interpolate(const OrcInterp* m, const OrcSurface* s, int rank, 
                 if (d2 < best) { best = d2; best_i = f; }
             }
             if (found == INT_MIN) found = -best_i;
+        }
+        if (rank == 3) {
+            const int sign = found < 0 ? -1 : 1;
+            const int tf = abs(found);
+            double b[3];
+            tri_shape(rows + tf, p, b);
+            int k = -1;
+            if (b[0] >= b[1] && b[0] >= b[2]) k = 0;
+            else if (b[1] >= b[0] && b[1] >= b[2]) k = 1;
+            else if (b[2] >= b[0] && b[2] >= b[1]) k = 2;
+            cell = k < 0 ? -1 : sign * (3 * tf + k);
+            cells[i] = cell;
+            /* LinearQuadrangles::interp_solution (:1922-1940): the quadrangle's hexes are the
+             * hexes of the triangle's two tets around the quadrangle's triangle vertex
+             * (TetgenMesh::calc_quad2hex2quad_mapping, src/TetgenMesh.cpp:614-645) */
+            const int q = abs(cell), tq = q / 3;
+            const int v = s->tris[3 * (size_t)tq + q % 3];
+            int hx[2];
+            for (int r = 0; r < 2; ++r) {
+                const int t = s->tri2tet[2 * (size_t)tq + r];
+                int loc = 0;
+                while (loc < 4 && m->tets[4 * (size_t)t + loc] != v) ++loc;
+                hx[r] = 4 * t + (loc < 4 ? loc : 0);
+            }
+            int hex;
+            if (fabs(tri_fast_distance(rows + tq, p)) <= 100.0 * ZERO) hex = hx[0];
+            else if (hex_pic(m, p, hx[0])) hex = hx[0];
+            else hex = hex_locate(m, p, hx[1]);
+            double w8[8];
+            hex_weights(m, p, abs(hex), w8);
+            weighted(m, m->hexs + 8 * (size_t)abs(hex), w8, 8, out + 5 * (size_t)i);
+            continue;
         }
         cell = found;
         cells[i] = cell;

@@ -93,7 +93,9 @@ void orc_locate_interpolate(const OrcInterp* m, int rank, int n_pts, const doubl
  * src/TetgenCells.cpp:387-412, and LinearTriangles::precompute), the chained triangle
  * location of a fresh reader (src/SolutionReader.cpp:43-55, 136-165) and the tet chosen
  * through the triangle's two tets. rank 1 interpolates linearly, rank 2 quadratically in
- * that tet. cells: triangle per point (negative = nearest-centroid fallback). */
+ * that tet; rank 3 (LinearQuadrangles, :1922-1993) works on the three quadrangles of each
+ * triangle and interpolates trilinearly in the hex of the quadrangle. cells: triangle (ranks
+ * 1, 2) or quadrangle 3*triangle+vertex (rank 3) per point (negative = nearest-centroid fallback). */
 typedef struct {
     int n_tris;
     const int32_t* tris;     /* 3 node ids per triangle */

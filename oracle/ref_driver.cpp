@@ -186,10 +186,13 @@ int main(int argc, char** argv) {
     if (n_tris > 0) {
         LinearTriangles lintri(&nodes, &lintet);
         QuadraticTriangles quadtri(&nodes, &lintri, &quadtet);
+        LinearQuadrangles linquad(&nodes, &lintri, &linhex);
         lintri.set_mesh(&mesh);
         quadtri.set_mesh(&mesh);
+        linquad.set_mesh(&mesh);
         lintri.precompute();
         quadtri.precompute();
+        linquad.precompute();
         std::vector<int32_t> tv(3 * (size_t)n_tris), t2t(2 * (size_t)n_tris);
         std::vector<double> tn(3 * (size_t)n_tris);
         for (int f = 0; f < n_tris; ++f) {
@@ -204,13 +207,14 @@ int main(int argc, char** argv) {
         put(fo, "tri_nodes", 'i', tv.size(), tv.data());
         put(fo, "tri2tet", 'i', t2t.size(), t2t.data());
         put(fo, "tri_norm", 'd', tn.size(), tn.data());
-        for (int rank = 1; rank <= 2; ++rank) {
+        for (int rank = 1; rank <= 3; ++rank) {
             std::vector<int32_t> cells(n_pts);
             std::vector<double> sol(5 * (size_t)n_pts);
             int cell = -1;
             for (int i = 0; i < n_pts; ++i) {
                 Point3 p(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
-                Solution s = rank == 1 ? lintri.locate_interpolate(p, cell) : quadtri.locate_interpolate(p, cell);
+                Solution s = rank == 1 ? lintri.locate_interpolate(p, cell)
+                             : rank == 2 ? quadtri.locate_interpolate(p, cell) : linquad.locate_interpolate(p, cell);
                 cells[i] = cell;
                 sol[5 * i] = s.vector.x; sol[5 * i + 1] = s.vector.y; sol[5 * i + 2] = s.vector.z;
                 sol[5 * i + 3] = s.scalar1; sol[5 * i + 4] = s.scalar2;

@@ -124,7 +124,7 @@ def surface_points(mesh: fg.Mesh, spec: dict, seed: int) -> np.ndarray:
 
 def make_surface_case(name: str, spec: dict, seed: int) -> dict:
     """The reference reads the mesh together with its vacuum/metal surface triangles (TetGen
-    recomputes their tet pairs) and interpolates on the surface for ranks 1 and 2."""
+    recomputes their tet pairs) and interpolates on the surface for ranks 1-3."""
     mesh = fg.Mesh.synthetic(**spec)
     s = mesh.sizes()
     tris, t2t, _ = mesh.surface()
@@ -143,7 +143,7 @@ def make_surface_case(name: str, spec: dict, seed: int) -> dict:
         pts=pts, tri_nodes=r["tri_nodes"].reshape(-1, 3), tri2tet=r["tri2tet"].reshape(-1, 2),
         tri_norm=r["tri_norm"].reshape(-1, 3),
     )
-    for rank in (1, 2):
+    for rank in (1, 2, 3):
         g[f"cells_s{rank}"] = r[f"cells_s{rank}"]
         g[f"interp_s{rank}"] = r[f"interp_s{rank}"].reshape(-1, 5)
     return g

@@ -94,7 +94,7 @@ def test_surface_fixture_matches_product_surface(name):
 
 
 @pytest.mark.parametrize("name", surface_cases())
-@pytest.mark.parametrize("rank", [1, 2])
+@pytest.mark.parametrize("rank", [1, 2, 3])
 def test_oracle_surface_interpolation_bit_exact(name, rank):
     g = load_surface(name)
     m = fg.Mesh.synthetic(**g["spec_kw"])

@@ -1,6 +1,6 @@
 """Surface (2-D) location and interpolation on the GPU: against the reference's golden vectors
-(LinearTriangles / QuadraticTriangles with TetGen's triangle/tet pairs, bit-exact cells and
-values) and against the oracle's restatement on larger point sets."""
+(LinearTriangles / QuadraticTriangles / LinearQuadrangles with TetGen's triangle/tet pairs,
+bit-exact cells and values) and against the oracle's restatement on larger point sets."""
 import numpy as np
 import pytest
 
@@ -21,7 +21,7 @@ def case(request):
     return g, m, f
 
 
-@pytest.mark.parametrize("rank", [1, 2])
+@pytest.mark.parametrize("rank", [1, 2, 3])
 def test_gpu_surface_interpolation_matches_reference_bit_exact(case, rank):
     g, m, f = case
     cells, out = f.interpolate_surface(g["pts"], rank=rank)
@@ -31,7 +31,7 @@ def test_gpu_surface_interpolation_matches_reference_bit_exact(case, rank):
     assert (cells < 0).any() and (cells > 0).any()
 
 
-@pytest.mark.parametrize("rank", [1, 2])
+@pytest.mark.parametrize("rank", [1, 2, 3])
 def test_gpu_surface_large_point_sets_match_oracle(rank):
     m = fg.Mesh.synthetic(**fg.CONFIG1)
     f = fg.Field(m)
