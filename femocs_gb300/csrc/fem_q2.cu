@@ -2,9 +2,12 @@
 //
 //   k_q2_cell_stiffness  K_e[i][j] = sum_q w_q |det J_q| grad N_i . grad N_j over 3x3x3 Gauss
 //                        points on the trilinear (Q1) map of the hex, one warp per cell: lanes
-//                        0..26 own the quadrature points for the Jacobians and the nodes for
-//                        the physical gradients, every lane accumulates 11-12 of the 378
-//                        upper-triangle entries (FP64: ~31k FMA per cell, the FP64 pipe bounds it)
+//                        0..26 own the quadrature points for the Jacobians (FP64) and the nodes
+//                        for the physical gradients, every lane accumulates 11-12 of the 378
+//                        upper-triangle entries. Gradients and the ~31k products per cell are
+//                        carried as FP32 hi/lo pairs with error-free products (FMA split) and
+//                        sums (Knuth's TwoSum): ~2^-48 relative per operation, run on the FP32
+//                        pipe (GB300's FP64 rate is 1/64 of FP32)
 //   k_q2_assemble_rows   row-owned gather of the element matrices into the saved SELL-layout
 //                        matrix, one warp per row: the row's columns in shared memory, one
 //                        cell at a time, lanes 0..26 place the cell's 27 contributions by binary
@@ -85,18 +88,50 @@ __device__ __forceinline__ int sym27(int i, int j) {
     return i * 27 - (i * (i - 1)) / 2 + (j - i);
 }
 
+// ---- FP32 hi/lo pairs (value = hi + lo, |lo| <= ulp(hi)/2); explicit _rn intrinsics so that
+// no product or sum is ever contracted or reassociated
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF df_of(double x) {
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ DF df_norm(float s, float e) {  // Fast2Sum, |s| >= |e|
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);  // exact rounding error of the leading product
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return df_norm(p, e);
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    return df_norm(s, e);
+}
+
 __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, const int32_t* __restrict__ cd,
                                                                      const double* __restrict__ dxyz,
                                                                      double* __restrict__ ke) {
     __shared__ double sX[kQ2Warps][8][3];
-    __shared__ double sInv[kQ2Warps][27][10];  // J^-1 (row major) and w |det J| per point
-    __shared__ double sG[kQ2Warps][27][3];
-    __shared__ double sGw[kQ2Warps][27][3];  // w |det J| times the gradients
+    __shared__ DF sInv[kQ2Warps][27][10];  // J^-1 (row major) and w |det J| per point
+    __shared__ DF sG[kQ2Warps][27][3];
+    __shared__ DF sGw[kQ2Warps][27][3];    // w |det J| times the gradients
     // shape-gradient tables in shared memory: lanes read them at different addresses, which
     // the constant cache would serialise
-    __shared__ double sDN[27 * 27 * 3];
+    __shared__ DF sDN[27 * 27 * 3];
     __shared__ double sD1[27 * 8 * 3];
-    for (int i = threadIdx.x; i < 27 * 27 * 3; i += blockDim.x) sDN[i] = c_q2_dN[i];
+    for (int i = threadIdx.x; i < 27 * 27 * 3; i += blockDim.x) sDN[i] = df_of(c_q2_dN[i]);
     for (int i = threadIdx.x; i < 27 * 8 * 3; i += blockDim.x) sD1[i] = c_q1_dN[i];
     __syncthreads();
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -119,24 +154,24 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
         const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
         const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
         const double id = 1.0 / det;
-        double* o = sInv[wid][lane];
-        o[0] = c00 * id;
-        o[3] = c01 * id;
-        o[6] = c02 * id;
-        o[1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-        o[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-        o[7] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-        o[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-        o[5] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-        o[8] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-        o[9] = c_q2_w[lane] * fabs(det);
+        DF* o = sInv[wid][lane];
+        o[0] = df_of(c00 * id);
+        o[3] = df_of(c01 * id);
+        o[6] = df_of(c02 * id);
+        o[1] = df_of((J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id);
+        o[4] = df_of((J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id);
+        o[7] = df_of((J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id);
+        o[2] = df_of((J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id);
+        o[5] = df_of((J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id);
+        o[8] = df_of((J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id);
+        o[9] = df_of(c_q2_w[lane] * fabs(det));
     }
-    double acc[12];
+    DF acc[12];
     int ei[12], ej[12];  // this lane's packed entries e = lane + 32 t, held in registers (a
                          // table read per entry would diverge across the warp)
 #pragma unroll
     for (int t = 0; t < 12; ++t) {
-        acc[t] = 0.0;
+        acc[t] = {0.0f, 0.0f};
         const int e = min(lane + 32 * t, 377);
         ei[t] = c_q2_ij[2 * e];
         ej[t] = c_q2_ij[2 * e + 1];
@@ -144,30 +179,32 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
     for (int q = 0; q < 27; ++q) {
         __syncwarp();
         if (lane < 27) {
-            const double* inv = sInv[wid][q];
-            const double* g = sDN + (q * 27 + lane) * 3;
+            const DF* inv = sInv[wid][q];
+            const DF* g = sDN + (q * 27 + lane) * 3;
             // physical gradient: (J^-T g)_a = sum_k inv[k][a] g_k; the weight folded into one copy
-            const double w = inv[9];
+            const DF w = inv[9];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                const double ga = inv[a] * g[0] + inv[3 + a] * g[1] + inv[6 + a] * g[2];
+                const DF ga = df_add(df_add(df_mul(inv[a], g[0]), df_mul(inv[3 + a], g[1])), df_mul(inv[6 + a], g[2]));
                 sG[wid][lane][a] = ga;
-                sGw[wid][lane][a] = w * ga;
+                sGw[wid][lane][a] = df_mul(w, ga);
             }
         }
         __syncwarp();
 #pragma unroll
         for (int t = 0; t < 12; ++t) {
-            const double* gi = sGw[wid][ei[t]];
-            const double* gj = sG[wid][ej[t]];
-            acc[t] += gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2];
+            const DF* gi = sGw[wid][ei[t]];
+            const DF* gj = sG[wid][ej[t]];
+            acc[t] = df_add(acc[t], df_mul(gi[0], gj[0]));
+            acc[t] = df_add(acc[t], df_mul(gi[1], gj[1]));
+            acc[t] = df_add(acc[t], df_mul(gi[2], gj[2]));
         }
     }
     double* o = ke + 378 * (size_t)c;
 #pragma unroll
     for (int t = 0; t < 12; ++t) {
         const int e = lane + 32 * t;
-        if (e < 378) o[e] = acc[t];
+        if (e < 378) o[e] = (double)acc[t].h + (double)acc[t].l;
     }
 }
 
