@@ -79,6 +79,8 @@ _PROTOS = {
     "fgb_field_clear_space_charge": (C.c_int, [vp]),
     "fgb_device_sync": (C.c_int, []),
     "fgb_mesh_q2_sizes": (C.c_int, [vp, i64p]),
+    "fgb_mesh_q1_sizes": (C.c_int, [vp, i64p]),
+    "fgb_mesh_structure_digest": (C.c_uint64, [vp, C.c_int, C.c_int]),
     "fgb_field_free": (None, [vp]),
     "fgb_field_sizes": (C.c_int, [vp, i64p]),
     "fgb_field_setup": (C.c_int, [vp, C.c_double, C.c_double]),

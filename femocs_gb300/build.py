@@ -72,7 +72,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         src = os.path.join(CSRC, f)
         obj = os.path.join(OUT, f[:-3] + ".o")
         extra = ["-fmad=false"] if f.endswith("_exact.cu") else []
-        cmd = [nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+        cmd = [nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp",
                "-Xptxas", "-warn-spills", *extra, *inc, "-c", src, "-o", obj]
         jobs.append((cmd, src, obj))
     with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:

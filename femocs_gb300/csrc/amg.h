@@ -44,6 +44,7 @@ struct AmgOptions {
     int max_coarse = 1500;   // dense solve below this size
     int max_dense = 4096;    // largest dense coarsest level accepted
     int max_levels = 10;
+    double level0_lambda = 0.0;  // > 0: lambda_max of D^-1 A on level 0, already estimated (device)
 };
 
 // fixed: 1 for Dirichlet rows (copper, and the anode when it is a Dirichlet boundary)

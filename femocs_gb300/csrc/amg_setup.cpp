@@ -295,7 +295,7 @@ AmgHost build_amg(const PreparedMesh& pm, const FemStructure& fs, const std::vec
     l0.P = P0;
     l0.R = transpose(P0);
     phase("geometric prolongation", n1);
-    l0.lambda = lambda_max(A0);
+    l0.lambda = opt.level0_lambda > 0 ? opt.level0_lambda : lambda_max(A0);
     phase("lambda_max level 0", n0);
     CsrD A1 = rap(l0.R, A0, l0.P);
     phase("Galerkin product level 1", n1);

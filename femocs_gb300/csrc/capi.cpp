@@ -81,6 +81,15 @@ NanotipSpec to_spec(const FgbNanotip* s) {
 }
 }  // namespace
 
+namespace {
+template <typename T>
+void fnv(uint64_t& h, const std::vector<T>& v) {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(v.data());
+    for (size_t i = 0; i < v.size() * sizeof(T); ++i) h = (h ^ p[i]) * 1099511628211ull;
+    h = (h ^ v.size()) * 1099511628211ull;
+}
+}  // namespace
+
 extern "C" {
 
 const char* femocs_last_error(void) { return last_error(); }
@@ -595,6 +604,30 @@ int fgb_field_q2_dofs(FGB_FIELD* f, int* dof_cell, int* dof_local) {
             if (dof_cell) dof_cell[d] = s.dof_cell[d];
             if (dof_local) dof_local[d] = s.dof_local[d];
         }
+        return 0;
+    });
+}
+uint64_t fgb_mesh_structure_digest(const FGB_MESH* m, int order, int region) {
+    uint64_t h = 1469598103934665603ull;
+    guarded([&] {
+        const FemStructure s = order == 2 ? build_q2_structure(*m->pm) : build_fem_structure(*m->pm, region);
+        fnv(h, s.dof2node); fnv(h, s.node2dof); fnv(h, s.cell_dofs); fnv(h, s.rowptr); fnv(h, s.col);
+        fnv(h, s.r2c_ptr); fnv(h, s.r2c_item); fnv(h, s.top_faces); fnv(h, s.r2f_ptr); fnv(h, s.r2f_item);
+        fnv(h, s.bc_kind); fnv(h, s.slice_ptr); fnv(h, s.slice_len); fnv(h, s.csr2sell); fnv(h, s.sell_col);
+        fnv(h, s.row_len); fnv(h, s.dof_xyz); fnv(h, s.dof_cell); fnv(h, s.dof_local);
+        return 0;
+    });
+    return h;
+}
+int fgb_mesh_q1_sizes(const FGB_MESH* m, int64_t* out4) {
+    return guarded([&] {
+        FemStructure s = build_fem_structure(*m->pm);
+        int mx = 0;
+        for (int v : s.row_len) mx = std::max(mx, v);
+        out4[0] = s.n_dofs;
+        out4[1] = s.nnz();
+        out4[2] = s.n_top_faces();
+        out4[3] = mx;
         return 0;
     });
 }

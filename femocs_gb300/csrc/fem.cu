@@ -16,6 +16,7 @@
 //                      the refinement update and the boundary values stay FP64
 #include <algorithm>
 #include <chrono>
+#include <omp.h>
 #include <cstdlib>
 #include <cmath>
 
@@ -643,7 +644,18 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
     }
     slice_ptr_.upload(fs_.slice_ptr, s);
     slice_len_.upload(fs_.slice_len, s);
-    sell_col_.upload(fs_.sell_col, s);
+    if (fs_.order == 2 && fs_.sell_col.empty()) {
+        // Q2 columns built on the device from the cells of each row
+        int max_cells = 0;
+        for (int d = 0; d < n_; ++d) max_cells = std::max(max_cells, fs_.r2c_ptr[d + 1] - fs_.r2c_ptr[d]);
+        sell_col_.resize(fs_.slice_ptr.back());
+        const int bad = q2_sell_columns(n_, (int)fs_.slice_len.size(), slice_ptr_.get(), slice_len_.get(),
+                                        row_len_.get(), r2c_ptr_.get(), r2c_item_.get(), cell_dofs_.get(), max_cells,
+                                        sell_col_.get(), s);
+        FGB_REQUIRE(bad == 0, "Q2 structure: device column count differs from the row length");
+    } else {
+        sell_col_.upload(fs_.sell_col, s);
+    }
     bc_.upload(fs_.bc_kind, s);
     if (fs_.order == 1) {
         std::vector<double> dxyz(3 * (size_t)n_);
@@ -991,7 +1003,9 @@ void FemDevice::ensure_amg(SolveStats* st) {
     download_matrix(vals, rhs);
     std::vector<int8_t> fixed(n_, 0);
     for (int d = 0; d < n_; ++d) fixed[d] = fs_.bc_kind[d] == 1 || (anode && fs_.bc_kind[d] == 2);
-    AmgHost h = build_amg(*pm_, fs_, vals, fixed);
+    AmgOptions ao;
+    ao.level0_lambda = estimate_lambda(15, kAmgLambdaSeed);  // the host estimate's start vector
+    AmgHost h = build_amg(*pm_, fs_, vals, fixed, ao);
     h.levels[0].cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 4;
     h.levels[0].cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.04;
     amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
@@ -1001,10 +1015,10 @@ void FemDevice::ensure_amg(SolveStats* st) {
     if (st) st->setup_ms = h.setup_ms;
 }
 
-double FemDevice::estimate_lambda(int iters) {
+double FemDevice::estimate_lambda(int iters, uint64_t seed) {
     // power iteration on D^-1 A from a fixed pseudo-random start, FP64 on the device
     std::vector<double> h(n_);
-    uint64_t sd = 0x9e3779b97f4a7c15ull;
+    uint64_t sd = seed;
     double nx = 0.0;
     for (int i = 0; i < n_; ++i) {
         sd = sd * 6364136223846793005ull + 1442695040888963407ull;
@@ -1034,6 +1048,7 @@ double FemDevice::estimate_lambda(int iters) {
 
 void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     const auto t0 = std::chrono::steady_clock::now();
+    SetupPhases phase("q2 multigrid");
     // coarse operator: the Q1 system of the same mesh and boundary conditions (the Q2 space
     // contains the Q1 space, P below is that embedding, so P^T A2 P equals the Q1 matrix up
     // to the quadrature), with the Q1 hierarchy underneath
@@ -1041,14 +1056,19 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
         q1_.reset(new FemDevice(*pm_, build_fem_structure(*pm_), stream_));
         q1_->q1_gauss_ = 3;
     }
+    phase("Q1 structure + upload");
     q1_->setup(applied_field_, applied_potential_);
     q1_->assemble(true, anode != 0);
     std::vector<double> v1, r1;
     q1_->download_matrix(v1, r1);
+    phase("Q1 assembly + download");
     const FemStructure& f1 = q1_->structure();
     std::vector<int8_t> fixed1(f1.n_dofs, 0);
     for (int d = 0; d < f1.n_dofs; ++d) fixed1[d] = f1.bc_kind[d] == 1 || (anode && f1.bc_kind[d] == 2);
-    AmgHost h1 = build_amg(*pm_, f1, v1, fixed1);
+    AmgOptions ao1;
+    ao1.level0_lambda = q1_->estimate_lambda(15, kAmgLambdaSeed);
+    AmgHost h1 = build_amg(*pm_, f1, v1, fixed1, ao1);
+    phase("Q1 hierarchy (host)");
     // the Q1 level is the coarse solve of the Q2 level: smooth it harder
     h1.levels[0].cheb_degree = 4;
     h1.levels[0].cheb_lo = 0.04;
@@ -1059,22 +1079,34 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     P.n_rows = n_;
     P.n_cols = f1.n_dofs;
     P.ptr.assign(n_ + 1, 0);
-    for (int d = 0; d < n_; ++d) {
+    // two passes (count, fill) over the rows in parallel; the row order fixes the layout
+    auto embed_row = [&](int d, int32_t* col, double* val) {
         const bool fixed = fs_.bc_kind[d] == 1 || (anode && fs_.bc_kind[d] == 2);
-        if (!fixed) {
-            int cr[8];
-            const int nk = q2_entity_corners(fs_.dof_local[d], cr);
-            const int hex = pm_->vac.cells[fs_.dof_cell[d]];
-            for (int q = 0; q < nk; ++q) {
-                const int v = f1.node2dof[pm_->hex.hexs[8 * (size_t)hex + cr[q]]];
-                if (v >= 0 && !fixed1[v]) {
-                    P.col.push_back(v);
-                    P.val.push_back(1.0 / nk);
+        if (fixed) return 0;
+        int cr[8];
+        const int nk = q2_entity_corners(fs_.dof_local[d], cr);
+        const int hex = pm_->vac.cells[fs_.dof_cell[d]];
+        int m = 0;
+        for (int q = 0; q < nk; ++q) {
+            const int v = f1.node2dof[pm_->hex.hexs[8 * (size_t)hex + cr[q]]];
+            if (v >= 0 && !fixed1[v]) {
+                if (col) {
+                    col[m] = v;
+                    val[m] = 1.0 / nk;
                 }
+                ++m;
             }
         }
-        P.ptr[d + 1] = (int64_t)P.col.size();
-    }
+        return m;
+    };
+#pragma omp parallel for schedule(static)
+    for (int d = 0; d < n_; ++d) P.ptr[d + 1] = embed_row(d, nullptr, nullptr);
+    for (int d = 0; d < n_; ++d) P.ptr[d + 1] += P.ptr[d];
+    P.col.resize(P.ptr[n_]);
+    P.val.resize(P.ptr[n_]);
+#pragma omp parallel for schedule(static)
+    for (int d = 0; d < n_; ++d) embed_row(d, &P.col[P.ptr[d]], &P.val[P.ptr[d]]);
+    phase("embedding P");
     AmgHost h;
     AmgHostLevel l0;
     l0.A.n_rows = l0.A.n_cols = n_;
@@ -1084,23 +1116,51 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     // matrix per cycle (config 2: 95 iterations / 1.11 s vs 84 / 1.23 s at degree 3)
     l0.cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 2;
     l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.1;
+    phase("lambda_max (device)");
     l0.R.n_rows = P.n_cols;
     l0.R.n_cols = P.n_rows;
     {
-        // R = P^T
-        l0.R.ptr.assign(P.n_cols + 1, 0);
-        for (int32_t c : P.col) l0.R.ptr[c + 1]++;
-        for (int i = 0; i < P.n_cols; ++i) l0.R.ptr[i + 1] += l0.R.ptr[i];
+        // R = P^T, rows of R in ascending P row order: each thread transposes a contiguous
+        // block of P rows into offsets counted per (column, block), so the result equals the
+        // sequential transpose
+        const int nt = std::max(1, omp_get_max_threads());
+        const int ncol = P.n_cols;
+        std::vector<int64_t> cnt((size_t)nt * ncol + 1, 0);  // [block][column]
+#pragma omp parallel num_threads(nt)
+        {
+            const int t = omp_get_thread_num();
+            const int r0 = (int)((int64_t)P.n_rows * t / nt), r1 = (int)((int64_t)P.n_rows * (t + 1) / nt);
+            int64_t* c = &cnt[(size_t)t * ncol];
+            for (int64_t k = P.ptr[r0]; k < P.ptr[r1]; ++k) c[P.col[k]]++;
+        }
+        l0.R.ptr.assign(ncol + 1, 0);
+        // column-major prefix over (column, block)
+        std::vector<int64_t> off((size_t)nt * ncol);
+        int64_t run = 0;
+        for (int c = 0; c < ncol; ++c) {
+            l0.R.ptr[c] = run;
+            for (int t = 0; t < nt; ++t) {
+                off[(size_t)t * ncol + c] = run;
+                run += cnt[(size_t)t * ncol + c];
+            }
+        }
+        l0.R.ptr[ncol] = run;
         l0.R.col.resize(P.nnz());
         l0.R.val.resize(P.nnz());
-        std::vector<int64_t> pos(l0.R.ptr.begin(), l0.R.ptr.end() - 1);
-        for (int i = 0; i < P.n_rows; ++i)
-            for (int64_t k = P.ptr[i]; k < P.ptr[i + 1]; ++k) {
-                const int64_t q = pos[P.col[k]]++;
-                l0.R.col[q] = i;
-                l0.R.val[q] = P.val[k];
-            }
+#pragma omp parallel num_threads(nt)
+        {
+            const int t = omp_get_thread_num();
+            const int r0 = (int)((int64_t)P.n_rows * t / nt), r1 = (int)((int64_t)P.n_rows * (t + 1) / nt);
+            int64_t* o = &off[(size_t)t * ncol];
+            for (int i = r0; i < r1; ++i)
+                for (int64_t k = P.ptr[i]; k < P.ptr[i + 1]; ++k) {
+                    const int64_t q = o[P.col[k]]++;
+                    l0.R.col[q] = i;
+                    l0.R.val[q] = P.val[k];
+                }
+        }
     }
+    phase("R = P^T");
     l0.P = std::move(P);
     h.levels.push_back(std::move(l0));
     for (auto& lv : h1.levels) h.levels.push_back(std::move(lv));
@@ -1119,6 +1179,7 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
         op.fixed = fixed_.get();
         amg_->set_level0_ebe(&op);
     }
+    phase("device hierarchy upload");
     amg_->smoother_timer.enabled = profiling_;
     amg_anode_ = anode;
     if (st) st->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

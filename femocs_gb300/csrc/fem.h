@@ -3,6 +3,9 @@
 // side, solution) with its assembly and solve entry points.
 #pragma once
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <memory>
 
 #include "prepared.h"
@@ -58,8 +61,29 @@ struct RegionCells {
 RegionCells region_cells(const PreparedMesh& pm, int region);
 
 FemStructure build_fem_structure(const PreparedMesh& pm, int region = kRegionVacuum);
+
+// FGB_SETUP_VERBOSE=1 prints the phases of the structure builders to stderr
+class SetupPhases {
+public:
+    explicit SetupPhases(const char* who) : who_(who), on_(std::getenv("FGB_SETUP_VERBOSE") != nullptr),
+                                            t_(std::chrono::steady_clock::now()) {}
+    void operator()(const char* what) {
+        const auto t = std::chrono::steady_clock::now();
+        if (on_)
+            std::fprintf(stderr, "%s: %-32s %9.1f ms\n", who_, what,
+                         std::chrono::duration<double, std::milli>(t - t_).count());
+        t_ = t;
+    }
+
+private:
+    const char* who_;
+    bool on_;
+    std::chrono::steady_clock::time_point t_;
+};
 // Q2 structure of the same vacuum hexahedra (see the order-2 notes above)
-FemStructure build_q2_structure(const PreparedMesh& pm);
+// sell_columns = false leaves sell_col empty (slice pointers and lengths are set): the device
+// fills it (q2_sell_columns, fem_q2.cu), the host copy would only be uploaded
+FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns = true);
 // lattice coordinates (a,b,c) of local Q2 node L, and the femocs vertex of a lattice corner
 inline void q2_lattice(int L, int& a, int& b, int& c) { a = L % 3; b = (L / 3) % 3; c = L / 9; }
 int q2_corner_vertex(int a, int b, int c);  // a,b,c in {0,2} -> femocs local vertex 0..7

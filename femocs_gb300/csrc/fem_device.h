@@ -53,6 +53,9 @@ int mixed_cg_grid(int n);
 
 class AmgDevice;
 
+// start vector of the multigrid setup's level-0 power iteration (amg_setup.cpp lambda_max)
+constexpr uint64_t kAmgLambdaSeed = 0x12345678abcdefull;
+
 struct SolveOptions {
     // 0: plain FP64 Jacobi-PCG; 1: FP32 Jacobi-PCG with FP64 reliable refinement (persistent
     // kernel); 2: FP64 CG preconditioned by an FP32 multigrid V-cycle
@@ -168,7 +171,8 @@ private:
     int amg_anode_ = -1;
     std::unique_ptr<FemDevice> q1_;   // Q2: the Q1 system of the same mesh, coarse level of the multigrid
     void build_q2_amg(int anode, SolveStats* st);
-    double estimate_lambda(int iters);  // largest eigenvalue of D^-1 A (FP64 power iteration)
+    // power iteration on D^-1 A (FP64, device) from the pseudo-random start of `seed`
+    double estimate_lambda(int iters, uint64_t seed = 0x9e3779b97f4a7c15ull);  // largest eigenvalue of D^-1 A (FP64 power iteration)
     bool profiling_ = false;
     int smooth_degree_ = 0;
     double smooth_lo_ = 0;

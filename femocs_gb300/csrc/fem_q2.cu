@@ -16,6 +16,7 @@
 //   k_sell_dirichlet     symmetric elimination on the SELL layout (FP64 + FP32 copies, D^-1)
 // Lattice: node L = a + 3b + 9c at reference coordinates (a-1, b-1, c-1); 1-D quadratic
 // Lagrange l0(t) = t(t-1)/2, l1(t) = 1 - t^2, l2(t) = t(t+1)/2.
+#include <climits>
 #include <cmath>
 #include <mutex>
 
@@ -208,6 +209,64 @@ __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_stiffness(int nc, con
     }
 }
 
+// one warp per row: gather the DoFs of the row's cells, bitonic sort (padded to a power of two
+// with INT_MAX), then keep the first of each run of equal values
+__global__ void __launch_bounds__(32) k_q2_sell_cols(int n, const int64_t* __restrict__ sptr,
+                                                     const int32_t* __restrict__ slen, const int32_t* __restrict__ row_len,
+                                                     const int32_t* __restrict__ r2c_ptr,
+                                                     const int32_t* __restrict__ r2c_item,
+                                                     const int32_t* __restrict__ cd, int32_t* __restrict__ scol,
+                                                     int* __restrict__ bad) {
+    extern __shared__ int32_t sc_buf[];
+    const int lane = threadIdx.x;
+    const int r = blockIdx.x;  // rows n.. only pad the last slice
+    const int s = r >> 5, rl = r & 31;
+    const int64_t base = sptr[s] + (int64_t)rl * 4;
+    const int len_s = slen[s];
+    int cnt = 0;
+    if (r < n) {
+        const int p0 = r2c_ptr[r], nc = r2c_ptr[r + 1] - p0;
+        const int m = 27 * nc;
+        int cap = 32;
+        while (cap < m) cap <<= 1;
+        for (int i = lane; i < cap; i += 32) {
+            int v = INT_MAX;
+            if (i < m) v = cd[27 * (size_t)(r2c_item[p0 + i / 27] / 27) + i % 27];
+            sc_buf[i] = v;
+        }
+        __syncwarp();
+        for (int k = 2; k <= cap; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < cap; i += 32) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const int a = sc_buf[i], b = sc_buf[ixj];
+                        const bool up = (i & k) == 0;
+                        if ((a > b) == up) {
+                            sc_buf[i] = b;
+                            sc_buf[ixj] = a;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (int b0 = 0; b0 < cap; b0 += 32) {
+            const int i = b0 + lane;
+            const int v = sc_buf[i];
+            const bool keep = v != INT_MAX && (i == 0 || sc_buf[i - 1] != v);
+            const unsigned msk = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const int jj = cnt + __popc(msk & ((1u << lane) - 1u));
+                if (jj < len_s) scol[base + (int64_t)(jj >> 2) * 128 + (jj & 3)] = v;
+            }
+            cnt += __popc(msk);
+        }
+        if (lane == 0 && cnt != row_len[r]) atomicAdd(bad, 1);
+    }
+    const int pad = r < n ? r : 0;
+    for (int jj = (r < n ? cnt : 0) + lane; jj < len_s; jj += 32) scol[base + (int64_t)(jj >> 2) * 128 + (jj & 3)] = pad;
+}
+
 __global__ void __launch_bounds__(32 * kQ2Warps) k_q2_assemble_rows(int n, int max_len, const int64_t* __restrict__ sptr,
                                                                     const int32_t* __restrict__ scol,
                                                                     const int32_t* __restrict__ row_len,
@@ -331,6 +390,26 @@ __global__ void k_sell_dirichlet(int n, const int64_t* __restrict__ sptr, const 
 void q2_cell_stiffness(int nc, const int32_t* cd, const double* dxyz, double* ke, cudaStream_t s) {
     upload_tables();
     FGB_LAUNCH(k_q2_cell_stiffness<<<grid_for(nc, kQ2Warps), 32 * kQ2Warps, 0, s>>>(nc, cd, dxyz, ke));
+}
+
+int q2_sell_columns(int n, int n_slices, const int64_t* sptr, const int32_t* slen, const int32_t* row_len,
+                    const int32_t* r2c_ptr, const int32_t* r2c_item, const int32_t* cell_dofs, int max_cells,
+                    int32_t* scol, cudaStream_t s) {
+    int cap = 32;
+    while (cap < 27 * max_cells) cap <<= 1;
+    const size_t smem = sizeof(int32_t) * (size_t)cap;
+    FGB_REQUIRE(smem <= 227 * 1024, "a Q2 row has too many cells for the shared-memory sort");
+    if (smem > 48 * 1024)
+        FGB_CUDA(cudaFuncSetAttribute(k_q2_sell_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DBuf<int> bad(1);
+    bad.zero(s);
+    FGB_LAUNCH(k_q2_sell_cols<<<32 * n_slices, 32, smem, s>>>(n, sptr, slen, row_len, r2c_ptr, r2c_item, cell_dofs,
+                                                              scol, bad.get()));
+    FGB_CUDA(cudaGetLastError());
+    int h = 0;
+    FGB_CUDA(cudaMemcpyAsync(&h, bad.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    FGB_CUDA(cudaStreamSynchronize(s));
+    return h;
 }
 
 void q2_assemble_rows(int n, int max_len, const int64_t* sptr, const int32_t* scol, const int32_t* row_len,

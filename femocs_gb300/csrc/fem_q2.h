@@ -9,6 +9,13 @@ namespace fgb {
 
 // 378 packed upper-triangle entries per cell
 void q2_cell_stiffness(int nc, const int32_t* cell_dofs, const double* dof_xyz, double* ke, cudaStream_t s);
+// SELL-32 columns of the Q2 rows: per row the sorted, unique DoFs of its cells (one warp per
+// row, bitonic sort in shared memory); padding = the row itself (0 past the last row).
+// max_cells = the longest row -> cell list. Returns the number of rows whose column count
+// differed from row_len (0 when the structure is consistent).
+int q2_sell_columns(int n, int n_slices, const int64_t* sptr, const int32_t* slen, const int32_t* row_len,
+                    const int32_t* r2c_ptr, const int32_t* r2c_item, const int32_t* cell_dofs, int max_cells,
+                    int32_t* scol, cudaStream_t s);
 // saved (pre-Dirichlet) matrix in the SELL layout of the structure
 void q2_assemble_rows(int n, int max_len, const int64_t* sptr, const int32_t* scol, const int32_t* row_len,
                       const int32_t* r2c_ptr, const int32_t* r2c_item, const int32_t* cell_dofs, const double* ke,

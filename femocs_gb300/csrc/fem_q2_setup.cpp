@@ -63,8 +63,9 @@ int q2_corner_vertex(int a, int b, int c) {
     return -1;
 }
 
-FemStructure build_q2_structure(const PreparedMesh& pm) {
+FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
     FemStructure fs;
+    SetupPhases phase("q2 structure");
     fs.order = 2;
     fs.npc = 27;
     fs.nfc = 9;
@@ -78,25 +79,35 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
     // ---- entities: vertices by compact vertex index, edges/faces by sorted corner nodes,
     // interiors by cell
     std::vector<int32_t> ent(27 * (size_t)nc, -1);  // entity id per (cell, L)
-    std::vector<EntityKey> ek;
-    ek.reserve(18 * (size_t)nc);
+    // 12 edges and 6 faces per cell, at fixed slots so that cells fill in parallel
+    int slot_of[27], n_corner[27], corner_tab[27][8];
+    {
+        int k = 0;
+        for (int L = 0; L < 27; ++L) {
+            n_corner[L] = corners_of(L, corner_tab[L]);
+            slot_of[L] = (n_corner[L] == 2 || n_corner[L] == 4) ? k++ : -1;
+        }
+        FGB_REQUIRE(k == 18, "Q2 lattice: 12 edges and 6 faces per cell");
+    }
+    std::vector<EntityKey> ek(18 * (size_t)nc);
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < nc; ++c)
         for (int L = 0; L < 27; ++L) {
-            int cr[8];
-            const int n = corners_of(L, cr);
+            const int n = n_corner[L];
             if (n == 1) {
-                ent[27 * (size_t)c + L] = pm.vac.node2vertex[cell_node(c, cr[0])];
+                ent[27 * (size_t)c + L] = pm.vac.node2vertex[cell_node(c, corner_tab[L][0])];
             } else if (n == 2 || n == 4) {
-                EntityKey e;
+                EntityKey& e = ek[18 * (size_t)c + slot_of[L]];
                 e.k = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MAX};
-                for (int q = 0; q < n; ++q) e.k[q] = cell_node(c, cr[q]);
+                for (int q = 0; q < n; ++q) e.k[q] = cell_node(c, corner_tab[L][q]);
                 std::sort(e.k.begin(), e.k.end());
                 e.cell = c;
                 e.local = (int8_t)L;
-                ek.push_back(e);
             }
         }
+    phase("entity keys");
     __gnu_parallel::sort(ek.begin(), ek.end());
+    phase("entity sort");
     int n_shared = 0;
     std::vector<int32_t> face_count;  // occurrences of each face entity (boundary faces: 1)
     std::vector<int32_t> ent_first;   // first (cell, L) of each shared entity
@@ -115,6 +126,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
     for (int c = 0; c < nc; ++c) ent[27 * (size_t)c + 13] = nvx + n_shared + c;
     fs.n_dofs = n_ent;
 
+    phase("entity ids");
     // entity -> one (cell, L) and its position
     std::vector<int32_t> e_cell(n_ent, -1);
     std::vector<int8_t> e_loc(n_ent, 0);
@@ -138,6 +150,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
         }
     }
 
+    phase("entity positions");
     // entity -> cells
     std::vector<int32_t> e2c_ptr(n_ent + 1, 0);
     for (int32_t e : ent) e2c_ptr[e + 1]++;
@@ -158,6 +171,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
         std::sort(l.begin(), l.end());
         l.erase(std::unique(l.begin(), l.end()), l.end());
     };
+    phase("entity -> cells");
     std::vector<int32_t> deg(n_ent);
 #pragma omp parallel
     {
@@ -169,6 +183,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
         }
     }
 
+    phase("row lengths");
     // ---- numbering: Morton order, then windows of 256 by decreasing row length
     double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
     for (int e = 0; e < n_ent; ++e)
@@ -197,13 +212,17 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
     // hexes); windows of 4096 keep SELL padding near 5 % (256: 44 %) while the gathers stay
     // inside a 32 KB stretch of the vector
     const int kWin = 4096;
+#pragma omp parallel for schedule(dynamic, 16)
     for (int w0 = 0; w0 < n_ent; w0 += kWin) {
         const int w1 = std::min(n_ent, w0 + kWin);
         std::stable_sort(dof2e.begin() + w0, dof2e.begin() + w1, [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
     }
+#pragma omp parallel for schedule(static)
     for (int d = 0; d < n_ent; ++d) e2dof[dof2e[d]] = d;
 
+    phase("Morton order, windows");
     fs.cell_dofs.resize(27 * (size_t)nc);
+#pragma omp parallel for schedule(static)
     for (size_t i = 0; i < ent.size(); ++i) fs.cell_dofs[i] = e2dof[ent[i]];
     fs.dof2node.assign(n_ent, -1);
     fs.node2dof.assign(pm.hex.n_nodes(), -1);
@@ -216,6 +235,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
     fs.dof_cell.resize(n_ent);
     fs.dof_local.resize(n_ent);
     fs.row_len.resize(n_ent);
+#pragma omp parallel for schedule(static)
     for (int d = 0; d < n_ent; ++d) {
         const int e = dof2e[d];
         for (int k = 0; k < 3; ++k) fs.dof_xyz[3 * (size_t)d + k] = exyz[3 * (size_t)e + k];
@@ -226,10 +246,12 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
     exyz.clear();
     exyz.shrink_to_fit();
 
+    phase("dof tables");
     // row -> (cell, local), ascending cell
     fs.r2c_ptr.assign(n_ent + 1, 0);
     for (int d = 0; d < n_ent; ++d) fs.r2c_ptr[d + 1] = fs.r2c_ptr[d] + (e2c_ptr[dof2e[d] + 1] - e2c_ptr[dof2e[d]]);
     fs.r2c_item.resize(fs.r2c_ptr[n_ent]);
+#pragma omp parallel for schedule(static)
     for (int d = 0; d < n_ent; ++d) {
         const int e = dof2e[d];
         int32_t* o = &fs.r2c_item[fs.r2c_ptr[d]];
@@ -237,6 +259,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
         std::sort(o, o + (e2c_ptr[e + 1] - e2c_ptr[e]));
     }
 
+    phase("row -> cells");
     // ---- SELL-32 with 4-wide row chunks, filled directly (second pass over the row sets)
     const int C = 32, W4 = 4;
     const int ns = (n_ent + C - 1) / C;
@@ -254,18 +277,23 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
         fs.slice_ptr[s + 1] = fs.slice_ptr[s] + (int64_t)m * C;
     }
     fs.n_entries = nz;
-    fs.sell_col.assign(fs.slice_ptr[ns], 0);
-#pragma omp parallel
-    {
+    if (sell_columns) fs.sell_col.assign(fs.slice_ptr[ns], 0);
+#pragma omp parallel if (sell_columns)
+    if (sell_columns) {
         std::vector<int32_t> l;
 #pragma omp for schedule(dynamic, 256)
         for (int s = 0; s < ns; ++s)
             for (int lane = 0; lane < C; ++lane) {
                 const int r = s * C + lane;
                 if (r < n_ent) {
-                    row_set(dof2e[r], l);
-                    for (int32_t& v : l) v = e2dof[v];
+                    // the row's columns: the DoFs of its cells (already renumbered), sorted, unique
+                    l.clear();
+                    for (int p = fs.r2c_ptr[r]; p < fs.r2c_ptr[r + 1]; ++p) {
+                        const int32_t* cdr = &fs.cell_dofs[27 * (size_t)(fs.r2c_item[p] / 27)];
+                        l.insert(l.end(), cdr, cdr + 27);
+                    }
                     std::sort(l.begin(), l.end());
+                    l.erase(std::unique(l.begin(), l.end()), l.end());
                 }
                 for (int j = 0; j < fs.slice_len[s]; ++j) {
                     const int64_t pos = fs.slice_ptr[s] + ((int64_t)(j / W4) * C + lane) * W4 + j % W4;
@@ -274,6 +302,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
             }
     }
 
+    phase("SELL columns");
     // ---- boundary faces: face entities owned by one vacuum cell (src/DealSolver.cpp:461-518)
     struct BF {
         int32_t cell;
@@ -336,6 +365,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm) {
         for (int f = 0; f < nt; ++f)
             for (int q = 0; q < 9; ++q) fs.r2f_item[pos[top[9 * (size_t)f + q]]++] = 9 * f + q;
     }
+    phase("boundary, r2f");
     return fs;
 }
 

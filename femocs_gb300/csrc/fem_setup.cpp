@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <parallel/algorithm>
 
 namespace fgb {
 
@@ -58,6 +59,7 @@ RegionCells region_cells(const PreparedMesh& pm, int region) {
 
 FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     FemStructure fs;
+    SetupPhases phase("q1 structure");
     const RegionCells rcs = region_cells(pm, region);
     const int nv = (int)rcs.vertex2node.size();
     const int nc = (int)rcs.cells.size();
@@ -73,6 +75,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
         for (int k = 0; k < 8; ++k)
             cv[8 * (size_t)c + k] = rcs.node2vertex[pm.hex.hexs[8 * (size_t)rcs.cells[c] + k]];
 
+    phase("region, cells");
     // vertex -> cells
     std::vector<int32_t> v2c_ptr(nv + 1, 0);
     for (int32_t v : cv) v2c_ptr[v + 1]++;
@@ -84,6 +87,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
             for (int k = 0; k < 8; ++k) v2c[pos[cv[8 * (size_t)c + k]]++] = 8 * c + k;
     }
 
+    phase("vertex -> cells");
     // neighbour sets (vertex numbering) and degrees
     std::vector<int32_t> deg(nv);
     std::vector<std::vector<int32_t>> nb(nv);
@@ -100,6 +104,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
         deg[v] = (int32_t)l.size();
     }
 
+    phase("neighbour sets");
     // Morton order, then windows of 256 sorted by decreasing degree
     double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
     for (int v = 0; v < nv; ++v)
@@ -119,7 +124,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
         }
         key[v] = {code, v};
     }
-    std::sort(key.begin(), key.end());
+    __gnu_parallel::sort(key.begin(), key.end());
     std::vector<int32_t> dof2v(nv);
     for (int i = 0; i < nv; ++i) dof2v[i] = key[i].second;
     const int W = 256;
@@ -131,6 +136,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     std::vector<int32_t> v2dof(nv);
     for (int d = 0; d < nv; ++d) v2dof[dof2v[d]] = d;
 
+    phase("Morton order, windows");
     fs.dof2node.resize(nv);
     fs.node2dof.assign(pm.hex.n_nodes(), -1);
     for (int d = 0; d < nv; ++d) {
@@ -158,6 +164,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     nb.clear();
     nb.shrink_to_fit();
 
+    phase("CSR columns");
     // row -> (cell, local), ascending cell
     fs.r2c_ptr.assign(nv + 1, 0);
     for (int d = 0; d < nv; ++d) fs.r2c_ptr[d + 1] = fs.r2c_ptr[d] + (v2c_ptr[dof2v[d] + 1] - v2c_ptr[dof2v[d]]);
@@ -167,8 +174,10 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
         std::copy(v2c.begin() + v2c_ptr[v], v2c.begin() + v2c_ptr[v + 1], fs.r2c_item.begin() + fs.r2c_ptr[d]);
     }
 
+    phase("row -> cells");
     // ---- boundary faces (src/DealSolver.cpp:461-518 via PoissonSolver::mark_mesh)
     std::vector<BFace> faces(6 * (size_t)nc);
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < nc; ++c)
         for (int f = 0; f < 6; ++f) {
             BFace& b = faces[6 * (size_t)c + f];
@@ -177,7 +186,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
             b.cell = c;
             b.face = (int8_t)f;
         }
-    std::sort(faces.begin(), faces.end(), [](const BFace& a, const BFace& b) {
+    __gnu_parallel::sort(faces.begin(), faces.end(), [](const BFace& a, const BFace& b) {
         for (int k = 0; k < 4; ++k)
             if (a.s[k] != b.s[k]) return a.s[k] < b.s[k];
         return a.cell < b.cell;
@@ -246,6 +255,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
             for (int q = 0; q < 4; ++q) fs.r2f_item[pos[top[4 * (size_t)f + q]]++] = 4 * f + q;
     }
 
+    phase("boundary faces");
     // ---- SELL-32 with 4-wide row chunks: slice s holds rows 32s..32s+31, padded to a length
     // that is a multiple of 4; entry j of lane l sits at ptr[s] + ((j/4)*32 + l)*4 + j%4, so a
     // warp reads 32 x 16 contiguous bytes of values (and of columns) per chunk
@@ -262,6 +272,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     }
     fs.sell_col.assign(fs.slice_ptr[ns], 0);
     fs.csr2sell.resize(fs.nnz());
+#pragma omp parallel for schedule(dynamic, 256)
     for (int s = 0; s < ns; ++s)
         for (int lane = 0; lane < C; ++lane) {
             const int r = s * C + lane;
@@ -275,6 +286,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
                 }
             }
         }
+    phase("SELL layout");
     return fs;
 }
 

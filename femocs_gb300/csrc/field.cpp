@@ -12,7 +12,7 @@ Field::Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream, int or
         FGB_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
         own_stream_ = true;
     }
-    fem_.reset(new FemDevice(*pm_, order == 2 ? build_q2_structure(*pm_) : build_fem_structure(*pm_), stream_));
+    fem_.reset(new FemDevice(*pm_, order == 2 ? build_q2_structure(*pm_, false) : build_fem_structure(*pm_), stream_));
     dm_.reset(new DeviceMesh(*pm_, stream_));
 }
 

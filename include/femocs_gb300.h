@@ -131,7 +131,11 @@ FGB_FIELD* fgb_field_create(const FGB_MESH* m);
 FGB_FIELD* fgb_field_create_order(const FGB_MESH* m, int order);
 /* Q2 fields: for every DoF one vacuum cell holding it and its lattice index L = a + 3b + 9c */
 int fgb_field_q2_dofs(FGB_FIELD* f, int* dof_cell, int* dof_local);
-/* Q2 structure of a mesh built on the host only: DoFs, nonzeros, top faces, longest row */
+/* Q1 / Q2 structure of a mesh built on the host only: DoFs, nonzeros, top faces, longest row */
+int fgb_mesh_q1_sizes(const FGB_MESH* m, int64_t* out4);
+/* 64-bit FNV-1a digest of every array of the host-built FEM structure (order 1 or 2; region 0
+ * vacuum, 1 bulk), for regression checks of the builders */
+uint64_t fgb_mesh_structure_digest(const FGB_MESH* m, int order, int region);
 int fgb_mesh_q2_sizes(const FGB_MESH* m, int64_t* out4);
 void fgb_field_free(FGB_FIELD* f);
 int fgb_field_sizes(const FGB_FIELD* f, int64_t* out4); /* n_dofs, nnz, n_top_faces, sell_entries */
