@@ -219,7 +219,7 @@ MESH_TABLES = ["tet_nodes", "tet_marker", "tet_nbor", "node_xyz", "node_marker",
                "vac_node2vertex", "vac_cells", "tet_search", "edgemax", "node_parents"]
 
 
-def mesh_prep_timing(spec):
+def mesh_prep_timing(spec, order=1):
     """Tet -> hex split, grouping and interpolation tables of the workload's mesh: host builder
     against the kernels (second device run; the first warms the allocator), tables compared
     byte for byte. Outside the timed steps (the bench mesh is prepared once)."""
@@ -233,9 +233,23 @@ def mesh_prep_timing(spec):
         for t in MESH_TABLES)
     th, td = mh.prep_timing(), md.prep_timing()
     s = md.sizes()
-    return {"tets": s["n_tets"], "hexes": s["n_hexs"], "nodes": s["n_nodes"], "host_ms": th["total_ms"],
-            "device_ms": td["total_ms"], "device_kernel_ms": td["kernel_ms"], "tables_equal": bool(equal),
-            "note": "device_ms includes the tet upload and the download of every table into host memory"}
+    out = {"tets": s["n_tets"], "hexes": s["n_hexs"], "nodes": s["n_nodes"], "host_ms": th["total_ms"],
+           "device_ms": td["total_ms"], "device_kernel_ms": td["kernel_ms"], "tables_equal": bool(equal),
+           "note": "device_ms includes the tet upload and the download of every table into host memory"}
+    del mh
+    # the rest of a re-mesh step on the device-prepared mesh: FEM structure + device system,
+    # multigrid hierarchy (built by the first solve), the first solve itself
+    t0 = time.perf_counter()
+    f = fg.Field(md, order=order)
+    field_ms = (time.perf_counter() - t0) * 1e3
+    f.setup(E0, 0.0)
+    f.assemble(True, False)
+    rc, st = f.solve(precision=2, rel_tol=REL_TOL, max_iter=100000)
+    out["remesh"] = {"order": order, "field_create_ms": field_ms, "multigrid_setup_ms": st["setup_ms"],
+                     "first_solve_ms": st["ms"] - st["setup_ms"],
+                     "note": "after the mesh preparation: host FEM structure (device SELL columns for Q2), "
+                             "uploads, host multigrid hierarchy"}
+    return out
 
 
 def surface_cpu_timing(spec, surf_pts, sample=2000):
@@ -428,7 +442,7 @@ def run_ours(args, world, rank):
     line["surface_interp"] = {"points": n_surf, "gpu_ms": surf_ms, "gpu_points_per_s": n_surf / (surf_ms * 1e-3),
                               "rank": 1, "note": "femocs_interpolate_surface_elfield path, device-resident points"}
     if rank == 0 and world == 1 and not args.no_cpu:
-        line["mesh_prep"] = mesh_prep_timing(spec)
+        line["mesh_prep"] = mesh_prep_timing(spec, order)
         line["surface_interp"].update(surface_cpu_timing(spec, pts[:n_surf]))
     if rank == 0:
         print(json.dumps(line), flush=True)
