@@ -4,6 +4,7 @@
 #include <chrono>
 #include <cstring>
 #include <memory>
+#include <omp.h>
 
 #include <thread>
 
@@ -798,6 +799,7 @@ int fgb_batch_add_synthetic(FGB_BATCH* b, int n, const FgbNanotip* specs, int n_
         std::vector<std::thread> pool;
         for (int t = 0; t < nt; ++t)
             pool.emplace_back([&, t] {
+                omp_set_num_threads(1);  // the meshes are the parallelism: no nested teams
                 try {
                     for (int i = next++; i < n; i = next++) {
                         auto pm = std::make_shared<PreparedMesh>(prepare_mesh(make_nanotip_mesh(to_spec(&specs[i]))));
@@ -960,6 +962,7 @@ int fgb_server_add_synthetic_runs(FGB_SERVER* s, int n, const FgbNanotip* specs,
         std::vector<std::thread> pool;
         for (int t = 0; t < nt; ++t)
             pool.emplace_back([&, t] {
+                omp_set_num_threads(1);  // the meshes are the parallelism: no nested teams
                 try {
                     for (int i = next++; i < n; i = next++) {
                         const NanotipSpec sp = to_spec(&specs[i]);

@@ -5,6 +5,8 @@
 
 #include "server.h"
 
+#include <omp.h>
+
 namespace fgb {
 
 namespace {
@@ -96,6 +98,7 @@ int FieldServer::place_pending(int n_threads) {
     std::vector<std::thread> pool;
     for (int t = 0; t < nt; ++t)
         pool.emplace_back([&, t] {
+                omp_set_num_threads(1);  // the meshes are the parallelism: no nested teams
             try {
                 for (size_t i = next++; i < todo.size(); i = next++) {
                     const int slot = b_.add_mesh(todo[i]->pm, (size_t)opt_.hbm_reserve);

@@ -125,3 +125,20 @@ def test_q2_structure_matches_independent_enumeration():
     s = Q2System(m.export("node_xyz"), m.export("hex_nodes"), m.export("vac_cells"), -0.1)
     assert q["n_dofs"] == s.n and q["nnz"] == s.nnz_pattern
     assert q["n_top_faces"] > 0 and s.fixed.sum() > 0
+
+
+def test_structure_builders_do_not_depend_on_thread_count():
+    """The parallel phases of the Q1 (vacuum, bulk) and Q2 structure builders give the same
+    structure as a single thread (every array hashed by fgb_mesh_structure_digest)."""
+    import subprocess
+    import sys
+    code = ("import femocs_gb300 as fg; from femocs_gb300._lib import load; "
+            "m = fg.Mesh.synthetic(radius=5.0, height=14.0, box_half=18.0, slab=4.0, top=40.0, h=3.0, growth=1.5, "
+            "margin=3.0); print([load().fgb_mesh_structure_digest(m.h, o, r) for o, r in ((1, 0), (1, 1), (2, 0))])")
+    env_root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    for nt in ("1", "5"):
+        env = dict(os.environ, OMP_NUM_THREADS=nt, PYTHONPATH=env_root)
+        outs.append(subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True,
+                                   timeout=300).stdout.strip())
+    assert outs[0] == outs[1] and outs[0].startswith("[")
