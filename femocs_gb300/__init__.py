@@ -193,7 +193,7 @@ class Field:
         return rc, _stats_dict(st)
 
     def set_outer_spmv(self, mode=1):
-        """Outer SpMV of the multigrid PCG: 1 FP32 hi/lo pairs, 0 FP64 matrix (default)."""
+        """Outer SpMV of the multigrid PCG: 1 FP32 hi/lo pairs (default), 0 FP64 matrix."""
         self._ok(load().fgb_field_set_outer_spmv(self.h, int(mode)))
 
     def set_level0_ebe(self, on=True):

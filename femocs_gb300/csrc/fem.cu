@@ -420,9 +420,9 @@ __device__ __forceinline__ void df_term(float& sh, float& sl, float ah, float al
 __global__ void __launch_bounds__(kBlock) k_cg_spmv_pq_df(int n, const int64_t* __restrict__ sptr,
                                                           const int32_t* __restrict__ slen,
                                                           const int32_t* __restrict__ scol, const float* __restrict__ vhi,
-                                                          const float* __restrict__ vlo, const float* __restrict__ phi,
-                                                          const float* __restrict__ plo, const double* __restrict__ p,
-                                                          double* __restrict__ q, double* partial, CgState* st) {
+                                                          const float* __restrict__ vlo, const float2* __restrict__ p2,
+                                                          const double* __restrict__ p, double* __restrict__ q,
+                                                          double* partial, CgState* st) {
     if (st->done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
@@ -430,18 +430,27 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_pq_df(int n, const int64_t* 
         const int s = i >> 5;
         const int64_t base = sptr[s] + (int64_t)(i & 31) * 4;
         const int nch = slen[s] >> 2;
-        float sh = 0.f, sl = 0.f;
-        for (int c = 0; c < nch; ++c) {
-            const int64_t o = base + (int64_t)c * 128;
+        // two chunks in flight, each with its own (hi, lo) accumulator; p as interleaved pairs
+        // (one 8-byte gather per nonzero)
+        float sh0 = 0.f, sl0 = 0.f, sh1 = 0.f, sl1 = 0.f;
+        auto chunk = [&](int64_t o, float& sh, float& sl) {
             const int4 ci = __ldg(reinterpret_cast<const int4*>(scol + o));
             const float4 hi = __ldg(reinterpret_cast<const float4*>(vhi + o));
             const float4 lo = __ldg(reinterpret_cast<const float4*>(vlo + o));
-            df_term(sh, sl, hi.x, lo.x, __ldg(phi + ci.x), __ldg(plo + ci.x));
-            df_term(sh, sl, hi.y, lo.y, __ldg(phi + ci.y), __ldg(plo + ci.y));
-            df_term(sh, sl, hi.z, lo.z, __ldg(phi + ci.z), __ldg(plo + ci.z));
-            df_term(sh, sl, hi.w, lo.w, __ldg(phi + ci.w), __ldg(plo + ci.w));
+            const float2 px = __ldg(p2 + ci.x), py = __ldg(p2 + ci.y), pz = __ldg(p2 + ci.z), pw = __ldg(p2 + ci.w);
+            df_term(sh, sl, hi.x, lo.x, px.x, px.y);
+            df_term(sh, sl, hi.y, lo.y, py.x, py.y);
+            df_term(sh, sl, hi.z, lo.z, pz.x, pz.y);
+            df_term(sh, sl, hi.w, lo.w, pw.x, pw.y);
+        };
+        int c = 0;
+        for (; c + 1 < nch; c += 2) {
+            chunk(base + (int64_t)c * 128, sh0, sl0);
+            chunk(base + (int64_t)(c + 1) * 128, sh1, sl1);
         }
-        const double qi = (double)sh + (double)sl;
+        if (c < nch) chunk(base + (int64_t)c * 128, sh0, sl0);
+        df_add(sh0, sl0, sh1, sl1);
+        const double qi = (double)sh0 + (double)sl0;
         q[i] = qi;
         v[0] = p[i] * qi;
     }
@@ -535,17 +544,14 @@ __global__ void k_to32(int n, const double* __restrict__ a, float* __restrict__ 
 
 // p = z (the V-cycle result, FP32), rz = r.z; phi/plo: the FP32 pair of p (may be null)
 __global__ void __launch_bounds__(kBlock) k_pcg_start(int n, const float* __restrict__ z32, const double* __restrict__ r,
-                                                      double* __restrict__ p, float* __restrict__ phi,
-                                                      float* __restrict__ plo, double* partial, CgState* st) {
+                                                      double* __restrict__ p, float2* __restrict__ p2, double* partial,
+                                                      CgState* st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (i < n) {
         const double zi = (double)z32[i];
         p[i] = zi;
-        if (phi) {
-            phi[i] = z32[i];
-            plo[i] = 0.f;
-        }
+        if (p2) p2[i] = make_float2(z32[i], 0.f);
         v[0] = r[i] * zi;
     }
     if (grid_reduce<1>(v, partial, &st->ticket)) st->rz = v[0];
@@ -607,17 +613,15 @@ __global__ void k_scale_copy64(int n, const double* __restrict__ a, double s, do
 
 // p = z + beta p (and its FP32 pair when phi is not null)
 __global__ void __launch_bounds__(kBlock) k_pcg_direction(int n, const float* __restrict__ z32, double* __restrict__ p,
-                                                          float* __restrict__ phi, float* __restrict__ plo,
-                                                          const CgState* st) {
+                                                          float2* __restrict__ p2, const CgState* st) {
     if (st->done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double pi = (double)z32[i] + st->beta * p[i];
     p[i] = pi;
-    if (phi) {
+    if (p2) {
         const float h = (float)pi;
-        phi[i] = h;
-        plo[i] = (float)(pi - (double)h);
+        p2[i] = make_float2(h, (float)(pi - (double)h));
     }
 }
 
@@ -1261,23 +1265,21 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     const bool df = outer_df_;
     if (df && status == 0) {
         ensure_split();
-        phi_.resize(n_);
-        plo_.resize(n_);
+        p2_.resize(n_);
     }
-    float* ph = df ? phi_.get() : nullptr;
-    float* pl = df ? plo_.get() : nullptr;
+    float2* p2 = df ? p2_.get() : nullptr;
     // Convergence is declared on the FP64 true residual b - A x: when the recursion reports
     // convergence, r is recomputed exactly and CG restarts from it if it is still above the
     // tolerance (the FP32-pair SpMV lets the recursive residual drift by ~2^-48 per term)
     while (status == 0) {
         FGB_LAUNCH(k_to32<<<gb, kBlock, 0, stream_>>>(n_, r64_.get(), r32_.get()));
         const float* z = amg_->vcycle(r32_.get());
-        FGB_LAUNCH(k_pcg_start<<<gb, kBlock, 0, stream_>>>(n_, z, r64_.get(), p64_.get(), ph, pl, partial_.get(), ds));
+        FGB_LAUNCH(k_pcg_start<<<gb, kBlock, 0, stream_>>>(n_, z, r64_.get(), p64_.get(), p2, partial_.get(), ds));
         while (true) {
             spmv_timer_.begin(stream_);
             if (df)
                 FGB_LAUNCH(k_cg_spmv_pq_df<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
-                                                                      sell32_.get(), sell_lo_.get(), ph, pl, p64_.get(),
+                                                                      sell32_.get(), sell_lo_.get(), p2, p64_.get(),
                                                                       q64_.get(), partial_.get(), ds));
             else
                 FGB_LAUNCH(k_cg_spmv_pq<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(),
@@ -1295,7 +1297,7 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
             }
             const float* zi = amg_->vcycle(r32_.get());
             FGB_LAUNCH(k_pcg_rz<<<gb, kBlock, 0, stream_>>>(n_, zi, r64_.get(), partial_.get(), ds));
-            FGB_LAUNCH(k_pcg_direction<<<gb, kBlock, 0, stream_>>>(n_, zi, p64_.get(), ph, pl, ds));
+            FGB_LAUNCH(k_pcg_direction<<<gb, kBlock, 0, stream_>>>(n_, zi, p64_.get(), p2, ds));
         }
         // true FP64 residual of the current x (also the restart residual)
         FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),

@@ -101,9 +101,9 @@ public:
     // Q2: apply the finest multigrid level element by element or through the assembled SELL
     // matrix (default: measured faster, the element products' row gather is scattered)
     void set_level0_ebe(bool on);
-    // outer SpMV of the multigrid PCG: 0 = FP64 matrix (default), 1 = FP32 hi/lo pairs with
-    // error-free products (FP64-accurate to ~2^-48 per term, off the FP64 pipe; measured 14 %
-    // faster per launch on Q2 config 2, not on Q1, and one extra iteration)
+    // outer SpMV of the multigrid PCG: 1 = FP32 hi/lo pairs with error-free products (default;
+    // FP64-accurate to ~2^-48 per term, off the FP64 pipe: config 2 Q2 2.27 vs 2.92 ms per
+    // launch, Q1 0.21 vs 0.25 ms), 0 = the FP64 matrix
     void set_outer_spmv(int mode);
     ~FemDevice();
 
@@ -178,9 +178,10 @@ private:
     double smooth_lo_ = 0;
     int q1_gauss_ = 2;  // Gauss points per direction of the Q1 element integrals
     bool level0_ebe_ = false;
-    bool outer_df_ = false;
+    bool outer_df_ = true;
     bool split_valid_ = false;
-    DBuf<float> sell_lo_, phi_, plo_;  // FP32 pair of the matrix values and of p
+    DBuf<float> sell_lo_;  // low FP32 part of the matrix values (high part: sell32_)
+    DBuf<float2> p2_;      // p as interleaved FP32 (hi, lo) pairs
     void ensure_split();
     DBuf<float> ke32_;      // Q2: FP32 copy of the packed element matrices (element-by-element level 0)
     DBuf<int8_t> fixed_;    // 1 on Dirichlet rows of the current anode mode

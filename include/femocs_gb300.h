@@ -161,9 +161,9 @@ int fgb_field_last_stats(const FGB_FIELD* f, double* out14);
 /* Q2 fields: apply the finest multigrid level element by element (1) or through the
  * assembled SELL matrix (0, default); the hierarchy is rebuilt at the next solve */
 int fgb_field_set_level0_ebe(FGB_FIELD* f, int on);
-/* outer SpMV of the multigrid PCG: 1 reads the matrix and the search direction as FP32 hi/lo
- * pairs with error-free products and compensated row sums (FP64-accurate to ~2^-48 per term,
- * off the FP64 pipe); 0 (default) uses the FP64 matrix */
+/* outer SpMV of the multigrid PCG: 1 (default) reads the matrix and the search direction as FP32
+ * hi/lo pairs with error-free products and compensated row sums (FP64-accurate to ~2^-48 per
+ * term, off the FP64 pipe); 0 uses the FP64 matrix */
 int fgb_field_set_outer_spmv(FGB_FIELD* f, int mode);
 /* Chebyshev smoothing of the finest multigrid level: steps before and after the coarse
  * correction (0: default, Q1 4, Q2 2) and the interval's lower end as a fraction of
