@@ -369,7 +369,7 @@ def run_ours(args, world, rank):
     nnz = field.nnz
     ebe = order == 2 and last["smoother_bytes"] != nnz * 8 + 24 * n
     kern = {
-        ("k_ebe_apply + k_ebe_cheb (level-0 Chebyshev smoothing, Q2 element by element, FP32)" if ebe else
+        ("k_cb_apply + k_cb_finish (level-0 Chebyshev smoothing, Q2 cell blocks, FP32)" if ebe else
          "k_cheb_step (level-0 Chebyshev smoothing, FP32)"): (
             sum(s["smoother_ms"] for s in solve_stats), sum(s["smoother_launches"] for s in solve_stats),
             last["smoother_bytes"], "smoother_ebe" if ebe else "smoother"),

@@ -197,8 +197,8 @@ class Field:
         self._ok(load().fgb_field_set_outer_spmv(self.h, int(mode)))
 
     def set_level0_ebe(self, on=True):
-        """Q2: finest multigrid level element by element (True) or through the SELL matrix
-        (False, the default)."""
+        """Q2: finest multigrid level element by element by cell blocks (True, the default) or
+        through the SELL matrix (False)."""
         self._ok(load().fgb_field_set_level0_ebe(self.h, int(on)))
 
     def set_smoothing(self, degree=0, lo=0.0):

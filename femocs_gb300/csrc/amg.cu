@@ -167,63 +167,207 @@ __global__ void __launch_bounds__(kB) k_csr_apply(int n, const int64_t* __restri
     y[i] = accumulate ? y[i] + acc : acc;
 }
 
-// ---- element-by-element level-0 operator (Q2)
-__device__ __forceinline__ int sym27f(int i, int j) {
-    if (i > j) { const int t = i; i = j; j = t; }
-    return i * 27 - (i * (i - 1)) / 2 + (j - i);
-}
+// ---- element-by-element level-0 operator (Q2) by cell blocks: one CTA per block
+constexpr int kCb = 256;
 
-// ye[27 c + i] = sum_j K_e[i][j] x[cd[27 c + j]], one warp per cell
-__global__ void __launch_bounds__(kB) k_ebe_apply(int nc, const int32_t* __restrict__ cd, const float* __restrict__ ke,
-                                                  const float* __restrict__ x, float* __restrict__ ye) {
-    __shared__ float sK[kB / 32][378];
-    __shared__ float sx[kB / 32][28];
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * (kB / 32) + wid;
-    if (c >= nc) return;  // whole warp leaves together
-    const float* kc = ke + 378 * (size_t)c;
-    for (int e = lane; e < 378; e += 32) sK[wid][e] = __ldg(kc + e);
-    if (lane < 27) sx[wid][lane] = __ldg(x + cd[27 * (size_t)c + lane]);
-    __syncwarp();
-    if (lane < 27) {
-        float acc = 0.f;
-#pragma unroll 9
-        for (int j = 0; j < 27; ++j) acc += sK[wid][sym27f(lane, j)] * sx[wid][j];
-        ye[27 * (size_t)c + lane] = acc;
+// final row update of a level-0 application: Chebyshev step (KIND 0) or residual (KIND 1)
+template <int KIND>
+__device__ __forceinline__ void l0_finish(int g, float ax, float xg, const float* __restrict__ b,
+                                          const float* __restrict__ dinv, float* __restrict__ xout,
+                                          float* __restrict__ d, float c1, float c2) {
+    const float ri = b[g] - ax;
+    if constexpr (KIND == 1) {
+        xout[g] = ri;
+    } else {
+        const float di = (c1 < 0.f ? 0.f : c1 * d[g]) + c2 * dinv[g] * ri;
+        d[g] = di;
+        xout[g] = xg + di;
     }
 }
 
-// row gather of the element products (ascending cell: fixed order), Dirichlet rows diag * x
-__device__ __forceinline__ float ebe_row(int i, const int32_t* __restrict__ r2c_ptr, const int32_t* __restrict__ r2c_item,
-                                         const float* __restrict__ ye, const int8_t* __restrict__ fixed,
-                                         const float* __restrict__ dinv, const float* __restrict__ x) {
-    if (fixed[i]) return x[i] / dinv[i];
-    float a = 0.f;
-    for (int p = r2c_ptr[i]; p < r2c_ptr[i + 1]; ++p) a += __ldg(ye + r2c_item[p]);
-    return a;
+constexpr int kCbPer = 16;     // block-local DoFs per thread at most (max_dofs <= 4096)
+constexpr int kCbMaxCells = 256;
+
+// shared memory of one block: its item lists (28 u16 per cell), x of its DoFs, the products
+__host__ __device__ inline size_t cb_smem_bytes(int max_cells, int max_dofs) {
+    return 56 * (size_t)max_cells + 4 * (size_t)max_dofs + 108 * (size_t)max_cells;
 }
 
-__global__ void __launch_bounds__(kB) k_ebe_cheb(int n, const int32_t* __restrict__ r2c_ptr,
-                                                 const int32_t* __restrict__ r2c_item, const float* __restrict__ ye,
-                                                 const int8_t* __restrict__ fixed, const float* __restrict__ dinv,
-                                                 const float* __restrict__ b, const float* __restrict__ xin,
-                                                 float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float ax = ebe_row(i, r2c_ptr, r2c_item, ye, fixed, dinv, xin);
-    const float di = (c1 < 0.f ? 0.f : c1 * d[i]) + c2 * dinv[i] * (b[i] - ax);
-    d[i] = di;
-    xout[i] = xin[i] + di;
+// One block per CTA, three phases separated by barriers:
+//  A  the block's item lists and x of its DoFs into shared memory (each thread's loads issued
+//     together, so the gathers overlap instead of queueing behind one another);
+//  B  K_e x_e of each cell: one warp per two cells, lane i < 27 owns row i. It holds K(i, i+t)
+//     for t = 0..13, takes x_{i+t} from lane i+t and hands K(i, i+t) x_i to lane i+t (indices
+//     mod 27), so every entry of the symmetric K_e is loaded once;
+//  C  the products of each DoF summed in item order; complete DoFs finished (Chebyshev update
+//     or residual), the others leave their partial sum in their slot.
+template <int KIND>
+__global__ void __launch_bounds__(kCb, 3) k_cb_apply(EbeOperator op, const float* __restrict__ dinv,
+                                                     const float* __restrict__ b, const float* __restrict__ xin,
+                                                     float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
+    extern __shared__ __align__(16) unsigned char cb_raw[];
+    const int blk = blockIdx.x;
+    const int p0 = op.cell_start[blk], nb = op.cell_start[blk + 1] - p0;
+    const int q0 = op.dof_start[blk], nq = op.dof_start[blk + 1] - q0;
+    uint16_t* sit = reinterpret_cast<uint16_t*>(cb_raw);
+    float* sx = reinterpret_cast<float*>(cb_raw + 56 * (size_t)op.max_cells);
+    float* sy = sx + op.max_dofs;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int il = lane < 27 ? lane : 26;  // lanes 27..31 shadow lane 26 and store nothing
+    const uint16_t* loc = op.loc + 27 * (size_t)p0;
+    // the element matrices of the warp's first two cells are requested first, so that they
+    // travel while phase A gathers
+    float k0[14], k1[14];
+    int l0 = 0, l1 = 0;
+    if (2 * warp < nb) {
+        const int c = 2 * warp, c1i = c + 1 < nb ? c + 1 : c;
+        const float* K0 = op.ke + 378 * (size_t)(p0 + c);
+        const float* K1 = op.ke + 378 * (size_t)(p0 + c1i);
+#pragma unroll
+        for (int t = 0; t < 14; ++t) {
+            k0[t] = __ldg(K0 + 27 * t + il);
+            k1[t] = __ldg(K1 + 27 * t + il);
+        }
+        l0 = __ldg(loc + 27 * c + il);
+        l1 = __ldg(loc + 27 * c1i + il);
+    }
+    {
+        const uint2* gi = reinterpret_cast<const uint2*>(op.items + 28 * (size_t)p0);
+        uint2* si = reinterpret_cast<uint2*>(sit);
+        const int nw = 7 * nb;
+        uint2 w8[7];
+#pragma unroll
+        for (int r = 0; r < 7; ++r) {
+            const int w = tid + r * kCb;
+            if (w < nw) w8[r] = __ldg(gi + w);
+        }
+#pragma unroll
+        for (int r0 = 0; r0 < kCbPer; r0 += 8) {
+            int gd[8];
+            float xv[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int k = tid + (r0 + r) * kCb;
+                gd[r] = k < nq ? __ldg(op.dof_list + q0 + k) : 0;
+            }
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int k = tid + (r0 + r) * kCb;
+                xv[r] = k < nq ? __ldg(xin + gd[r]) : 0.f;
+            }
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int k = tid + (r0 + r) * kCb;
+                if (k < nq) sx[k] = xv[r];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 7; ++r) {
+            const int w = tid + r * kCb;
+            if (w < nw) si[w] = w8[r];
+        }
+    }
+    __syncthreads();
+    for (int c = 2 * warp; c < nb; c += 2 * (kCb / 32)) {
+        const int c1i = c + 1 < nb ? c + 1 : c;
+        if (c != 2 * warp) {
+            const float* K0 = op.ke + 378 * (size_t)(p0 + c);
+            const float* K1 = op.ke + 378 * (size_t)(p0 + c1i);
+#pragma unroll
+            for (int t = 0; t < 14; ++t) {
+                k0[t] = __ldg(K0 + 27 * t + il);
+                k1[t] = __ldg(K1 + 27 * t + il);
+            }
+            l0 = __ldg(loc + 27 * c + il);
+            l1 = __ldg(loc + 27 * c1i + il);
+        }
+        const float x0 = sx[l0];
+        const float x1 = sx[l1];
+        float y0 = k0[0] * x0, y1 = k1[0] * x1;
+#pragma unroll
+        for (int t = 1; t < 14; ++t) {
+            int up = lane + t;
+            if (up >= 27) up -= 27;
+            int dn = lane - t;
+            if (dn < 0) dn += 27;
+            const float xu0 = __shfl_sync(0xffffffffu, x0, up);
+            const float xu1 = __shfl_sync(0xffffffffu, x1, up);
+            const float tr0 = __shfl_sync(0xffffffffu, k0[t] * x0, dn);
+            const float tr1 = __shfl_sync(0xffffffffu, k1[t] * x1, dn);
+            y0 = fmaf(k0[t], xu0, y0) + tr0;
+            y1 = fmaf(k1[t], xu1, y1) + tr1;
+        }
+        if (lane < 27) {
+            sy[27 * c + lane] = y0;
+            if (c1i != c) sy[27 * c1i + lane] = y1;
+        }
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int r0 = 0; r0 < kCbPer; r0 += 8) {
+        if (tid + r0 * kCb >= nq) break;
+        int e0[8], e1[8], sl[8], g[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int k = tid + (r0 + r) * kCb;
+            const bool v = k < nq;
+            e1[r] = v ? __ldg(op.item_end + q0 + k) : 0;
+            e0[r] = v && k ? __ldg(op.item_end + q0 + k - 1) : 0;
+            sl[r] = v ? __ldg(op.slot + q0 + k) : -2;
+            g[r] = v ? __ldg(op.dof_list + q0 + k) : 0;
+        }
+        float ax[8], bv[8], dv[8], dd[8];
+        int fx[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const bool own = sl[r] == -1;
+            bv[r] = own ? b[g[r]] : 0.f;
+            dv[r] = own ? dinv[g[r]] : 1.f;
+            dd[r] = own && KIND == 0 && c1 >= 0.f ? d[g[r]] : 0.f;
+            fx[r] = own ? op.fixed[g[r]] : 0;
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            float a = 0.f;
+            for (int e = e0[r]; e < e1[r]; ++e) a += sy[sit[e]];
+            ax[r] = a;
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            if (sl[r] >= 0) {
+                op.partial[sl[r]] = ax[r];
+            } else if (sl[r] == -1) {
+                const float xs = sx[tid + (r0 + r) * kCb];
+                const float ri = bv[r] - (fx[r] ? xs / dv[r] : ax[r]);
+                if constexpr (KIND == 1) {
+                    xout[g[r]] = ri;
+                } else {
+                    const float di = (c1 < 0.f ? 0.f : c1 * dd[r]) + c2 * dv[r] * ri;
+                    d[g[r]] = di;
+                    xout[g[r]] = xs + di;
+                }
+            }
+        }
+    }
 }
 
-__global__ void __launch_bounds__(kB) k_ebe_residual(int n, const int32_t* __restrict__ r2c_ptr,
-                                                     const int32_t* __restrict__ r2c_item, const float* __restrict__ ye,
-                                                     const int8_t* __restrict__ fixed, const float* __restrict__ dinv,
-                                                     const float* __restrict__ b, const float* __restrict__ x,
-                                                     float* __restrict__ r) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    r[i] = b[i] - ebe_row(i, r2c_ptr, r2c_item, ye, fixed, dinv, x);
+// DoFs split over blocks: their partial sums in ascending block order
+template <int KIND>
+__global__ void __launch_bounds__(kB) k_cb_finish(EbeOperator op, const float* __restrict__ dinv,
+                                                  const float* __restrict__ b, const float* __restrict__ xin,
+                                                  float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= op.n_bnd) return;
+    const int g = op.bnd_dofs[j];
+    const float xg = xin[g];
+    float ax = 0.f;
+    if (op.fixed[g]) {
+        ax = xg / dinv[g];
+    } else {
+        for (int s = op.bnd_ptr[j]; s < op.bnd_ptr[j + 1]; ++s) ax += op.partial[s];
+    }
+    l0_finish<KIND>(g, ax, xg, b, dinv, xout, d, c1, c2);
 }
 
 // threads per row for a CSR operator of average row length `avg`
@@ -450,16 +594,21 @@ void AmgDevice::set_level0_ebe(const EbeOperator* op) {
     }
     ebe_ = *op;
     ebe_on_ = true;
-    ye_.resize(27 * (size_t)op->n_cells);
+    FGB_REQUIRE(op->max_cells <= kCbMaxCells && op->max_dofs <= kCbPer * kCb, "cell blocks too large");
+    const size_t smem = cb_smem_bytes(op->max_cells, op->max_dofs);
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 }
 
 double AmgDevice::smoother_bytes() const {
     const double n = lv_[0]->n;
     if (!ebe_on_) return (double)nnz0_ * 8.0 + 24.0 * n;
-    const double nc = ebe_.n_cells;
-    // apply: element matrix, cell DoF list, products written, x gathered once per row;
-    // finish: row pointers, items, products gathered, b, D^-1, d read+written, x in/out, flag
-    return nc * (378.0 * 4 + 27.0 * 4 + 27.0 * 4) + n * 4 + (n + 1) * 4 + nc * 27.0 * 8 + n * 25.0;
+    // per cell: K_e (378 x 4), its loc list (27 x 2) and items (28 x 2); per block-local DoF: DoF
+    // id, item end, slot and the gathered x; per DoF: b, D^-1, d in and out, x out, the
+    // Dirichlet flag; per slot: the partial written and read; per split
+    // DoF: its id and slot range
+    return ebe_.n_cells * (378.0 * 4 + 110.0) + (double)ebe_.n_local * 14.0 + n * 21.0 + ebe_.n_slots * 8.0 +
+           ebe_.n_bnd * 8.0;
 }
 
 // one level-0 operator application fused with the Chebyshev update (kind 0) or the residual
@@ -468,14 +617,17 @@ void AmgDevice::level0_apply(int kind, const float* xin, float* xout, float c1, 
     AmgDevLevel& L = *lv_[0];
     const int g = grid_for(L.n, kB);
     if (ebe_on_) {
-        FGB_LAUNCH(k_ebe_apply<<<grid_for(ebe_.n_cells, kB / 32), kB, 0, stream_>>>(ebe_.n_cells, ebe_.cell_dofs, ebe_.ke,
-                                                                                 xin, ye_.get()));
-        if (kind == 0)
-            FGB_LAUNCH(k_ebe_cheb<<<g, kB, 0, stream_>>>(L.n, ebe_.r2c_ptr, ebe_.r2c_item, ye_.get(), ebe_.fixed, L.dinv,
-                                                         L.bin, xin, xout, L.d.get(), c1, c2));
-        else
-            FGB_LAUNCH(k_ebe_residual<<<g, kB, 0, stream_>>>(L.n, ebe_.r2c_ptr, ebe_.r2c_item, ye_.get(), ebe_.fixed,
-                                                             L.dinv, L.bin, xin, xout));
+        const size_t smem = cb_smem_bytes(ebe_.max_cells, ebe_.max_dofs);
+        const int gb = grid_for(ebe_.n_bnd, kB);
+        if (kind == 0) {
+            FGB_LAUNCH(k_cb_apply<0><<<ebe_.n_blocks, kCb, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, L.d.get(),
+                                                                            c1, c2));
+            if (gb) FGB_LAUNCH(k_cb_finish<0><<<gb, kB, 0, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, L.d.get(), c1, c2));
+        } else {
+            FGB_LAUNCH(k_cb_apply<1><<<ebe_.n_blocks, kCb, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, nullptr,
+                                                                            0.f, 0.f));
+            if (gb) FGB_LAUNCH(k_cb_finish<1><<<gb, kB, 0, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, nullptr, 0.f, 0.f));
+        }
         return;
     }
     const Op A{L.n, L.sptr, L.slen, L.scol, L.val, L.dinv};

@@ -53,16 +53,26 @@ AmgHost build_amg(const PreparedMesh& pm, const FemStructure& fs, const std::vec
 
 struct AmgDevLevel;
 
-// Element-by-element form of a level-0 operator (Q2): y = sum over cells of K_e x_e, rows of
-// Dirichlet DoFs replaced by diag * x -- the eliminated operator on vectors that vanish on the
-// Dirichlet DoFs, which every V-cycle vector does
+// Element-by-element form of a level-0 operator (Q2), applied by cell blocks (cell_blocks.h):
+// y = sum over cells of K_e x_e, rows of Dirichlet DoFs replaced by diag * x -- the eliminated
+// operator on vectors that vanish on the Dirichlet DoFs, which every V-cycle vector does
 struct EbeOperator {
-    int n_cells = 0;
-    const int32_t* cell_dofs = nullptr;  // 27 per cell, lattice order
-    const float* ke = nullptr;           // 378 packed upper-triangle entries per cell
-    const int32_t* r2c_ptr = nullptr;    // row -> items 27*cell+local, ascending cell
-    const int32_t* r2c_item = nullptr;
-    const int8_t* fixed = nullptr;       // 1 on Dirichlet rows
+    int n_cells = 0, n_blocks = 0, max_cells = 0, max_dofs = 0, n_bnd = 0, n_slots = 0;
+    int64_t n_local = 0;
+    // 378 per block position, cyclic half of K_e: entry 27 t + i = K_e(i, (i + t) mod 27),
+    // t = 0..13 (27 is odd, so every off-diagonal pair appears exactly once)
+    const float* ke = nullptr;
+    const int32_t* cell_start = nullptr;  // block -> first position
+    const int32_t* dof_start = nullptr;   // block -> first local DoF entry
+    const int32_t* dof_list = nullptr;    // local entry -> global DoF
+    const uint16_t* item_end = nullptr;   // local entry -> end of its items (block-relative)
+    const int32_t* slot = nullptr;        // local entry -> partial slot, -1 when complete
+    const uint16_t* loc = nullptr;        // 27 per position: local entry of each lattice DoF
+    const uint16_t* items = nullptr;      // 28 per position: products grouped by local entry
+    const int32_t* bnd_dofs = nullptr;    // DoFs split over blocks
+    const int32_t* bnd_ptr = nullptr;     // their slots bnd_ptr[j] .. bnd_ptr[j+1]-1, ascending block
+    float* partial = nullptr;             // n_slots
+    const int8_t* fixed = nullptr;        // 1 on Dirichlet rows
 };
 
 // Device side of the hierarchy and the V-cycle (amg.cu).
@@ -85,8 +95,8 @@ public:
     // apply level 0 element by element (null operator: back to the SELL matrix)
     void set_level0_ebe(const EbeOperator* op);
     bool level0_ebe() const { return ebe_on_; }
-    // algorithmic bytes of one level-0 smoothing step (SELL: nnz*8 + 24 n; element by element:
-    // the packed element matrices, cell DoF lists, per-(cell, local) products and row gathers)
+    // algorithmic bytes of one level-0 smoothing step (SELL: nnz*8 + 24 n; cell blocks: the
+    // element matrices, the block tables, x per block-local DoF, the vectors, the partial sums)
     double smoother_bytes() const;
 
 private:
@@ -94,7 +104,6 @@ private:
     void level0_apply(int kind, const float* xin, float* xout, float c1, float c2);  // 0 cheb, 1 residual
     EbeOperator ebe_;
     bool ebe_on_ = false;
-    DBuf<float> ye_;
     int64_t nnz0_ = 0;
     cudaStream_t stream_;
     std::vector<std::unique_ptr<AmgDevLevel>> lv_;

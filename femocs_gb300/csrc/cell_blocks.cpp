@@ -1,0 +1,153 @@
+// Host construction of the Q2 cell blocks (see cell_blocks.h). Deterministic for any thread
+// count: every block is built from its own cells alone, and the offsets come from prefix sums
+// over blocks in order.
+#include "cell_blocks.h"
+
+#include <omp.h>
+
+#include <algorithm>
+
+#include "common.h"
+
+namespace fgb {
+
+namespace {
+
+// sorted (DoF << 16 | item) keys of the cells at positions [p0, p1); returns the number of
+// distinct DoFs
+int block_keys(const FemStructure& fs, const std::vector<int32_t>& perm, int p0, int p1, uint64_t* keys) {
+    const int m = 27 * (p1 - p0);
+    for (int p = p0; p < p1; ++p) {
+        const int32_t* cd = fs.cell_dofs.data() + 27 * (size_t)perm[p];
+        for (int l = 0; l < 27; ++l) {
+            const int item = 27 * (p - p0) + l;
+            keys[item] = ((uint64_t)(uint32_t)cd[l] << 16) | (uint64_t)item;
+        }
+    }
+    std::sort(keys, keys + m);
+    int d = 0;
+    for (int e = 0; e < m; ++e)
+        if (e == 0 || (keys[e] >> 16) != (keys[e - 1] >> 16)) ++d;
+    return d;
+}
+
+// split [p0, p1) into halves until every part holds at most max_dofs DoFs; parts are appended
+// in position order with their keys left sorted in `keys` (offset 27 * p)
+void split_block(const FemStructure& fs, const std::vector<int32_t>& perm, int p0, int p1, int max_dofs,
+                 uint64_t* keys, std::vector<std::pair<int, int>>& parts) {
+    const int d = block_keys(fs, perm, p0, p1, keys + 27 * (size_t)p0);
+    if (d <= max_dofs || p1 - p0 == 1) {
+        parts.push_back({p1, d});
+        return;
+    }
+    const int mid = p0 + (p1 - p0) / 2;
+    split_block(fs, perm, p0, mid, max_dofs, keys, parts);
+    split_block(fs, perm, mid, p1, max_dofs, keys, parts);
+}
+
+}  // namespace
+
+CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block, int max_dofs) {
+    FGB_REQUIRE(fs.order == 2, "cell blocks are built for Q2 structures");
+    FGB_REQUIRE(cells_per_block >= 1 && 27 * cells_per_block <= 65535, "27 x cells per block must fit 16 bits");
+    FGB_REQUIRE(max_dofs >= 27 && max_dofs <= 4096, "block DoF limit out of range");
+    CellBlocks cb;
+    const int nc = fs.n_cells, n = fs.n_dofs;
+    cb.n_cells = nc;
+    cb.n_dofs = n;
+    // cells in ascending order of their interior DoF (lattice index 13)
+    std::vector<int32_t> owner(n, -1);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nc; ++c) owner[fs.cell_dofs[27 * (size_t)c + 13]] = c;
+    cb.perm.reserve(nc);
+    for (int d = 0; d < n; ++d)
+        if (owner[d] >= 0) cb.perm.push_back(owner[d]);
+    FGB_REQUIRE((int)cb.perm.size() == nc, "every cell owns one interior DoF");
+    std::vector<int32_t>().swap(owner);
+
+    // blocks: chunks of cells_per_block positions, halved while too many DoFs
+    std::vector<uint64_t> keys(27 * (size_t)nc);
+    const int n_chunks = (nc + cells_per_block - 1) / cells_per_block;
+    std::vector<std::vector<std::pair<int, int>>> parts(n_chunks);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int k = 0; k < n_chunks; ++k)
+        split_block(fs, cb.perm, k * cells_per_block, std::min(nc, (k + 1) * cells_per_block), max_dofs, keys.data(),
+                    parts[k]);
+    cb.cell_start.push_back(0);
+    cb.dof_start.push_back(0);
+    for (const auto& pv : parts)
+        for (const auto& pd : pv) {
+            cb.max_cells = std::max(cb.max_cells, pd.first - cb.cell_start.back());
+            cb.max_dofs = std::max(cb.max_dofs, pd.second);
+            cb.cell_start.push_back(pd.first);
+            cb.dof_start.push_back(cb.dof_start.back() + pd.second);
+        }
+    cb.n_blocks = (int)cb.cell_start.size() - 1;
+    const int64_t ne = cb.dof_start.back();
+    FGB_REQUIRE(ne < (int64_t)1 << 31, "too many block-local DoFs");
+    cb.dof_list.resize(ne);
+    cb.item_end.resize(ne);
+    cb.slot.resize(ne);
+    cb.loc.resize(27 * (size_t)nc);
+    cb.items.assign(28 * (size_t)nc, 0);
+
+    // local DoFs, items and completeness per block; slots numbered in block order
+    std::vector<int32_t> n_inc(cb.n_blocks + 1, 0);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int b = 0; b < cb.n_blocks; ++b) {
+        const int p0 = cb.cell_start[b], p1 = cb.cell_start[b + 1];
+        const uint64_t* kb = keys.data() + 27 * (size_t)p0;
+        const int m = 27 * (p1 - p0);
+        int k = -1, inc = 0;
+        for (int e = 0; e < m; ++e) {
+            const int32_t dof = (int32_t)(kb[e] >> 16);
+            const int item = (int)(kb[e] & 0xffff);
+            if (e == 0 || dof != (int32_t)(kb[e - 1] >> 16)) {
+                ++k;
+                cb.dof_list[cb.dof_start[b] + k] = dof;
+            }
+            cb.items[28 * (size_t)p0 + e] = (uint16_t)item;
+            cb.loc[27 * (size_t)p0 + item] = (uint16_t)k;
+            cb.item_end[cb.dof_start[b] + k] = (uint16_t)(e + 1);
+        }
+        for (int q = cb.dof_start[b]; q < cb.dof_start[b + 1]; ++q) {
+            const int dof = cb.dof_list[q];
+            const int e0 = q == cb.dof_start[b] ? 0 : cb.item_end[q - 1];
+            const bool complete = cb.item_end[q] - e0 == fs.r2c_ptr[dof + 1] - fs.r2c_ptr[dof];
+            cb.slot[q] = complete ? -1 : inc++;
+        }
+        n_inc[b + 1] = inc;
+    }
+    std::vector<uint64_t>().swap(keys);
+    for (int b = 0; b < cb.n_blocks; ++b) n_inc[b + 1] += n_inc[b];
+    cb.n_slots = n_inc[cb.n_blocks];
+    std::vector<int32_t> slot_dof(cb.n_slots);
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < cb.n_blocks; ++b)
+        for (int q = cb.dof_start[b]; q < cb.dof_start[b + 1]; ++q)
+            if (cb.slot[q] >= 0) {
+                cb.slot[q] += n_inc[b];
+                slot_dof[cb.slot[q]] = cb.dof_list[q];
+            }
+
+    // slots renumbered by DoF: the slots of boundary DoF j are bnd_ptr[j] .. bnd_ptr[j+1]-1 in
+    // ascending block order (block-order slot s ascends with the block)
+    std::vector<int32_t> cnt(n, 0);
+    for (int s = 0; s < cb.n_slots; ++s) ++cnt[slot_dof[s]];
+    std::vector<int32_t> first(n, -1);
+    cb.bnd_ptr.push_back(0);
+    for (int d = 0; d < n; ++d)
+        if (cnt[d]) {
+            first[d] = cb.bnd_ptr.back();
+            cb.bnd_dofs.push_back(d);
+            cb.bnd_ptr.push_back(cb.bnd_ptr.back() + cnt[d]);
+        }
+    std::vector<int32_t> renum(cb.n_slots);
+    for (int s = 0; s < cb.n_slots; ++s) renum[s] = first[slot_dof[s]]++;
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < ne; ++q)
+        if (cb.slot[q] >= 0) cb.slot[q] = renum[cb.slot[q]];
+    return cb;
+}
+
+}  // namespace fgb

@@ -22,9 +22,18 @@
 
 #include "amg.h"
 #include "fem_device.h"
+#include "cell_blocks.h"
 #include "fem_q2.h"
 
 namespace fgb {
+
+struct FemDevice::CellBlocksDev {
+    int n_blocks = 0, max_cells = 0, max_dofs = 0, n_bnd = 0, n_slots = 0;
+    int64_t n_local = 0;
+    DBuf<int32_t> perm, cell_start, dof_start, dof_list, slot, bnd_dofs, bnd_ptr;
+    DBuf<uint16_t> item_end, loc, items;
+    DBuf<float> partial;
+};
 
 std::atomic<long long> g_kernel_launches{0};
 
@@ -591,10 +600,20 @@ __global__ void __launch_bounds__(kBlock) k_pcg_rz(int n, const float* __restric
     }
 }
 
-__global__ void k_to_float(long long n, const double* __restrict__ a, float* __restrict__ b) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
+// element matrices (378 packed upper-triangle FP64 entries per cell) to FP32 in block order and
+// cyclic-half layout: entry 27 t + i of position p is K(i, (i + t) mod 27) of cell perm[p]
+__global__ void k_ke_cyclic(long long total, const int32_t* __restrict__ perm, const double* __restrict__ ke,
+                            float* __restrict__ out) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const long long p = idx / 378;
+    const int e = (int)(idx - p * 378), t = e / 27, i = e - 27 * t;
+    int j = i + t;
+    if (j >= 27) j -= 27;
+    const int lo = i < j ? i : j, hi = i < j ? j : i;
+    out[idx] = (float)ke[378 * (size_t)perm[p] + lo * 27 - (lo * (lo - 1)) / 2 + (hi - lo)];
 }
+
 
 __global__ void k_fixed_flags(int n, const int8_t* __restrict__ bc, int anode, int8_t* __restrict__ fixed) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -631,6 +650,7 @@ __global__ void __launch_bounds__(kBlock) k_pcg_direction(int n, const float* __
 FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t stream)
     : fs_(std::move(fs)), pm_(&pm), stream_(stream), n_(fs_.n_dofs), nc_(fs_.n_cells) {
     cudaStream_t s = stream_;
+    level0_ebe_ = fs_.order == 2;
     cell_dofs_.upload(fs_.cell_dofs, s);
     r2c_ptr_.upload(fs_.r2c_ptr, s);
     r2c_item_.upload(fs_.r2c_item, s);
@@ -759,11 +779,7 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
             q2_cell_stiffness(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), stream_);
             q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
                              r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
-            if (level0_ebe_) {
-                ke32_.resize(378 * (size_t)nc_);
-                FGB_LAUNCH(k_to_float<<<grid_for(378LL * nc_, kBlock), kBlock, 0, stream_>>>(378LL * nc_, ke_.get(),
-                                                                                             ke32_.get()));
-            }
+            if (level0_ebe_) refresh_ke32();
         }
         fixed_.resize(n_);
         FGB_LAUNCH(k_fixed_flags<<<gb, kBlock, 0, stream_>>>(n_, bc_.get(), anode_dirichlet ? 1 : 0, fixed_.get()));
@@ -1173,13 +1189,27 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
                              dinv32_.get()));
     if (level0_ebe_) {
-        FGB_REQUIRE(ke32_.size() == 378 * (size_t)nc_, "element matrices not assembled");
+        if (ke32_.size() != 378 * (size_t)nc_) refresh_ke32();
+        CellBlocksDev& c = *cb_;
         EbeOperator op;
         op.n_cells = nc_;
-        op.cell_dofs = cell_dofs_.get();
+        op.n_blocks = c.n_blocks;
+        op.max_cells = c.max_cells;
+        op.max_dofs = c.max_dofs;
+        op.n_bnd = c.n_bnd;
+        op.n_slots = c.n_slots;
+        op.n_local = c.n_local;
         op.ke = ke32_.get();
-        op.r2c_ptr = r2c_ptr_.get();
-        op.r2c_item = r2c_item_.get();
+        op.cell_start = c.cell_start.get();
+        op.dof_start = c.dof_start.get();
+        op.dof_list = c.dof_list.get();
+        op.item_end = c.item_end.get();
+        op.slot = c.slot.get();
+        op.loc = c.loc.get();
+        op.items = c.items.get();
+        op.bnd_dofs = c.bnd_dofs.get();
+        op.bnd_ptr = c.bnd_ptr.get();
+        op.partial = c.partial.get();
         op.fixed = fixed_.get();
         amg_->set_level0_ebe(&op);
     }
@@ -1219,6 +1249,41 @@ void FemDevice::ensure_split() {
 void FemDevice::set_outer_spmv(int mode) {
     FGB_REQUIRE(mode == 0 || mode == 1, "outer SpMV mode 0 (FP64) or 1 (FP32 pairs)");
     outer_df_ = mode == 1;
+}
+
+void FemDevice::ensure_cell_blocks() {
+    if (cb_) return;
+    SetupPhases phase("cell blocks");
+    CellBlocks h = build_cell_blocks(fs_);
+    phase("host build");
+    auto c = std::make_unique<CellBlocksDev>();
+    c->n_blocks = h.n_blocks;
+    c->max_cells = h.max_cells;
+    c->max_dofs = h.max_dofs;
+    c->n_bnd = (int)h.bnd_dofs.size();
+    c->n_slots = h.n_slots;
+    c->n_local = h.local_entries();
+    c->perm.upload(h.perm, stream_);
+    c->cell_start.upload(h.cell_start, stream_);
+    c->dof_start.upload(h.dof_start, stream_);
+    c->dof_list.upload(h.dof_list, stream_);
+    c->slot.upload(h.slot, stream_);
+    c->bnd_dofs.upload(h.bnd_dofs, stream_);
+    c->bnd_ptr.upload(h.bnd_ptr, stream_);
+    c->item_end.upload(h.item_end, stream_);
+    c->loc.upload(h.loc, stream_);
+    c->items.upload(h.items, stream_);
+    c->partial.resize(std::max(1, h.n_slots));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    phase("upload");
+    cb_ = std::move(c);
+}
+
+void FemDevice::refresh_ke32() {
+    ensure_cell_blocks();
+    ke32_.resize(378 * (size_t)nc_);
+    FGB_LAUNCH(k_ke_cyclic<<<grid_for(378LL * nc_, kBlock), kBlock, 0, stream_>>>(378LL * nc_, cb_->perm.get(),
+                                                                                 ke_.get(), ke32_.get()));
 }
 
 void FemDevice::set_level0_ebe(bool on) {

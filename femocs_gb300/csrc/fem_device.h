@@ -98,8 +98,9 @@ public:
     // coarse correction) and the lower end of the interval as a fraction of lambda_max;
     // 0 keeps the default (Q1: 4 and 0.04; Q2: 2 and 0.1). Drops the current hierarchy.
     void set_smoothing(int degree, double lo);
-    // Q2: apply the finest multigrid level element by element or through the assembled SELL
-    // matrix (default: measured faster, the element products' row gather is scattered)
+    // Q2: apply the finest multigrid level element by element, by cell blocks (cell_blocks.h;
+    // default: 4.3 vs 8.95 GB per smoothing step on config 2), or through the assembled SELL
+    // matrix; the hierarchy is rebuilt at the next solve
     void set_level0_ebe(bool on);
     // outer SpMV of the multigrid PCG: 1 = FP32 hi/lo pairs with error-free products (default;
     // FP64-accurate to ~2^-48 per term, off the FP64 pipe: config 2 Q2 2.27 vs 2.92 ms per
@@ -183,7 +184,11 @@ private:
     DBuf<float> sell_lo_;  // low FP32 part of the matrix values (high part: sell32_)
     DBuf<float2> p2_;      // p as interleaved FP32 (hi, lo) pairs
     void ensure_split();
-    DBuf<float> ke32_;      // Q2: FP32 copy of the packed element matrices (element-by-element level 0)
+    DBuf<float> ke32_;      // Q2: FP32 element matrices in block order, cyclic half (EbeOperator)
+    struct CellBlocksDev;
+    std::unique_ptr<CellBlocksDev> cb_;
+    void ensure_cell_blocks();
+    void refresh_ke32();    // element matrices (ke_) into ke32_
     DBuf<int8_t> fixed_;    // 1 on Dirichlet rows of the current anode mode
     LaunchTimer spmv_timer_;
     int n_, nc_;

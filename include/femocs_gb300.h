@@ -158,8 +158,9 @@ int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol,
  * levels, and with profiling on (multigrid path): level-0 smoother ms, smoother launches,
  * outer FP64 SpMV ms, SpMV launches; algorithmic bytes of one level-0 smoothing step */
 int fgb_field_last_stats(const FGB_FIELD* f, double* out14);
-/* Q2 fields: apply the finest multigrid level element by element (1) or through the
- * assembled SELL matrix (0, default); the hierarchy is rebuilt at the next solve */
+/* Q2 fields: apply the finest multigrid level element by element by cell blocks (1, default:
+ * half the bytes of the SELL matrix) or through the assembled SELL matrix (0); the hierarchy is
+ * rebuilt at the next solve */
 int fgb_field_set_level0_ebe(FGB_FIELD* f, int on);
 /* outer SpMV of the multigrid PCG: 1 (default) reads the matrix and the search direction as FP32
  * hi/lo pairs with error-free products and compensated row sums (FP64-accurate to ~2^-48 per

@@ -134,8 +134,9 @@ def test_q2_pipeline_against_q1(q2):
 
 
 def test_q2_level0_element_by_element_matches_sell(q2):
-    """The finest multigrid level applied element by element is the same operator as the
-    assembled SELL matrix (FP32 rounding aside): same convergence, same solution."""
+    """The finest multigrid level applied element by element (cell blocks, the default) is the
+    same operator as the assembled SELL matrix (FP32 rounding aside): same convergence, same
+    solution."""
     m, f, keys = q2
     out = {}
     for ebe in (True, False):
@@ -145,7 +146,7 @@ def test_q2_level0_element_by_element_matches_sell(q2):
         rc, st = f.solve(precision=2, rel_tol=1e-10)
         assert rc > 0 and st["status"] == 1
         out[ebe] = (st["iterations"], f.solution())
-    f.set_level0_ebe(False)
+    f.set_level0_ebe(True)
     assert abs(out[True][0] - out[False][0]) <= 2
     x = out[False][1]
     assert np.abs(out[True][1] - x).max() <= 2e3 * 1e-10 * np.abs(x).max()
