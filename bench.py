@@ -52,8 +52,9 @@ SSOR_ITERS = {"config1": 268, "config2": 617, "probe": 0}
 Q2_SSOR_RATIO = 2.55
 # DRAM bytes (read + write) per row of one launch of the hot multigrid kernels, from ncu
 # captures of the Q2 probe workload (profiles/k_cheb_step_level0_q2_probe.md: 61.9 nonzeros per
-# row, as config 2's Q2 rows); a launch's traffic scales with its rows
-KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6}
+# row, as config 2's Q2 rows; profiles/k_cb_apply_level0_q2_probe.md: the cell-block step,
+# k_cb_apply + k_cb_finish); a launch's traffic scales with its rows
+KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6, ("smoother_ebe", 2): 261.8}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -365,7 +366,8 @@ def run_ours(args, world, rank):
     #     nonzero, and 24 B per row (b, x gathered once, D^-1 read; d read + written; x written);
     #     Q2 element by element: the solver's own count (AmgDevice::smoother_bytes)
     #   outer SpMV (k_cg_spmv_pq_df, FP64-accurate from FP32 hi/lo pairs): 4 + 4 B value + 4 B
-    #     column per nonzero, 24 B per row (p pair gathered once, p read, q written)
+    #     column per nonzero, 24 B per row (p pair gathered once, p read, q written); Q2 over
+    #     cell blocks: the solver's own count (FemDevice::outer_spmv_bytes)
     nnz = field.nnz
     ebe = order == 2 and last["smoother_bytes"] != nnz * 8 + 24 * n
     kern = {
@@ -373,9 +375,10 @@ def run_ours(args, world, rank):
          "k_cheb_step (level-0 Chebyshev smoothing, FP32)"): (
             sum(s["smoother_ms"] for s in solve_stats), sum(s["smoother_launches"] for s in solve_stats),
             last["smoother_bytes"], "smoother_ebe" if ebe else "smoother"),
-        "k_cg_spmv_pq_df (outer FP64-accurate SpMV from FP32 pairs + p.q)": (
+        ("k_cb_spmv_df + k_cb_spmv_finish (outer FP64-accurate SpMV + p.q, Q2 cell blocks, FP32 pairs)"
+         if order == 2 else "k_cg_spmv_pq_df (outer FP64-accurate SpMV from FP32 pairs + p.q)"): (
             sum(s["spmv_ms"] for s in solve_stats), sum(s["spmv_launches"] for s in solve_stats),
-            nnz * 12 + 24 * n, "spmv_df"),
+            field.outer_spmv_bytes(), "spmv_cb" if order == 2 else "spmv_df"),
     }
     name, (tot_ms, cnt, bytes_per_launch, key) = max(kern.items(), key=lambda kv: kv[1][0])
     launch_ms = tot_ms / max(cnt, 1)

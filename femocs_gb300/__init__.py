@@ -193,8 +193,16 @@ class Field:
         return rc, _stats_dict(st)
 
     def set_outer_spmv(self, mode=1):
-        """Outer SpMV of the multigrid PCG: 1 FP32 hi/lo pairs (default), 0 FP64 matrix."""
+        """Outer SpMV of the multigrid PCG: 1 the SELL matrix as FP32 hi/lo pairs (Q1 default),
+        2 the same arithmetic over cell blocks (Q2 default), 0 the FP64 SELL matrix."""
         self._ok(load().fgb_field_set_outer_spmv(self.h, int(mode)))
+
+    def outer_spmv_bytes(self):
+        """Algorithmic bytes of one outer SpMV launch in the current mode."""
+        b = load().fgb_field_outer_spmv_bytes(self.h)
+        if b < 0:
+            raise RuntimeError(last_error())
+        return b
 
     def set_level0_ebe(self, on=True):
         """Q2: finest multigrid level element by element by cell blocks (True, the default) or

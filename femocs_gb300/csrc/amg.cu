@@ -595,9 +595,10 @@ void AmgDevice::set_level0_ebe(const EbeOperator* op) {
     ebe_ = *op;
     ebe_on_ = true;
     FGB_REQUIRE(op->max_cells <= kCbMaxCells && op->max_dofs <= kCbPer * kCb, "cell blocks too large");
-    const size_t smem = cb_smem_bytes(op->max_cells, op->max_dofs);
-    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the cap is a property of the kernel, shared by every mesh: always the largest block's
+    const int cap = (int)cb_smem_bytes(kCbMaxCells, kCbPer * kCb);
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
 }
 
 double AmgDevice::smoother_bytes() const {

@@ -443,6 +443,11 @@ int fgb_field_last_stats(const FGB_FIELD* f, double* out14) {
 int fgb_field_set_outer_spmv(FGB_FIELD* f, int mode) {
     return guarded([&] { f->f->fem().set_outer_spmv(mode); return 0; });
 }
+double fgb_field_outer_spmv_bytes(const FGB_FIELD* f) {
+    double b = -1;
+    guarded([&] { b = f->f->fem().outer_spmv_bytes(); return 0; });
+    return b;
+}
 int fgb_field_set_level0_ebe(FGB_FIELD* f, int on) {
     return guarded([&] { f->f->fem().set_level0_ebe(on != 0); return 0; });
 }

@@ -91,6 +91,17 @@ private:
 };
 
 inline int grid_for(long long n, int block) { return (int)((n + block - 1) / block); }
+// grid of a grid-stride kernel that ends in a grid-wide reduction: at most 2048 threads per SM,
+// so that the last CTA's sum over the per-CTA partials stays a few steps long
+inline int reduce_grid(long long n, int block) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms <= 0)
+        sms = 152;
+    const int cap = sms * (2048 / block);
+    const int g = grid_for(n, block);
+    return g < cap ? (g > 0 ? g : 1) : cap;
+}
 
 // Device time of one kernel inside a sequence of launches on one stream: an event pair is
 // recorded around each timed launch while enabled; collect() sums the pairs after the

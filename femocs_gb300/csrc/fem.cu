@@ -336,9 +336,19 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* partial, un
     double acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+    // four partials per thread in flight (L2 reads, after the fence), added in ascending order
+    const int nb = (int)gridDim.x, bd = (int)blockDim.x;
+    for (int b = threadIdx.x; b < nb; b += 4 * bd) {
+        double t[4][NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) acc[k] += ((volatile double*)partial)[(size_t)NV * b + k];
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < NV; ++k) t[u][k] = b + u * bd < nb ? __ldcg(partial + (size_t)NV * (b + u * bd) + k) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < NV; ++k) acc[k] += t[u][k];
+    }
     __syncthreads();
     block_reduce<NV>(acc, sh);
     if (threadIdx.x == 0) {
@@ -433,9 +443,8 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_pq_df(int n, const int64_t* 
                                                           const double* __restrict__ p, double* __restrict__ q,
                                                           double* partial, CgState* st) {
     if (st->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
-    if (i < n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int s = i >> 5;
         const int64_t base = sptr[s] + (int64_t)(i & 31) * 4;
         const int nch = slen[s] >> 2;
@@ -461,7 +470,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_pq_df(int n, const int64_t* 
         df_add(sh0, sl0, sh1, sl1);
         const double qi = (double)sh0 + (double)sl0;
         q[i] = qi;
-        v[0] = p[i] * qi;
+        v[0] += p[i] * qi;
     }
     if (grid_reduce<1>(v, partial, &st->ticket)) {
         st->pq = v[0];
@@ -513,20 +522,18 @@ __global__ void __launch_bounds__(kBlock) k_residual64(int n, const int64_t* __r
                                                        const int32_t* __restrict__ scol, const double* __restrict__ sval,
                                                        const double* __restrict__ x, const double* __restrict__ b,
                                                        double* __restrict__ r, double* partial, CgState* st) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
-    if (i < n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double ri = b[i] - sell_row(i, sptr, slen, scol, sval, x);
         r[i] = ri;
-        v[0] = ri * ri;
+        v[0] += ri * ri;
     }
     if (grid_reduce<1>(v, partial, &st->ticket)) st->rr = v[0];
 }
 
 __global__ void k_norm2(int n, const double* __restrict__ a, double* partial, CgState* st) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
-    if (i < n) v[0] = a[i] * a[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[0] += a[i] * a[i];
     if (grid_reduce<1>(v, partial, &st->ticket)) st->rr = v[0];
 }
 
@@ -555,13 +562,12 @@ __global__ void k_to32(int n, const double* __restrict__ a, float* __restrict__ 
 __global__ void __launch_bounds__(kBlock) k_pcg_start(int n, const float* __restrict__ z32, const double* __restrict__ r,
                                                       double* __restrict__ p, float2* __restrict__ p2, double* partial,
                                                       CgState* st) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
-    if (i < n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double zi = (double)z32[i];
         p[i] = zi;
         if (p2) p2[i] = make_float2(z32[i], 0.f);
-        v[0] = r[i] * zi;
+        v[0] += r[i] * zi;
     }
     if (grid_reduce<1>(v, partial, &st->ticket)) st->rz = v[0];
 }
@@ -571,15 +577,14 @@ __global__ void __launch_bounds__(kBlock) k_pcg_update(int n, double* __restrict
                                                        const double* __restrict__ p, const double* __restrict__ q,
                                                        float* __restrict__ r32, double* partial, CgState* st) {
     if (st->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const double alpha = st->alpha;
     double v[1] = {0.0};
-    if (i < n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         x[i] += alpha * p[i];
         const double ri = r[i] - alpha * q[i];
         r[i] = ri;
         r32[i] = (float)ri;
-        v[0] = ri * ri;
+        v[0] += ri * ri;
     }
     if (grid_reduce<1>(v, partial, &st->ticket)) {
         st->iter += 1;
@@ -591,9 +596,8 @@ __global__ void __launch_bounds__(kBlock) k_pcg_update(int n, double* __restrict
 __global__ void __launch_bounds__(kBlock) k_pcg_rz(int n, const float* __restrict__ z32, const double* __restrict__ r,
                                                    double* partial, CgState* st) {
     if (st->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
-    if (i < n) v[0] = r[i] * (double)z32[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[0] += r[i] * (double)z32[i];
     if (grid_reduce<1>(v, partial, &st->ticket)) {
         st->beta = v[0] / st->rz;
         st->rz = v[0];
@@ -603,7 +607,7 @@ __global__ void __launch_bounds__(kBlock) k_pcg_rz(int n, const float* __restric
 // element matrices (378 packed upper-triangle FP64 entries per cell) to FP32 in block order and
 // cyclic-half layout: entry 27 t + i of position p is K(i, (i + t) mod 27) of cell perm[p]
 __global__ void k_ke_cyclic(long long total, const int32_t* __restrict__ perm, const double* __restrict__ ke,
-                            float* __restrict__ out) {
+                            float* __restrict__ out, float* __restrict__ out_lo) {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (idx >= total) return;
     const long long p = idx / 378;
@@ -611,7 +615,10 @@ __global__ void k_ke_cyclic(long long total, const int32_t* __restrict__ perm, c
     int j = i + t;
     if (j >= 27) j -= 27;
     const int lo = i < j ? i : j, hi = i < j ? j : i;
-    out[idx] = (float)ke[378 * (size_t)perm[p] + lo * 27 - (lo * (lo - 1)) / 2 + (hi - lo)];
+    const double v = ke[378 * (size_t)perm[p] + lo * 27 - (lo * (lo - 1)) / 2 + (hi - lo)];
+    const float h = (float)v;
+    out[idx] = h;
+    if (out_lo) out_lo[idx] = (float)(v - (double)h);
 }
 
 
@@ -644,6 +651,233 @@ __global__ void __launch_bounds__(kBlock) k_pcg_direction(int n, const float* __
     }
 }
 
+// ---- outer SpMV of the Q2 multigrid PCG by cell blocks (the level-0 smoother's blocks,
+// cell_blocks.h), FP64-accurate from FP32 pairs: q = A p and p.q. K_e as hi/lo pairs in the
+// cyclic-half layout; lane i < 27 of a warp owns row i of a cell, forms K(i, i+t) p_{i+t} with
+// an error-free product and hands the pair K(i, i+t) p_i (product, rounding error + cross terms)
+// to lane i+t, all sums compensated (TwoSum). Columns and rows of Dirichlet DoFs follow the
+// eliminated matrix: p is taken as 0 on them and their q is diag * p.
+struct CbSpmvArgs {
+    int n_blocks, max_cells, max_dofs, n_bnd;
+    const float* khi;
+    const float* klo;
+    const int32_t* cell_start;
+    const int32_t* dof_start;
+    const int32_t* dof_list;
+    const int32_t* slot;
+    const int32_t* bnd_dofs;
+    const int32_t* bnd_ptr;
+    const uint16_t* item_end;
+    const uint16_t* loc;
+    const uint16_t* items;
+    const int8_t* fixed;
+    float2* pair;   // partial (hi, lo) sums of the split DoFs, one per slot
+    double* dot;    // p.q partials: one per block, then one per CTA of the finishing kernel
+};
+constexpr int kCbT = 256;
+__host__ __device__ inline size_t cbdf_smem_bytes(int max_cells, int max_dofs) {
+    return 56 * (size_t)max_cells + 8 * (size_t)max_dofs + 216 * (size_t)max_cells;
+}
+
+// one cell's row i (lane) of K_e p_e, (hi, lo) pair; kh/kl: K(i, i+t), t = 0..13
+__device__ __forceinline__ void cb_row_df(const float (&kh)[14], const float (&kl)[14], float ph, float pl, int lane,
+                                          float& sh, float& sl) {
+    sh = 0.f;
+    sl = 0.f;
+    df_term(sh, sl, kh[0], kl[0], ph, pl);
+#pragma unroll
+    for (int t = 1; t < 14; ++t) {
+        int up = lane + t;
+        if (up >= 27) up -= 27;
+        int dn = lane - t;
+        if (dn < 0) dn += 27;
+        const float uh = __shfl_sync(0xffffffffu, ph, up);
+        const float ul = __shfl_sync(0xffffffffu, pl, up);
+        const float prod = __fmul_rn(kh[t], ph);
+        const float perr = __fmaf_rn(kh[t], ph, -prod);
+        const float cross = __fadd_rn(__fmaf_rn(kh[t], pl, __fmul_rn(kl[t], ph)), perr);
+        const float rp = __shfl_sync(0xffffffffu, prod, dn);
+        const float rc = __shfl_sync(0xffffffffu, cross, dn);
+        df_term(sh, sl, kh[t], kl[t], uh, ul);
+        df_add(sh, sl, rp, rc);
+    }
+}
+
+__global__ void __launch_bounds__(kCbT, 2) k_cb_spmv_df(CbSpmvArgs a, const float2* __restrict__ p2,
+                                                        const double* __restrict__ p, const double* __restrict__ dinv,
+                                                        double* __restrict__ q, const CgState* st) {
+    if (st->done) return;
+    extern __shared__ __align__(16) unsigned char cbdf_raw[];
+    __shared__ double red[32];
+    const int blk = blockIdx.x;
+    const int p0 = a.cell_start[blk], nb = a.cell_start[blk + 1] - p0;
+    const int q0 = a.dof_start[blk], nq = a.dof_start[blk + 1] - q0;
+    uint16_t* sit = reinterpret_cast<uint16_t*>(cbdf_raw);
+    float2* sp = reinterpret_cast<float2*>(cbdf_raw + 56 * (size_t)a.max_cells);
+    float2* sy = sp + a.max_dofs;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int il = lane < 27 ? lane : 26;  // lanes 27..31 shadow lane 26 and store nothing
+    {
+        const uint2* gi = reinterpret_cast<const uint2*>(a.items + 28 * (size_t)p0);
+        uint2* si = reinterpret_cast<uint2*>(sit);
+        const int nw = 7 * nb;
+        uint2 w8[7];
+#pragma unroll
+        for (int r = 0; r < 7; ++r) {
+            const int w = tid + r * kCbT;
+            if (w < nw) w8[r] = __ldg(gi + w);
+        }
+#pragma unroll
+        for (int r0 = 0; r0 < 16; r0 += 8) {
+            int gd[8];
+            float2 pv[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int k = tid + (r0 + r) * kCbT;
+                gd[r] = k < nq ? __ldg(a.dof_list + q0 + k) : 0;
+            }
+            int fx[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int k = tid + (r0 + r) * kCbT;
+                pv[r] = k < nq ? __ldg(p2 + gd[r]) : make_float2(0.f, 0.f);
+                fx[r] = k < nq ? a.fixed[gd[r]] : 0;
+            }
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                if (fx[r]) pv[r] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int k = tid + (r0 + r) * kCbT;
+                if (k < nq) sp[k] = pv[r];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 7; ++r) {
+            const int w = tid + r * kCbT;
+            if (w < nw) si[w] = w8[r];
+        }
+    }
+    __syncthreads();
+    const uint16_t* loc = a.loc + 27 * (size_t)p0;
+    for (int c = 2 * warp; c < nb; c += 2 * (kCbT / 32)) {
+        const int c1i = c + 1 < nb ? c + 1 : c;
+        float kh0[14], kl0[14], kh1[14], kl1[14];
+        const size_t o0 = 378 * (size_t)(p0 + c), o1 = 378 * (size_t)(p0 + c1i);
+#pragma unroll
+        for (int t = 0; t < 14; ++t) {
+            kh0[t] = __ldg(a.khi + o0 + 27 * t + il);
+            kl0[t] = __ldg(a.klo + o0 + 27 * t + il);
+            kh1[t] = __ldg(a.khi + o1 + 27 * t + il);
+            kl1[t] = __ldg(a.klo + o1 + 27 * t + il);
+        }
+        const float2 v0 = sp[__ldg(loc + 27 * c + il)];
+        const float2 v1 = sp[__ldg(loc + 27 * c1i + il)];
+        float h0, l0, h1, l1;
+        cb_row_df(kh0, kl0, v0.x, v0.y, lane, h0, l0);
+        cb_row_df(kh1, kl1, v1.x, v1.y, lane, h1, l1);
+        if (lane < 27) {
+            sy[27 * c + lane] = make_float2(h0, l0);
+            if (c1i != c) sy[27 * c1i + lane] = make_float2(h1, l1);
+        }
+    }
+    __syncthreads();
+    double v[1] = {0.0};
+#pragma unroll 1
+    for (int r0 = 0; r0 < 16; r0 += 8) {
+        if (tid + r0 * kCbT >= nq) break;
+        int e0[8], e1[8], sl[8], g[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int k = tid + (r0 + r) * kCbT;
+            const bool ok = k < nq;
+            e1[r] = ok ? __ldg(a.item_end + q0 + k) : 0;
+            e0[r] = ok && k ? __ldg(a.item_end + q0 + k - 1) : 0;
+            sl[r] = ok ? __ldg(a.slot + q0 + k) : -2;
+            g[r] = ok ? __ldg(a.dof_list + q0 + k) : 0;
+        }
+        double pf[8], dv[8];
+        int fx[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const bool own = sl[r] == -1;
+            pf[r] = own ? p[g[r]] : 0.0;
+            fx[r] = own ? a.fixed[g[r]] : 0;
+            dv[r] = own && fx[r] ? dinv[g[r]] : 1.0;
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            float h = 0.f, l = 0.f;
+            for (int e = e0[r]; e < e1[r]; ++e) {
+                const float2 y = sy[sit[e]];
+                df_add(h, l, y.x, y.y);
+            }
+            if (sl[r] >= 0) {
+                a.pair[sl[r]] = make_float2(h, l);
+            } else if (sl[r] == -1) {
+                const double qg = fx[r] ? pf[r] / dv[r] : (double)h + (double)l;
+                q[g[r]] = qg;
+                v[0] += pf[r] * qg;
+            }
+        }
+    }
+    block_reduce<1>(v, red);
+    if (tid == 0) a.dot[blk] = v[0];
+}
+
+// the split DoFs: their slot pairs summed in ascending block order; then p.q over all blocks
+// and CTAs (fixed order) and alpha = rz / p.q
+__global__ void __launch_bounds__(kBlock) k_cb_spmv_finish(CbSpmvArgs a, const double* __restrict__ p,
+                                                           const double* __restrict__ dinv, double* __restrict__ q,
+                                                           CgState* st) {
+    if (st->done) return;
+    __shared__ double red[32];
+    __shared__ bool last;
+    double v[1] = {0.0};
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < a.n_bnd; j += gridDim.x * blockDim.x) {
+        const int g = a.bnd_dofs[j];
+        const double pg = p[g];
+        double qg;
+        if (a.fixed[g]) {
+            qg = pg / dinv[g];
+        } else {
+            float h = 0.f, l = 0.f;
+            for (int s = a.bnd_ptr[j]; s < a.bnd_ptr[j + 1]; ++s) {
+                const float2 y = a.pair[s];
+                df_add(h, l, y.x, y.y);
+            }
+            qg = (double)h + (double)l;
+        }
+        q[g] = qg;
+        v[0] += pg * qg;
+    }
+    block_reduce<1>(v, red);
+    if (threadIdx.x == 0) {
+        a.dot[a.n_blocks + blockIdx.x] = v[0];
+        __threadfence();
+        last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double acc[1] = {0.0};
+    const int total = a.n_blocks + (int)gridDim.x, bd = (int)blockDim.x;
+    for (int b = threadIdx.x; b < total; b += 4 * bd) {
+        double t[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t[u] = b + u * bd < total ? __ldcg(a.dot + b + u * bd) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[0] += t[u];
+    }
+    __syncthreads();
+    block_reduce<1>(acc, red);
+    if (threadIdx.x == 0) {
+        st->pq = acc[0];
+        st->alpha = st->rz / acc[0];
+        st->ticket = 0;
+    }
+}
+
 }  // namespace
 
 // ==================================================================== FemDevice
@@ -651,6 +885,7 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
     : fs_(std::move(fs)), pm_(&pm), stream_(stream), n_(fs_.n_dofs), nc_(fs_.n_cells) {
     cudaStream_t s = stream_;
     level0_ebe_ = fs_.order == 2;
+    outer_mode_ = fs_.order == 2 ? 2 : 1;
     cell_dofs_.upload(fs_.cell_dofs, s);
     r2c_ptr_.upload(fs_.r2c_ptr, s);
     r2c_item_.upload(fs_.r2c_item, s);
@@ -779,7 +1014,7 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
             q2_cell_stiffness(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), stream_);
             q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
                              r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
-            if (level0_ebe_) refresh_ke32();
+            if (level0_ebe_ || outer_mode_ == 2) refresh_ke32();
         }
         fixed_.resize(n_);
         FGB_LAUNCH(k_fixed_flags<<<gb, kBlock, 0, stream_>>>(n_, bc_.get(), anode_dirichlet ? 1 : 0, fixed_.get()));
@@ -940,7 +1175,7 @@ int FemDevice::solve_plain(const SolveOptions& opt, SolveStats* st) {
     const int gb = grid_for(n_, kBlock);
     CgState* ds = state_.get();
     // ||b||
-    FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
+    FGB_LAUNCH(k_norm2<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
     FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
     FGB_CUDA(cudaStreamSynchronize(stream_));
     const double bnorm = std::sqrt(h_state_->rr);
@@ -971,7 +1206,7 @@ int FemDevice::solve_plain(const SolveOptions& opt, SolveStats* st) {
 int FemDevice::solve_mixed(const SolveOptions& opt, SolveStats* st) {
     const int gb = grid_for(n_, kBlock);
     CgState* ds = state_.get();
-    FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
+    FGB_LAUNCH(k_norm2<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
     FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
     FGB_CUDA(cudaStreamSynchronize(stream_));
     const double bnorm = std::sqrt(h_state_->rr);
@@ -1054,7 +1289,7 @@ double FemDevice::estimate_lambda(int iters, uint64_t seed) {
         FGB_LAUNCH(k_sell_spmv<double><<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
                                                                    sell64_.get(), p64_.get(), q64_.get()));
         FGB_LAUNCH(k_scale_mul<<<gb, kBlock, 0, stream_>>>(n_, q64_.get(), dinv64_.get(), 1.0));
-        FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, q64_.get(), partial_.get(), ds));
+        FGB_LAUNCH(k_norm2<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, q64_.get(), partial_.get(), ds));
         FGB_CUDA(cudaMemcpyAsync(h_state_ + 1, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
         FGB_CUDA(cudaStreamSynchronize(stream_));
         const double ny = std::sqrt(h_state_[1].rr);
@@ -1247,8 +1482,9 @@ void FemDevice::ensure_split() {
 }
 
 void FemDevice::set_outer_spmv(int mode) {
-    FGB_REQUIRE(mode == 0 || mode == 1, "outer SpMV mode 0 (FP64) or 1 (FP32 pairs)");
-    outer_df_ = mode == 1;
+    FGB_REQUIRE(mode >= 0 && mode <= 2, "outer SpMV mode 0 (FP64), 1 (FP32 pairs) or 2 (cell blocks)");
+    FGB_REQUIRE(mode != 2 || fs_.order == 2, "the cell-block outer SpMV is for Q2 fields");
+    outer_mode_ = mode;
 }
 
 void FemDevice::ensure_cell_blocks() {
@@ -1282,8 +1518,18 @@ void FemDevice::ensure_cell_blocks() {
 void FemDevice::refresh_ke32() {
     ensure_cell_blocks();
     ke32_.resize(378 * (size_t)nc_);
-    FGB_LAUNCH(k_ke_cyclic<<<grid_for(378LL * nc_, kBlock), kBlock, 0, stream_>>>(378LL * nc_, cb_->perm.get(),
-                                                                                 ke_.get(), ke32_.get()));
+    if (outer_mode_ == 2) ke32lo_.resize(378 * (size_t)nc_);
+    FGB_LAUNCH(k_ke_cyclic<<<grid_for(378LL * nc_, kBlock), kBlock, 0, stream_>>>(
+        378LL * nc_, cb_->perm.get(), ke_.get(), ke32_.get(), outer_mode_ == 2 ? ke32lo_.get() : nullptr));
+}
+
+double FemDevice::outer_spmv_bytes() const {
+    if (outer_mode_ != 2 || !cb_) return (double)fs_.nnz() * 12.0 + 24.0 * n_;
+    // per cell: K_e hi + lo (378 x 8), loc (27 x 2) and items (28 x 2); per block-local DoF: its
+    // id, item end, slot, the p pair gathered and the Dirichlet flag; per DoF: q written and p
+    // read for p.q; per slot: the pair written and read; per split DoF: its id and slot range
+    const CellBlocksDev& c = *cb_;
+    return nc_ * (3024.0 + 110.0) + (double)c.n_local * 19.0 + 16.0 * n_ + 16.0 * c.n_slots + 8.0 * c.n_bnd;
 }
 
 void FemDevice::set_level0_ebe(bool on) {
@@ -1310,7 +1556,7 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     st->levels = amg_->n_levels();
     const int gb = grid_for(n_, kBlock);
     CgState* ds = state_.get();
-    FGB_LAUNCH(k_norm2<<<gb, kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
+    FGB_LAUNCH(k_norm2<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
     FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
     FGB_CUDA(cudaStreamSynchronize(stream_));
     const double bnorm = std::sqrt(h_state_->rr);
@@ -1327,10 +1573,33 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     int status = 0, it = 0, restarts = 0;
     double rr_true = h_state_->rr;
     if (rr_true <= init.tol2 || bnorm == 0) status = 1;
-    const bool df = outer_df_;
+    const int mode = outer_mode_;
+    const bool df = mode >= 1;
+    CbSpmvArgs ca{};
+    int cb_grid = 1;
+    size_t cb_smem = 0;
     if (df && status == 0) {
-        ensure_split();
+        if (mode == 1) ensure_split();
         p2_.resize(n_);
+    }
+    if (mode == 2 && status == 0) {
+        ensure_cell_blocks();
+        if (ke32_.size() != 378 * (size_t)nc_ || ke32lo_.size() != 378 * (size_t)nc_) refresh_ke32();
+        CellBlocksDev& c = *cb_;
+        cb_grid = reduce_grid(c.n_bnd, kBlock);
+        cb_pair_.resize(std::max(1, c.n_slots));
+        cb_dot_.resize((size_t)c.n_blocks + cb_grid);
+        cb_smem = cbdf_smem_bytes(c.max_cells, c.max_dofs);
+        if (!cb_spmv_attr_) {
+            // the cap is a property of the kernel, shared by every mesh: always the largest block's
+            FGB_REQUIRE(c.max_cells <= 256 && c.max_dofs <= 4096, "cell blocks too large");
+            FGB_CUDA(cudaFuncSetAttribute(k_cb_spmv_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)cbdf_smem_bytes(256, 4096)));
+            cb_spmv_attr_ = true;
+        }
+        ca = CbSpmvArgs{c.n_blocks, c.max_cells, c.max_dofs, c.n_bnd, ke32_.get(), ke32lo_.get(), c.cell_start.get(),
+                        c.dof_start.get(), c.dof_list.get(), c.slot.get(), c.bnd_dofs.get(), c.bnd_ptr.get(),
+                        c.item_end.get(), c.loc.get(), c.items.get(), fixed_.get(), cb_pair_.get(), cb_dot_.get()};
     }
     float2* p2 = df ? p2_.get() : nullptr;
     // Convergence is declared on the FP64 true residual b - A x: when the recursion reports
@@ -1339,10 +1608,14 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     while (status == 0) {
         FGB_LAUNCH(k_to32<<<gb, kBlock, 0, stream_>>>(n_, r64_.get(), r32_.get()));
         const float* z = amg_->vcycle(r32_.get());
-        FGB_LAUNCH(k_pcg_start<<<gb, kBlock, 0, stream_>>>(n_, z, r64_.get(), p64_.get(), p2, partial_.get(), ds));
+        FGB_LAUNCH(k_pcg_start<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, z, r64_.get(), p64_.get(), p2, partial_.get(), ds));
         while (true) {
             spmv_timer_.begin(stream_);
-            if (df)
+            if (mode == 2) {
+                FGB_LAUNCH(k_cb_spmv_df<<<ca.n_blocks, kCbT, cb_smem, stream_>>>(ca, p2, p64_.get(), dinv64_.get(),
+                                                                                 q64_.get(), ds));
+                FGB_LAUNCH(k_cb_spmv_finish<<<cb_grid, kBlock, 0, stream_>>>(ca, p64_.get(), dinv64_.get(), q64_.get(), ds));
+            } else if (df)
                 FGB_LAUNCH(k_cg_spmv_pq_df<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
                                                                       sell32_.get(), sell_lo_.get(), p2, p64_.get(),
                                                                       q64_.get(), partial_.get(), ds));
@@ -1351,7 +1624,7 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
                                                                             sell_col_.get(), sell64_.get(), p64_.get(),
                                                                             q64_.get(), partial_.get(), ds));
             spmv_timer_.end(stream_);
-            FGB_LAUNCH(k_pcg_update<<<gb, kBlock, 0, stream_>>>(n_, x_.get(), r64_.get(), p64_.get(), q64_.get(), r32_.get(),
+            FGB_LAUNCH(k_pcg_update<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, x_.get(), r64_.get(), p64_.get(), q64_.get(), r32_.get(),
                                                                partial_.get(), ds));
             FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
             FGB_CUDA(cudaStreamSynchronize(stream_));
@@ -1361,7 +1634,7 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
                 break;
             }
             const float* zi = amg_->vcycle(r32_.get());
-            FGB_LAUNCH(k_pcg_rz<<<gb, kBlock, 0, stream_>>>(n_, zi, r64_.get(), partial_.get(), ds));
+            FGB_LAUNCH(k_pcg_rz<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, zi, r64_.get(), partial_.get(), ds));
             FGB_LAUNCH(k_pcg_direction<<<gb, kBlock, 0, stream_>>>(n_, zi, p64_.get(), p2, ds));
         }
         // true FP64 residual of the current x (also the restart residual)

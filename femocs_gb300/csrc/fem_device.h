@@ -102,10 +102,14 @@ public:
     // default: 4.3 vs 8.95 GB per smoothing step on config 2), or through the assembled SELL
     // matrix; the hierarchy is rebuilt at the next solve
     void set_level0_ebe(bool on);
-    // outer SpMV of the multigrid PCG: 1 = FP32 hi/lo pairs with error-free products (default;
-    // FP64-accurate to ~2^-48 per term, off the FP64 pipe: config 2 Q2 2.27 vs 2.92 ms per
-    // launch, Q1 0.21 vs 0.25 ms), 0 = the FP64 matrix
+    // outer SpMV of the multigrid PCG: 1 = the SELL matrix as FP32 hi/lo pairs with error-free
+    // products (Q1 default; FP64-accurate to ~2^-48 per term, off the FP64 pipe), 2 = the same
+    // arithmetic element by element over the cell blocks (Q2 default: half the bytes of the
+    // assembled pairs), 0 = the FP64 SELL matrix
     void set_outer_spmv(int mode);
+    int outer_spmv() const { return outer_mode_; }
+    // algorithmic bytes of one outer SpMV launch in the current mode
+    double outer_spmv_bytes() const;
     ~FemDevice();
 
     // PoissonSolver::setup + assemble verbs (src/PoissonSolver.cpp:162-210)
@@ -179,7 +183,7 @@ private:
     double smooth_lo_ = 0;
     int q1_gauss_ = 2;  // Gauss points per direction of the Q1 element integrals
     bool level0_ebe_ = false;
-    bool outer_df_ = true;
+    int outer_mode_ = 1;
     bool split_valid_ = false;
     DBuf<float> sell_lo_;  // low FP32 part of the matrix values (high part: sell32_)
     DBuf<float2> p2_;      // p as interleaved FP32 (hi, lo) pairs
@@ -188,7 +192,11 @@ private:
     struct CellBlocksDev;
     std::unique_ptr<CellBlocksDev> cb_;
     void ensure_cell_blocks();
-    void refresh_ke32();    // element matrices (ke_) into ke32_
+    void refresh_ke32();    // element matrices (ke_) into ke32_ (and ke32lo_ for outer mode 2)
+    DBuf<float> ke32lo_;    // low FP32 parts of the element matrices, same layout as ke32_
+    DBuf<float2> cb_pair_;  // outer mode 2: partial (hi, lo) sums of the split DoFs
+    DBuf<double> cb_dot_;   // outer mode 2: p.q partials
+    bool cb_spmv_attr_ = false;
     DBuf<int8_t> fixed_;    // 1 on Dirichlet rows of the current anode mode
     LaunchTimer spmv_timer_;
     int n_, nc_;

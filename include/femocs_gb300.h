@@ -162,10 +162,14 @@ int fgb_field_last_stats(const FGB_FIELD* f, double* out14);
  * half the bytes of the SELL matrix) or through the assembled SELL matrix (0); the hierarchy is
  * rebuilt at the next solve */
 int fgb_field_set_level0_ebe(FGB_FIELD* f, int on);
-/* outer SpMV of the multigrid PCG: 1 (default) reads the matrix and the search direction as FP32
- * hi/lo pairs with error-free products and compensated row sums (FP64-accurate to ~2^-48 per
- * term, off the FP64 pipe); 0 uses the FP64 matrix */
+/* outer SpMV of the multigrid PCG: 1 (Q1 default) reads the SELL matrix and the search
+ * direction as FP32 hi/lo pairs with error-free products and compensated row sums (FP64-accurate
+ * to ~2^-48 per term, off the FP64 pipe); 2 (Q2 default, Q2 only) does the same arithmetic
+ * element by element over cell blocks (half the bytes); 0 uses the FP64 SELL matrix */
 int fgb_field_set_outer_spmv(FGB_FIELD* f, int mode);
+/* algorithmic bytes of one outer SpMV launch in the current mode (cell-block counts once the
+ * blocks exist, i.e. after the first solve in mode 2) */
+double fgb_field_outer_spmv_bytes(const FGB_FIELD* f);
 /* Chebyshev smoothing of the finest multigrid level: steps before and after the coarse
  * correction (0: default, Q1 4, Q2 2) and the interval's lower end as a fraction of
  * lambda_max (0: default, Q1 0.04, Q2 0.1); the hierarchy is rebuilt at the next solve */
