@@ -196,9 +196,10 @@ __host__ __device__ inline size_t cb_smem_bytes(int max_cells, int max_dofs) {
 // One block per CTA, three phases separated by barriers:
 //  A  the block's item lists and x of its DoFs into shared memory (each thread's loads issued
 //     together, so the gathers overlap instead of queueing behind one another);
-//  B  K_e x_e of each cell: one warp per two cells, lane i < 27 owns row i. It holds K(i, i+t)
-//     for t = 0..13, takes x_{i+t} from lane i+t and hands K(i, i+t) x_i to lane i+t (indices
-//     mod 27), so every entry of the symmetric K_e is loaded once;
+//  B  K_e x_e of each cell: one warp per cell, lane i < 27 owns row i. It holds K(i, i+t) for
+//     t = 0..13 (seven float2 loads), takes x_{i+t} from lane i+t and hands K(i, i+t) x_i to
+//     lane i+t (indices mod 27), so every entry of the symmetric K_e is loaded once; the next
+//     cell's matrix is loaded while the current one is applied;
 //  C  the products of each DoF summed in item order; complete DoFs finished (Chebyshev update
 //     or residual), the others leave their partial sum in their slot.
 template <int KIND>
@@ -216,22 +217,22 @@ __global__ void __launch_bounds__(kCb, 3) k_cb_apply(EbeOperator op, const float
     const int lane = tid & 31, warp = tid >> 5;
     const int il = lane < 27 ? lane : 26;  // lanes 27..31 shadow lane 26 and store nothing
     const uint16_t* loc = op.loc + 27 * (size_t)p0;
-    // the element matrices of the warp's first two cells are requested first, so that they
-    // travel while phase A gathers
-    float k0[14], k1[14];
-    int l0 = 0, l1 = 0;
-    if (2 * warp < nb) {
-        const int c = 2 * warp, c1i = c + 1 < nb ? c + 1 : c;
-        const float* K0 = op.ke + 378 * (size_t)(p0 + c);
-        const float* K1 = op.ke + 378 * (size_t)(p0 + c1i);
+    // cells of warp w: w, w + 8, w + 16, ...; two register sets (A, B) alternate so that the
+    // next cell's element matrix is in flight while the current one is applied. The first
+    // cell's is requested before phase A, so that it travels while the gathers run.
+    float kA[14], kB[14];
+    int lA = 0, lB = 0;
+    auto load_cell = [&](int c, float (&k)[14], int& l) {
+        const float2* K = reinterpret_cast<const float2*>(op.ke + 378 * (size_t)(p0 + c));
 #pragma unroll
-        for (int t = 0; t < 14; ++t) {
-            k0[t] = __ldg(K0 + 27 * t + il);
-            k1[t] = __ldg(K1 + 27 * t + il);
+        for (int u = 0; u < 7; ++u) {
+            const float2 v = __ldg(K + 27 * u + il);
+            k[2 * u] = v.x;
+            k[2 * u + 1] = v.y;
         }
-        l0 = __ldg(loc + 27 * c + il);
-        l1 = __ldg(loc + 27 * c1i + il);
-    }
+        l = __ldg(loc + 27 * c + il);
+    };
+    if (warp < nb) load_cell(warp, kA, lA);
     {
         const uint2* gi = reinterpret_cast<const uint2*>(op.items + 28 * (size_t)p0);
         uint2* si = reinterpret_cast<uint2*>(sit);
@@ -269,39 +270,31 @@ __global__ void __launch_bounds__(kCb, 3) k_cb_apply(EbeOperator op, const float
         }
     }
     __syncthreads();
-    for (int c = 2 * warp; c < nb; c += 2 * (kCb / 32)) {
-        const int c1i = c + 1 < nb ? c + 1 : c;
-        if (c != 2 * warp) {
-            const float* K0 = op.ke + 378 * (size_t)(p0 + c);
-            const float* K1 = op.ke + 378 * (size_t)(p0 + c1i);
+    // source lanes of the shuffles, (lane +- t) mod 27, the same for every cell
+    int up[14], dn[14];
 #pragma unroll
-            for (int t = 0; t < 14; ++t) {
-                k0[t] = __ldg(K0 + 27 * t + il);
-                k1[t] = __ldg(K1 + 27 * t + il);
-            }
-            l0 = __ldg(loc + 27 * c + il);
-            l1 = __ldg(loc + 27 * c1i + il);
-        }
-        const float x0 = sx[l0];
-        const float x1 = sx[l1];
-        float y0 = k0[0] * x0, y1 = k1[0] * x1;
+    for (int t = 1; t < 14; ++t) {
+        up[t] = lane + t >= 27 ? lane + t - 27 : lane + t;
+        dn[t] = lane - t < 0 ? lane - t + 27 : lane - t;
+    }
+    auto apply_cell = [&](int c, const float (&k)[14], int l) {
+        const float x = sx[l];
+        float y = k[0] * x;
 #pragma unroll
         for (int t = 1; t < 14; ++t) {
-            int up = lane + t;
-            if (up >= 27) up -= 27;
-            int dn = lane - t;
-            if (dn < 0) dn += 27;
-            const float xu0 = __shfl_sync(0xffffffffu, x0, up);
-            const float xu1 = __shfl_sync(0xffffffffu, x1, up);
-            const float tr0 = __shfl_sync(0xffffffffu, k0[t] * x0, dn);
-            const float tr1 = __shfl_sync(0xffffffffu, k1[t] * x1, dn);
-            y0 = fmaf(k0[t], xu0, y0) + tr0;
-            y1 = fmaf(k1[t], xu1, y1) + tr1;
+            const float xu = __shfl_sync(0xffffffffu, x, up[t]);
+            const float tr = __shfl_sync(0xffffffffu, k[t] * x, dn[t]);
+            y = fmaf(k[t], xu, y) + tr;
         }
-        if (lane < 27) {
-            sy[27 * c + lane] = y0;
-            if (c1i != c) sy[27 * c1i + lane] = y1;
-        }
+        if (lane < 27) sy[27 * c + lane] = y;
+    };
+    constexpr int kW = kCb / 32;
+    for (int c = warp; c < nb; c += 2 * kW) {
+        if (c + kW < nb) load_cell(c + kW, kB, lB);
+        apply_cell(c, kA, lA);
+        if (c + kW >= nb) break;
+        if (c + 2 * kW < nb) load_cell(c + 2 * kW, kA, lA);
+        apply_cell(c + kW, kB, lB);
     }
     __syncthreads();
 #pragma unroll 1

@@ -59,8 +59,8 @@ struct AmgDevLevel;
 struct EbeOperator {
     int n_cells = 0, n_blocks = 0, max_cells = 0, max_dofs = 0, n_bnd = 0, n_slots = 0;
     int64_t n_local = 0;
-    // 378 per block position, cyclic half of K_e: entry 27 t + i = K_e(i, (i + t) mod 27),
-    // t = 0..13 (27 is odd, so every off-diagonal pair appears exactly once)
+    // 378 per block position, cyclic half of K_e: K_e(i, (i + t) mod 27) for t = 0..13 (27 is
+    // odd, so every off-diagonal pair appears exactly once), stored at 54 (t / 2) + 2 i + t % 2
     const float* ke = nullptr;
     const int32_t* cell_start = nullptr;  // block -> first position
     const int32_t* dof_start = nullptr;   // block -> first local DoF entry

@@ -605,13 +605,14 @@ __global__ void __launch_bounds__(kBlock) k_pcg_rz(int n, const float* __restric
 }
 
 // element matrices (378 packed upper-triangle FP64 entries per cell) to FP32 in block order and
-// cyclic-half layout: entry 27 t + i of position p is K(i, (i + t) mod 27) of cell perm[p]
+// cyclic-half layout, t paired: entry 54 u + 2 i + s of position p is K(i, (i + t) mod 27) of
+// cell perm[p] with t = 2 u + s (u = 0..6, s = 0, 1), so lane i reads (t, t+1) as one float2
 __global__ void k_ke_cyclic(long long total, const int32_t* __restrict__ perm, const double* __restrict__ ke,
                             float* __restrict__ out, float* __restrict__ out_lo) {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (idx >= total) return;
     const long long p = idx / 378;
-    const int e = (int)(idx - p * 378), t = e / 27, i = e - 27 * t;
+    const int e = (int)(idx - p * 378), u = e / 54, rem = e - 54 * u, i = rem >> 1, t = 2 * u + (rem & 1);
     int j = i + t;
     if (j >= 27) j -= 27;
     const int lo = i < j ? i : j, hi = i < j ? j : i;
@@ -760,26 +761,37 @@ __global__ void __launch_bounds__(kCbT, 2) k_cb_spmv_df(CbSpmvArgs a, const floa
     }
     __syncthreads();
     const uint16_t* loc = a.loc + 27 * (size_t)p0;
-    for (int c = 2 * warp; c < nb; c += 2 * (kCbT / 32)) {
-        const int c1i = c + 1 < nb ? c + 1 : c;
-        float kh0[14], kl0[14], kh1[14], kl1[14];
-        const size_t o0 = 378 * (size_t)(p0 + c), o1 = 378 * (size_t)(p0 + c1i);
+    // one warp per cell (w, w + 8, ...); two register sets alternate so that the next cell's
+    // hi/lo element matrix is in flight while the current one is applied
+    float hA[14], lA[14], hB[14], lB[14];
+    int iA = 0, iB = 0;
+    auto load_cell = [&](int c, float (&kh)[14], float (&kl)[14], int& li) {
+        const float2* hp = reinterpret_cast<const float2*>(a.khi + 378 * (size_t)(p0 + c));
+        const float2* lp = reinterpret_cast<const float2*>(a.klo + 378 * (size_t)(p0 + c));
 #pragma unroll
-        for (int t = 0; t < 14; ++t) {
-            kh0[t] = __ldg(a.khi + o0 + 27 * t + il);
-            kl0[t] = __ldg(a.klo + o0 + 27 * t + il);
-            kh1[t] = __ldg(a.khi + o1 + 27 * t + il);
-            kl1[t] = __ldg(a.klo + o1 + 27 * t + il);
+        for (int u = 0; u < 7; ++u) {
+            const float2 x = __ldg(hp + 27 * u + il), y = __ldg(lp + 27 * u + il);
+            kh[2 * u] = x.x;
+            kh[2 * u + 1] = x.y;
+            kl[2 * u] = y.x;
+            kl[2 * u + 1] = y.y;
         }
-        const float2 v0 = sp[__ldg(loc + 27 * c + il)];
-        const float2 v1 = sp[__ldg(loc + 27 * c1i + il)];
-        float h0, l0, h1, l1;
-        cb_row_df(kh0, kl0, v0.x, v0.y, lane, h0, l0);
-        cb_row_df(kh1, kl1, v1.x, v1.y, lane, h1, l1);
-        if (lane < 27) {
-            sy[27 * c + lane] = make_float2(h0, l0);
-            if (c1i != c) sy[27 * c1i + lane] = make_float2(h1, l1);
-        }
+        li = __ldg(loc + 27 * c + il);
+    };
+    auto apply_cell = [&](int c, const float (&kh)[14], const float (&kl)[14], int li) {
+        const float2 pv = sp[li];
+        float h, l;
+        cb_row_df(kh, kl, pv.x, pv.y, lane, h, l);
+        if (lane < 27) sy[27 * c + lane] = make_float2(h, l);
+    };
+    constexpr int kW = kCbT / 32;
+    if (warp < nb) load_cell(warp, hA, lA, iA);
+    for (int c = warp; c < nb; c += 2 * kW) {
+        if (c + kW < nb) load_cell(c + kW, hB, lB, iB);
+        apply_cell(c, hA, lA, iA);
+        if (c + kW >= nb) break;
+        if (c + 2 * kW < nb) load_cell(c + 2 * kW, hA, lA, iA);
+        apply_cell(c + kW, hB, lB, iB);
     }
     __syncthreads();
     double v[1] = {0.0};
