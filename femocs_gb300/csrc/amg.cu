@@ -518,6 +518,10 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
 AmgDevice::~AmgDevice() = default;
 
 int AmgDevice::n_levels() const { return (int)lv_.size(); }
+void AmgDevice::set_level0_lambda(double lambda) {
+    FGB_REQUIRE(lambda > 0 && std::isfinite(lambda), "level-0 lambda_max must be positive");
+    lv_[0]->lambda = lambda;
+}
 std::string AmgDevice::describe() const { return desc_; }
 
 void AmgDevice::cycle(int l) {

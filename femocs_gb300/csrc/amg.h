@@ -92,6 +92,9 @@ public:
     double time_smoother(int reps);
     // event pairs around every level-0 Chebyshev step of the V-cycles (when enabled)
     LaunchTimer smoother_timer;
+    // largest eigenvalue of D^-1 A on level 0 (the smoothing interval): refreshed when the
+    // level-0 matrix changes under a kept hierarchy
+    void set_level0_lambda(double lambda);
     // apply level 0 element by element (null operator: back to the SELL matrix)
     void set_level0_ebe(const EbeOperator* op);
     bool level0_ebe() const { return ebe_on_; }

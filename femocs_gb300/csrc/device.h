@@ -115,6 +115,15 @@ public:
         for (cudaEvent_t e : ev_) cudaEventDestroy(e);
     }
     bool enabled = false;
+    // create the events of n launches ahead (event creation is a host call that would otherwise
+    // fall inside the timed region)
+    void reserve(int n) {
+        while ((int)ev_.size() < 2 * n) {
+            cudaEvent_t e;
+            FGB_CUDA(cudaEventCreate(&e));
+            ev_.push_back(e);
+        }
+    }
     void begin(cudaStream_t s) {
         if (enabled) FGB_CUDA(cudaEventRecord(next(), s));
     }

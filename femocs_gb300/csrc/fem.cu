@@ -40,6 +40,7 @@ std::atomic<long long> g_kernel_launches{0};
 namespace {
 
 constexpr int kBlock = 256;
+constexpr int kProfiledLaunches = 512;  // timing events created ahead per solve (grow on demand)
 __constant__ double c_hx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
 __constant__ double c_hy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
 __constant__ double c_hz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
@@ -1050,6 +1051,10 @@ void FemDevice::assemble_from_ke(bool anode_dirichlet) {
     anode_dirichlet_ = anode_dirichlet;
     split_valid_ = false;
     assemble_q1_rows(true, anode_dirichlet);
+    // a kept multigrid hierarchy stays a symmetric positive definite preconditioner (its
+    // coarse levels are those of an earlier matrix of the same pattern); level 0 is the new
+    // matrix itself, so its smoothing interval follows the new lambda_max
+    if (amg_ && amg_anode_ == (anode_dirichlet ? 1 : 0)) amg_->set_level0_lambda(estimate_lambda(15, kAmgLambdaSeed));
 }
 
 void FemDevice::assemble_q1_rows(bool matrix, bool anode_dirichlet) {
@@ -1278,6 +1283,7 @@ void FemDevice::ensure_amg(SolveStats* st) {
     amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
                              dinv32_.get()));
     amg_->smoother_timer.enabled = profiling_;
+    if (profiling_) amg_->smoother_timer.reserve(4 * kProfiledLaunches);
     amg_anode_ = anode;
     if (st) st->setup_ms = h.setup_ms;
 }
@@ -1462,6 +1468,7 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     }
     phase("device hierarchy upload");
     amg_->smoother_timer.enabled = profiling_;
+    if (profiling_) amg_->smoother_timer.reserve(4 * kProfiledLaunches);
     amg_anode_ = anode;
     if (st) st->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -1560,7 +1567,11 @@ void FemDevice::set_smoothing(int degree, double lo) {
 void FemDevice::set_profiling(bool on) {
     profiling_ = on;
     spmv_timer_.enabled = on;
-    if (amg_) amg_->smoother_timer.enabled = on;
+    if (on) spmv_timer_.reserve(kProfiledLaunches);
+    if (amg_) {
+        amg_->smoother_timer.enabled = on;
+        if (on) amg_->smoother_timer.reserve(4 * kProfiledLaunches);
+    }
 }
 
 int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {

@@ -78,3 +78,26 @@ def test_flat_slab_known_answers():
     rc, _ = h.solve_heat(1e-12, np.zeros(h.n_faces), rel_tol=1e-12)
     T, _ = h.nodes()
     np.testing.assert_allclose(T[bulk], 300.0, rtol=1e-12)
+
+
+def test_consecutive_heat_steps_match_oracle(small):
+    """Two implicit-Euler steps: the second assembles a new matrix (kappa(T) of the first
+    step's temperatures) under the kept multigrid hierarchy; both match the oracle's chain."""
+    m, b, h = small
+    h.setup(300.0, 2.44e-8, 3.4496e-24)
+    c, _ = h.surface_faces()
+    j = 2e-3 * (1.0 + c[:, 2] / SMALL["height"])
+    q = 1e-9 * (1.0 + 0.5 * c[:, 0] / SMALL["box_half"])
+    rc, _ = h.solve_current(j, precision=2, rel_tol=1e-12)
+    assert rc > 0
+    phi_o = b.current(j)
+    dt = 1e-13
+    T_o = np.full(b.n, 300.0)
+    v2n = b.vertex2node
+    for step in range(2):
+        rc, st = h.solve_heat(dt, q, precision=2, rel_tol=1e-12)
+        assert rc > 0 and st["status"] == 1, (step, st)
+        T_o = b.heat(T_o, phi_o, dt, q, TAB_T, TAB_RHO, 2.44e-8, 3.4496e-24, 300.0)
+        T_node, _ = h.nodes()
+        rise = T_o - 300.0
+        assert np.abs((T_node[v2n] - 300.0) - rise).max() <= 1e-7 * np.abs(rise).max(), step
