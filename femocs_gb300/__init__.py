@@ -110,6 +110,17 @@ class Mesh:
             raise RuntimeError(last_error())
         return dict(n_dofs=int(o[0]), nnz=int(o[1]), n_top_faces=int(o[2]), max_row=int(o[3]))
 
+    def cell_blocks(self, cells_per_block=256, max_dofs=4096):
+        """Cell blocks of the Q2 structure (host-built and validated against every invariant the
+        Q2 element-by-element kernels rely on): counts and a digest of all arrays."""
+        o = np.zeros(8, dtype=np.int64)
+        if load().fgb_mesh_cell_blocks(self.h, int(cells_per_block), int(max_dofs), ptr(o, i64p)) != 0:
+            raise RuntimeError(last_error())
+        keys = ("n_blocks", "max_cells", "max_dofs", "n_local", "n_slots", "n_split", "n_complete")
+        d = dict(zip(keys, (int(v) for v in o[:7])))
+        d["digest"] = int(o[7].view(np.uint64))
+        return d
+
     def export(self, name):
         s = self.sizes()
         shapes = {

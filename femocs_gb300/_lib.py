@@ -79,6 +79,7 @@ _PROTOS = {
     "fgb_field_clear_space_charge": (C.c_int, [vp]),
     "fgb_device_sync": (C.c_int, []),
     "fgb_mesh_q2_sizes": (C.c_int, [vp, i64p]),
+    "fgb_mesh_cell_blocks": (C.c_int, [vp, C.c_int, C.c_int, i64p]),
     "fgb_mesh_q1_sizes": (C.c_int, [vp, i64p]),
     "fgb_mesh_structure_digest": (C.c_uint64, [vp, C.c_int, C.c_int]),
     "fgb_field_free": (None, [vp]),

@@ -10,6 +10,7 @@
 
 #include "batch.h"
 #include "bulk.h"
+#include "cell_blocks.h"
 #include "facade.h"
 #include "server.h"
 #include "femocs_gb300.h"
@@ -634,6 +635,22 @@ int fgb_mesh_q1_sizes(const FGB_MESH* m, int64_t* out4) {
         out4[1] = s.nnz();
         out4[2] = s.n_top_faces();
         out4[3] = mx;
+        return 0;
+    });
+}
+int fgb_mesh_cell_blocks(const FGB_MESH* m, int cells_per_block, int max_dofs, int64_t* out8) {
+    return guarded([&] {
+        const FemStructure s = build_q2_structure(*m->pm);
+        const CellBlocks cb = build_cell_blocks(s, cells_per_block, max_dofs);
+        const uint64_t h = validate_cell_blocks(s, cb, cells_per_block, max_dofs);
+        out8[0] = cb.n_blocks;
+        out8[1] = cb.max_cells;
+        out8[2] = cb.max_dofs;
+        out8[3] = cb.local_entries();
+        out8[4] = cb.n_slots;
+        out8[5] = (int64_t)cb.bnd_dofs.size();
+        out8[6] = s.n_dofs - (int64_t)cb.bnd_dofs.size();
+        std::memcpy(&out8[7], &h, sizeof(h));
         return 0;
     });
 }

@@ -150,4 +150,95 @@ CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block, int ma
     return cb;
 }
 
+namespace {
+template <typename T>
+void digest(uint64_t& h, const std::vector<T>& v) {
+    const unsigned char* b = reinterpret_cast<const unsigned char*>(v.data());
+    for (size_t i = 0; i < v.size() * sizeof(T); ++i) h = (h ^ b[i]) * 1099511628211ull;
+}
+}  // namespace
+
+uint64_t validate_cell_blocks(const FemStructure& fs, const CellBlocks& cb, int cells_per_block, int max_dofs) {
+    const int nc = fs.n_cells, n = fs.n_dofs;
+    FGB_REQUIRE(cb.n_cells == nc && cb.n_dofs == n && (int)cb.perm.size() == nc, "cell blocks: sizes");
+    std::vector<char> seen(nc, 0);
+    for (int p = 0; p < nc; ++p) {
+        const int c = cb.perm[p];
+        FGB_REQUIRE(c >= 0 && c < nc && !seen[c], "cell blocks: perm is not a permutation");
+        seen[c] = 1;
+        if (p) FGB_REQUIRE(fs.cell_dofs[27 * (size_t)c + 13] > fs.cell_dofs[27 * (size_t)cb.perm[p - 1] + 13],
+                           "cell blocks: cells not in interior-DoF order");
+    }
+    FGB_REQUIRE((int)cb.cell_start.size() == cb.n_blocks + 1 && cb.cell_start[0] == 0 && cb.cell_start.back() == nc,
+                "cell blocks: block ranges");
+    FGB_REQUIRE((int)cb.dof_start.size() == cb.n_blocks + 1 && cb.dof_start[0] == 0 &&
+                    cb.dof_start.back() == (int64_t)cb.dof_list.size(),
+                "cell blocks: local DoF ranges");
+    std::vector<int32_t> total(n, 0), blocks_of(n, 0), complete_in(n, -1);
+    for (int b = 0; b < cb.n_blocks; ++b) {
+        const int p0 = cb.cell_start[b], nb = cb.cell_start[b + 1] - p0;
+        const int q0 = cb.dof_start[b], nq = cb.dof_start[b + 1] - q0;
+        FGB_REQUIRE(nb >= 1 && nb <= cells_per_block && nb <= cb.max_cells, "cell blocks: block size");
+        FGB_REQUIRE(nq >= 1 && nq <= max_dofs && nq <= cb.max_dofs, "cell blocks: block DoF count");
+        std::vector<char> used(27 * (size_t)nb, 0);
+        for (int k = 0; k < nq; ++k) {
+            const int dof = cb.dof_list[q0 + k];
+            FGB_REQUIRE(dof >= 0 && dof < n, "cell blocks: DoF id");
+            if (k) FGB_REQUIRE(dof > cb.dof_list[q0 + k - 1], "cell blocks: local DoFs not ascending");
+            const int e0 = k ? cb.item_end[q0 + k - 1] : 0, e1 = cb.item_end[q0 + k];
+            FGB_REQUIRE(e1 > e0 && e1 <= 27 * nb, "cell blocks: item range");
+            for (int e = e0; e < e1; ++e) {
+                const int it = cb.items[28 * (size_t)p0 + e];
+                FGB_REQUIRE(it < 27 * nb && !used[it], "cell blocks: item repeated or out of range");
+                if (e > e0) FGB_REQUIRE(it > cb.items[28 * (size_t)p0 + e - 1], "cell blocks: items not ascending");
+                used[it] = 1;
+                const int p = p0 + it / 27, l = it % 27;
+                FGB_REQUIRE(fs.cell_dofs[27 * (size_t)cb.perm[p] + l] == dof, "cell blocks: item maps to another DoF");
+                FGB_REQUIRE(cb.loc[27 * (size_t)p + l] == k, "cell blocks: loc does not map back");
+            }
+            const int cnt = e1 - e0, want = fs.r2c_ptr[dof + 1] - fs.r2c_ptr[dof];
+            total[dof] += cnt;
+            ++blocks_of[dof];
+            if (cnt == want) {
+                FGB_REQUIRE(cb.slot[q0 + k] == -1 && complete_in[dof] < 0, "cell blocks: complete DoF with a slot");
+                complete_in[dof] = b;
+            } else {
+                FGB_REQUIRE(cb.slot[q0 + k] >= 0 && cb.slot[q0 + k] < cb.n_slots, "cell blocks: split DoF without a slot");
+            }
+        }
+        for (int it = 0; it < 27 * nb; ++it) FGB_REQUIRE(used[it], "cell blocks: product not summed");
+    }
+    // split DoFs: one slot per block, ascending block = ascending slot, slots bnd_ptr[j].. of j
+    FGB_REQUIRE((int)cb.bnd_ptr.size() == (int)cb.bnd_dofs.size() + 1 && cb.bnd_ptr.back() == cb.n_slots,
+                "cell blocks: split-DoF ranges");
+    std::vector<int32_t> bnd_index(n, -1);
+    for (size_t j = 0; j < cb.bnd_dofs.size(); ++j) {
+        const int d = cb.bnd_dofs[j];
+        FGB_REQUIRE(bnd_index[d] < 0 && (j == 0 || d > cb.bnd_dofs[j - 1]), "cell blocks: split DoFs not ascending");
+        bnd_index[d] = (int)j;
+    }
+    std::vector<int32_t> next_slot(cb.bnd_dofs.size(), 0);
+    for (size_t j = 0; j < cb.bnd_dofs.size(); ++j) next_slot[j] = cb.bnd_ptr[j];
+    for (int b = 0; b < cb.n_blocks; ++b)
+        for (int q = cb.dof_start[b]; q < cb.dof_start[b + 1]; ++q) {
+            if (cb.slot[q] < 0) continue;
+            const int j = bnd_index[cb.dof_list[q]];
+            FGB_REQUIRE(j >= 0 && cb.slot[q] == next_slot[j]++, "cell blocks: slots not in block order");
+        }
+    for (int d = 0; d < n; ++d) {
+        const int want = fs.r2c_ptr[d + 1] - fs.r2c_ptr[d];
+        FGB_REQUIRE(total[d] == want, "cell blocks: DoF products do not cover its cells");
+        const bool split = bnd_index[d] >= 0;
+        FGB_REQUIRE(split != (complete_in[d] >= 0), "cell blocks: DoF neither complete nor split");
+        if (split) FGB_REQUIRE(cb.bnd_ptr[bnd_index[d] + 1] - cb.bnd_ptr[bnd_index[d]] == blocks_of[d] &&
+                                   next_slot[bnd_index[d]] == cb.bnd_ptr[bnd_index[d] + 1],
+                               "cell blocks: split DoF slot count");
+    }
+    uint64_t h = 1469598103934665603ull;
+    digest(h, cb.perm); digest(h, cb.cell_start); digest(h, cb.dof_start); digest(h, cb.dof_list);
+    digest(h, cb.item_end); digest(h, cb.slot); digest(h, cb.loc); digest(h, cb.items);
+    digest(h, cb.bnd_dofs); digest(h, cb.bnd_ptr);
+    return h;
+}
+
 }  // namespace fgb

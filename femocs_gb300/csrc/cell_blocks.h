@@ -39,4 +39,10 @@ struct CellBlocks {
 // DoFs (at most 4096); 27 * cells_per_block must fit 16 bits
 CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block = 256, int max_dofs = 4096);
 
+// every invariant the kernels rely on (throws fgb::Error naming the first violation): the
+// permutation, the block ranges and limits, local DoFs ascending, loc and items mapping back
+// to the cells' DoFs, each DoF complete in one block or holding one slot per block in block
+// order; returns a 64-bit digest of all arrays
+uint64_t validate_cell_blocks(const FemStructure& fs, const CellBlocks& cb, int cells_per_block, int max_dofs);
+
 }  // namespace fgb

@@ -137,6 +137,11 @@ int fgb_mesh_q1_sizes(const FGB_MESH* m, int64_t* out4);
  * vacuum, 1 bulk), for regression checks of the builders */
 uint64_t fgb_mesh_structure_digest(const FGB_MESH* m, int order, int region);
 int fgb_mesh_q2_sizes(const FGB_MESH* m, int64_t* out4);
+/* cell blocks of the mesh's Q2 structure (the element-by-element level 0 and outer SpMV of
+ * Q2 fields), built on the host and checked against every invariant the kernels rely on;
+ * out8 = blocks, largest block's cells, largest block's DoFs, block-local DoF entries, slots,
+ * DoFs split over blocks, DoFs complete in one block, 64-bit digest of all arrays */
+int fgb_mesh_cell_blocks(const FGB_MESH* m, int cells_per_block, int max_dofs, int64_t* out8);
 void fgb_field_free(FGB_FIELD* f);
 int fgb_field_sizes(const FGB_FIELD* f, int64_t* out4); /* n_dofs, nnz, n_top_faces, sell_entries */
 /* PoissonSolver::setup(field, potential): applied_field is the Neumann value on the top

@@ -142,3 +142,41 @@ def test_structure_builders_do_not_depend_on_thread_count():
         outs.append(subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True,
                                    timeout=300).stdout.strip())
     assert outs[0] == outs[1] and outs[0].startswith("[")
+
+
+@pytest.mark.parametrize("cells,max_dofs", [(256, 4096), (64, 1024), (16, 200), (1, 27)])
+def test_cell_blocks_invariants(cells, max_dofs):
+    """The Q2 cell blocks (host-built) pass every invariant the element-by-element kernels rely
+    on (validated in the library), for the default limits and for limits that force blocks to
+    be halved down to a single hex: every DoF is complete in one block or split with one slot
+    per block."""
+    m = fg.Mesh.synthetic(radius=5.0, height=14.0, box_half=18.0, slab=4.0, top=40.0, h=3.0, growth=1.5, margin=3.0)
+    q = m.q2_sizes()
+    cb = m.cell_blocks(cells, max_dofs)
+    assert cb["n_complete"] + cb["n_split"] == q["n_dofs"]
+    assert cb["max_cells"] <= cells and cb["max_dofs"] <= max_dofs
+    assert cb["n_local"] >= q["n_dofs"] and cb["n_slots"] >= 2 * cb["n_split"]
+    if cells == 1:
+        assert cb["n_blocks"] == m.sizes()["n_vac_cells"]
+
+
+def test_cell_blocks_reject_bad_limits():
+    m = fg.Mesh.synthetic(radius=5.0, height=14.0, box_half=18.0, slab=4.0, top=40.0, h=4.0, growth=1.6, margin=3.0)
+    with pytest.raises(RuntimeError):
+        m.cell_blocks(4096, 4096)   # 27 x 4096 items do not fit 16 bits
+    with pytest.raises(RuntimeError):
+        m.cell_blocks(256, 8192)    # a block's DoFs must fit the kernels' 4096
+
+
+def test_cell_blocks_do_not_depend_on_thread_count():
+    import subprocess
+    import sys
+    code = ("import femocs_gb300 as fg; m = fg.Mesh.synthetic(radius=5.0, height=14.0, box_half=18.0, slab=4.0, "
+            "top=40.0, h=3.0, growth=1.5, margin=3.0); print(m.cell_blocks(64, 1024))")
+    env_root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    for nt in ("1", "5"):
+        env = dict(os.environ, OMP_NUM_THREADS=nt, PYTHONPATH=env_root)
+        outs.append(subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True,
+                                   timeout=300).stdout.strip())
+    assert outs[0] == outs[1] and "digest" in outs[0]
