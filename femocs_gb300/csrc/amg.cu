@@ -363,6 +363,11 @@ __global__ void __launch_bounds__(kB) k_cb_finish(EbeOperator op, const float* _
     l0_finish<KIND>(g, ax, xg, b, dinv, xout, d, c1, c2);
 }
 
+// threads per row of a transfer operator: rows of up to ~8 entries (the Q2 -> Q1 embedding
+// averages 3.2) are read by one thread each, so a warp keeps 32 rows' gathers in flight
+int tpr_for(double avg);
+int transfer_tpr(double avg) { return avg <= 8.0 ? 1 : tpr_for(avg); }
+
 // threads per row for a CSR operator of average row length `avg`
 int tpr_for(double avg) {
     if (avg <= 3.0) return 1;
@@ -495,8 +500,8 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
             lv->n_coarse = hl.P.n_cols;
             upload_csr32(hl.P, lv->p_ptr, lv->p_col, lv->p_val, stream);
             upload_csr32(hl.R, lv->r_ptr, lv->r_col, lv->r_val, stream);
-            lv->p_tpr = tpr_for((double)hl.P.nnz() / std::max(1, hl.P.n_rows));
-            lv->r_tpr = tpr_for((double)hl.R.nnz() / std::max(1, hl.R.n_rows));
+            lv->p_tpr = transfer_tpr((double)hl.P.nnz() / std::max(1, hl.P.n_rows));
+            lv->r_tpr = transfer_tpr((double)hl.R.nnz() / std::max(1, hl.R.n_rows));
         }
         lv->b.resize(lv->n);
         lv->xa.resize(lv->n);
