@@ -208,6 +208,10 @@ class Field:
         2 the same arithmetic over cell blocks (Q2 default), 0 the FP64 SELL matrix."""
         self._ok(load().fgb_field_set_outer_spmv(self.h, int(mode)))
 
+    def set_cell_blocks(self, cells_per_block=256, max_dofs=4096):
+        """Q2: limits of the cell blocks (hexes 1..256, DoFs 27..4096 per block)."""
+        self._ok(load().fgb_field_set_cell_blocks(self.h, int(cells_per_block), int(max_dofs)))
+
     def outer_spmv_bytes(self):
         """Algorithmic bytes of one outer SpMV launch in the current mode."""
         b = load().fgb_field_outer_spmv_bytes(self.h)

@@ -93,6 +93,7 @@ _PROTOS = {
     "fgb_field_set_level0_ebe": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_outer_spmv": (C.c_int, [vp, C.c_int]),
     "fgb_field_outer_spmv_bytes": (C.c_double, [vp]),
+    "fgb_field_set_cell_blocks": (C.c_int, [vp, C.c_int, C.c_int]),
     "fgb_field_amg_levels": (C.c_int, [vp, C.c_char_p, C.c_int]),
     "fgb_field_export_phi_nodes": (C.c_int, [vp, dp]),
     "fgb_field_import_phi_nodes": (C.c_int, [vp, dp]),

@@ -444,6 +444,9 @@ int fgb_field_last_stats(const FGB_FIELD* f, double* out14) {
 int fgb_field_set_outer_spmv(FGB_FIELD* f, int mode) {
     return guarded([&] { f->f->fem().set_outer_spmv(mode); return 0; });
 }
+int fgb_field_set_cell_blocks(FGB_FIELD* f, int cells_per_block, int max_dofs) {
+    return guarded([&] { f->f->fem().set_cell_blocks(cells_per_block, max_dofs); return 0; });
+}
 double fgb_field_outer_spmv_bytes(const FGB_FIELD* f) {
     double b = -1;
     guarded([&] { b = f->f->fem().outer_spmv_bytes(); return 0; });

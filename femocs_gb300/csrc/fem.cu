@@ -1509,7 +1509,7 @@ void FemDevice::set_outer_spmv(int mode) {
 void FemDevice::ensure_cell_blocks() {
     if (cb_) return;
     SetupPhases phase("cell blocks");
-    CellBlocks h = build_cell_blocks(fs_);
+    CellBlocks h = build_cell_blocks(fs_, cb_cells_, cb_max_dofs_);
     phase("host build");
     auto c = std::make_unique<CellBlocksDev>();
     c->n_blocks = h.n_blocks;
@@ -1549,6 +1549,18 @@ double FemDevice::outer_spmv_bytes() const {
     // read for p.q; per slot: the pair written and read; per split DoF: its id and slot range
     const CellBlocksDev& c = *cb_;
     return nc_ * (3024.0 + 110.0) + (double)c.n_local * 19.0 + 16.0 * n_ + 16.0 * c.n_slots + 8.0 * c.n_bnd;
+}
+
+void FemDevice::set_cell_blocks(int cells_per_block, int max_dofs) {
+    FGB_REQUIRE(fs_.order == 2, "cell blocks are for Q2 fields");
+    FGB_REQUIRE(cells_per_block >= 1 && cells_per_block <= 256 && max_dofs >= 27 && max_dofs <= 4096,
+                "cell blocks: 1..256 hexes and 27..4096 DoFs per block");
+    cb_cells_ = cells_per_block;
+    cb_max_dofs_ = max_dofs;
+    cb_.reset();
+    ke32_.release();
+    ke32lo_.release();
+    amg_.reset();
 }
 
 void FemDevice::set_level0_ebe(bool on) {

@@ -108,6 +108,9 @@ public:
     // assembled pairs), 0 = the FP64 SELL matrix
     void set_outer_spmv(int mode);
     int outer_spmv() const { return outer_mode_; }
+    // limits of the Q2 cell blocks (hexes per block, DoFs per block: at most 256 and 4096);
+    // drops the blocks, the converted element matrices and the hierarchy
+    void set_cell_blocks(int cells_per_block, int max_dofs);
     // algorithmic bytes of one outer SpMV launch in the current mode
     double outer_spmv_bytes() const;
     ~FemDevice();
@@ -197,6 +200,7 @@ private:
     DBuf<float2> cb_pair_;  // outer mode 2: partial (hi, lo) sums of the split DoFs
     DBuf<double> cb_dot_;   // outer mode 2: p.q partials
     bool cb_spmv_attr_ = false;
+    int cb_cells_ = 256, cb_max_dofs_ = 4096;
     DBuf<int8_t> fixed_;    // 1 on Dirichlet rows of the current anode mode
     LaunchTimer spmv_timer_;
     int n_, nc_;

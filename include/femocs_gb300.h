@@ -172,6 +172,9 @@ int fgb_field_set_level0_ebe(FGB_FIELD* f, int on);
  * to ~2^-48 per term, off the FP64 pipe); 2 (Q2 default, Q2 only) does the same arithmetic
  * element by element over cell blocks (half the bytes); 0 uses the FP64 SELL matrix */
 int fgb_field_set_outer_spmv(FGB_FIELD* f, int mode);
+/* Q2 fields: limits of the cell blocks (hexes per block 1..256, DoFs per block 27..4096;
+ * default 256 and 4096); the blocks and the hierarchy are rebuilt at the next solve */
+int fgb_field_set_cell_blocks(FGB_FIELD* f, int cells_per_block, int max_dofs);
 /* algorithmic bytes of one outer SpMV launch in the current mode (cell-block counts once the
  * blocks exist, i.e. after the first solve in mode 2) */
 double fgb_field_outer_spmv_bytes(const FGB_FIELD* f);

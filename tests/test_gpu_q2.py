@@ -150,3 +150,31 @@ def test_q2_level0_element_by_element_matches_sell(q2):
     assert abs(out[True][0] - out[False][0]) <= 2
     x = out[False][1]
     assert np.abs(out[True][1] - x).max() <= 2e3 * 1e-10 * np.abs(x).max()
+
+
+@pytest.mark.parametrize("anode", [False, True])
+def test_q2_cell_block_limits_give_the_same_solve(anode):
+    """The cell-block level 0 and outer SpMV equal the assembled SELL operators for any block
+    limits: single-hex blocks (every DoF but the interior ones split over blocks, all partial
+    sums through the slots), small blocks halved for their DoF limit, the default blocks —
+    same PCG iterations (within 2), same solution within the tolerance; with the anode as a
+    Dirichlet boundary too."""
+    m = fg.Mesh.synthetic(**SMALL)
+    f = fg.Field(m, order=2)
+    f.set_level0_ebe(False)
+    f.set_outer_spmv(0)
+    f.setup(-E0, 3.0)
+    f.assemble(True, anode)
+    rc, st = f.solve(precision=2, rel_tol=1e-10)
+    assert rc > 0 and st["status"] == 1
+    it_ref, x_ref = st["iterations"], f.solution()
+    f.set_level0_ebe(True)
+    f.set_outer_spmv(2)
+    for cells, max_dofs in ((1, 27), (16, 300), (256, 4096)):
+        f.set_cell_blocks(cells, max_dofs)
+        f.setup(-E0, 3.0)
+        f.assemble(True, anode)
+        rc, st = f.solve(precision=2, rel_tol=1e-10)
+        assert rc > 0 and st["status"] == 1 and st["rel_residual"] <= 1e-10, (cells, st)
+        assert abs(st["iterations"] - it_ref) <= 2, (cells, st["iterations"], it_ref)
+        assert np.abs(f.solution() - x_ref).max() <= 2e3 * 1e-10 * np.abs(x_ref).max(), cells
