@@ -9,9 +9,11 @@
 //   k_dense_solve    x = A_c^-1 b on the coarsest level (one warp per row)
 // Chebyshev smoothing of D^-1 A on [0.1, 1.1] x lambda_max, degree 2 before and after the
 // coarse correction (the same polynomial, so the cycle is a symmetric preconditioner).
-// Level 0 runs on the solver's SELL-32 matrix, one thread per row; coarser levels and the
-// transfer operators are CSR with 1..32 threads per row, chosen from the average row length
-// (the aggregated levels get denser, up to hundreds of entries per row).
+// Level 0 runs on the solver's SELL-32 matrix, one thread per row, or for Q2 element by
+// element over cell blocks (k_cb_apply, k_cb_finish: one CTA per block of hexes, products
+// summed on chip, cell_blocks.h); coarser levels are CSR with 1..32 threads per row, chosen
+// from the average row length (the aggregated levels get denser, up to hundreds of entries
+// per row), the transfer operators one thread per row up to 8 entries.
 #include <cmath>
 #include <sstream>
 

@@ -95,7 +95,7 @@ public:
     // largest eigenvalue of D^-1 A on level 0 (the smoothing interval): refreshed when the
     // level-0 matrix changes under a kept hierarchy
     void set_level0_lambda(double lambda);
-    // apply level 0 element by element (null operator: back to the SELL matrix)
+    // apply level 0 element by element over cell blocks (null operator: back to the SELL matrix)
     void set_level0_ebe(const EbeOperator* op);
     bool level0_ebe() const { return ebe_on_; }
     // algorithmic bytes of one level-0 smoothing step (SELL: nnz*8 + 24 n; cell blocks: the

@@ -14,6 +14,11 @@
 //                      scalars in device memory, replayed from a CUDA graph
 //   mixed precision    FP32 inner PCG inside FP64 iterative refinement; the true residual,
 //                      the refinement update and the boundary values stay FP64
+//   k_pcg_*, k_cg_spmv_pq_df, k_cb_spmv_df
+//                      FP64 CG preconditioned by the FP32 multigrid V-cycle (amg.cu), its
+//                      A p FP64-accurate from FP32 pairs: the SELL matrix, or for Q2 the
+//                      element matrices over the cell blocks (cell_blocks.h)
+//   k_ke_cyclic        Q2 element matrices into the cell blocks' FP32 (hi, lo) layout
 #include <algorithm>
 #include <chrono>
 #include <omp.h>
