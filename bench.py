@@ -122,6 +122,12 @@ class ClockSampler:
             threading.Thread(target=self._read, daemon=True).start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # nvidia-smi's start-up (driver/NVML initialisation) stalls this process's CUDA calls:
+        # the timed region starts after its first sample
+        t0 = time.time()
+        while not self.lines and self.proc.poll() is None and time.time() - t0 < 5.0:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
