@@ -161,25 +161,38 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
         for (int c = 0; c < nc; ++c)
             for (int L = 0; L < 27; ++L) e2c[pos[ent[27 * (size_t)c + L]]++] = 27 * c + L;
     }
-    // row lengths (union of the DoFs of the incident cells)
-    auto row_set = [&](int e, std::vector<int32_t>& l) {
-        l.clear();
-        for (int p = e2c_ptr[e]; p < e2c_ptr[e + 1]; ++p) {
-            const int c = e2c[p] / 27;
-            for (int L = 0; L < 27; ++L) l.push_back(ent[27 * (size_t)c + L]);
-        }
-        std::sort(l.begin(), l.end());
-        l.erase(std::unique(l.begin(), l.end()), l.end());
-    };
     phase("entity -> cells");
+    // row length = number of distinct entities of the incident cells, counted with a stamped
+    // open-addressing set per thread (no sort: the columns themselves are built later)
+    int max_inc = 1;
+    for (int e = 0; e < n_ent; ++e) max_inc = std::max(max_inc, e2c_ptr[e + 1] - e2c_ptr[e]);
+    int tab = 64;
+    while (tab < 2 * 27 * max_inc) tab *= 2;
     std::vector<int32_t> deg(n_ent);
 #pragma omp parallel
     {
-        std::vector<int32_t> l;
+        std::vector<int32_t> key(tab);
+        std::vector<uint32_t> stamp(tab, 0);
+        uint32_t cur = 0;
+        const uint32_t mask = (uint32_t)tab - 1;
 #pragma omp for schedule(dynamic, 4096)
         for (int e = 0; e < n_ent; ++e) {
-            row_set(e, l);
-            deg[e] = (int32_t)l.size();
+            ++cur;
+            int cnt = 0;
+            for (int p = e2c_ptr[e]; p < e2c_ptr[e + 1]; ++p) {
+                const int32_t* ce = &ent[27 * (size_t)(e2c[p] / 27)];
+                for (int L = 0; L < 27; ++L) {
+                    const int32_t k = ce[L];
+                    uint32_t h = ((uint32_t)k * 2654435761u) & mask;
+                    while (stamp[h] == cur && key[h] != k) h = (h + 1) & mask;
+                    if (stamp[h] != cur) {
+                        stamp[h] = cur;
+                        key[h] = k;
+                        ++cnt;
+                    }
+                }
+            }
+            deg[e] = cnt;
         }
     }
 
