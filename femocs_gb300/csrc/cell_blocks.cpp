@@ -52,6 +52,7 @@ CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block, int ma
     FGB_REQUIRE(cells_per_block >= 1 && 27 * cells_per_block <= 65535, "27 x cells per block must fit 16 bits");
     FGB_REQUIRE(max_dofs >= 27 && max_dofs <= 4096, "block DoF limit out of range");
     CellBlocks cb;
+    SetupPhases phase("cell blocks build");
     const int nc = fs.n_cells, n = fs.n_dofs;
     cb.n_cells = nc;
     cb.n_dofs = n;
@@ -64,6 +65,7 @@ CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block, int ma
         if (owner[d] >= 0) cb.perm.push_back(owner[d]);
     FGB_REQUIRE((int)cb.perm.size() == nc, "every cell owns one interior DoF");
     std::vector<int32_t>().swap(owner);
+    phase("hex order");
 
     // blocks: chunks of cells_per_block positions, halved while too many DoFs
     std::vector<uint64_t> keys(27 * (size_t)nc);
@@ -83,6 +85,7 @@ CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block, int ma
             cb.dof_start.push_back(cb.dof_start.back() + pd.second);
         }
     cb.n_blocks = (int)cb.cell_start.size() - 1;
+    phase("block cuts (sorted keys)");
     const int64_t ne = cb.dof_start.back();
     FGB_REQUIRE(ne < (int64_t)1 << 31, "too many block-local DoFs");
     cb.dof_list.resize(ne);
@@ -119,6 +122,7 @@ CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block, int ma
         n_inc[b + 1] = inc;
     }
     std::vector<uint64_t>().swap(keys);
+    phase("local DoFs, items");
     for (int b = 0; b < cb.n_blocks; ++b) n_inc[b + 1] += n_inc[b];
     cb.n_slots = n_inc[cb.n_blocks];
     std::vector<int32_t> slot_dof(cb.n_slots);
@@ -147,6 +151,7 @@ CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block, int ma
 #pragma omp parallel for schedule(static)
     for (int64_t q = 0; q < ne; ++q)
         if (cb.slot[q] >= 0) cb.slot[q] = renum[cb.slot[q]];
+    phase("slots");
     return cb;
 }
 
