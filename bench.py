@@ -51,9 +51,9 @@ SSOR_ITERS = {"config1": 268, "config2": 617, "probe": 0}
 # uses 617 x 2.55
 Q2_SSOR_RATIO = 2.55
 # DRAM bytes (read + write) per row of one launch of the hot multigrid kernels, from ncu
-# captures of the Q2 probe workload (profiles/k_cheb_step_level0_q2_probe.md: 61.9 nonzeros per
-# row, as config 2's Q2 rows; profiles/k_cb_apply_level0_q2_probe.md: the cell-block step,
-# k_cb_apply + k_cb_finish); a launch's traffic scales with its rows
+# captures of the Q2 probe workload (the SELL level-0 Chebyshev step at 61.9 nonzeros per row,
+# as config 2's Q2 rows; the cell-block step, k_cb_apply + k_cb_finish); a launch's traffic
+# scales with its rows
 KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6, ("smoother_ebe", 2): 261.8}
 FALLBACK_HBM_GBS = 6800.0
 
@@ -109,11 +109,18 @@ class ClockSampler:
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,uuid")
 
     def __init__(self):
         self.lines = []
         self.proc = None
+        # nvidia-smi numbers GPUs physically and ignores CUDA_VISIBLE_DEVICES: rows are kept by
+        # the UUID of the device this process computes on
+        try:
+            import femocs_gb300 as fg
+            self.uuid = fg.device_info()[2]
+        except Exception:  # noqa: BLE001 -- no device: the sampler reports itself unavailable
+            self.uuid = None
 
     def start(self):
         try:
@@ -133,7 +140,7 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self, gpu_index=0):
+    def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         time.sleep(0.25)
@@ -146,7 +153,9 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9 or not f[0].isdigit() or int(f[0]) != gpu_index:
+            if len(f) < 10 or not f[0].isdigit():
+                continue
+            if (f[9] != self.uuid) if self.uuid else int(f[0]) != 0:
                 continue
             try:
                 sm.append(float(f[1]))
@@ -157,7 +166,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "uuid": self.uuid}
 
 
 def dist_setup():
@@ -327,7 +336,7 @@ def run_ours(args, world, rank):
     field.mark(1)
     dev_ms = field.elapsed(0, 1)
     launches = lib.fgb_kernel_launches() - launches0
-    clocks = sampler.stop(0)
+    clocks = sampler.stop()
     field.set_profiling(False)
     dev_ms = reduce_max(world, dev_ms)
     ms_per_step = dev_ms / args.steps
@@ -560,7 +569,7 @@ def run_batch(args, world, rank):
     b.mark(1)
     dev_ms = reduce_max(world, b.elapsed(0, 1))
     launches = lib.fgb_kernel_launches() - launches0
-    clocks = sampler.stop(0)
+    clocks = sampler.stop()
     res = results[-1]
     its = np.array([res[s_]["iterations"] for s_ in slots])
     conv = sum(res[s_]["status"] == 1 for s_ in slots)
@@ -664,7 +673,7 @@ def run_serve(args, world, rank):
                       "p50_post_ms": float(np.median(rec["t_done"] - rec["t_solved"]) * 1e3),
                       "iterations_mean": float(rec["iterations"].mean()), "wall_s": wall})
     launches = lib.fgb_kernel_launches() - launches0
-    clocks = sampler.stop(0)
+    clocks = sampler.stop()
     srv.stop()
     info = srv.info()
     # plain FP64 Jacobi-CG: cold single-mesh solve latency of a few runs' meshes

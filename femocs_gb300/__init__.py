@@ -498,11 +498,27 @@ class Femocs:
             raise RuntimeError(last_error())
         return _stats_dict(st)
 
+    def enhancement(self):
+        """M/A field-enhancement ratio of the last run's check (0 when it did not run)."""
+        v = C.c_double(0)
+        if self.lib.fgb_femocs_enhancement(self.h, C.byref(v)) != 0:
+            raise RuntimeError(last_error())
+        return v.value
+
     def parse_double(self, cmd):
         v = C.c_double(0)
         rv = C.c_int(0)
         self.lib.femocs_parse_double(self.h, C.byref(rv), cmd.encode(), C.byref(v))
         return rv.value, v.value
+
+
+def device_info():
+    """(free bytes, total bytes, UUID as nvidia-smi prints it) of the current device."""
+    fr, tot = C.c_size_t(0), C.c_size_t(0)
+    uuid = C.create_string_buffer(48)
+    if load().fgb_device_info(C.byref(fr), C.byref(tot), uuid) != 0:
+        raise RuntimeError(last_error())
+    return fr.value, tot.value, uuid.value.decode()
 
 
 class DeviceBuffer:

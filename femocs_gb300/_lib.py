@@ -45,6 +45,7 @@ _PROTOS = {
     "femocs_parse_string": (None, [vp, ip, C.c_char_p, C.c_char_p]),
     "femocs_last_solve": (None, [vp, ip, dp]),
     "fgb_femocs_last_stats": (C.c_int, [vp, dp]),
+    "fgb_femocs_enhancement": (C.c_int, [vp, dp]),
     "femocs_last_error": (C.c_char_p, []),
     "fgb_kernel_launches": (C.c_longlong, []),
     # Part 2
@@ -78,6 +79,7 @@ _PROTOS = {
     "fgb_field_space_charge": (C.c_int, [vp, C.c_int, vp, vp, C.c_double, C.c_int, ip]),
     "fgb_field_clear_space_charge": (C.c_int, [vp]),
     "fgb_device_sync": (C.c_int, []),
+    "fgb_device_info": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.c_char_p]),
     "fgb_mesh_q2_sizes": (C.c_int, [vp, i64p]),
     "fgb_mesh_cell_blocks": (C.c_int, [vp, C.c_int, C.c_int, i64p]),
     "fgb_mesh_q1_sizes": (C.c_int, [vp, i64p]),

@@ -2,6 +2,7 @@
 // reported through retval = 1 (reference convention) or a NULL / negative return, with the
 // message available from femocs_last_error().
 #include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <omp.h>
@@ -189,6 +190,9 @@ static void stats13(const SolveStats& s, double* out) {
 }
 int fgb_femocs_last_stats(FEMOCS* h, double* out14) {
     return guarded([&] { stats13(h->f->last_stats(), out14); return 0; });
+}
+int fgb_femocs_enhancement(FEMOCS* h, double* ratio) {
+    return guarded([&] { *ratio = h->f->last_enhancement(); return 0; });
 }
 
 // ---------------------------------------------------------------- Part 2: meshes
@@ -495,6 +499,26 @@ int fgb_field_space_charge(FGB_FIELD* f, int n, const double* d_xyz, const int* 
 }
 int fgb_device_sync(void) {
     return guarded([&] { FGB_CUDA(cudaDeviceSynchronize()); return 0; });
+}
+int fgb_device_info(size_t* free_bytes, size_t* total_bytes, char* uuid) {
+    return guarded([&] {
+        size_t fr = 0, tot = 0;
+        FGB_CUDA(cudaMemGetInfo(&fr, &tot));
+        if (free_bytes) *free_bytes = fr;
+        if (total_bytes) *total_bytes = tot;
+        if (uuid) {
+            int dev = 0;
+            FGB_CUDA(cudaGetDevice(&dev));
+            cudaDeviceProp p;
+            FGB_CUDA(cudaGetDeviceProperties(&p, dev));
+            const unsigned char* b = reinterpret_cast<const unsigned char*>(p.uuid.bytes);
+            // the form nvidia-smi prints: GPU-8-4-4-4-12 hex digits
+            std::snprintf(uuid, 48, "GPU-%02x%02x%02x%02x-%02x%02x-%02x%02x-%02x%02x-%02x%02x%02x%02x%02x%02x", b[0],
+                          b[1], b[2], b[3], b[4], b[5], b[6], b[7], b[8], b[9], b[10], b[11], b[12], b[13], b[14],
+                          b[15]);
+        }
+        return 0;
+    });
 }
 int fgb_field_clear_space_charge(FGB_FIELD* f) {
     return guarded([&] { f->f->fem().clear_space_charge(); return 0; });

@@ -91,6 +91,19 @@ bool ConfigScript::get(const std::string& key, bool& v) const {
     if (is >> r) { v = r != 0; return true; }
     return false;
 }
+int ConfigScript::get_args(const std::string& key, std::vector<double>& args) const {
+    const std::string k = lower(key);
+    int n = 0;
+    for (const auto& c : data_)
+        if (c.size() >= 2 && c[0] == k)
+            for (size_t i = 0; i < args.size() && i + 1 < c.size(); ++i) {
+                std::istringstream is(c[i + 1]);
+                double r;
+                if (is >> r) { args[i] = r; ++n; }
+            }
+    return n;
+}
+
 void ConfigScript::set(const std::string& key, const std::string& v) {
     const std::string k = lower(key);
     for (auto& c : data_)
@@ -116,7 +129,6 @@ void FemocsFacade::read_params() {
     conf_.get("anode_bc", abc);
     anode_dirichlet_ = abc == "dirichlet";
     conf_.get("radius", radius_);
-    conf_.get("tip_height", tip_height_);
     // GPU-specific keys
     conf_.get("gpu_rel_tol", rel_tol_);
     conf_.get("gpu_inner_tol", inner_tol_);
@@ -130,9 +142,16 @@ void FemocsFacade::read_params() {
     FGB_REQUIRE(prep == "device" || prep == "host", "gpu_mesh_prep must be device or host");
     mesh_prep_device_ = prep == "device";
     FGB_REQUIRE(element_order_ == 1 || element_order_ == 2, "gpu_element_order must be 1 or 2");
-    double lim[2];
-    if (conf_.get("field_limit_min", lim[0])) field_min_ = lim[0];
-    if (conf_.get("field_limit_max", lim[1])) field_max_ = lim[1];
+    // field_tolerance: one value t gives [1-t, 1+t], two give [min, max] (src/Config.cpp:285-292)
+    std::vector<double> lim = {0.0, 0.0};
+    const int n_lim = conf_.get_args("field_tolerance", lim);
+    if (n_lim == 1) {
+        field_min_ = 1.0 - lim[0];
+        field_max_ = 1.0 + lim[0];
+    } else if (n_lim == 2) {
+        field_min_ = lim[0];
+        field_max_ = lim[1];
+    }
 }
 
 std::shared_ptr<const PreparedMesh> FemocsFacade::prepare(TetMesh&& tm) {
@@ -237,17 +256,24 @@ int FemocsFacade::run(int timestep, double time) {
         set_last_error("field solver did not complete normally, #CG=" + std::to_string(-rc));
         return 1;
     }
-    // FieldReader::check_limits (src/SolutionReader.cpp:538-556) when the tip geometry is known
-    if (radius_ > 0 && field_min_ != field_max_ && E0_ != 0) {
+    // FieldReader::check_limits over the nodal solutions (src/SolutionReader.cpp:538-556, called
+    // from src/ProjectRunaway.cpp:444) with the parameters of set_check_params (:568-588):
+    // tip height = z extent of the surface triangles, box height = z extent of the mesh nodes
+    // (src/ProjectRunaway.cpp:354); a Dirichlet anode gives E0 = V0 / box height
+    last_enhancement_ = 0.0;
+    const double e0_check = anode_dirichlet_ ? V0_ / (mesh_->bbox_max[2] - mesh_->bbox_min[2]) : E0_;
+    if (radius_ > 0 && field_min_ != field_max_ && e0_check != 0) {
         const double emax = field_->interp().max_field_norm();
+        const double tip_h = surface_z_extent();
         double r1 = radius_, r2 = radius_;
-        if (tip_height_ > radius_) { r2 = tip_height_; r1 = std::sqrt(tip_height_ * radius_); }
+        if (tip_h > radius_) { r2 = tip_h; r1 = std::sqrt(tip_h * radius_); }
         double g2 = 3.0;
         if (r2 > r1) {
             const double nu = r2 / r1, zeta = std::sqrt(nu * nu - 1);
             g2 = std::pow(zeta, 3.0) / (nu * std::log(zeta + nu) - zeta);
         }
-        const double beta = std::fabs(std::fabs(emax / E0_) / g2);
+        const double beta = std::fabs(std::fabs(emax / e0_check) / g2);
+        last_enhancement_ = beta;
         if (beta < field_min_ || beta > field_max_) {
             set_last_error("field enhancement is out of limits, M/A=" + std::to_string(beta));
             return 1;
@@ -264,6 +290,18 @@ int FemocsFacade::run(int timestep, double time) {
         field_->interpolate_host((int)surf_ids_.size(), p.data(), rank_, surf_cells_.data(), surf_interp_.data(), nullptr);
     }
     return 0;
+}
+
+double FemocsFacade::surface_z_extent() const {
+    const std::vector<int32_t>& tris = mesh_->surf.tris;
+    if (tris.empty()) return 0.0;
+    double lo = 1e300, hi = -1e300;
+    for (int32_t v : tris) {
+        const double z = mesh_->tet.xyz[3 * (size_t)v + 2];
+        lo = std::min(lo, z);
+        hi = std::max(hi, z);
+    }
+    return hi - lo;
 }
 
 int FemocsFacade::interp_points(int n, const double* x, const double* y, const double* z, std::vector<int32_t>& cells,

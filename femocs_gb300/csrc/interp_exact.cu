@@ -740,7 +740,10 @@ void* g_noalloc_addr[256] = {};  // device address of g_noalloc_scratch, per dev
 
 // Device address of the scratch array on the current device. The host-side symbol
 // g_noalloc_scratch is only a stand-in and must never be passed to a kernel; the address is
-// looked up once per device (with that device current) by the first call on that device.
+// looked up once per device, with that device current, when the first DeviceMesh is built
+// there (which also loads this file's module, so the allocation-free calls themselves do no
+// set-up). The address is cached per device ordinal: a device reset while the library is
+// loaded is unsupported, since the cached address would then be stale.
 static int32_t* noalloc_scratch() {
     int dev = 0;
     FGB_CUDA(cudaGetDevice(&dev));
@@ -853,6 +856,9 @@ DeviceMesh::DeviceMesh(const PreparedMesh& pm, cudaStream_t stream)
     sol_.zero(s);
     counters_.resize(8);
     set_surface(pm);
+    // set-up of the allocation-free entry point on this device: module load and the scratch
+    // array's address, here rather than in a timestep loop or a stream capture
+    (void)noalloc_scratch();
     FGB_CUDA(cudaStreamSynchronize(s));
     // host copies of the search tables are no longer needed
     grid_.seed.clear(); grid_.ptr.clear(); grid_.tets.clear(); grid_.cxyz.clear();

@@ -75,6 +75,10 @@ void femocs_import_mesh(FEMOCS* femocs, int* retval, int n_nodes, const double* 
 void femocs_last_solve(FEMOCS* femocs, int* retval, double* out8);
 /* the 14 statistics of fgb_field_last_stats for the last femocs_run */
 int fgb_femocs_last_stats(FEMOCS* femocs, double* out14);
+/* M/A field-enhancement ratio of the last femocs_run (FieldReader::check_limits,
+ * src/SolutionReader.cpp:538-556; limits from `field_tolerance`); 0 when the check did not run
+ * (no `radius`, equal limits or a zero applied field) */
+int fgb_femocs_enhancement(FEMOCS* femocs, double* ratio);
 const char* femocs_last_error(void);
 /* number of CUDA kernels the library has launched so far (all handles) */
 long long fgb_kernel_launches(void);
@@ -199,6 +203,9 @@ int fgb_field_space_charge(FGB_FIELD* f, int n, const double* d_xyz, const int* 
 int fgb_field_clear_space_charge(FGB_FIELD* f);
 /* wait for all work of this process on the current device */
 int fgb_device_sync(void);
+/* free and total device memory of the current device (cudaMemGetInfo) and, when uuid is not
+ * NULL (room for 48 chars), its UUID in the form nvidia-smi prints ("GPU-xxxxxxxx-...") */
+int fgb_device_info(size_t* free_bytes, size_t* total_bytes, char* uuid);
 /* the solution in the field's own DoF order (n_dofs values) */
 int fgb_field_export_solution(FGB_FIELD* f, double* x);
 int fgb_field_import_phi_nodes(FGB_FIELD* f, const double* phi_nodes);
@@ -226,7 +233,7 @@ int fgb_field_interpolate_surface_device(FGB_FIELD* f, int n, const double* d_xy
  * device-memory footprint fixed at start-up, and pipelines that cannot afford the device
  * synchronisation a cudaMalloc implies. This entry point calls no cudaMalloc, cudaFree or
  * other allocating routine: its per-point scratch is a fixed file-scope device array that
- * every GPU loading the library keeps (about 5.2 MB) until the process exits.
+ * every GPU on which a field is built keeps (about 5.2 MB) until the process exits.
  *   - at most 262144 points per call; larger n returns 1 with a message, nothing launched;
  *   - the caller passes device pointers for the points (3n doubles), the cells (n ints, or
  *     NULL) and the results (5n doubles); results are identical to fgb_field_interpolate_device;
@@ -234,8 +241,11 @@ int fgb_field_interpolate_surface_device(FGB_FIELD* f, int n, const double* d_xy
  *     stream has completed the call;
  *   - all calls share the scratch array, so calls that overlap on the GPU (from different
  *     streams, threads or fields) race: serialise them;
- *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress,
- *     with that device current); make that first call before any stream capture.
+ *   - the array's device address is looked up (cudaGetSymbolAddress, with the device current)
+ *     when the first field is built on each device, so the array is held from then on and
+ *     the calls themselves do no set-up;
+ *   - a device reset (cudaDeviceReset) while the library is loaded is unsupported: the cached
+ *     address of the array would be stale.
  * Returns 0 on success, 1 on error (femocs_last_error). */
 int fgb_field_interpolate_device_noalloc(FGB_FIELD* f, int n, const double* d_xyz, int rank, int* d_cells,
                                          double* d_out5);

@@ -90,3 +90,57 @@ def test_fp64_mode_and_import_mesh(tmp_path):
     assert fem.run() == 0
     st = fem.last_solve()
     assert st["outer"] == 0 and st["status"] == 1
+
+
+def analytic_enhancement(radius, tip_height):
+    """FieldReader::get_analyt_enhancement (src/SolutionReader.cpp:526-536) with the radii of
+    set_check_params (:579-586)."""
+    r1 = r2 = radius
+    if tip_height > radius:
+        r2, r1 = tip_height, np.sqrt(tip_height * radius)
+    if r2 <= r1:
+        return 3.0
+    nu = r2 / r1
+    zeta = np.sqrt(nu * nu - 1)
+    return zeta ** 3 / (nu * np.log(zeta + nu) - zeta)
+
+
+@pytest.mark.parametrize("anode", ["neumann", "dirichlet"])
+def test_field_enhancement_check(tmp_path, anode):
+    """femocs_run fails (retval 1) exactly when M/A leaves the field_tolerance window
+    (FieldReader::check_limits, src/SolutionReader.cpp:538-556). E0 is `elfield` for a Neumann
+    anode and Vappl / box height for a Dirichlet one (set_check_params, :568-588); the tip
+    height is the z extent of the surface triangles (src/ProjectRunaway.cpp:354)."""
+    m = fg.Mesh.synthetic(**TIP)
+    xyz = m.export("node_xyz").reshape(-1, 3)
+    tris, _, _ = m.surface()
+    zs = xyz[np.asarray(tris).reshape(-1), 2]
+    n_tet_nodes = m.sizes()["n_tetnodes"]
+    box_h = xyz[:n_tet_nodes, 2].max() - xyz[:n_tet_nodes, 2].min()
+    V0 = 25.0
+    bc = f"anode_bc {anode}\nVappl {V0}\nradius {TIP['radius']}\n"
+
+    def run(tol_line):
+        conf = tmp_path / f"{anode}_{abs(hash(tol_line))}.conf"
+        write_conf(conf, bc + tol_line)
+        fem = fg.Femocs(str(conf))
+        return fem, fem.run()
+
+    fem, rv = run("field_tolerance 1e-6 1e6")
+    assert rv == 0
+    beta = fem.enhancement()
+    # the same ratio from the nodal field this run recovered
+    f = fem.field(m.sizes())
+    e_max = np.linalg.norm(f.nodal()[:, :3], axis=1).max()
+    e0 = V0 / box_h if anode == "dirichlet" else -0.1
+    expect = abs(e_max / e0) / analytic_enhancement(TIP["radius"], zs.max() - zs.min())
+    assert beta > 0 and abs(beta - expect) <= 1e-12 * expect, (beta, expect)
+    # inside the window: success; on either side of it: failure with the reference's message
+    assert run(f"field_tolerance {0.99 * beta} {1.01 * beta}")[1] == 0
+    for window in (f"{1.01 * beta} {2 * beta}", f"{0.5 * beta} {0.99 * beta}"):
+        fem, rv = run("field_tolerance " + window)
+        assert rv == 1 and "enhancement" in fg.last_error()
+    # one argument t gives the window [1 - t, 1 + t] (src/Config.cpp:285-292)
+    t = abs(beta - 1.0)
+    assert run(f"field_tolerance {t * 1.01}")[1] == 0
+    assert run(f"field_tolerance {t * 0.99}")[1] == 1

@@ -5,8 +5,8 @@ footprint at start-up, cannot let a library call cudaMalloc inside the timestep 
 cudaMalloc synchronises the device, stalling an asynchronous pipeline). This entry point keeps
 its per-point scratch in a fixed device array instead. Its results must equal those of the
 allocating entry point, fgb_field_interpolate_device, exactly, including on a second call in a
-row (the shared array still holds the first call's data), and oversize requests must be
-refused before anything runs.
+row (the shared array still holds the first call's data); the calls must leave the device's
+free memory unchanged; and oversize requests must be refused before anything runs.
 
 This file is collected last so that a stopping run has executed every other test first; it
 also passes alone in a fresh process.
@@ -74,3 +74,24 @@ def test_noalloc_refuses_more_points_than_its_scratch(field_and_points):
     rc = lib.fgb_field_interpolate_device_noalloc(f.h, 262145, None, 3, None, None)
     assert rc == 1
     assert "262144" in fg.last_error()
+
+
+def test_noalloc_calls_allocate_no_device_memory(field_and_points):
+    """Free device memory (cudaMemGetInfo) is the same before and after two allocation-free
+    calls, with every buffer the calls use allocated beforehand."""
+    _, _, f, pts, _ = field_and_points
+    lib = load()
+    n = len(pts)
+    d_pts = fg.DeviceBuffer(24 * n)
+    d_pts.upload(np.ascontiguousarray(pts, dtype=np.float64))
+    d_cells = fg.DeviceBuffer(4 * n)
+    d_out = fg.DeviceBuffer(40 * n)
+    args = (f.h, n, C.c_void_p(d_pts.ptr), 3, C.c_void_p(d_cells.ptr), C.c_void_p(d_out.ptr))
+    assert lib.fgb_field_interpolate_device_noalloc(*args) == 0, fg.last_error()
+    assert lib.fgb_device_sync() == 0
+    free0, _, _ = fg.device_info()
+    for _ in range(2):
+        assert lib.fgb_field_interpolate_device_noalloc(*args) == 0, fg.last_error()
+    assert lib.fgb_device_sync() == 0
+    free1, _, _ = fg.device_info()
+    assert free1 == free0, (free0, free1)
