@@ -206,14 +206,14 @@ def measured_hbm_peak():
 
 
 # ----------------------------------------------------------------------------------------
-def cpu_baseline(field, workload, n_points, pts, spec, order=1, budget_s=15.0):
+def cpu_baseline(field, workload, n_points, pts, spec, order=1, budget_s=15.0, sysm=None):
     """Oracle restatement of the reference CPU path on the host cores (1 thread, like the
     reference default n_omp=1): SSOR(1.2)-PCG iterations on the same assembled system (the
     GPU's own matrix, Q1 or Q2), timed live and multiplied by the iteration count to 1e-9."""
-    import numpy as np
     import oracle as orc
-    rowptr, col, val, rhs, d2n = field.system()
-    sysm = orc.System(csr=(rowptr, col, val, rhs))
+    if sysm is None:
+        rowptr, col, val, rhs, d2n = field.system()
+        sysm = orc.System(csr=(rowptr, col, val, rhs))
     t_it = sysm.ssor_cg_fixed(2)
     n_it = max(3, min(200, int(0.7 * budget_s / max(t_it / 2, 1e-6))))
     t = sysm.ssor_cg_fixed(n_it)
@@ -285,6 +285,95 @@ def surface_cpu_timing(spec, surf_pts, sample=2000):
     return {"cpu_points_per_s": len(pts) / dt, "cpu_sample": len(pts), "cpu_kind": "port", "cpu_cores": 1}
 
 
+PARITY_PREFIX = 20000   # points of the timed list checked against the oracle's chain
+PARITY_PROBES = 300     # vacuum probes checked as a chain of their own (full scans in the oracle)
+
+
+def parity_snapshot(fem, spec, field, n_points, d_cells, d_out):
+    """What the last timed step produced: the solution (DoF order), the nodal solution and the
+    first PARITY_PREFIX located cells and interpolated values."""
+    import numpy as np
+    import femocs_gb300 as fg
+    m = fg.Mesh.synthetic(**spec)
+    n_pre = min(PARITY_PREFIX, n_points)
+    return {"mesh": m, "x": field.solution(), "nodal": fem.field(m.sizes()).nodal(),
+            "cells": d_cells.download(np.zeros(n_points, dtype=np.int32))[:n_pre].copy(),
+            "out": d_out.download(np.zeros((n_points, 5)))[:n_pre].copy()}
+
+
+def interp_parity(fem, snap, pts, n_surf):
+    """Location and interpolation of the timed step against the oracle's sequential chain
+    (src/SolutionReader.cpp:136-165) with the GPU's own nodal solution: the first
+    PARITY_PREFIX points of the timed list (a prefix replays the same chain) and a sample of
+    the random vacuum probes as a chain of their own. Cells and values must be bit-exact."""
+    import numpy as np
+    import oracle as orc
+    from oracle import pipeline
+    m = snap["mesh"]
+    tab = pipeline.tables(m, snap["nodal"])
+    cells, out = snap["cells"], snap["out"]
+    n_pre = len(cells)
+    out_parity = {}
+    t0 = time.perf_counter()
+    rc, ro = orc.locate_interpolate(tab, RANK, pts[:n_pre])
+    out_parity["prefix"] = {"points": int(n_pre), "cells_bit_exact": bool(np.array_equal(cells, rc)),
+                            "values_bit_exact": bool(np.array_equal(out.view(np.int64), ro.view(np.int64))),
+                            "oracle_s": time.perf_counter() - t0,
+                            "note": "first points of the timed step's output (surface atoms first)"}
+    n_probe = len(pts) - n_surf
+    if n_probe > 0:
+        rng = np.random.default_rng(31)
+        probes = np.ascontiguousarray(pts[n_surf:][np.sort(rng.choice(n_probe, size=min(PARITY_PROBES, n_probe),
+                                                                      replace=False))])
+        f = fem.field(m.sizes())
+        f.set_nodal(snap["nodal"])
+        c, o = f.interpolate(probes, rank=RANK)
+        t0 = time.perf_counter()
+        rc, ro = orc.locate_interpolate(tab, RANK, probes)
+        out_parity["probes"] = {"points": int(len(probes)), "cells_bit_exact": bool(np.array_equal(c, rc)),
+                                "values_bit_exact": bool(np.array_equal(o.view(np.int64), ro.view(np.int64))),
+                                "oracle_s": time.perf_counter() - t0,
+                                "note": "random vacuum probes as their own chain (the oracle scans the mesh)"}
+    return out_parity
+
+
+def config1_parity():
+    """Per-result parity at the R = 2 nm configuration (Q1, 2.8e5 DoFs) against the oracle's
+    FP64 SSOR(1.2)-CG solve to 1e-13 (src/DealSolver.cpp:443-459), nodal field and smoothing
+    (src/Interpolator.cpp:125-170) and the sequential location of the surface atoms: the
+    default solver at 1e-9 and FP32-Jacobi with FP64 refinement at 1e-9 and 1e-12."""
+    import numpy as np
+    import femocs_gb300 as fg
+    import oracle as orc
+    from oracle import pipeline
+    m = fg.Mesh.synthetic(**fg.CONFIG1)
+    atoms, types = fg.synth_atoms(fg.CONFIG1, seed=12345)
+    surf = np.ascontiguousarray(atoms[types == 2])
+    t0 = time.perf_counter()
+    sol, info = pipeline.reference_solution(m, -E0, rel_tol=1e-13)
+    ref_cells, ref_out = orc.locate_interpolate(pipeline.tables(m, sol), RANK, surf)
+    res = {"workload": "config1: nanotip R=2 nm H=8 nm, box 20 nm, top 60 nm, Q1", "n_dofs": info["n_dofs"],
+           "surface_atoms": int(len(surf)), "rank": RANK, "oracle_ssor_iterations": info["ssor_iterations"],
+           "oracle_rel_residual": info["rel_residual"], "oracle_s": time.perf_counter() - t0,
+           "max_abs_phi": float(np.abs(sol[:, 4]).max()), "runs": []}
+    system, v2n = info["system"], info["vertex2node"]
+    f = fg.Field(m)
+    for precision, tol in ((2, 1e-9), (1, 1e-9), (1, 1e-12)):
+        f.setup(-E0)
+        f.assemble(True, False)
+        rc, st = f.solve(precision=precision, rel_tol=tol, max_iter=100000)
+        x = f.phi_nodes()[v2n]
+        r = float(np.linalg.norm(system.spmv(x) - system.rhs) / np.linalg.norm(system.rhs))
+        f.extract(True)
+        c, o = f.interpolate(surf, rank=RANK)
+        p = pipeline.point_parity(c, o, ref_cells, ref_out)
+        p.update(solver={2: "FP64 CG + FP32 multigrid", 1: "FP32 Jacobi-PCG + FP64 refinement"}[precision],
+                 rel_tol=tol, converged=bool(st["status"] == 1), iterations=st["iterations"],
+                 rel_residual_oracle=r)
+        res["runs"].append(p)
+    return res
+
+
 def run_ours(args, world, rank):
     import numpy as np
     import femocs_gb300 as fg
@@ -338,6 +427,8 @@ def run_ours(args, world, rank):
     launches = lib.fgb_kernel_launches() - launches0
     clocks = sampler.stop()
     field.set_profiling(False)
+    snap = (parity_snapshot(fem, spec, field, n_points, d_cells, d_out)
+            if rank == 0 and world == 1 and not args.no_parity else None)
     dev_ms = reduce_max(world, dev_ms)
     ms_per_step = dev_ms / args.steps
     value = n * args.steps * world / (dev_ms * 1e-3)
@@ -454,8 +545,26 @@ def run_ours(args, world, rank):
         # count (ncu -s/-c for a launch list of exactly the timed region)
         "timed_launch_range": [launches0, launches],
     }
+    sysm = None
+    if snap is not None:
+        # parity of the timed step's results: the FP64 true residual recomputed by the oracle's
+        # SpMV on the system the GPU solved, and location/interpolation against the oracle
+        import oracle as orc
+        t0 = time.perf_counter()
+        rowptr, col, val, rhs, d2n = field.system()
+        sysm = orc.System(csr=(rowptr, col, val, rhs))
+        r_orc = float(np.linalg.norm(sysm.spmv(snap["x"]) - rhs) / np.linalg.norm(rhs))
+        del rowptr, col, val
+        line["parity"] = {"rel_residual_oracle": r_orc, "rel_residual_gpu": last["rel_residual"],
+                          "residual_note": "||b - A x|| / ||b|| of the last timed solve, recomputed by the "
+                                           "oracle's FP64 SpMV on the exported system",
+                          "export_and_spmv_s": time.perf_counter() - t0}
+        line["parity"].update(interp_parity(fem, snap, pts, n_surf))
+        if args.workload != "config1":
+            line["parity"]["config1"] = config1_parity()
     if rank == 0 and world == 1 and not args.no_cpu and SSOR_ITERS.get(args.workload):
-        line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec, order)
+        line["cpu_baseline"] = cpu_baseline(field, args.workload, n_points, pts, spec, order, sysm=sysm)
+    del sysm, snap
     line["surface_interp"] = {"points": n_surf, "gpu_ms": surf_ms, "gpu_points_per_s": n_surf / (surf_ms * 1e-3),
                               "rank": 1, "note": "femocs_interpolate_surface_elfield path, device-resident points"}
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -721,6 +830,7 @@ def main():
     ap.add_argument("--order", type=int, default=0, choices=[0, 1, 2],
                     help="element order (default: 2 for config2/probe, 1 for config1)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-parity", action="store_true", help="skip the parity checks against the oracle")
     args = ap.parse_args()
     world, rank, _ = dist_setup()
     if args.impl == "reference":

@@ -8,3 +8,4 @@ vectors produced by the reference's own compiled sources (see oracle/ref_driver.
 tests/golden/make_golden.py).
 """
 from .oracle_lib import *  # noqa: F401,F403
+from . import pipeline  # noqa: F401

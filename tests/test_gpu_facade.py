@@ -5,7 +5,7 @@ import pytest
 
 import femocs_gb300 as fg
 import oracle as orc
-from util import oracle_tables
+from oracle import pipeline
 
 pytestmark = pytest.mark.gpu
 TIP = dict(radius=10.0, height=30.0, box_half=40.0, slab=10.0, top=120.0, h=5.0, growth=1.4, margin=6.0)
@@ -29,6 +29,10 @@ gpu_rel_tol 1e-12
 
 
 def test_run_interpolate_export(tmp_path):
+    """femocs_run + femocs_interpolate_elfield/phi + femocs_export_data through the C ABI
+    against the oracle: the reference's FP64 SSOR-CG solve (to 1e-13), nodal field, smoothing
+    and sequential rank-3 location/interpolation. Cells and flags bit-exact; phi and E within
+    the error of a solve at the configured 1e-12 relative residual."""
     conf = tmp_path / "in.conf"
     write_conf(conf)
     fem = fg.Femocs(str(conf))
@@ -37,23 +41,21 @@ def test_run_interpolate_export(tmp_path):
     assert fem.run() == 0
     st = fem.last_solve()
     assert st["status"] == 1 and st["rel_residual"] <= 1.05e-12
-    # interpolation at arbitrary points equals a direct field evaluation of the same mesh
+    m = fg.Mesh.synthetic(**TIP)
+    sol, _ = pipeline.reference_solution(m, 0.1, rel_tol=1e-13)
+    tab = pipeline.tables(m, sol)
+    phi_tol = 50 * 1e-12 * np.abs(sol[:, 4]).max()
+    e_tol = 500 * 1e-12 * np.linalg.norm(sol[:, :3], axis=1).max()
     pts = fg.synth_probes(TIP, 500, seed=2)
     rv, Ex, Ey, Ez, En, flag = fem.interpolate_elfield(pts[:, 0], pts[:, 1], pts[:, 2])
     assert rv == 0
     rv, phi, flag2 = fem.interpolate_phi(pts[:, 0], pts[:, 1], pts[:, 2])
     assert rv == 0 and np.array_equal(flag, flag2)
-    m = fg.Mesh.synthetic(**TIP)
-    f = fg.Field(m)
-    f.setup(0.1)
-    f.assemble(True, False)
-    f.solve(precision=1, rel_tol=1e-12)
-    f.extract(True)
-    cells, out = f.interpolate(pts, rank=3)
-    np.testing.assert_array_equal(flag, (cells < 0).astype(np.int32))
-    np.testing.assert_allclose(np.c_[Ex, Ey, Ez], out[:, :3], rtol=1e-9, atol=1e-12)
-    np.testing.assert_allclose(phi, out[:, 4], rtol=1e-9, atol=1e-12)
-    np.testing.assert_allclose(En, np.linalg.norm(out[:, :3], axis=1), rtol=1e-9, atol=1e-12)
+    ref_cells, ref = orc.locate_interpolate(tab, 3, pts)
+    np.testing.assert_array_equal(flag, (ref_cells < 0).astype(np.int32))
+    np.testing.assert_allclose(np.c_[Ex, Ey, Ez], ref[:, :3], rtol=0, atol=e_tol)
+    np.testing.assert_allclose(phi, ref[:, 4], rtol=0, atol=phi_tol)
+    np.testing.assert_allclose(En, np.linalg.norm(np.c_[Ex, Ey, Ez], axis=1), rtol=1e-15, atol=0)
     # export by atom id: surface atoms only, others stay zero (overwrite mode, capital label)
     rv, e = fem.export_data(len(types), "Elfield")
     assert rv == 0
@@ -61,12 +63,12 @@ def test_run_interpolate_export(tmp_path):
     surf = types == 2
     # (a surface atom whose fallback cell is a bulk tet gets the empty value 0, as in the reference)
     assert np.all(e[~surf] == 0) and np.mean(np.linalg.norm(e[surf], axis=1) > 0) > 0.5
-    sc, so = f.interpolate(atoms[surf], rank=3)
-    np.testing.assert_allclose(e[surf], so[:, :3], rtol=1e-9, atol=1e-12)
+    sc, so = orc.locate_interpolate(tab, 3, atoms[surf])
+    np.testing.assert_allclose(e[surf], so[:, :3], rtol=0, atol=e_tol)
     # append mode with the exact label adds to the caller's data
     rv, pot = fem.export_data(len(types), "potential")
     assert rv == 0
-    np.testing.assert_allclose(pot[surf], so[:, 4], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(pot[surf], so[:, 4], rtol=0, atol=phi_tol)
 
 
 def test_errors_are_return_codes(tmp_path):

@@ -4,7 +4,8 @@ import os
 import numpy as np
 
 import femocs_gb300 as fg
-import oracle as orc
+import oracle as orc  # noqa: F401
+from oracle import pipeline
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 SPEC_KEYS = ("radius", "height", "box_half", "slab", "top", "h", "growth", "margin")
@@ -31,24 +32,13 @@ def load_surface(name):
 
 
 def oracle_tables(mesh, sol):
-    s = mesh.sizes()
-    tets = mesh.export("tet_nodes")
-    xyz = mesh.export("node_xyz")
-    det, ctr = orc.tet_tables(tets, xyz[: 3 * s["n_tetnodes"]])
-    nptr, nidx = orc.neighbour_lists(s["n_tetnodes"], tets, mesh.export("tet_nbor"))
-    return dict(tets=tets, search=mesh.export("tet_search"), det=det, centroid=ctr, nbr_ptr=nptr, nbr_idx=nidx,
-                hexs=mesh.export("hex_nodes"), hexf=mesh.export("hex_coeffs"), quad_nodes=mesh.export("quad_nodes"),
-                sol=sol)
+    return pipeline.tables(mesh, sol)
 
 
 def vacuum_system_inputs(mesh):
     """Vertex coordinates and vacuum cells in the reference's vertex numbering
     (ascending mesh node ids of the vacuum hexes, src/DealSolver.cpp:192-208)."""
-    n2v = mesh.export("vac_node2vertex")
-    xyz = mesh.export("node_xyz").reshape(-1, 3)
-    v2n = np.flatnonzero(n2v >= 0)
-    cells = mesh.export("hex_nodes").reshape(-1, 8)[mesh.export("vac_cells")]
-    return xyz[v2n], n2v[cells], v2n
+    return pipeline.vacuum_inputs(mesh)
 
 
 def bits_equal(a, b):
