@@ -354,7 +354,10 @@ def config1_parity():
     ref_cells, ref_out = orc.locate_interpolate(pipeline.tables(m, sol), RANK, surf)
     res = {"workload": "config1: nanotip R=2 nm H=8 nm, box 20 nm, top 60 nm, Q1", "n_dofs": info["n_dofs"],
            "surface_atoms": int(len(surf)), "rank": RANK, "oracle_ssor_iterations": info["ssor_iterations"],
-           "oracle_rel_residual": info["rel_residual"], "oracle_s": time.perf_counter() - t0,
+           "oracle_rel_residual": info["rel_residual"], "oracle_rel_floor": info["rel_floor"],
+           "oracle_s": time.perf_counter() - t0,
+           "note": "residuals in the oracle's system, compensated (Dot2); rel_floor = 2^-53 ||(|b|+|A||x|)||/||b||, "
+                   "the FP64 rounding floor (two assemblies differ by about that much)",
            "max_abs_phi": float(np.abs(sol[:, 4]).max()), "runs": []}
     system, v2n = info["system"], info["vertex2node"]
     f = fg.Field(m)
@@ -363,13 +366,15 @@ def config1_parity():
         f.assemble(True, False)
         rc, st = f.solve(precision=precision, rel_tol=tol, max_iter=100000)
         x = f.phi_nodes()[v2n]
-        r = float(np.linalg.norm(system.spmv(x) - system.rhs) / np.linalg.norm(system.rhs))
+        bnorm = float(np.linalg.norm(system.rhs))
+        r_abs, floor_abs = system.residual(x)
         f.extract(True)
         c, o = f.interpolate(surf, rank=RANK)
         p = pipeline.point_parity(c, o, ref_cells, ref_out)
         p.update(solver={2: "FP64 CG + FP32 multigrid", 1: "FP32 Jacobi-PCG + FP64 refinement"}[precision],
-                 rel_tol=tol, converged=bool(st["status"] == 1), iterations=st["iterations"],
-                 rel_residual_oracle=r)
+                 rel_tol=tol, status={1: "converged", 2: "at the FP64 floor"}.get(st["status"], st["status"]),
+                 iterations=st["iterations"], rel_residual_gpu=st["rel_residual"],
+                 rel_residual_oracle=r_abs / bnorm, rel_floor=floor_abs / bnorm)
         res["runs"].append(p)
     return res
 
@@ -553,11 +558,13 @@ def run_ours(args, world, rank):
         t0 = time.perf_counter()
         rowptr, col, val, rhs, d2n = field.system()
         sysm = orc.System(csr=(rowptr, col, val, rhs))
-        r_orc = float(np.linalg.norm(sysm.spmv(snap["x"]) - rhs) / np.linalg.norm(rhs))
+        r_abs, floor_abs = sysm.residual(snap["x"])
+        r_orc = r_abs / float(np.linalg.norm(rhs))
         del rowptr, col, val
         line["parity"] = {"rel_residual_oracle": r_orc, "rel_residual_gpu": last["rel_residual"],
+                          "rel_floor": floor_abs / float(np.linalg.norm(rhs)),
                           "residual_note": "||b - A x|| / ||b|| of the last timed solve, recomputed by the "
-                                           "oracle's FP64 SpMV on the exported system",
+                                           "oracle (compensated) on the exported system",
                           "export_and_spmv_s": time.perf_counter() - t0}
         line["parity"].update(interp_parity(fem, snap, pts, n_surf))
         if args.workload != "config1":

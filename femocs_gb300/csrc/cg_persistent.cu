@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "compensated.cuh"
 #include "fem_device.h"
 
 namespace cg = cooperative_groups;
@@ -51,6 +52,14 @@ __device__ __forceinline__ double sell_dot64(int i, const MixedArgs& a, const do
         acc1 += v23.x * x[ci.z] + v23.y * x[ci.w];
     }
     return acc0 + acc1;
+}
+
+// b_i - (A x)_i with the FP64 matrix, compensated when the tolerance nears the FP64 floor
+// (mag: |b_i| + sum |a_ij x_j| of the compensated evaluation, 0 otherwise)
+__device__ __forceinline__ double true_residual(int i, const MixedArgs& a, double& mag) {
+    mag = 0.0;
+    return a.comp ? sell_residual_dot2(i, a.sptr, a.slen, a.scol, a.s64, a.x, a.b[i], mag)
+                  : a.b[i] - sell_dot64(i, a, a.x);
 }
 
 // q_i = sum_j a_ij (z_j + beta * pold_j): the new direction is formed on the fly
@@ -97,7 +106,8 @@ __device__ __forceinline__ void grid_sum(cg::grid_group& grid, double (&v)[NV], 
         if (lane == 0) sh[k][wid] = t;
     }
     __syncthreads();
-    double* P = partial + (size_t)buf * 2 * gridDim.x;
+    static_assert(NV <= kMixedSumMax, "grid_sum buffers hold kMixedSumMax values per CTA");
+    double* P = partial + (size_t)buf * kMixedSumMax * gridDim.x;
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
@@ -130,9 +140,10 @@ __global__ void __launch_bounds__(kThreads) k_mixed_cg(MixedArgs a) {
     int buf = 0;
 
     // ---- true residual of the initial guess, z = D^-1 r, d = 0, p_old = 0
-    double v2[2] = {0.0, 0.0};
+    double v2[3] = {0.0, 0.0, 0.0};
     for (int i = t0; i < a.n; i += G) {
-        const double ri = a.b[i] - sell_dot64(i, a, a.x);
+        double mag;
+        const double ri = true_residual(i, a, mag);
         const float r32 = (float)ri;
         const float z32 = a.dinv32[i] * r32;
         a.r[i] = r32;
@@ -141,12 +152,13 @@ __global__ void __launch_bounds__(kThreads) k_mixed_cg(MixedArgs a) {
         a.pa[i] = 0.f;
         v2[0] += (double)r32 * (double)z32;
         v2[1] += ri * ri;
+        v2[2] += mag * mag;
     }
-    grid_sum<2>(grid, v2, a.partial, buf);
+    grid_sum<3>(grid, v2, a.partial, buf);
     buf ^= 1;
     double gamma = v2[0], rr = v2[1];
     double rr_ref = rr;  // residual at the last refinement
-    int it = 0, updates = 0, status = 0;
+    int it = 0, updates = 0, status = 0, stalls = 0;
     float beta = 0.f;
     float* pold = a.pa;
     float* pnew = a.pb;
@@ -192,25 +204,33 @@ __global__ void __launch_bounds__(kThreads) k_mixed_cg(MixedArgs a) {
                 a.d[i] = 0.f;
             }
             grid.sync();
-            double u2[2] = {0.0, 0.0};
+            double u2[3] = {0.0, 0.0, 0.0};
             for (int i = t0; i < a.n; i += G) {
-                const double ri = a.b[i] - sell_dot64(i, a, a.x);
+                double mag;
+                const double ri = true_residual(i, a, mag);
                 const float r32 = (float)ri;
                 const float z32 = a.dinv32[i] * r32;
                 a.r[i] = r32;
                 a.z[i] = z32;
                 u2[0] += (double)r32 * (double)z32;
                 u2[1] += ri * ri;
+                u2[2] += mag * mag;
             }
-            grid_sum<2>(grid, u2, a.partial, buf);
+            grid_sum<3>(grid, u2, a.partial, buf);
             buf ^= 1;
             ++updates;
             gamma_new = u2[0];
             rr = u2[1];
+            // a refinement that does not halve the true residual norm makes no progress;
+            // four in a row end the solve (rounding floor reached) instead of running to max_iter
+            stalls = rr > 0.25 * rr_ref ? stalls + 1 : 0;
             rr_ref = rr;
             if (rr <= a.tol2) { status = 1; break; }
+            // compensated: within twice the FP64 floor is as converged as FP64 can hold x
+            if (a.comp && rr <= 4.0 * kFloorScale2 * u2[2]) { status = kStatusFloor; break; }
             if (it >= a.max_iter) { status = -1; break; }
             if (!(rr == rr)) { status = -2; break; }
+            if (stalls >= 4) { status = -3; break; }
         }
         beta = (float)(gamma_new / gamma);
         gamma = gamma_new;

@@ -26,6 +26,7 @@
 #include <cmath>
 
 #include "amg.h"
+#include "compensated.cuh"
 #include "fem_device.h"
 #include "cell_blocks.h"
 #include "fem_q2.h"
@@ -523,18 +524,25 @@ __global__ void __launch_bounds__(kBlock) k_cg_direction(int n, const T* __restr
     p[i] = z[i] + (T)st->beta * p[i];
 }
 
-// FP64 residual r = b - A x with its squared norm.
+// FP64 residual r = b - A x with its squared norm; comp: each row's product compensated
+// (Dot2, as accurate as twice the working precision) for tolerances near the FP64 floor.
 __global__ void __launch_bounds__(kBlock) k_residual64(int n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
                                                        const int32_t* __restrict__ scol, const double* __restrict__ sval,
                                                        const double* __restrict__ x, const double* __restrict__ b,
-                                                       double* __restrict__ r, double* partial, CgState* st) {
-    double v[1] = {0.0};
+                                                       double* __restrict__ r, double* partial, CgState* st, int comp) {
+    double v[2] = {0.0, 0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double ri = b[i] - sell_row(i, sptr, slen, scol, sval, x);
+        double mag = 0.0;
+        const double ri = comp ? sell_residual_dot2(i, sptr, slen, scol, sval, x, b[i], mag)
+                               : b[i] - sell_row(i, sptr, slen, scol, sval, x);
         r[i] = ri;
         v[0] += ri * ri;
+        v[1] += mag * mag;
     }
-    if (grid_reduce<1>(v, partial, &st->ticket)) st->rr = v[0];
+    if (grid_reduce<2>(v, partial, &st->ticket)) {
+        st->rr = v[0];
+        st->ff = v[1];
+    }
 }
 
 __global__ void k_norm2(int n, const double* __restrict__ a, double* partial, CgState* st) {
@@ -958,7 +966,7 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
     x_.zero(s);
     r64_.resize(n_); p64_.resize(n_); q64_.resize(n_); z64_.resize(n_);
     r32_.resize(n_); p32_.resize(n_); p32b_.resize(n_); q32_.resize(n_); z32_.resize(n_); d32_.resize(n_);
-    partial_.resize(std::max<size_t>(2 * (size_t)grid_for(n_, kBlock), 4 * (size_t)mixed_cg_grid(n_)) + 64);
+    partial_.resize(std::max<size_t>(2 * (size_t)grid_for(n_, kBlock), 2 * kMixedSumMax * (size_t)mixed_cg_grid(n_)) + 64);
     mixed_.resize(1);
     FGB_CUDA(cudaMallocHost(&h_mixed_, sizeof(MixedResult)));
     state_.resize(2);
@@ -1192,6 +1200,11 @@ static double tol2_of(const SolveOptions& opt, double bnorm) {
     const double t = std::max(opt.rel_tol * bnorm, opt.abs_tol);
     return t * t;
 }
+// true residuals are evaluated compensated when the relative tolerance approaches the FP64
+// rounding floor of b - A x
+static int compensated_residual(const SolveOptions& opt) {
+    return opt.rel_tol > 0 && opt.rel_tol < kCompensatedResidualBelow ? 1 : 0;
+}
 
 int FemDevice::solve_plain(const SolveOptions& opt, SolveStats* st) {
     const int gb = grid_for(n_, kBlock);
@@ -1216,13 +1229,13 @@ int FemDevice::solve_plain(const SolveOptions& opt, SolveStats* st) {
     const int cg_status = h_state_->status;
     // true residual
     FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(), x_.get(),
-                                             rhs_.get(), r64_.get(), partial_.get(), ds));
+                                             rhs_.get(), r64_.get(), partial_.get(), ds, compensated_residual(opt)));
     FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
     FGB_CUDA(cudaStreamSynchronize(stream_));
     const double rn = std::sqrt(h_state_->rr);
     st->rel_residual = bnorm > 0 ? rn / bnorm : rn;
     st->status = bnorm == 0 ? 1 : cg_status;
-    return st->status == 1 ? st->iterations : -st->iterations;
+    return st->status >= 1 ? st->iterations : -st->iterations;
 }
 
 int FemDevice::solve_mixed(const SolveOptions& opt, SolveStats* st) {
@@ -1254,6 +1267,7 @@ int FemDevice::solve_mixed(const SolveOptions& opt, SolveStats* st) {
     a.tol2 = tol2_of(opt, bnorm);
     a.ru2 = opt.inner_tol * opt.inner_tol;
     a.max_iter = opt.max_iter;
+    a.comp = compensated_residual(opt);
     FGB_CUDA(cudaEventRecord(kev0_, stream_));
     launch_mixed_cg(a, stream_);
     FGB_CUDA(cudaEventRecord(kev1_, stream_));
@@ -1266,7 +1280,7 @@ int FemDevice::solve_mixed(const SolveOptions& opt, SolveStats* st) {
     st->outer = h_mixed_->updates;
     st->status = bnorm == 0 ? 1 : h_mixed_->status;
     st->rel_residual = bnorm > 0 ? std::sqrt(h_mixed_->rr) / bnorm : std::sqrt(h_mixed_->rr);
-    return st->status == 1 ? st->iterations : -st->iterations;
+    return st->status >= 1 ? st->iterations : -st->iterations;
 }
 
 void FemDevice::ensure_amg(SolveStats* st) {
@@ -1607,7 +1621,8 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     FGB_CUDA(cudaMemcpyAsync(ds, &init, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
     // r = b - A x (FP64), stop if already converged
     FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(),
-                                                       x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
+                                                       x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds,
+                                                       compensated_residual(opt)));
     FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
     FGB_CUDA(cudaStreamSynchronize(stream_));
     int status = 0, it = 0, restarts = 0;
@@ -1679,10 +1694,18 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
         }
         // true FP64 residual of the current x (also the restart residual)
         FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
-                                                           sell64_.get(), x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds));
+                                                           sell64_.get(), x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds,
+                                                           compensated_residual(opt)));
         FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
         FGB_CUDA(cudaStreamSynchronize(stream_));
         rr_true = h_state_->rr;
+        // with a compensated residual, a solution within twice the FP64 floor is as converged
+        // as FP64 can hold it: success (kStatusFloor), no restart on rounding noise
+        const bool at_floor = compensated_residual(opt) && rr_true <= 4.0 * kFloorScale2 * h_state_->ff;
+        if (status == 1 && rr_true > init.tol2 && at_floor) {
+            status = kStatusFloor;
+            break;
+        }
         if (status != 1 || rr_true <= init.tol2 || restarts >= 3 || it >= opt.max_iter) {
             if (status == 1 && rr_true > init.tol2) status = -1;  // recursion converged, x did not
             break;
@@ -1703,7 +1726,7 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     st->smoother_ms = amg_->smoother_timer.collect(&st->smoother_launches);
     st->smoother_bytes = amg_->smoother_bytes();
     st->spmv_ms = spmv_timer_.collect(&st->spmv_launches);
-    return st->status == 1 ? it : -it;
+    return st->status >= 1 ? it : -it;
 }
 
 }  // namespace fgb

@@ -14,7 +14,9 @@ namespace fgb {
 // replayed from a CUDA graph without host round trips.
 struct CgState {
     double rz, rz_new, pq, alpha, beta, rr, rr0, tol2;
-    int iter, max_iter, done, status;  // status: 1 converged, -1 max_iter, -2 breakdown/NaN
+    double ff;  // sum of squared row magnitudes |b| + |A||x| of the last compensated residual
+    int iter, max_iter, done, status;  // status: 1 converged, 2 at the FP64 floor, -1 max_iter,
+                                       // -2 breakdown/NaN, -3 no progress
     unsigned int ticket;
     int pad;
 };
@@ -24,6 +26,9 @@ struct MixedResult {
     int iterations, updates, status, pad;
     double rr;
 };
+
+// most values one grid-wide sum of the persistent mixed-precision CG reduces at once
+constexpr int kMixedSumMax = 3;
 
 // Arguments of the persistent mixed-precision CG kernel (cg_persistent.cu).
 struct MixedArgs {
@@ -42,11 +47,12 @@ struct MixedArgs {
     float* pa;
     float* pb;
     float* q;
-    double* partial;  // 2 buffers x 2 values x grid CTAs
+    double* partial;  // 2 buffers x kMixedSumMax values x grid CTAs
     MixedResult* out;
     double tol2;
     double ru2;       // squared reliable-update factor
     int max_iter;
+    int comp;         // true residuals compensated (Dot2) when the tolerance nears the FP64 floor
 };
 void launch_mixed_cg(const MixedArgs& args, cudaStream_t stream);
 int mixed_cg_grid(int n);

@@ -158,7 +158,11 @@ int fgb_field_assemble(FGB_FIELD* f, int full_run, int anode_dirichlet);
  * inner_tol: residual reduction between FP64 refinements (<= 0: default 0.1).
  * stats (may be NULL): iterations, refinements, status, rel_residual, bnorm, ms; a 7th slot
  * preset to -1 receives the device time of the solver kernel alone.
- * Returns #iterations (>0) or -#iterations when not converged. */
+ * status: 1 converged; 2 converged to the FP64 floor (rel_tol below 1e-10 evaluates the true
+ * residual compensated, and a solution whose residual is within twice 2^-53 |(|b| + |A||x|)|
+ * is as accurate as an FP64 vector can be on that system); -1 iteration cap; -2 breakdown or
+ * NaN; -3 FP64 refinements stopped reducing the residual (precision 1).
+ * Returns #iterations (>0) when the status is 1 or 2, else -#iterations. */
 int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol, int max_iter, double inner_tol,
                     double* stats6);
 /* phi per vacuum dof order is internal; these export per hex-mesh node (n_nodes values) */

@@ -298,7 +298,13 @@ void orc_free_system(OrcSystem* s) {
     memset(s, 0, sizeof(*s));
 }
 
+/* threads of the SpMV and vector operations of the CG (the SSOR sweeps stay sequential, as
+ * deal.II's PreconditionSSOR); 1 (default) keeps every sum in a fixed order */
+static int g_threads = 1;
+void orc_set_threads(int n) { g_threads = n > 0 ? n : 1; }
+
 void orc_spmv(const OrcSystem* s, const double* x, double* y) {
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
     for (int r = 0; r < s->n; ++r) {
         double acc = 0.0;
         for (int64_t k = s->rowptr[r]; k < s->rowptr[r + 1]; ++k) acc += s->val[k] * x[s->col[k]];
@@ -306,8 +312,32 @@ void orc_spmv(const OrcSystem* s, const double* x, double* y) {
     }
 }
 
+/* ||b - A x||_2 with every row's dot product compensated (Dot2 of Ogita, Rump and Oishi,
+ * SIAM J. Sci. Comput. 26, 2005: FMA-split products, TwoSum additions), and the FP64
+ * rounding floor of a plain evaluation, 2^-53 ||(|b| + |A||x|)||_2 */
+void orc_residual_comp(const OrcSystem* s, const double* x, double* out2) {
+    double rr = 0.0, ff = 0.0;
+    for (int r = 0; r < s->n; ++r) {
+        double p = s->rhs[r], err = 0.0, mag = fabs(s->rhs[r]);
+        for (int64_t k = s->rowptr[r]; k < s->rowptr[r + 1]; ++k) {
+            const double a = -s->val[k], xv = x[s->col[k]];
+            const double h = a * xv, e = fma(a, xv, -h);
+            const double t = p + h, z = t - p, q = (p - (t - z)) + (h - z);
+            p = t;
+            err += q + e;
+            mag += fabs(h);
+        }
+        const double ri = p + err;
+        rr += ri * ri;
+        ff += mag * mag;
+    }
+    out2[0] = sqrt(rr);
+    out2[1] = ldexp(sqrt(ff), -53);
+}
+
 static double dot(int n, const double* a, const double* b) {
     double s = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : s) num_threads(g_threads) if (g_threads > 1)
     for (int i = 0; i < n; ++i) s += a[i] * b[i];
     return s;
 }
@@ -372,8 +402,10 @@ static int cg_core(const OrcSystem* s, double* x, int precond /*0 id,1 ssor,2 ja
             orc_spmv(s, d, Ad);
             double alpha = dot(n, d, Ad);
             alpha = gh / alpha;
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
             for (int i = 0; i < n; ++i) x[i] += alpha * d[i];
             double gg = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : gg) num_threads(g_threads) if (g_threads > 1)
             for (int i = 0; i < n; ++i) { g[i] += alpha * Ad[i]; gg += g[i] * g[i]; }
             res = sqrt(fabs(gg));
             if (fixed_it) { if (it >= fixed_it) break; }
@@ -385,6 +417,7 @@ static int cg_core(const OrcSystem* s, double* x, int precond /*0 id,1 ssor,2 ja
             double beta = gh;
             gh = dot(n, g, h);
             beta = gh / beta;
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
             for (int i = 0; i < n; ++i) d[i] = beta * d[i] - h[i];
         }
     }

@@ -47,15 +47,30 @@ void orc_free_system(OrcSystem* sys);
 int orc_system_from_csr(int n, const int64_t* rowptr, const int32_t* col, const double* val, const double* rhs,
                         const double* x0, OrcSystem* sys);
 
+/* Q2 (27-node) vacuum system (oracle/q2_oracle.c): cells = 8 femocs-ordered node ids per
+ * vacuum hex, xyz of all nodes, bc = Neumann value on the top (-E0), n_threads for the cell
+ * matrices and the sparsity (0: OpenMP default; results do not depend on it). cell_dofs
+ * (27 * n_cells) receives the DoF of each lattice node; timing_ms (2, may be NULL) the
+ * milliseconds of the cell matrices and of their serial scatter. */
+int orc_q2_build_system(int n_nodes, const double* xyz, int n_cells, const int32_t* cells, double bc,
+                        int anode_dirichlet, double v0, int n_threads, int32_t* cell_dofs, OrcSystem* sys,
+                        double* timing_ms);
+
 /* deal.II SolverCG + PreconditionSSOR(omega) (src/DealSolver.cpp:443-459); omega <= 0 gives
  * the identity preconditioner. Stop when ||b-Ax||_2 <= tol. Returns #iterations or
  * -#iterations when max_it is reached. */
 int orc_ssor_cg(const OrcSystem* sys, double* x, double omega, double tol, int max_it);
 /* Jacobi-preconditioned CG with the same stop test (plain GPU-CG counterpart). */
 int orc_jacobi_cg(const OrcSystem* sys, double* x, double tol, int max_it);
+/* threads of the CG's SpMV and vector operations (default 1: every sum in a fixed order);
+ * the SSOR sweeps are always sequential, as deal.II's PreconditionSSOR */
+void orc_set_threads(int n);
 /* timing helper: run exactly n_it SSOR-CG iterations regardless of convergence */
 double orc_ssor_cg_fixed(const OrcSystem* sys, double* x, double omega, int n_it);
 void orc_spmv(const OrcSystem* sys, const double* x, double* y);
+/* out2[0] = ||b - A x||_2 with compensated (Dot2) row products; out2[1] = the rounding floor
+ * of a plain FP64 evaluation, 2^-53 ||(|b| + |A||x|)||_2 */
+void orc_residual_comp(const OrcSystem* sys, const double* x, double* out2);
 
 /* ---------- nodal field (src/Interpolator.cpp:125-140 + src/InterpolatorCells.cpp:1462-1505) ----
  * phi: per node of the hex mesh; out E: 3 per node, only nodes with is_vac[node] are set.  */

@@ -10,6 +10,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "femocs_oracle.c")
+SRCS = [SRC, os.path.join(HERE, "q2_oracle.c")]
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboracle.so")
 
@@ -18,17 +19,17 @@ ip = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
 i8p = C.POINTER(C.c_int8)
 
-__all__ = ["build_oracle", "lib", "tet_tables", "System", "neighbour_lists", "nodal_field", "smooth_field",
+__all__ = ["build_oracle", "lib", "tet_tables", "System", "Q2CSystem", "neighbour_lists", "nodal_field", "smooth_field",
            "locate_interpolate", "surface_interpolate", "read_records", "write_msh", "test_solution"]
 
 
 def build_oracle(force=False):
     os.makedirs(OUT, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "femocs_oracle.h"))):
+            [os.path.getmtime(f) for f in SRCS] + [os.path.getmtime(os.path.join(HERE, "femocs_oracle.h"))]):
         return LIB
-    subprocess.run(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-ffp-contract=off", SRC, "-o", LIB, "-lm"],
-                   check=True)
+    subprocess.run(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", *SRCS, "-o", LIB,
+                    "-lm"], check=True)
     return LIB
 
 
@@ -57,12 +58,16 @@ def lib():
         L.orc_tet_tables.argtypes = [C.c_int, ip, dp, dp, dp]
         L.orc_build_system.argtypes = [C.c_int, dp, C.c_int, ip, C.c_double, C.c_int, C.c_double, C.POINTER(OrcSystem)]
         L.orc_free_system.argtypes = [C.POINTER(OrcSystem)]
+        L.orc_q2_build_system.argtypes = [C.c_int, dp, C.c_int, ip, C.c_double, C.c_int, C.c_double, C.c_int, ip,
+                                          C.POINTER(OrcSystem), dp]
         L.orc_system_from_csr.argtypes = [C.c_int, i64p, ip, dp, dp, dp, C.POINTER(OrcSystem)]
         L.orc_ssor_cg.argtypes = [C.POINTER(OrcSystem), dp, C.c_double, C.c_double, C.c_int]
         L.orc_jacobi_cg.argtypes = [C.POINTER(OrcSystem), dp, C.c_double, C.c_int]
         L.orc_ssor_cg_fixed.argtypes = [C.POINTER(OrcSystem), dp, C.c_double, C.c_int]
         L.orc_ssor_cg_fixed.restype = C.c_double
         L.orc_spmv.argtypes = [C.POINTER(OrcSystem), dp, dp]
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_residual_comp.argtypes = [C.POINTER(OrcSystem), dp, dp]
         L.orc_nodal_field.argtypes = [C.c_int, dp, C.c_int, ip, ip, i8p, dp, dp]
         L.orc_smooth_field.argtypes = [C.c_int, dp, ip, ip, C.c_double, dp]
         L.orc_locate_interpolate.argtypes = [C.POINTER(OrcInterp), C.c_int, C.c_int, dp, ip, dp]
@@ -128,15 +133,68 @@ class System:
         it = lib().orc_jacobi_cg(C.byref(self.s), _p(x), tol, max_it)
         return it, x
 
-    def ssor_cg_fixed(self, n_it, omega=1.2):
+    def ssor_cg_fixed(self, n_it, omega=1.2, threads=1):
+        """seconds of exactly n_it SSOR-CG iterations; `threads` for the SpMV and vector
+        operations (the SSOR sweeps are sequential)"""
         x = self.x0.copy()
-        return lib().orc_ssor_cg_fixed(C.byref(self.s), _p(x), omega, n_it)
+        lib().orc_set_threads(int(threads))
+        try:
+            return lib().orc_ssor_cg_fixed(C.byref(self.s), _p(x), omega, n_it)
+        finally:
+            lib().orc_set_threads(1)
+
+    def residual(self, x):
+        """(||b - A x|| compensated, rounding floor of a plain FP64 evaluation), both absolute"""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(2)
+        lib().orc_residual_comp(C.byref(self.s), _p(x), _p(out))
+        return float(out[0]), float(out[1])
 
     def spmv(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros(self.n)
         lib().orc_spmv(C.byref(self.s), _p(x), _p(y))
         return y
+
+
+class Q2CSystem(System):
+    """Q2 vacuum system from oracle/q2_oracle.c (same system as oracle/q2_oracle.py, fast
+    enough for the benchmark meshes). node_xyz: all nodes; cells: 8 femocs-ordered node ids
+    per vacuum hex; bc: Neumann value on the top (-E0). Arrays are views of the C memory.
+    cell_dofs (n_cells, 27): DoF of each lattice node; dof_node: mesh node of each vertex DoF
+    (-1 for edge, face and interior DoFs); timing_ms: cell matrices, serial scatter, total."""
+
+    def __init__(self, node_xyz, cells, bc, anode_dirichlet=False, v0=0.0, n_threads=0):
+        import time
+        self.s = OrcSystem()
+        xyz = np.ascontiguousarray(node_xyz, dtype=np.float64).reshape(-1)
+        cl = np.ascontiguousarray(cells, dtype=np.int32).reshape(-1, 8)
+        nc = len(cl)
+        self.cell_dofs = np.zeros((nc, 27), dtype=np.int32)
+        tm = np.zeros(2)
+        t0 = time.perf_counter()
+        rc = lib().orc_q2_build_system(len(xyz) // 3, _p(xyz), nc, _p(cl, ip), bc, int(anode_dirichlet), v0,
+                                       int(n_threads), _p(self.cell_dofs, ip), C.byref(self.s), _p(tm))
+        total = (time.perf_counter() - t0) * 1e3
+        if rc:
+            raise MemoryError("oracle Q2 system build failed")
+        n, nnz = self.s.n, self.s.nnz
+        self.n = n
+        self.rowptr = np.ctypeslib.as_array(self.s.rowptr, shape=(n + 1,))
+        self.col = np.ctypeslib.as_array(self.s.col, shape=(nnz,))
+        self.val = np.ctypeslib.as_array(self.s.val, shape=(nnz,))
+        self.rhs = np.ctypeslib.as_array(self.s.rhs, shape=(n,))
+        self.x0 = np.ctypeslib.as_array(self.s.x, shape=(n,)).copy()
+        self.constrained = np.ctypeslib.as_array(self.s.constrained, shape=(n,))
+        self.dof_node = np.full(n, -1, dtype=np.int32)
+        for L, k in Q2_CORNER_LATTICE.items():
+            self.dof_node[self.cell_dofs[:, L]] = cl[:, k]
+        self.timing_ms = {"cell_matrices": float(tm[0]), "scatter": float(tm[1]), "total": total}
+
+
+# lattice node (x fastest, 0..26) of each femocs hex vertex k: (hx + 1, hy + 1, hz + 1)
+Q2_CORNER_LATTICE = {((1 + hx) + 3 * (1 + hy) + 9 * (1 + hz)): k for k, (hx, hy, hz) in enumerate(
+    zip([-1, 1, 1, -1, -1, 1, 1, -1], [-1, -1, 1, 1, -1, -1, 1, 1], [-1, -1, -1, -1, 1, 1, 1, 1]))}
 
 
 def neighbour_lists(n_nodes, tets, face_nbr):

@@ -4,20 +4,21 @@ phi = 0 on the metal, field interpolated onto all of its surface atoms (rank 1, 
 reference default).
 
 The oracle solves the reference's system with deal.II's SSOR(1.2)-CG restated
-(src/DealSolver.cpp:443-459), restarted from its true residual down to the FP64 rounding
-floor (~1.5e-12 relative on this mesh), recovers and smooths the nodal
-field (src/Interpolator.cpp:125-170) and locates/interpolates the atoms sequentially
-(src/SolutionReader.cpp:136-165). Against it, per solver and tolerance:
+(src/DealSolver.cpp:443-459), restarted from its true residual until that stops falling,
+recovers and smooths the nodal field (src/Interpolator.cpp:125-170) and locates/interpolates
+the atoms sequentially (src/SolutionReader.cpp:136-165). Against it, per solver and tolerance:
 
-* the relative FP64 residual of the GPU solution, recomputed by the oracle's SpMV on the
-  oracle's own system;
+* the relative residual of the GPU solution in the oracle's own system, evaluated
+  compensated (Dot2), within the tolerance plus twice the FP64 floor 2^-53 |(|b| + |A||x|)|
+  / |b| (the two assemblies sum element contributions in different orders, which moves the
+  system by that much; on this mesh the floor is ~2e-12, so a 1e-12 solve ends on it);
+* the solver's status: converged (1) or at the FP64 floor (2);
 * located cells: bit-exact;
-* max |dphi| at the atoms, relative to max |phi|: below 50 x tol;
-* max relative |dE| at the atoms (points whose field is above 1e-3 of the largest; atoms
-  located in metal carry the empty value 0): below 500 x tol.
+* max |dphi| at the atoms below 0.01 x t x max |phi| and max relative |dE| at the atoms
+  (points whose field is above 1e-3 of the largest; atoms located in metal carry the empty
+  value 0) below 5 x t, with t = max(tol, 2 x floor).
 
-The bounds are a few times the errors measured on a GB300 (stated in the design notes); a
-solve at relative residual tol on this mesh moves phi by about 10 x tol of its range.
+The bounds are several times the errors measured on a GB300 (stated in the design notes).
 Solvers: the default FP64 CG with the FP32 multigrid preconditioner (precision 2) and FP32
 Jacobi-PCG with FP64 refinement (precision 1), at 1e-9 and 1e-12.
 """
@@ -52,24 +53,26 @@ def test_config1_results_match_reference_solve(config1, precision, tol):
     f.setup(E0)
     f.assemble(True, False)
     rc, st = f.solve(precision=precision, rel_tol=tol, max_iter=100000)
-    assert rc > 0 and st["status"] == 1, st
+    assert rc > 0 and st["status"] in (1, 2), st
     system, v2n = info["system"], info["vertex2node"]
     x = f.phi_nodes()[v2n]
-    r = float(np.linalg.norm(system.spmv(x) - system.rhs) / np.linalg.norm(system.rhs))
+    bnorm = float(np.linalg.norm(system.rhs))
+    r_abs, floor_abs = system.residual(x)
+    r, floor = r_abs / bnorm, floor_abs / bnorm
     f.extract(smoothen=True)
     cells, out = f.interpolate(surf, rank=1)
     p = pipeline.point_parity(cells, out, ref_cells, ref_out)
-    p.update(precision=precision, tol=tol, iterations=st["iterations"], rel_residual_gpu=st["rel_residual"],
-             rel_residual_oracle=r, oracle_ssor_iterations=info["ssor_iterations"])
+    p.update(precision=precision, tol=tol, status=st["status"], iterations=st["iterations"],
+             rel_residual_gpu=st["rel_residual"], rel_residual_oracle=r, rel_floor=floor,
+             oracle_ssor_iterations=info["ssor_iterations"], oracle_rel_residual=info["rel_residual"])
     print(json.dumps(p))
     out_dir = os.environ.get("FGB_PARITY_OUT")
     if out_dir:
         with open(os.path.join(out_dir, f"parity_config1_p{precision}_{tol:g}.json"), "w") as fh:
             json.dump(p, fh)
-    # the product's matrix equals the oracle's to rounding, so its residual in the oracle's
-    # system is its own, up to the FP64 rounding floor of b - A x (the oracle's own solve
-    # reaches ~1.5e-12 on this mesh, so at tol = 1e-12 both sit on that floor)
-    assert r <= 1.1 * tol + 2 * info["rel_residual"], r
+    assert r <= 1.1 * tol + 2 * floor, (r, floor)
+    assert st["status"] == 1 or tol < 2 * floor, st  # the floor status only where the floor is above tol
     assert p["cells_bit_exact"], p["cells_differing"]
-    assert p["max_abs_dphi"] <= 50 * tol * np.abs(sol[:, 4]).max(), p
-    assert p["max_rel_dE"] <= 500 * tol, p
+    t = max(tol, 2 * floor)
+    assert p["max_abs_dphi"] <= 0.01 * t * np.abs(sol[:, 4]).max(), p
+    assert p["max_rel_dE"] <= 5 * t, p
