@@ -51,7 +51,7 @@ int orc_system_from_csr(int n, const int64_t* rowptr, const int32_t* col, const 
  * vacuum hex, xyz of all nodes, bc = Neumann value on the top (-E0), n_threads for the cell
  * matrices and the sparsity (0: OpenMP default; results do not depend on it). cell_dofs
  * (27 * n_cells) receives the DoF of each lattice node; timing_ms (2, may be NULL) the
- * milliseconds of the cell matrices and of their serial scatter. */
+ * milliseconds of the cell matrices and of their scatter into the CSR matrix. */
 int orc_q2_build_system(int n_nodes, const double* xyz, int n_cells, const int32_t* cells, double bc,
                         int anode_dirichlet, double v0, int n_threads, int32_t* cell_dofs, OrcSystem* sys,
                         double* timing_ms);

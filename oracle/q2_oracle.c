@@ -10,9 +10,10 @@
  *   - element = tensor quadratic Lagrange hexahedron on the trilinear map of the cell,
  *     K_e[i][j] = sum_q w_q |det J_q| grad N_i . grad N_j over 3x3x3 Gauss points, the Q2
  *     analogue of PoissonSolver::assemble_local_cell (src/PoissonSolver.cpp:239-263); cell
- *     matrices are computed in parallel and scattered serially in cell order, as the
- *     reference's WorkStream assembly does (src/PoissonSolver.cpp:213-237, copier
- *     src/DealSolver.cpp:65-72), so the sums do not depend on the thread count;
+ *     matrices are computed in parallel and every matrix entry sums its cell contributions in
+ *     cell order, as the reference's WorkStream copier does serially (src/PoissonSolver.cpp:
+ *     213-237, src/DealSolver.cpp:65-72): threads own interleaved rows, so the sums do not
+ *     depend on the thread count;
  *   - boundary marking as DealSolver::mark_boundary (src/DealSolver.cpp:461-518): faces of one
  *     cell; x/y extremes of the face centroids are the natural sides, z max the top (Neumann
  *     value bc on 3x3 Gauss points, src/DealSolver.cpp:390-430), every other boundary face
@@ -328,12 +329,23 @@ int orc_q2_build_system(int n_nodes, const double* xyz, int n_cells, const int32
         const double t1 = omp_get_wtime();
         t_local += t1 - t0;
 #endif
-        for (int i = 0; i < m; ++i) {
-            const int32_t* cd = cell_dofs + 27 * (size_t)(c0 + i);
-            const double* K = Kbuf + 729 * (size_t)i;
-            for (int a = 0; a < 27; ++a) {
-                const int r = cd[a];
-                for (int b = 0; b < 27; ++b) sys->val[find_col(sys, r, cd[b])] += K[27 * a + b];
+        /* each thread owns the rows r with r % T == its id and walks the cells in order, so
+         * every entry still sums its cell contributions in cell order */
+#pragma omp parallel
+        {
+            int tid = 0, T = 1;
+#ifdef _OPENMP
+            tid = omp_get_thread_num();
+            T = omp_get_num_threads();
+#endif
+            for (int i = 0; i < m; ++i) {
+                const int32_t* cd = cell_dofs + 27 * (size_t)(c0 + i);
+                const double* K = Kbuf + 729 * (size_t)i;
+                for (int a = 0; a < 27; ++a) {
+                    const int r = cd[a];
+                    if (r % T != tid) continue;
+                    for (int b = 0; b < 27; ++b) sys->val[find_col(sys, r, cd[b])] += K[27 * a + b];
+                }
             }
         }
 #ifdef _OPENMP

@@ -1,0 +1,82 @@
+"""The solve against the reference's own analytic answer: a conducting hemisphere on a grounded
+plane in a uniform field, FieldReader::get_analyt_potential / get_analyt_field
+(src/SolutionReader.cpp:501-524), on boundary-fitted meshes refined three times (tests/analytic.py).
+
+Measured at the mesh nodes with 1.2 R < r < 4 R (away from the hemisphere, where the polyhedral
+surface differs from the sphere, and from the box, where the exact solution is not quite the
+box's boundary data):
+
+* phi at every vacuum node: the error falls at rate ~2 per halving of h for Q1 and Q2 (Q2 is
+  held to second order by the straight-faced approximation of the sphere); required >= 1.6
+  between consecutive levels and a finest error below 0.5 % of max |phi| there;
+* the recovered nodal E (src/Interpolator.cpp:125-140) at the tet vertices with 1.5 R < r < 4 R
+  (beyond the first radial layer of the coarsest mesh): required rate >= 0.8 between
+  consecutive levels. (At face- and tet-centroid nodes the reference's
+  three-neighbour gradient shortcut, src/InterpolatorCells.cpp:1462-1505, does not converge
+  in the max norm on the non-orthogonal corners of the split hexahedra; it is reproduced bit
+  for bit and so not asserted here.)
+* the M/A field-enhancement ratio of the reference's check (src/SolutionReader.cpp:526-556)
+  with the hemisphere's analytic enhancement 3 approaches 1.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import femocs_gb300 as fg
+from analytic import analytic_field, analytic_phi, hemisphere_mesh
+
+pytestmark = pytest.mark.gpu
+R, BOX, E0 = 10.0, 200.0, -0.1
+LEVELS = (4, 8, 16)
+
+
+@pytest.fixture(scope="module")
+def meshes():
+    return {n: fg.Mesh.from_arrays(*hemisphere_mesh(n, R, BOX)) for n in LEVELS}
+
+
+def node_errors(m, f):
+    X = m.export("node_xyz").reshape(-1, 3)
+    r = np.linalg.norm(X, axis=1)
+    vac = m.export("vac_node2vertex") >= 0
+    sel = vac & (r > 1.2 * R) & (r < 4 * R)
+    tv = vac & (r > 1.5 * R) & (r < 4 * R) & (m.export("node_marker") == 1)
+    phi = f.phi_nodes()
+    E = f.nodal()[:, :3]
+    e_phi = np.abs(phi[sel] - analytic_phi(X[sel], E0, R)).max()
+    phi_scale = np.abs(analytic_phi(X[sel], E0, R)).max()
+    e_E = np.linalg.norm(E[tv] - analytic_field(X[tv], E0, R), axis=1).max()
+    m_over_a = np.linalg.norm(E[vac], axis=1).max() / abs(E0) / 3.0
+    return float(e_phi), float(phi_scale), float(e_E), float(m_over_a)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_hemisphere_converges_to_reference_formula(meshes, order):
+    rows = []
+    for n in LEVELS:
+        m = meshes[n]
+        f = fg.Field(m, order=order)
+        f.setup(-E0)
+        f.assemble(True, False)
+        rc, st = f.solve(precision=2, rel_tol=1e-11, max_iter=20000)
+        assert rc > 0, st
+        f.extract(smoothen=True)
+        e_phi, scale, e_E, ma = node_errors(m, f)
+        rows.append({"n": n, "dofs": f.n_dofs, "max_dphi": e_phi, "max_phi": scale, "max_dE_tet_vertices": e_E,
+                     "M_over_A": ma, "iterations": st["iterations"]})
+    for a, b in zip(rows, rows[1:]):
+        b["rate_phi"] = float(np.log2(a["max_dphi"] / b["max_dphi"]))
+        b["rate_E"] = float(np.log2(a["max_dE_tet_vertices"] / b["max_dE_tet_vertices"]))
+    print(json.dumps({"order": order, "levels": rows}))
+    out_dir = os.environ.get("FGB_PARITY_OUT")
+    if out_dir:
+        with open(os.path.join(out_dir, f"analytic_hemisphere_q{order}.json"), "w") as fh:
+            json.dump({"order": order, "levels": rows}, fh)
+    for b in rows[1:]:
+        assert b["rate_phi"] >= 1.6, rows
+        assert b["rate_E"] >= 0.8, rows
+    assert rows[-1]["max_dphi"] <= 5e-3 * rows[-1]["max_phi"], rows
+    # M/A moves toward 1 with refinement and ends within 10 %
+    assert abs(rows[-1]["M_over_A"] - 1) <= abs(rows[0]["M_over_A"] - 1) and abs(rows[-1]["M_over_A"] - 1) < 0.1, rows
