@@ -561,7 +561,10 @@ def run_ours(args, world, rank):
         if args.workload != "config1":
             line["parity"]["config1"] = config1_parity()
     if rank == 0 and world == 1 and not args.no_cpu and args.workload in ("config1", "config2"):
-        line["cpu_baseline"] = cpu_baseline(field, args.workload, order, sysm=sysm)
+        try:
+            line["cpu_baseline"] = cpu_baseline(field, args.workload, order, sysm=sysm)
+        except RuntimeError as e:  # no full-solve iteration count recorded for this system
+            line["cpu_baseline"] = {"unavailable": str(e)}
     del sysm, snap
     line["surface_interp"] = {"points": n_surf, "gpu_ms": surf_ms, "gpu_points_per_s": n_surf / (surf_ms * 1e-3),
                               "rank": 1, "note": "femocs_interpolate_surface_elfield path, device-resident points"}

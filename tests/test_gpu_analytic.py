@@ -9,9 +9,10 @@ box's boundary data):
 * phi at every vacuum node: the error falls at rate ~2 per halving of h for Q1 and Q2 (Q2 is
   held to second order by the straight-faced approximation of the sphere); required >= 1.6
   between consecutive levels and a finest error below 0.5 % of max |phi| there;
-* the recovered nodal E (src/Interpolator.cpp:125-140) at the tet vertices with 1.5 R < r < 4 R
-  (beyond the first radial layer of the coarsest mesh): required rate >= 0.8 between
-  consecutive levels. (At face- and tet-centroid nodes the reference's
+* the recovered nodal E (src/Interpolator.cpp:125-140, before the smoothing step, whose
+  weighted neighbourhood average adds an O(h) bias and is checked bit for bit against the
+  reference elsewhere) at the tet vertices with 1.5 R < r < 4 R (beyond the first radial layer
+  of the coarsest mesh): required rate >= 0.8 between consecutive levels. (At face- and tet-centroid nodes the reference's
   three-neighbour gradient shortcut, src/InterpolatorCells.cpp:1462-1505, does not converge
   in the max norm on the non-orthogonal corners of the split hexahedra; it is reproduced bit
   for bit and so not asserted here.)
@@ -44,11 +45,14 @@ def node_errors(m, f):
     sel = vac & (r > 1.2 * R) & (r < 4 * R)
     tv = vac & (r > 1.5 * R) & (r < 4 * R) & (m.export("node_marker") == 1)
     phi = f.phi_nodes()
+    f.extract(smoothen=False)
     E = f.nodal()[:, :3]
     e_phi = np.abs(phi[sel] - analytic_phi(X[sel], E0, R)).max()
     phi_scale = np.abs(analytic_phi(X[sel], E0, R)).max()
     e_E = np.linalg.norm(E[tv] - analytic_field(X[tv], E0, R), axis=1).max()
-    m_over_a = np.linalg.norm(E[vac], axis=1).max() / abs(E0) / 3.0
+    # the enhancement check reads the smoothed nodal field, as the reference's does
+    f.extract(smoothen=True)
+    m_over_a = np.linalg.norm(f.nodal()[vac, :3], axis=1).max() / abs(E0) / 3.0
     return float(e_phi), float(phi_scale), float(e_E), float(m_over_a)
 
 
@@ -62,7 +66,6 @@ def test_hemisphere_converges_to_reference_formula(meshes, order):
         f.assemble(True, False)
         rc, st = f.solve(precision=2, rel_tol=1e-11, max_iter=20000)
         assert rc > 0, st
-        f.extract(smoothen=True)
         e_phi, scale, e_E, ma = node_errors(m, f)
         rows.append({"n": n, "dofs": f.n_dofs, "max_dphi": e_phi, "max_phi": scale, "max_dE_tet_vertices": e_E,
                      "M_over_A": ma, "iterations": st["iterations"]})
