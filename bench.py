@@ -571,6 +571,9 @@ def run_ours(args, world, rank):
     if rank == 0 and world == 1 and not args.no_cpu:
         line["mesh_prep"] = mesh_prep_timing(spec, order)
         line["surface_interp"].update(surface_cpu_timing(spec, pts[:n_surf]))
+    if rank == 0 and world == 1 and args.workload == "config2" and not args.no_extra:
+        del field, fem
+        line.update(batch_and_serve_summaries(args, world, rank))
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -652,6 +655,37 @@ def workload_config(workload, spec, order, n_dofs, nnz, n_points, n_surf, world)
             "n_surface_atoms": int(n_surf), "interpolation_rank": RANK, "rel_tol": REL_TOL,
             "l2": "inputs larger than L2 (FP64 matrix %.0f MB)" % (nnz * 12 / 1e6),
             "parallelism": f"replicas x{world} (independent solves, no exchange)"}
+
+
+def batch_and_serve_summaries(args, world, rank):
+    """Compact results of the batched (256 meshes) and served (64 MD runs, Poisson arrivals)
+    workloads for the default line; `--workload batch` / `--workload serve` give the full lines."""
+    import copy
+    a = copy.copy(args)
+    a.steps, a.warmup, a.meshes, a.sample = 2, 1, 256, 8
+    bl = run_batch(a, world, rank, quiet=True)
+    sp = bl["sample_vs_plain_fp64_cg"]
+    out = {"batch": {"workload": bl["config"]["workload"], "meshes": bl["config"]["n_meshes"],
+                     "total_dofs": bl["config"]["total_dofs"], "dof_per_s": bl["value"],
+                     "ms_per_step": bl["ms_per_step"], "solves_per_s": bl["batch"]["solves_per_s"],
+                     "converged": bl["batch"]["converged"], "iterations_p50": bl["batch"]["iterations_p50"],
+                     "kernels_per_iteration": bl["batch"]["kernels_per_iteration"], "build_s": bl["batch"]["build_s"],
+                     "steps": a.steps, "clocks": bl["clocks"],
+                     "sample_vs_plain_fp64_cg": {k: sp[k] for k in ("meshes", "dofs", "batched_ms", "plain_sequential_ms",
+                                                                    "solves_per_s_batched", "solves_per_s_plain",
+                                                                    "speedup")}}}
+    a = copy.copy(args)
+    a.rates, a.duration, a.runs = [50.0, 200.0, 1000.0], 2.0, 64
+    sl = run_serve(a, world, rank, quiet=True)
+    out["serve"] = {"workload": sl["config"]["workload"], "total_dofs": sl["config"]["total_dofs"],
+                    "saturation_solves_per_s": sl["value"],
+                    "rates": [{k: d[k] for k in ("rate", "requests", "completed", "converged", "solves_per_s", "p50_ms",
+                                                 "p99_ms", "p50_queue_ms", "p50_solve_ms", "p50_post_ms", "iterations_mean")}
+                              for d in sl["sweep"]],
+                    "plain_fp64_cg_served_one_at_a_time": sl["plain_fp64_cg_served_one_at_a_time"],
+                    "speedup_vs_plain": sl["speedup_vs_plain"], "iters_per_launch": a.iters_per_launch,
+                    "build_s": sl["build_s"], "clocks": sl["clocks"]}
+    return out
 
 
 def run_reference(args, world, rank):
@@ -753,7 +787,7 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args, world, rank):
+def run_batch(args, world, rank, quiet=False):
     """256 independent nanotip meshes (tip radius 1-6 nm, aspect 2-8, field 0.5-3 GV/m, Q1
     meshes of 2e4-8e5 vacuum hexes, log-uniform) resident in one batch. One step = a cold
     (zero start) solve of every mesh to 1e-9, all meshes in one graph-captured WHILE loop.
@@ -839,11 +873,61 @@ def run_batch(args, world, rank):
                                     "speedup": float(sum(plain_ms)) / batch_sample_ms},
         "clocks": clocks, "gpu_launches": launches,
     }
-    if rank == 0:
+    if rank == 0 and not quiet:
         print(json.dumps(line), flush=True)
+    return line
 
 
-def run_serve(args, world, rank):
+def serve_plain_baseline(specs, base, n_atoms, runs, steps=3, seed=5):
+    """Like-for-like baseline of the serving loop: the same MD-step requests (atoms displaced by
+    N(0, 0.02 A), applied field within 1 % of the run's base field, solve warm-started from the
+    run's previous phi to 1e-9, nodal field + smoothing, location + interpolation at the run's
+    atoms, results copied to the host) served one at a time with the plain FP64 Jacobi-PCG.
+    Each run is first solved cold, as the serving loop's warm-up does."""
+    import numpy as np
+    import femocs_gb300 as fg
+    rng = np.random.default_rng(17)
+    times, iters = [], []
+    for r in runs:
+        spec = specs[r]
+        m = fg.Mesh.synthetic(**spec)
+        f = fg.Field(m)
+        atoms, types = fg.synth_atoms(spec, seed=seed + 7919 * r)
+        surf = atoms[types == 2]
+        if len(surf) >= n_atoms:
+            pts = surf[(np.arange(n_atoms) * len(surf)) // n_atoms]
+        else:
+            pts = np.r_[surf, fg.synth_probes(spec, n_atoms - len(surf), seed=seed + 104729 * r)]
+        d_pts = fg.DeviceBuffer(24 * len(pts))
+        d_cells = fg.DeviceBuffer(4 * len(pts))
+        d_out = fg.DeviceBuffer(40 * len(pts))
+        out = np.zeros((len(pts), 5))
+        f.setup(base[r])
+        f.assemble(True, False)
+        f.solve(precision=0, rel_tol=REL_TOL, max_iter=100000)
+        for _ in range(steps):
+            pts = pts + rng.normal(0.0, 0.02, pts.shape)
+            t0 = time.perf_counter()
+            phi = f.phi_nodes()
+            f.setup(base[r] * (1.0 + 0.01 * rng.standard_normal()))
+            f.set_phi_nodes(phi)
+            f.assemble(False, False)
+            rc, st = f.solve(precision=0, rel_tol=REL_TOL, max_iter=100000)
+            f.extract(True)
+            d_pts.upload(np.ascontiguousarray(pts))
+            f.interpolate_device(len(pts), d_pts.ptr, RANK, d_cells.ptr, d_out.ptr)
+            d_out.download(out)
+            times.append(time.perf_counter() - t0)
+            iters.append(st["iterations"])
+        del f, m
+    return {"runs": [int(r) for r in runs], "requests": len(times), "p50_ms": float(np.median(times) * 1e3),
+            "mean_ms": float(np.mean(times) * 1e3), "iterations_mean": float(np.mean(iters)),
+            "solves_per_s": float(len(times) / np.sum(times)),
+            "note": "the serving loop's request (atom step, warm start, nodal field, interpolation, host copy) "
+                    "one at a time with plain FP64 Jacobi-PCG"}
+
+
+def run_serve(args, world, rank, quiet=False):
     """64 concurrent MD runs (half the config-0 tip, half random batch-style tips), ~5e4
     atoms each, resident; Poisson arrivals swept over rates; each request displaces its run's
     atoms by N(0, 0.02 A), re-solves warm-started with an applied field within 1% of the
@@ -898,16 +982,10 @@ def run_serve(args, world, rank):
     clocks = sampler.stop()
     srv.stop()
     info = srv.info()
-    # plain FP64 Jacobi-CG: cold single-mesh solve latency of a few runs' meshes
-    plain = []
-    for r in [0, half, n_runs - 1]:
-        m = fg.Mesh.synthetic(**specs[r])
-        f = fg.Field(m)
-        f.setup(-float(base[r]))
-        f.assemble(True, False)
-        rc, st = f.solve(precision=0, rel_tol=REL_TOL, max_iter=100000)
-        plain.append({"run": r, "dofs": f.n_dofs, "ms": st["ms"], "iterations": st["iterations"]})
-        del f, m
+    # like-for-like: the same requests one at a time with the plain FP64 Jacobi-PCG, on runs of
+    # both halves (config-1 tips and random batch tips)
+    sample_runs = sorted(set([0, 1, half, half + 1, n_runs - 1]))
+    plain = serve_plain_baseline(specs, base, args.atoms, sample_runs)
     best = max(sweep, key=lambda d: d["solves_per_s"])
     line = {
         "metric": "solves/s and p50/p99 latency at 1e-9 rel. residual (serving, Poisson arrivals)",
@@ -918,11 +996,13 @@ def run_serve(args, world, rank):
                                f"{args.atoms} atoms each, sigma 0.02 A per step, Poisson arrivals",
                    "total_dofs": int(dofs.sum()), "rates": args.rates, "iters_per_launch": args.iters_per_launch},
         "sweep": sweep, "build_s": build_s, "max_requests_in_flight": info["max_in_flight"],
-        "solver_launches": info["solver_launches"], "plain_fp64_cg_cold_solves": plain,
+        "solver_launches": info["solver_launches"], "plain_fp64_cg_served_one_at_a_time": plain,
+        "speedup_vs_plain": best["solves_per_s"] / plain["solves_per_s"],
         "clocks": clocks, "gpu_launches": launches,
     }
-    if rank == 0:
+    if rank == 0 and not quiet:
         print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -944,6 +1024,7 @@ def main():
                     help="element order (default: 2 for config2/probe, 1 for config1)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-parity", action="store_true", help="skip the parity checks against the oracle")
+    ap.add_argument("--no-extra", action="store_true", help="config2: skip the batch and serving summaries")
     args = ap.parse_args()
     world, rank, _ = dist_setup()
     if args.impl == "reference":

@@ -224,6 +224,15 @@ class Field:
         through the SELL matrix (False)."""
         self._ok(load().fgb_field_set_level0_ebe(self.h, int(on)))
 
+    def set_level0_stream(self, on=True):
+        """Q2 level 0 by cell blocks: element matrices through the bulk-copy ring (True) or
+        loaded by the applying warps (False)."""
+        self._ok(load().fgb_field_set_level0_stream(self.h, int(on)))
+
+    def set_coarse_cycles(self, level=0, cycles=1):
+        """Multigrid: cycles of level+1 per coarse-grid correction at `level` (1 = V-cycle)."""
+        self._ok(load().fgb_field_set_coarse_cycles(self.h, level, cycles))
+
     def set_smoothing(self, degree=0, lo=0.0):
         """Chebyshev degree and interval of the finest multigrid level (0: defaults)."""
         self._ok(load().fgb_field_set_smoothing(self.h, int(degree), float(lo)))

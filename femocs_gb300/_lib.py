@@ -91,6 +91,8 @@ _PROTOS = {
     "fgb_field_solve": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, dp]),
     "fgb_field_last_stats": (C.c_int, [vp, dp]),
     "fgb_field_set_profiling": (C.c_int, [vp, C.c_int]),
+    "fgb_field_set_coarse_cycles": (C.c_int, [vp, C.c_int, C.c_int]),
+    "fgb_field_set_level0_stream": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_smoothing": (C.c_int, [vp, C.c_int, C.c_double]),
     "fgb_field_set_level0_ebe": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_outer_spmv": (C.c_int, [vp, C.c_int]),

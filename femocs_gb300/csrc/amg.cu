@@ -39,6 +39,7 @@ struct AmgDevLevel {
     DBuf<int32_t> p_col, r_col;
     DBuf<float> p_val, r_val;
     DBuf<float> b, xa, xb, d, r;
+    DBuf<float> xacc, rtmp;      // repeated coarse cycles: the summed result, the residual
     const float* bin = nullptr;  // right-hand side of this level (level 0: the caller's vector)
     float* x = nullptr;          // result of the last cycle on this level
 };
@@ -146,6 +147,11 @@ __global__ void __launch_bounds__(kB) k_cheb_step(Op A, const float* __restrict_
     xout[i] = xin[i] + di;
 }
 
+__global__ void k_add_f(int n, const float* __restrict__ y, float* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += y[i];
+}
+
 template <int TPR>
 __global__ void __launch_bounds__(kB) k_residual(Op A, const float* __restrict__ b, const float* __restrict__ x,
                                                  float* __restrict__ r) {
@@ -190,9 +196,57 @@ __device__ __forceinline__ void l0_finish(int g, float ax, float xg, const float
 constexpr int kCbPer = 16;     // block-local DoFs per thread at most (max_dofs <= 4096)
 constexpr int kCbMaxCells = 256;
 
+// Streamed variant: a producer warp copies each block's element matrices (contiguous in block
+// order, 1512 B per cell) with cp.async.bulk into a ring of kCbRing slots of kCbChunk cells,
+// one cell per consumer warp per slot; full/empty mbarriers pace it. A copy starts on the
+// 16-byte boundary at or below its first cell (cells alternate between 0 and 8 bytes past
+// one) and never reads past the array: the last <= 8 bytes of the array are loaded plainly.
+constexpr int kCbRing = 4;
+constexpr int kCbChunk = kCb / 32;                  // cells per slot = consumer warps
+constexpr int kCbSlot = kCbChunk * 1512 + 16;       // bytes per slot (alignment slack)
+constexpr unsigned kCbSpin = 1u << 22;              // try_wait rounds before a wait gives up
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// wait for the phase of the given parity to complete, at most kCbSpin rounds
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (unsigned i = 0; i < kCbSpin; ++i) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// barrier over the consumer warps of the streamed kernel (the producer does not take part)
+__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kCb) : "memory"); }
+
 // shared memory of one block: its item lists (28 u16 per cell), x of its DoFs, the products
 __host__ __device__ inline size_t cb_smem_bytes(int max_cells, int max_dofs) {
     return 56 * (size_t)max_cells + 4 * (size_t)max_dofs + 108 * (size_t)max_cells;
+}
+// the streamed variant: the same, then (128-byte aligned) the ring and its full/empty barriers
+__host__ __device__ inline size_t cb_stream_smem_bytes(int max_cells, int max_dofs) {
+    return ((cb_smem_bytes(max_cells, max_dofs) + 127) & ~(size_t)127) + kCbRing * (size_t)kCbSlot + 2 * kCbRing * 8;
 }
 
 // One block per CTA, three phases separated by barriers:
@@ -204,11 +258,14 @@ __host__ __device__ inline size_t cb_smem_bytes(int max_cells, int max_dofs) {
 //     cell's matrix is loaded while the current one is applied;
 //  C  the products of each DoF summed in item order; complete DoFs finished (Chebyshev update
 //     or residual), the others leave their partial sum in their slot.
-template <int KIND>
-__global__ void __launch_bounds__(kCb, 3) k_cb_apply(EbeOperator op, const float* __restrict__ dinv,
-                                                     const float* __restrict__ b, const float* __restrict__ xin,
-                                                     float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
-    extern __shared__ __align__(16) unsigned char cb_raw[];
+//
+// STREAM: the element matrices come through the bulk-copy ring instead (one more warp, the
+// producer; phases separated by a barrier over the consumer warps only).
+template <int KIND, bool STREAM>
+__global__ void __launch_bounds__(STREAM ? kCb + 32 : kCb, STREAM ? 2 : 3)
+    k_cb_apply(EbeOperator op, const float* __restrict__ dinv, const float* __restrict__ b,
+               const float* __restrict__ xin, float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
+    extern __shared__ __align__(128) unsigned char cb_raw[];
     const int blk = blockIdx.x;
     const int p0 = op.cell_start[blk], nb = op.cell_start[blk + 1] - p0;
     const int q0 = op.dof_start[blk], nq = op.dof_start[blk + 1] - q0;
@@ -219,6 +276,56 @@ __global__ void __launch_bounds__(kCb, 3) k_cb_apply(EbeOperator op, const float
     const int lane = tid & 31, warp = tid >> 5;
     const int il = lane < 27 ? lane : 26;  // lanes 27..31 shadow lane 26 and store nothing
     const uint16_t* loc = op.loc + 27 * (size_t)p0;
+    // ring and barriers after the phase buffers (128-byte aligned)
+    unsigned char* ring = cb_raw + ((cb_smem_bytes(op.max_cells, op.max_dofs) + 127) & ~(size_t)127);
+    uint64_t* full = reinterpret_cast<uint64_t*>(ring + kCbRing * (size_t)kCbSlot);
+    uint64_t* empty = full + kCbRing;
+    const int n_chunks = (nb + kCbChunk - 1) / kCbChunk;
+    if constexpr (STREAM) {
+        if (tid == 0) {
+            for (int s = 0; s < kCbRing; ++s) {
+                mbar_init(&full[s], 1);
+                mbar_init(&empty[s], kCbChunk);
+            }
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (warp == kCb / 32) {
+            // producer: chunk j (cells 8j .. 8j+7 of the block) into slot j % kCbRing
+            if (lane == 0) {
+                const unsigned char* base = reinterpret_cast<const unsigned char*>(op.ke);
+                const int64_t end = 4 * op.n_ke;  // bytes in the array
+                for (int j = 0; j < n_chunks; ++j) {
+                    const int sl = j % kCbRing;
+                    if (j >= kCbRing && !mbar_wait(&empty[sl], ((j / kCbRing) - 1) & 1)) {
+                        atomicOr(op.err, 1u);
+                        break;
+                    }
+                    const int cells = min(kCbChunk, nb - j * kCbChunk);
+                    const int64_t src = 1512 * (int64_t)(p0 + j * kCbChunk);
+                    const int64_t a = src & 15;
+                    int64_t n = (1512 * (int64_t)cells + a + 15) & ~(int64_t)15;
+                    unsigned char* dst = ring + sl * (size_t)kCbSlot;
+                    int64_t tail = 0;  // bytes past the last 16-byte boundary of the array
+                    if (src - a + n > end) {
+                        tail = end - (src - a + n - 16);
+                        n -= 16;
+                    }
+                    if (tail > 0) {
+                        // the array's last bytes (a multiple of 4, at most 8): plain loads and
+                        // stores before the arrive, whose release makes them visible to the
+                        // consumers that acquire the completed phase
+                        for (int64_t k = 0; k < tail; k += 4)
+                            *reinterpret_cast<unsigned*>(dst + n + k) =
+                                __ldg(reinterpret_cast<const unsigned*>(base + src - a + n + k));
+                    }
+                    mbar_expect_tx(&full[sl], (unsigned)n);
+                    bulk_g2s(dst, base + src - a, (unsigned)n, &full[sl]);
+                }
+            }
+            return;
+        }
+    }
     // cells of warp w: w, w + 8, w + 16, ...; two register sets (A, B) alternate so that the
     // next cell's element matrix is in flight while the current one is applied. The first
     // cell's is requested before phase A, so that it travels while the gathers run.
@@ -234,7 +341,7 @@ __global__ void __launch_bounds__(kCb, 3) k_cb_apply(EbeOperator op, const float
         }
         l = __ldg(loc + 27 * c + il);
     };
-    if (warp < nb) load_cell(warp, kA, lA);
+    if (!STREAM && warp < nb) load_cell(warp, kA, lA);
     {
         const uint2* gi = reinterpret_cast<const uint2*>(op.items + 28 * (size_t)p0);
         uint2* si = reinterpret_cast<uint2*>(sit);
@@ -271,7 +378,8 @@ __global__ void __launch_bounds__(kCb, 3) k_cb_apply(EbeOperator op, const float
             if (w < nw) si[w] = w8[r];
         }
     }
-    __syncthreads();
+    if constexpr (STREAM) consumers_sync();
+    else __syncthreads();
     // source lanes of the shuffles, (lane +- t) mod 27, the same for every cell
     int up[14], dn[14];
 #pragma unroll
@@ -291,14 +399,41 @@ __global__ void __launch_bounds__(kCb, 3) k_cb_apply(EbeOperator op, const float
         if (lane < 27) sy[27 * c + lane] = y;
     };
     constexpr int kW = kCb / 32;
-    for (int c = warp; c < nb; c += 2 * kW) {
-        if (c + kW < nb) load_cell(c + kW, kB, lB);
-        apply_cell(c, kA, lA);
-        if (c + kW >= nb) break;
-        if (c + 2 * kW < nb) load_cell(c + 2 * kW, kA, lA);
-        apply_cell(c + kW, kB, lB);
+    if constexpr (STREAM) {
+        bool ok = true;
+        for (int j = 0; j < n_chunks; ++j) {
+            const int sl = j % kCbRing;
+            if (ok && !mbar_wait(&full[sl], (j / kCbRing) & 1)) {
+                ok = false;
+                if (lane == 0) atomicOr(op.err, 2u);
+            }
+            const int c = j * kCbChunk + warp;
+            if (ok && c < nb) {
+                const int64_t src = 1512 * (int64_t)(p0 + j * kCbChunk);
+                const float2* K = reinterpret_cast<const float2*>(ring + sl * (size_t)kCbSlot + (src & 15) + 1512 * warp);
+#pragma unroll
+                for (int u = 0; u < 7; ++u) {
+                    const float2 v = K[27 * u + il];
+                    kA[2 * u] = v.x;
+                    kA[2 * u + 1] = v.y;
+                }
+                lA = __ldg(loc + 27 * c + il);
+                apply_cell(c, kA, lA);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[sl]);
+        }
+        consumers_sync();
+    } else {
+        for (int c = warp; c < nb; c += 2 * kW) {
+            if (c + kW < nb) load_cell(c + kW, kB, lB);
+            apply_cell(c, kA, lA);
+            if (c + kW >= nb) break;
+            if (c + 2 * kW < nb) load_cell(c + 2 * kW, kA, lA);
+            apply_cell(c + kW, kB, lB);
+        }
+        __syncthreads();
     }
-    __syncthreads();
 #pragma unroll 1
     for (int r0 = 0; r0 < kCbPer; r0 += 8) {
         if (tid + r0 * kCb >= nq) break;
@@ -524,6 +659,12 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
 
 AmgDevice::~AmgDevice() = default;
 
+void AmgDevice::set_coarse_cycles(int level, int cycles) {
+    FGB_REQUIRE(level >= 0 && cycles >= 1 && cycles <= 8, "coarse cycles: level >= 0, 1..8 cycles");
+    if ((int)coarse_cycles_.size() <= level) coarse_cycles_.resize(level + 1, 1);
+    coarse_cycles_[level] = cycles;
+}
+
 int AmgDevice::n_levels() const { return (int)lv_.size(); }
 void AmgDevice::set_level0_lambda(double lambda) {
     FGB_REQUIRE(lambda > 0 && std::isfinite(lambda), "level-0 lambda_max must be positive");
@@ -575,6 +716,24 @@ void AmgDevice::cycle(int l) {
     FGB_TPR_DISPATCH(k_csr_apply, L.r_tpr, C.n, stream_, C.n, L.r_ptr.get(), L.r_col.get(), L.r_val.get(), L.r.get(),
                      C.b.get(), 0);
     cycle(l + 1);
+    const int ncyc = l < (int)coarse_cycles_.size() ? coarse_cycles_[l] : 1;
+    if (ncyc > 1 && l + 1 < (int)lv_.size() - 1) {
+        // further cycles of the next level on the residual of the sum so far (the coarsest
+        // level is solved exactly, so repeating it adds nothing)
+        if (C.xacc.size() != (size_t)C.n) C.xacc.resize(C.n);
+        if (C.rtmp.size() != (size_t)C.n) C.rtmp.resize(C.n);
+        FGB_CUDA(cudaMemcpyAsync(C.xacc.get(), C.x, sizeof(float) * C.n, cudaMemcpyDeviceToDevice, stream_));
+        const Op AC{C.n, C.sptr, C.slen, C.scol, C.val, C.dinv};
+        const int gc = grid_for(C.n, kB);
+        for (int k = 1; k < ncyc; ++k) {
+            FGB_TPR_DISPATCH(k_residual, C.tpr, C.n, stream_, AC, C.b.get(), C.xacc.get(), C.rtmp.get());
+            C.bin = C.rtmp.get();
+            cycle(l + 1);
+            C.bin = C.b.get();
+            FGB_LAUNCH(k_add_f<<<gc, kB, 0, stream_>>>(C.n, C.x, C.xacc.get()));
+        }
+        C.x = C.xacc.get();
+    }
     FGB_TPR_DISPATCH(k_csr_apply, L.p_tpr, L.n, stream_, L.n, L.p_ptr.get(), L.p_col.get(), L.p_val.get(), C.x,
                      L.xb.get(), 1);
     // post-smoothing (same polynomial) from the corrected xb; even steps write xa, odd ones xb
@@ -599,10 +758,25 @@ void AmgDevice::set_level0_ebe(const EbeOperator* op) {
     ebe_ = *op;
     ebe_on_ = true;
     FGB_REQUIRE(op->max_cells <= kCbMaxCells && op->max_dofs <= kCbPer * kCb, "cell blocks too large");
+    FGB_REQUIRE(op->n_ke == 378LL * op->n_cells, "element matrices: 378 floats per cell");
+    if (ebe_err_.size() != 1) ebe_err_.resize(1);
+    FGB_CUDA(cudaMemsetAsync(ebe_err_.get(), 0, sizeof(unsigned), stream_));
+    ebe_.err = ebe_err_.get();
     // the cap is a property of the kernel, shared by every mesh: always the largest block's
     const int cap = (int)cb_smem_bytes(kCbMaxCells, kCbPer * kCb);
-    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    const int cap_s = (int)cb_stream_smem_bytes(kCbMaxCells, kCbPer * kCb);
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_s));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_s));
+}
+
+unsigned AmgDevice::level0_errors() {
+    if (!ebe_on_ || ebe_err_.size() != 1) return 0;
+    unsigned h = 0;
+    FGB_CUDA(cudaMemcpyAsync(&h, ebe_err_.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    return h;
 }
 
 double AmgDevice::smoother_bytes() const {
@@ -622,16 +796,29 @@ void AmgDevice::level0_apply(int kind, const float* xin, float* xout, float c1, 
     AmgDevLevel& L = *lv_[0];
     const int g = grid_for(L.n, kB);
     if (ebe_on_) {
-        const size_t smem = cb_smem_bytes(ebe_.max_cells, ebe_.max_dofs);
         const int gb = grid_for(ebe_.n_bnd, kB);
-        if (kind == 0) {
-            FGB_LAUNCH(k_cb_apply<0><<<ebe_.n_blocks, kCb, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, L.d.get(),
-                                                                            c1, c2));
-            if (gb) FGB_LAUNCH(k_cb_finish<0><<<gb, kB, 0, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, L.d.get(), c1, c2));
+        if (stream_ke_) {
+            const size_t smem = cb_stream_smem_bytes(ebe_.max_cells, ebe_.max_dofs);
+            if (kind == 0)
+                FGB_LAUNCH(k_cb_apply<0, true><<<ebe_.n_blocks, kCb + 32, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout,
+                                                                                          L.d.get(), c1, c2));
+            else
+                FGB_LAUNCH(k_cb_apply<1, true><<<ebe_.n_blocks, kCb + 32, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout,
+                                                                                          nullptr, 0.f, 0.f));
         } else {
-            FGB_LAUNCH(k_cb_apply<1><<<ebe_.n_blocks, kCb, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, nullptr,
-                                                                            0.f, 0.f));
-            if (gb) FGB_LAUNCH(k_cb_finish<1><<<gb, kB, 0, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, nullptr, 0.f, 0.f));
+            const size_t smem = cb_smem_bytes(ebe_.max_cells, ebe_.max_dofs);
+            if (kind == 0)
+                FGB_LAUNCH(k_cb_apply<0, false><<<ebe_.n_blocks, kCb, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout,
+                                                                                      L.d.get(), c1, c2));
+            else
+                FGB_LAUNCH(k_cb_apply<1, false><<<ebe_.n_blocks, kCb, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout,
+                                                                                      nullptr, 0.f, 0.f));
+        }
+        if (gb) {
+            if (kind == 0)
+                FGB_LAUNCH(k_cb_finish<0><<<gb, kB, 0, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, L.d.get(), c1, c2));
+            else
+                FGB_LAUNCH(k_cb_finish<1><<<gb, kB, 0, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, nullptr, 0.f, 0.f));
         }
         return;
     }

@@ -73,6 +73,8 @@ struct EbeOperator {
     const int32_t* bnd_ptr = nullptr;     // their slots bnd_ptr[j] .. bnd_ptr[j+1]-1, ascending block
     float* partial = nullptr;             // n_slots
     const int8_t* fixed = nullptr;        // 1 on Dirichlet rows
+    int64_t n_ke = 0;                     // floats in ke (378 per cell)
+    unsigned* err = nullptr;              // bounded waits of the streamed kernel that timed out
 };
 
 // Device side of the hierarchy and the V-cycle (amg.cu).
@@ -97,21 +99,33 @@ public:
     void set_level0_lambda(double lambda);
     // apply level 0 element by element over cell blocks (null operator: back to the SELL matrix)
     void set_level0_ebe(const EbeOperator* op);
+    // level-0 element matrices streamed into a shared-memory ring by bulk copies (1, default)
+    // or loaded by the warps that apply them (0)
+    void set_level0_stream(bool on) { stream_ke_ = on; }
+    // nonzero when a bounded wait of the streamed kernel ran out (the result is then invalid)
+    unsigned level0_errors();
     bool level0_ebe() const { return ebe_on_; }
     // algorithmic bytes of one level-0 smoothing step (SELL: nnz*8 + 24 n; cell blocks: the
     // element matrices, the block tables, x per block-local DoF, the vectors, the partial sums)
     double smoother_bytes() const;
+    // coarse-grid correction of level `level` by `cycles` stationary cycles of the next level
+    // (1: V-cycle; 2 at level 0: two Q1 cycles per Q2 correction). Each further cycle starts
+    // from the residual of the sum so far, so the preconditioner stays symmetric.
+    void set_coarse_cycles(int level, int cycles);
 
 private:
     void cycle(int l);
     void level0_apply(int kind, const float* xin, float* xout, float c1, float c2);  // 0 cheb, 1 residual
     EbeOperator ebe_;
     bool ebe_on_ = false;
+    bool stream_ke_ = true;
+    DBuf<unsigned> ebe_err_;
     int64_t nnz0_ = 0;
     cudaStream_t stream_;
     std::vector<std::unique_ptr<AmgDevLevel>> lv_;
     DBuf<float> coarse_inv_;
     int n_coarse_ = 0;
+    std::vector<int> coarse_cycles_;
     std::string desc_;
 };
 

@@ -459,6 +459,12 @@ double fgb_field_outer_spmv_bytes(const FGB_FIELD* f) {
 int fgb_field_set_level0_ebe(FGB_FIELD* f, int on) {
     return guarded([&] { f->f->fem().set_level0_ebe(on != 0); return 0; });
 }
+int fgb_field_set_level0_stream(FGB_FIELD* f, int on) {
+    return guarded([&] { f->f->fem().set_level0_stream(on != 0); return 0; });
+}
+int fgb_field_set_coarse_cycles(FGB_FIELD* f, int level, int cycles) {
+    return guarded([&] { f->f->fem().set_coarse_cycles(level, cycles); return 0; });
+}
 int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo) {
     return guarded([&] { f->f->fem().set_smoothing(degree, lo); return 0; });
 }

@@ -1483,7 +1483,9 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
         op.bnd_ptr = c.bnd_ptr.get();
         op.partial = c.partial.get();
         op.fixed = fixed_.get();
+        op.n_ke = 378LL * nc_;
         amg_->set_level0_ebe(&op);
+        amg_->set_level0_stream(level0_stream_);
     }
     phase("device hierarchy upload");
     amg_->smoother_timer.enabled = profiling_;
@@ -1595,6 +1597,17 @@ void FemDevice::set_smoothing(int degree, double lo) {
     amg_.reset();
 }
 
+void FemDevice::set_level0_stream(bool on) {
+    level0_stream_ = on;
+    if (amg_) amg_->set_level0_stream(on);
+}
+
+void FemDevice::set_coarse_cycles(int level, int cycles) {
+    FGB_REQUIRE(level >= 0 && level < 16 && cycles >= 1 && cycles <= 8, "coarse cycles: level 0..15, 1..8 cycles");
+    if ((int)coarse_cycles_.size() <= level) coarse_cycles_.resize(level + 1, 1);
+    coarse_cycles_[level] = cycles;
+}
+
 void FemDevice::set_profiling(bool on) {
     profiling_ = on;
     spmv_timer_.enabled = on;
@@ -1607,6 +1620,7 @@ void FemDevice::set_profiling(bool on) {
 
 int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     ensure_amg(st);
+    for (int l = 0; l < (int)coarse_cycles_.size(); ++l) amg_->set_coarse_cycles(l, coarse_cycles_[l]);
     st->levels = amg_->n_levels();
     const int gb = grid_for(n_, kBlock);
     CgState* ds = state_.get();
@@ -1723,6 +1737,9 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     const double rn = std::sqrt(rr_true);
     st->rel_residual = bnorm > 0 ? rn / bnorm : rn;
     st->status = bnorm == 0 ? 1 : status;
+    if (const unsigned e = amg_->level0_errors())
+        throw Error("level-0 smoother: a bounded wait of the streamed element matrices ran out (code " +
+                    std::to_string(e) + ")");
     st->smoother_ms = amg_->smoother_timer.collect(&st->smoother_launches);
     st->smoother_bytes = amg_->smoother_bytes();
     st->spmv_ms = spmv_timer_.collect(&st->spmv_launches);

@@ -104,6 +104,11 @@ public:
     // coarse correction) and the lower end of the interval as a fraction of lambda_max;
     // 0 keeps the default (Q1: 4 and 0.04; Q2: 2 and 0.1). Drops the current hierarchy.
     void set_smoothing(int degree, double lo);
+    // Q2 level 0 by cell blocks: element matrices streamed by bulk copies (default) or loaded
+    // by the applying warps
+    void set_level0_stream(bool on);
+    // multigrid: cycles of level+1 per coarse-grid correction at `level` (1 = V-cycle)
+    void set_coarse_cycles(int level, int cycles);
     // Q2: apply the finest multigrid level element by element, by cell blocks (cell_blocks.h;
     // default: 4.3 vs 8.95 GB per smoothing step on config 2), or through the assembled SELL
     // matrix; the hierarchy is rebuilt at the next solve
@@ -189,6 +194,8 @@ private:
     double estimate_lambda(int iters, uint64_t seed = 0x9e3779b97f4a7c15ull);  // largest eigenvalue of D^-1 A (FP64 power iteration)
     bool profiling_ = false;
     int smooth_degree_ = 0;
+    std::vector<int> coarse_cycles_;
+    bool level0_stream_ = true;
     double smooth_lo_ = 0;
     int q1_gauss_ = 2;  // Gauss points per direction of the Q1 element integrals
     bool level0_ebe_ = false;

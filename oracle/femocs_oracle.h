@@ -2,11 +2,13 @@
  *
  * TEST INFRASTRUCTURE ONLY: this is the checker (and the timed CPU baseline in bench.py),
  * never part of the product. It restates, in plain C, the reference FEMOCS algorithms for
- * the path; every function cites the reference file:line it follows. Parity of the FEM
- * solve (assembly, boundary conditions, SSOR-CG) is UNPINNED against the reference itself,
- * because that part of the reference runs inside deal.II 9.2, which is not available; the
- * cell-location, interpolation, nodal-field and smoothing parts are pinned against golden
- * vectors produced by the reference's own compiled sources (oracle/ref_driver.cpp).
+ * the path; every function cites the reference file:line it follows. The FEM solve
+ * (assembly, boundary conditions, SSOR-CG) cannot be pinned bit for bit against the
+ * reference, because that part of the reference runs inside deal.II 9.2, which is not
+ * available; it is pinned to the reference's analytic hemisphere-on-plane answer
+ * (src/SolutionReader.cpp:501-524) by a convergence test. The cell-location, interpolation,
+ * nodal-field and smoothing parts are pinned against golden vectors produced by the
+ * reference's own compiled sources (oracle/ref_driver.cpp).
  */
 #ifndef FEMOCS_ORACLE_H
 #define FEMOCS_ORACLE_H

@@ -178,3 +178,25 @@ def test_q2_cell_block_limits_give_the_same_solve(anode):
         assert rc > 0 and st["status"] == 1 and st["rel_residual"] <= 1e-10, (cells, st)
         assert abs(st["iterations"] - it_ref) <= 2, (cells, st["iterations"], it_ref)
         assert np.abs(f.solution() - x_ref).max() <= 2e3 * 1e-10 * np.abs(x_ref).max(), cells
+
+
+@pytest.mark.parametrize("cells,max_dofs", [(1, 27), (5, 150), (256, 4096)])
+def test_q2_streamed_element_matrices_are_bit_identical(cells, max_dofs):
+    """The level-0 element matrices streamed through the bulk-copy ring (default) and loaded by
+    the applying warps give bit-identical solves: the same products in the same order. Block
+    limits cover one-cell blocks (every chunk partial, copies starting 8 bytes past a
+    16-byte boundary for odd cells, the array's last bytes loaded plainly), blocks of five
+    cells (odd chunk sizes) and the default blocks (full chunks, rings reused)."""
+    m = fg.Mesh.synthetic(**SMALL)
+    f = fg.Field(m, order=2)
+    f.set_cell_blocks(cells, max_dofs)
+    out = {}
+    for stream in (False, True):
+        f.set_level0_stream(stream)
+        f.setup(-E0)
+        f.assemble(True, False)
+        rc, st = f.solve(precision=2, rel_tol=1e-10)
+        assert rc > 0 and st["status"] == 1, st
+        out[stream] = (st["iterations"], f.solution())
+    assert out[True][0] == out[False][0]
+    assert np.array_equal(out[True][1].view(np.int64), out[False][1].view(np.int64))
