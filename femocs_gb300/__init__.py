@@ -226,7 +226,7 @@ class Field:
 
     def set_level0_stream(self, on=True):
         """Q2 level 0 by cell blocks: element matrices through the bulk-copy ring (True) or
-        loaded by the applying warps (False)."""
+        loaded by the applying warps (False, the default)."""
         self._ok(load().fgb_field_set_level0_stream(self.h, int(on)))
 
     def set_coarse_cycles(self, level=0, cycles=1):

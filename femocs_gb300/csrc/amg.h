@@ -99,8 +99,8 @@ public:
     void set_level0_lambda(double lambda);
     // apply level 0 element by element over cell blocks (null operator: back to the SELL matrix)
     void set_level0_ebe(const EbeOperator* op);
-    // level-0 element matrices streamed into a shared-memory ring by bulk copies (1, default)
-    // or loaded by the warps that apply them (0)
+    // level-0 element matrices streamed into a shared-memory ring by bulk copies (1) or loaded
+    // by the warps that apply them (0, default: measured faster, see the design notes)
     void set_level0_stream(bool on) { stream_ke_ = on; }
     // nonzero when a bounded wait of the streamed kernel ran out (the result is then invalid)
     unsigned level0_errors();
@@ -118,7 +118,7 @@ private:
     void level0_apply(int kind, const float* xin, float* xout, float c1, float c2);  // 0 cheb, 1 residual
     EbeOperator ebe_;
     bool ebe_on_ = false;
-    bool stream_ke_ = true;
+    bool stream_ke_ = false;
     DBuf<unsigned> ebe_err_;
     int64_t nnz0_ = 0;
     cudaStream_t stream_;

@@ -104,8 +104,8 @@ public:
     // coarse correction) and the lower end of the interval as a fraction of lambda_max;
     // 0 keeps the default (Q1: 4 and 0.04; Q2: 2 and 0.1). Drops the current hierarchy.
     void set_smoothing(int degree, double lo);
-    // Q2 level 0 by cell blocks: element matrices streamed by bulk copies (default) or loaded
-    // by the applying warps
+    // Q2 level 0 by cell blocks: element matrices streamed by bulk copies or loaded by the
+    // applying warps (default)
     void set_level0_stream(bool on);
     // multigrid: cycles of level+1 per coarse-grid correction at `level` (1 = V-cycle)
     void set_coarse_cycles(int level, int cycles);
@@ -195,7 +195,7 @@ private:
     bool profiling_ = false;
     int smooth_degree_ = 0;
     std::vector<int> coarse_cycles_;
-    bool level0_stream_ = true;
+    bool level0_stream_ = false;
     double smooth_lo_ = 0;
     int q1_gauss_ = 2;  // Gauss points per direction of the Q1 element integrals
     bool level0_ebe_ = false;

@@ -182,8 +182,8 @@ def test_q2_cell_block_limits_give_the_same_solve(anode):
 
 @pytest.mark.parametrize("cells,max_dofs", [(1, 27), (5, 150), (256, 4096)])
 def test_q2_streamed_element_matrices_are_bit_identical(cells, max_dofs):
-    """The level-0 element matrices streamed through the bulk-copy ring (default) and loaded by
-    the applying warps give bit-identical solves: the same products in the same order. Block
+    """The level-0 element matrices streamed through the bulk-copy ring and loaded by the
+    applying warps (the default) give bit-identical solves: the same products in the same order. Block
     limits cover one-cell blocks (every chunk partial, copies starting 8 bytes past a
     16-byte boundary for odd cells, the array's last bytes loaded plainly), blocks of five
     cells (odd chunk sizes) and the default blocks (full chunks, rings reused)."""
