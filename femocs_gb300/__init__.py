@@ -224,6 +224,20 @@ class Field:
         through the SELL matrix (False)."""
         self._ok(load().fgb_field_set_level0_ebe(self.h, int(on)))
 
+    def set_ke_tensor(self, on=True):
+        """Q2 element matrices on the tensor cores (True) or as FP32 hi/lo pairs (False)."""
+        self._ok(load().fgb_field_set_ke_tensor(self.h, int(on)))
+
+    def element_matrices(self):
+        """Element matrices of the last full assembly (Q2: (cells, 378) packed upper triangles)."""
+        n = int(load().fgb_field_export_element_matrices(self.h, None))
+        if n < 0:
+            raise RuntimeError(last_error())
+        out = np.zeros(max(n, 1))
+        if load().fgb_field_export_element_matrices(self.h, ptr(out)) < 0:
+            raise RuntimeError(last_error())
+        return out[:n]
+
     def set_level0_stream(self, on=True):
         """Q2 level 0 by cell blocks: element matrices through the bulk-copy ring (True) or
         loaded by the applying warps (False, the default)."""

@@ -80,6 +80,7 @@ _PROTOS = {
     "fgb_field_clear_space_charge": (C.c_int, [vp]),
     "fgb_device_sync": (C.c_int, []),
     "fgb_device_info": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.c_char_p]),
+    "fgb_tc_selftest": (C.c_int, [dp]),
     "fgb_mesh_q2_sizes": (C.c_int, [vp, i64p]),
     "fgb_mesh_cell_blocks": (C.c_int, [vp, C.c_int, C.c_int, i64p]),
     "fgb_mesh_q1_sizes": (C.c_int, [vp, i64p]),
@@ -93,6 +94,8 @@ _PROTOS = {
     "fgb_field_set_profiling": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_coarse_cycles": (C.c_int, [vp, C.c_int, C.c_int]),
     "fgb_field_set_level0_stream": (C.c_int, [vp, C.c_int]),
+    "fgb_field_set_ke_tensor": (C.c_int, [vp, C.c_int]),
+    "fgb_field_export_element_matrices": (C.c_longlong, [vp, dp]),
     "fgb_field_set_smoothing": (C.c_int, [vp, C.c_int, C.c_double]),
     "fgb_field_set_level0_ebe": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_outer_spmv": (C.c_int, [vp, C.c_int]),

@@ -13,6 +13,7 @@
 #include "bulk.h"
 #include "cell_blocks.h"
 #include "facade.h"
+#include "fem_q2.h"
 #include "server.h"
 #include "femocs_gb300.h"
 #include "mesh_prep.h"
@@ -459,6 +460,19 @@ double fgb_field_outer_spmv_bytes(const FGB_FIELD* f) {
 int fgb_field_set_level0_ebe(FGB_FIELD* f, int on) {
     return guarded([&] { f->f->fem().set_level0_ebe(on != 0); return 0; });
 }
+int fgb_field_set_ke_tensor(FGB_FIELD* f, int on) {
+    return guarded([&] { f->f->fem().set_ke_tensor(on != 0); return 0; });
+}
+long long fgb_field_export_element_matrices(FGB_FIELD* f, double* out) {
+    try {
+        FemDevice& fem = f->f->fem();
+        if (out) fem.export_element_matrices(out);
+        return (long long)fem.element_matrix_values();
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return -1;
+    }
+}
 int fgb_field_set_level0_stream(FGB_FIELD* f, int on) {
     return guarded([&] { f->f->fem().set_level0_stream(on != 0); return 0; });
 }
@@ -505,6 +519,9 @@ int fgb_field_space_charge(FGB_FIELD* f, int n, const double* d_xyz, const int* 
 }
 int fgb_device_sync(void) {
     return guarded([&] { FGB_CUDA(cudaDeviceSynchronize()); return 0; });
+}
+int fgb_tc_selftest(double* max_err) {
+    return guarded([&] { *max_err = tc_selftest(); return 0; });
 }
 int fgb_device_info(size_t* free_bytes, size_t* total_bytes, char* uuid) {
     return guarded([&] {

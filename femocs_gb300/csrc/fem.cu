@@ -1037,7 +1037,10 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
     const int gb = grid_for(n_, kBlock);
     if (fs_.order == 2) {
         if (full_run) {
-            q2_cell_stiffness(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), stream_);
+            if (ke_tensor_)
+                q2_cell_stiffness_tc(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), tc_scratch_, tc_err_, stream_);
+            else
+                q2_cell_stiffness(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), stream_);
             q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
                              r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
             if (level0_ebe_ || outer_mode_ == 2) refresh_ke32();
@@ -1595,6 +1598,14 @@ void FemDevice::set_smoothing(int degree, double lo) {
     smooth_degree_ = degree;
     smooth_lo_ = lo;
     amg_.reset();
+}
+
+void FemDevice::set_ke_tensor(bool on) { ke_tensor_ = on; }
+
+void FemDevice::export_element_matrices(double* out) {
+    const size_t n = ke_.size();
+    FGB_CUDA(cudaMemcpyAsync(out, ke_.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
 }
 
 void FemDevice::set_level0_stream(bool on) {

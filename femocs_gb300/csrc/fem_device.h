@@ -104,6 +104,12 @@ public:
     // coarse correction) and the lower end of the interval as a fraction of lambda_max;
     // 0 keeps the default (Q1: 4 and 0.04; Q2: 2 and 0.1). Drops the current hierarchy.
     void set_smoothing(int degree, double lo);
+    // Q2 element matrices on the tensor cores (q2_ke_tc.cu, default) or the FP32 pipe (FP32
+    // hi/lo pairs)
+    void set_ke_tensor(bool on);
+    // element matrices of the last full assembly (Q1: 64 per cell, Q2: 378 packed per cell)
+    void export_element_matrices(double* out);
+    size_t element_matrix_values() const { return ke_.size(); }
     // Q2 level 0 by cell blocks: element matrices streamed by bulk copies or loaded by the
     // applying warps (default)
     void set_level0_stream(bool on);
@@ -196,6 +202,9 @@ private:
     int smooth_degree_ = 0;
     std::vector<int> coarse_cycles_;
     bool level0_stream_ = false;
+    bool ke_tensor_ = true;
+    DBuf<unsigned char> tc_scratch_;  // tensor-core element matrices: slices per persistent CTA
+    DBuf<unsigned> tc_err_;
     double smooth_lo_ = 0;
     int q1_gauss_ = 2;  // Gauss points per direction of the Q1 element integrals
     bool level0_ebe_ = false;

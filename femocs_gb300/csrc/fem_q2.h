@@ -9,6 +9,14 @@ namespace fgb {
 
 // 378 packed upper-triangle entries per cell
 void q2_cell_stiffness(int nc, const int32_t* cell_dofs, const double* dof_xyz, double* ke, cudaStream_t s);
+// the same 378 entries per cell on the tensor cores (q2_ke_tc.cu): per-cell factors in FP64,
+// error-free BF16 slices, tcgen05 products with FP32 accumulators in tensor memory, levels
+// combined in FP64; scratch (per persistent CTA) and err are the caller's reusable buffers
+void q2_cell_stiffness_tc(int nc, const int32_t* cell_dofs, const double* dof_xyz, double* ke,
+                          DBuf<unsigned char>& scratch, DBuf<unsigned>& err, cudaStream_t s);
+// one 128 x 48 x 32 BF16 tensor-core product of small integers on the device against the
+// host's: the largest absolute difference (0 when descriptors and TMEM layout are right)
+double tc_selftest();
 // SELL-32 columns of the Q2 rows: per row the sorted, unique DoFs of its cells (one warp per
 // row, bitonic sort in shared memory); padding = the row itself (0 past the last row).
 // max_cells = the longest row -> cell list. Returns the number of rows whose column count

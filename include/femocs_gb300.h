@@ -190,6 +190,13 @@ double fgb_field_outer_spmv_bytes(const FGB_FIELD* f);
  * correction (0: default, Q1 4, Q2 2) and the interval's lower end as a fraction of
  * lambda_max (0: default, Q1 0.04, Q2 0.1); the hierarchy is rebuilt at the next solve */
 int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo);
+/* Q2 fields: element matrices of the full assembly on the tensor cores (1, default: per-cell
+ * factors in FP64, error-free BF16 slices, tcgen05 products accumulated exactly in FP32, levels
+ * combined as FP32 pairs into FP64) or on the FP32 pipe as FP32 hi/lo pairs (0) */
+int fgb_field_set_ke_tensor(FGB_FIELD* f, int on);
+/* element matrices of the last full assembly (Q1: 64 per cell; Q2: 378 packed upper-triangle
+ * entries per cell, row by row); returns the number of values (out may be NULL), -1 on error */
+long long fgb_field_export_element_matrices(FGB_FIELD* f, double* out);
 /* Q2 fields, level 0 by cell blocks: the element matrices reach the applying warps through a
  * shared-memory ring filled by bulk copies from a producer warp (1) or by their own loads (0,
  * default: 0.86 against 1.19 ms per smoothing step on the 1.7e7-DoF benchmark mesh) */
@@ -215,6 +222,10 @@ int fgb_field_space_charge(FGB_FIELD* f, int n, const double* d_xyz, const int* 
 int fgb_field_clear_space_charge(FGB_FIELD* f);
 /* wait for all work of this process on the current device */
 int fgb_device_sync(void);
+/* tensor-core self check on the current device: one 128 x 48 x 32 BF16 product of small
+ * integers through the library's tcgen05 path against the host's; *max_err = largest absolute
+ * difference (0 expected) */
+int fgb_tc_selftest(double* max_err);
 /* free and total device memory of the current device (cudaMemGetInfo) and, when uuid is not
  * NULL (room for 48 chars), its UUID in the form nvidia-smi prints ("GPU-xxxxxxxx-...") */
 int fgb_device_info(size_t* free_bytes, size_t* total_bytes, char* uuid);
