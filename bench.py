@@ -44,9 +44,10 @@ RANK = 1           # interpolation_rank default of the reference (src/Config.cpp
 N_POINTS = {"config2": 1_000_000, "config1": 100_000, "probe": 200_000}
 # DRAM bytes (read + write) per row of one launch of the hot multigrid kernels, from ncu
 # captures of the Q2 probe workload (the SELL level-0 Chebyshev step at 61.9 nonzeros per row,
-# as config 2's Q2 rows; the cell-block step, k_cb_apply + k_cb_finish); a launch's traffic
-# scales with its rows
-KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6, ("smoother_ebe", 2): 261.8}
+# as config 2's Q2 rows; the cell-block step, k_cb_apply + k_cb_finish, from the element
+# matrices and matrix-free from the FP16 geometric factors); a launch's traffic scales with
+# its rows
+KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6, ("smoother_ebe", 2): 261.8, ("smoother_mf16", 2): 113.0}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -398,6 +399,9 @@ def run_ours(args, world, rank):
     d_out = fg.DeviceBuffer(40 * n_points)
 
     solve_stats = []
+    # Q2 level 0: the matrix-free smoother from FP16 geometric factors is the default; stated
+    # here so that the line names the kind in use (FP32 when a factor exceeds the FP16 range)
+    l0_kind = field.set_level0_operator(2) if order == 2 else 0
 
     def step(precision):
         field.setup(-E0, 0.0)
@@ -435,6 +439,20 @@ def run_ours(args, world, rank):
     solve_ms = [s["ms"] for s in solve_stats]
     last = solve_stats[-1]
     levels = field.amg_levels().split()
+    # the same solve with the level-0 smoother reading the element matrices (the memory-bound
+    # kernel the matrix-free default replaced), for the roofline comparison
+    ke_cmp = None
+    if order == 2 and l0_kind != 0:
+        field.set_level0_operator(0)
+        field.set_profiling(True)
+        st0 = step(2)
+        field.set_profiling(False)
+        field.set_level0_operator(l0_kind)
+        ms0 = st0["smoother_ms"] / max(st0["smoother_launches"], 1)
+        ke_cmp = {"kernel": "k_cb_apply + k_cb_finish, element matrices (FP32 K_e, 1512 B per hex)",
+                  "launch_ms": ms0, "bytes_per_launch": st0["smoother_bytes"],
+                  "gbs": st0["smoother_bytes"] / (ms0 * 1e-3) / 1e9, "iterations": st0["iterations"],
+                  "solve_ms": st0["ms"]}
 
     # the same step with the plain FP64 Jacobi-PCG, and with FP32 Jacobi-PCG + FP64 refinement
     plain = [step(0) for _ in range(min(2, args.steps))]
@@ -476,11 +494,18 @@ def run_ours(args, world, rank):
     #     cell blocks: the solver's own count (FemDevice::outer_spmv_bytes)
     nnz = field.nnz
     ebe = order == 2 and last["smoother_bytes"] != nnz * 8 + 24 * n
+    l0_name, l0_key = {
+        0: ("k_cb_apply + k_cb_finish (level-0 Chebyshev smoothing, Q2 cell blocks, FP32 element matrices)",
+            "smoother_ebe"),
+        1: ("k_cb_apply + k_cb_finish (level-0 Chebyshev smoothing, Q2 cell blocks, matrix-free from FP32 "
+            "geometric factors by sum factorisation)", "smoother_mf32"),
+        2: ("k_cb_apply + k_cb_finish (level-0 Chebyshev smoothing, Q2 cell blocks, matrix-free from FP16 "
+            "geometric factors by sum factorisation)", "smoother_mf16")}[l0_kind] if ebe else (
+        "k_cheb_step (level-0 Chebyshev smoothing, FP32)", "smoother")
     kern = {
-        ("k_cb_apply + k_cb_finish (level-0 Chebyshev smoothing, Q2 cell blocks, FP32)" if ebe else
-         "k_cheb_step (level-0 Chebyshev smoothing, FP32)"): (
+        l0_name: (
             sum(s["smoother_ms"] for s in solve_stats), sum(s["smoother_launches"] for s in solve_stats),
-            last["smoother_bytes"], "smoother_ebe" if ebe else "smoother"),
+            last["smoother_bytes"], l0_key),
         ("k_cb_spmv_df + k_cb_spmv_finish (outer FP64-accurate SpMV + p.q, Q2 cell blocks, FP32 pairs)"
          if order == 2 else "k_cg_spmv_pq_df (outer FP64-accurate SpMV from FP32 pairs + p.q)"): (
             sum(s["spmv_ms"] for s in solve_stats), sum(s["spmv_launches"] for s in solve_stats),
@@ -534,7 +559,8 @@ def run_ours(args, world, rank):
                      "other": {k: {"ms": v[0], "launches": v[1], "gbs": v[2] / (v[0] / max(v[1], 1) * 1e-3) / 1e9}
                                for k, v in kern.items() if k != name},
                      "peak_kind": peak_kind, "spmv_fp32_launch_ms": spmv32_ms, "spmv_fp64_launch_ms": spmv64_ms,
-                     "spmv_fp32_gbs": (nnz * 8 + 12 * n) / (spmv32_ms * 1e-3) / 1e9},
+                     "spmv_fp32_gbs": (nnz * 8 + 12 * n) / (spmv32_ms * 1e-3) / 1e9,
+                     "element_matrix_smoother": (dict(ke_cmp, frac=ke_cmp["gbs"] / peak) if ke_cmp else None)},
         "clocks": clocks,
         "gpu_launches": launches,
         # index of the first timed launch among all of this process's kernel launches, and the
@@ -680,10 +706,12 @@ def batch_and_serve_summaries(args, world, rank):
     out["serve"] = {"workload": sl["config"]["workload"], "total_dofs": sl["config"]["total_dofs"],
                     "saturation_solves_per_s": sl["value"],
                     "rates": [{k: d[k] for k in ("rate", "requests", "completed", "converged", "solves_per_s", "p50_ms",
-                                                 "p99_ms", "p50_queue_ms", "p50_solve_ms", "p50_post_ms", "iterations_mean")}
+                                                 "p99_ms", "p50_queue_ms", "p50_solve_ms", "p50_post_ms", "p99_queue_ms",
+                                                 "p99_solve_ms", "p99_post_ms", "iterations_mean")}
                               for d in sl["sweep"]],
                     "plain_fp64_cg_served_one_at_a_time": sl["plain_fp64_cg_served_one_at_a_time"],
                     "speedup_vs_plain": sl["speedup_vs_plain"], "iters_per_launch": a.iters_per_launch,
+                    "idle_iters": a.idle_iters, "stop_at_first": bool(a.stop_at_first),
                     "build_s": sl["build_s"], "clocks": sl["clocks"]}
     return out
 
@@ -946,6 +974,7 @@ def run_serve(args, world, rank, quiet=False):
     base = np.r_[np.full(half, 0.1), rfields]
     b = fg.Batch()
     srv = fg.Server(b, rel_tol=REL_TOL, max_iter=1000, iters_per_launch=args.iters_per_launch, rank=RANK)
+    srv.set_launch_policy(args.idle_iters, args.stop_at_first)
     t0 = time.perf_counter()
     srv.add_synthetic_runs(specs, n_atoms=args.atoms, seed=5)
     build_s = time.perf_counter() - t0
@@ -977,6 +1006,9 @@ def run_serve(args, world, rank, quiet=False):
                       "p50_queue_ms": float(np.median(rec["t_admit"] - rec["t_submit"]) * 1e3),
                       "p50_solve_ms": float(np.median(rec["t_solved"] - rec["t_admit"]) * 1e3),
                       "p50_post_ms": float(np.median(rec["t_done"] - rec["t_solved"]) * 1e3),
+                      "p99_queue_ms": float(np.percentile(rec["t_admit"] - rec["t_submit"], 99) * 1e3),
+                      "p99_solve_ms": float(np.percentile(rec["t_solved"] - rec["t_admit"], 99) * 1e3),
+                      "p99_post_ms": float(np.percentile(rec["t_done"] - rec["t_solved"], 99) * 1e3),
                       "iterations_mean": float(rec["iterations"].mean()), "wall_s": wall})
     launches = lib.fgb_kernel_launches() - launches0
     clocks = sampler.stop()
@@ -994,7 +1026,8 @@ def run_serve(args, world, rank, quiet=False):
         "dtype": "f64 CG / f32 multigrid preconditioner", "data": "synthetic (seeded nanotips, FCC surface atoms)",
         "config": {"workload": f"serve: {n_runs} MD runs ({half} config-0 tips, {n_runs - half} random tips), "
                                f"{args.atoms} atoms each, sigma 0.02 A per step, Poisson arrivals",
-                   "total_dofs": int(dofs.sum()), "rates": args.rates, "iters_per_launch": args.iters_per_launch},
+                   "total_dofs": int(dofs.sum()), "rates": args.rates, "iters_per_launch": args.iters_per_launch,
+                   "idle_iters": args.idle_iters, "stop_at_first": bool(args.stop_at_first)},
         "sweep": sweep, "build_s": build_s, "max_requests_in_flight": info["max_in_flight"],
         "solver_launches": info["solver_launches"], "plain_fp64_cg_served_one_at_a_time": plain,
         "speedup_vs_plain": best["solves_per_s"] / plain["solves_per_s"],
@@ -1019,6 +1052,10 @@ def main():
     ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000])
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--iters-per-launch", type=int, default=4)
+    ap.add_argument("--idle-iters", type=int, default=0,
+                    help="serve: solver iterations per launch while no request waits (0: --iters-per-launch)")
+    ap.add_argument("--stop-at-first", action="store_true",
+                    help="serve: end a launch after the iteration in which a solve finished")
     ap.add_argument("--points", type=int, default=0)
     ap.add_argument("--order", type=int, default=0, choices=[0, 1, 2],
                     help="element order (default: 2 for config2/probe, 1 for config1)")

@@ -243,6 +243,19 @@ class Field:
         loaded by the applying warps (False, the default)."""
         self._ok(load().fgb_field_set_level0_stream(self.h, int(on)))
 
+    def set_level0_operator(self, kind):
+        """Q2 level 0 by cell blocks: 0 element matrices, 1 / 2 geometric factors in FP32 / FP16
+        applied by sum factorisation. Returns the kind in use."""
+        rc = load().fgb_field_set_level0_operator(self.h, int(kind))
+        if rc < 0:
+            raise RuntimeError(last_error())
+        return rc
+
+    def set_level0_prefetch(self, cells):
+        """Q2 level 0 by cell blocks: L2 prefetch of the element matrices `cells` cells ahead of
+        each warp's loads (0 = off)."""
+        self._ok(load().fgb_field_set_level0_prefetch(self.h, int(cells)))
+
     def set_coarse_cycles(self, level=0, cycles=1):
         """Multigrid: cycles of level+1 per coarse-grid correction at `level` (1 = V-cycle)."""
         self._ok(load().fgb_field_set_coarse_cycles(self.h, level, cycles))
@@ -769,6 +782,11 @@ class Server:
     def _ok(self, rc):
         if rc != 0:
             raise RuntimeError(last_error())
+
+    def set_launch_policy(self, idle_iters=0, stop_at_first=False):
+        """Before start(): iterations per launch while no request waits (0: iters_per_launch),
+        and whether a launch ends after the iteration in which one of its solves finished."""
+        self._ok(load().fgb_server_set_launch_policy(self.h, int(idle_iters), int(bool(stop_at_first))))
 
     def add_run(self, mesh: Mesh, xyz, seed=1):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)

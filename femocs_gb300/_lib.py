@@ -94,6 +94,8 @@ _PROTOS = {
     "fgb_field_set_profiling": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_coarse_cycles": (C.c_int, [vp, C.c_int, C.c_int]),
     "fgb_field_set_level0_stream": (C.c_int, [vp, C.c_int]),
+    "fgb_field_set_level0_prefetch": (C.c_int, [vp, C.c_int]),
+    "fgb_field_set_level0_operator": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_ke_tensor": (C.c_int, [vp, C.c_int]),
     "fgb_field_export_element_matrices": (C.c_longlong, [vp, dp]),
     "fgb_field_set_smoothing": (C.c_int, [vp, C.c_int, C.c_double]),
@@ -148,6 +150,7 @@ _PROTOS = {
     # Part 4: serving
     "fgb_server_create": (vp, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]),
     "fgb_server_free": (None, [vp]),
+    "fgb_server_set_launch_policy": (C.c_int, [vp, C.c_int, C.c_int]),
     "fgb_server_add_run": (C.c_int, [vp, vp, dp, C.c_int, C.c_ulonglong]),
     "fgb_server_add_synthetic_runs": (C.c_int, [vp, C.c_int, C.POINTER(FgbNanotip), C.c_int, C.c_ulonglong, C.c_int]),
     "fgb_server_place_pending": (C.c_int, [vp, C.c_int]),

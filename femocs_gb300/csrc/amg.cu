@@ -17,6 +17,8 @@
 #include <cmath>
 #include <sstream>
 
+#include <cuda_fp16.h>
+
 #include "amg.h"
 
 namespace fgb {
@@ -237,12 +239,58 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+// L2 prefetch of bytes [off, off + len) of an array of `total` bytes: the 16-byte-aligned
+// span around them (a cell's element matrix starts 0 or 8 bytes past a boundary), clipped to
+// the array's last full 16 bytes
+__device__ __forceinline__ void prefetch_l2(const void* base, int64_t total, int64_t off, int64_t len) {
+    const int64_t a = off & ~(int64_t)15;
+    int64_t e = (off + len + 15) & ~(int64_t)15;
+    const int64_t end = total & ~(int64_t)15;
+    if (e > end) e = end;
+    if (e > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<const char*>(base) + a),
+                     "r"((unsigned)(e - a))
+                     : "memory");
+}
+
+// Level-0 operator of three cells at once from their geometric factors, by sum
+// factorisation: lane l < 27 of a warp works on cell g = l / 9 of the group and owns the
+// 1-D pencil p = l % 9 of its 3 x 3 x 3 lattice, so every contraction is three
+// independent 3-term sums in registers with constant coefficients; the pencils are
+// transposed between the stages through a per-warp shared-memory scratch (3 x 170 floats;
+// every store writes 9 consecutive words per cell, every lane reads 3 consecutive words).
+// Stages (lattice node (a, b, c) = a + 3b + 9c, Gauss point (qx, qy, qz)):
+//   1  lane (a, b):   T1 = S_z u, T2 = D_z u over c            -> W[qz][a][b]
+//   2  lane (a, qz):  A1 = S_y T1, A2 = D_y T1, A3 = S_y T2     -> X[qy][qz][a]
+//   3  lane (qy, qz): reference gradient (D_x A1, S_x A2, S_x A3) at qx = 0..2, flux
+//                     C_q g, then the transposed x contraction  -> Y[a][qz][qy]
+//   4  lane (a, qz):  E1 = S_y^T B1 + D_y^T B2, E2 = S_y^T B3    -> Z[b][a][qz]
+//   5  lane (a, b):   v = S_z^T E1 + D_z^T E2 at c = 0..2
+// with S[q][a] = l_a(t_q), D[q][a] = l_a'(t_q). K_e = sum_q B_q^T C_q B_q is the Q2
+// element matrix, so v equals K_e u up to FP32 rounding.
+__device__ __forceinline__ constexpr float sfS(int q, int a) {
+    return a == 0 ? 0.5f * ((q - 1) * 0.7745966692414834f) * ((q - 1) * 0.7745966692414834f - 1.f)
+                  : (a == 1 ? 1.f - ((q - 1) * 0.7745966692414834f) * ((q - 1) * 0.7745966692414834f)
+                            : 0.5f * ((q - 1) * 0.7745966692414834f) * ((q - 1) * 0.7745966692414834f + 1.f));
+}
+__device__ __forceinline__ constexpr float sfD(int q, int a) {
+    return a == 0 ? (q - 1) * 0.7745966692414834f - 0.5f
+                  : (a == 1 ? -2.f * ((q - 1) * 0.7745966692414834f) : (q - 1) * 0.7745966692414834f + 0.5f);
+}
+// floats per cell: two regions of 81 (W then Y, X then Z); 170 = 10 mod 32 banks, so the
+// three cells' 9-word rows written by one store fall into disjoint banks
+constexpr int kSfScratch = 170;
+constexpr int kSfWarpBytes = 3 * kSfScratch * 4;
 // barrier over the consumer warps of the streamed kernel (the producer does not take part)
 __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kCb) : "memory"); }
 
 // shared memory of one block: its item lists (28 u16 per cell), x of its DoFs, the products
 __host__ __device__ inline size_t cb_smem_bytes(int max_cells, int max_dofs) {
     return 56 * (size_t)max_cells + 4 * (size_t)max_dofs + 108 * (size_t)max_cells;
+}
+// the geometric-factor variants: the same, then (16-byte aligned) the warps' scratch
+__host__ __device__ inline size_t cb_geo_smem_bytes(int max_cells, int max_dofs) {
+    return ((cb_smem_bytes(max_cells, max_dofs) + 15) & ~(size_t)15) + (kCb / 32) * (size_t)kSfWarpBytes;
 }
 // the streamed variant: the same, then (128-byte aligned) the ring and its full/empty barriers
 __host__ __device__ inline size_t cb_stream_smem_bytes(int max_cells, int max_dofs) {
@@ -259,12 +307,21 @@ __host__ __device__ inline size_t cb_stream_smem_bytes(int max_cells, int max_do
 //  C  the products of each DoF summed in item order; complete DoFs finished (Chebyshev update
 //     or residual), the others leave their partial sum in their slot.
 //
-// STREAM: the element matrices come through the bulk-copy ring instead (one more warp, the
-// producer; phases separated by a barrier over the consumer warps only).
-template <int KIND, bool STREAM>
-__global__ void __launch_bounds__(STREAM ? kCb + 32 : kCb, STREAM ? 2 : 3)
+// SRC selects where phase B takes each cell's operator from:
+//  kSrcKe    the element matrices, loaded by the applying warps (above);
+//  kSrcRing  the element matrices through the bulk-copy ring (one more warp, the producer;
+//            phases separated by a barrier over the consumer warps only);
+//  kSrcGeo / kSrcGeo16  the geometric factors C_q of the 27 Gauss points (FP32 / FP16, 648 /
+//            324 bytes per cell instead of 1512), applied by sum factorisation over the
+//            cells' 1-D pencils (three cells per warp, see sfS / sfD).
+constexpr int kSrcKe = 0, kSrcRing = 1, kSrcGeo = 2, kSrcGeo16 = 3;
+template <int KIND, int SRC>
+__global__ void __launch_bounds__(SRC == kSrcRing ? kCb + 32 : kCb, SRC == kSrcRing ? 2 : 3)
     k_cb_apply(EbeOperator op, const float* __restrict__ dinv, const float* __restrict__ b,
                const float* __restrict__ xin, float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
+    constexpr bool STREAM = SRC == kSrcRing;
+    constexpr bool GEO = SRC == kSrcGeo || SRC == kSrcGeo16;
+    constexpr int kGeoBytes = SRC == kSrcGeo16 ? 324 : 648;  // geometric factors per cell
     extern __shared__ __align__(128) unsigned char cb_raw[];
     const int blk = blockIdx.x;
     const int p0 = op.cell_start[blk], nb = op.cell_start[blk + 1] - p0;
@@ -331,7 +388,22 @@ __global__ void __launch_bounds__(STREAM ? kCb + 32 : kCb, STREAM ? 2 : 3)
     // cell's is requested before phase A, so that it travels while the gathers run.
     float kA[14], kB[14];
     int lA = 0, lB = 0;
+    constexpr int kW = kCb / 32;
+    // optional L2 prefetch, op.prefetch cells ahead of each warp's loads: the warp's first
+    // cells are requested here, then every load requests the cell op.prefetch steps later,
+    // so the DRAM stream runs ahead of the register double buffer (and through phase A)
+    const int pf = STREAM ? 0 : op.prefetch;
+    auto prefetch_cell = [&](int c) {
+        if constexpr (GEO)
+            prefetch_l2(op.geo, kGeoBytes * (int64_t)op.n_cells, kGeoBytes * (int64_t)(p0 + c), kGeoBytes);
+        else
+            prefetch_l2(op.ke, 4 * op.n_ke, 1512 * (int64_t)(p0 + c), 1512);
+    };
+    if (pf > 0 && lane == 0)
+        for (int k = 1; k < pf; ++k)
+            if (warp + k * kW < nb) prefetch_cell(warp + k * kW);
     auto load_cell = [&](int c, float (&k)[14], int& l) {
+        if (pf > 0 && lane == 0 && c + pf * kW < nb) prefetch_cell(c + pf * kW);
         const float2* K = reinterpret_cast<const float2*>(op.ke + 378 * (size_t)(p0 + c));
 #pragma unroll
         for (int u = 0; u < 7; ++u) {
@@ -341,7 +413,47 @@ __global__ void __launch_bounds__(STREAM ? kCb + 32 : kCb, STREAM ? 2 : 3)
         }
         l = __ldg(loc + 27 * c + il);
     };
-    if (!STREAM && warp < nb) load_cell(warp, kA, lA);
+    // geometric factors: groups of three consecutive cells per warp (group t of the block =
+    // cells 3t .. 3t + 2; warp w takes t = w, w + 8, ...), lane l < 27 on cell 3t + l / 9 and
+    // pencil l % 9; cg = (C00, C11, C22, C01, C02, C12) at the lane's three Gauss points
+    // qx = 0..2 (pairs stored at [(qx, pair m), pencil] per cell), lc = the block-local entries
+    // of the pencil's three lattice nodes
+    const bool act = lane < 27;
+    const int sg = act ? lane / 9 : 2, pp = act ? lane % 9 : 8;
+    const int pa = pp % 3, pb = pp / 3;
+    const int n_groups = (nb + 2) / 3;
+    float cg[18];
+    int lc[3];
+    auto load_group = [&](int t) {
+        if (pf > 0 && lane == 0 && 3 * (t + pf * kW) < nb)
+            prefetch_l2(op.geo, kGeoBytes * (int64_t)op.n_cells, kGeoBytes * (int64_t)(p0 + 3 * (t + pf * kW)),
+                        3 * kGeoBytes);
+        const int cell = min(3 * t + sg, nb - 1);
+        if constexpr (SRC == kSrcGeo16) {
+            const __half2* G = reinterpret_cast<const __half2*>(op.geo) + 81 * (size_t)(p0 + cell) + pp;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const float2 v = __half22float2(__ldg(G + 9 * k));
+                cg[2 * k] = v.x;
+                cg[2 * k + 1] = v.y;
+            }
+        } else {
+            const float2* G = reinterpret_cast<const float2*>(op.geo) + 81 * (size_t)(p0 + cell) + pp;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const float2 v = __ldg(G + 9 * k);
+                cg[2 * k] = v.x;
+                cg[2 * k + 1] = v.y;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) lc[c] = __ldg(loc + 27 * cell + pp + 9 * c);
+    };
+    if constexpr (GEO) {
+        if (warp < n_groups) load_group(warp);
+    } else if (!STREAM && warp < nb) {
+        load_cell(warp, kA, lA);
+    }
     {
         const uint2* gi = reinterpret_cast<const uint2*>(op.items + 28 * (size_t)p0);
         uint2* si = reinterpret_cast<uint2*>(sit);
@@ -398,7 +510,6 @@ __global__ void __launch_bounds__(STREAM ? kCb + 32 : kCb, STREAM ? 2 : 3)
         }
         if (lane < 27) sy[27 * c + lane] = y;
     };
-    constexpr int kW = kCb / 32;
     if constexpr (STREAM) {
         bool ok = true;
         for (int j = 0; j < n_chunks; ++j) {
@@ -424,6 +535,116 @@ __global__ void __launch_bounds__(STREAM ? kCb + 32 : kCb, STREAM ? 2 : 3)
             if (lane == 0) mbar_arrive(&empty[sl]);
         }
         consumers_sync();
+    } else if constexpr (GEO) {
+        // the warp's scratch: region 1 holds W then Y, region 2 holds X then Z (each 81 floats)
+        float* R1 = reinterpret_cast<float*>(cb_raw + ((cb_smem_bytes(op.max_cells, op.max_dofs) + 15) & ~(size_t)15) +
+                                             warp * (size_t)kSfWarpBytes) +
+                    sg * kSfScratch;
+        float* R2 = R1 + 81;
+        for (int t = warp; t < n_groups; t += kW) {
+            const int cell = 3 * t + sg;
+            // 1  lane (a, b) = (pa, pb): contraction over c
+            float u[3], T1[3], T2[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) u[c] = sx[lc[c]];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                T1[q] = fmaf(sfS(q, 0), u[0], fmaf(sfS(q, 1), u[1], sfS(q, 2) * u[2]));
+                T2[q] = fmaf(sfD(q, 0), u[0], fmaf(sfD(q, 1), u[1], sfD(q, 2) * u[2]));
+            }
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    R1[9 * q + 3 * pa + pb] = T1[q];
+                    R1[27 + 9 * q + 3 * pa + pb] = T2[q];
+                }
+            }
+            __syncwarp();
+            // 2  lane (a, qz) = (pa, pb): contraction over b
+            float t1[3], t2[3], A1[3], A2[3], A3[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                t1[j] = R1[9 * pb + 3 * pa + j];
+                t2[j] = R1[27 + 9 * pb + 3 * pa + j];
+            }
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                A1[q] = fmaf(sfS(q, 0), t1[0], fmaf(sfS(q, 1), t1[1], sfS(q, 2) * t1[2]));
+                A2[q] = fmaf(sfD(q, 0), t1[0], fmaf(sfD(q, 1), t1[1], sfD(q, 2) * t1[2]));
+                A3[q] = fmaf(sfS(q, 0), t2[0], fmaf(sfS(q, 1), t2[1], sfS(q, 2) * t2[2]));
+            }
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    R2[9 * q + 3 * pb + pa] = A1[q];
+                    R2[27 + 9 * q + 3 * pb + pa] = A2[q];
+                    R2[54 + 9 * q + 3 * pb + pa] = A3[q];
+                }
+            }
+            __syncwarp();
+            // 3  lane (qy, qz) = (pa, pb): gradient at qx = 0..2, flux, transposed contraction over qx
+            float a1[3], a2[3], a3[3], fx[3], fy[3], fz[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                a1[j] = R2[9 * pa + 3 * pb + j];
+                a2[j] = R2[27 + 9 * pa + 3 * pb + j];
+                a3[j] = R2[54 + 9 * pa + 3 * pb + j];
+            }
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float gx = fmaf(sfD(q, 0), a1[0], fmaf(sfD(q, 1), a1[1], sfD(q, 2) * a1[2]));
+                const float gy = fmaf(sfS(q, 0), a2[0], fmaf(sfS(q, 1), a2[1], sfS(q, 2) * a2[2]));
+                const float gz = fmaf(sfS(q, 0), a3[0], fmaf(sfS(q, 1), a3[1], sfS(q, 2) * a3[2]));
+                const float* C = cg + 6 * q;
+                fx[q] = fmaf(C[0], gx, fmaf(C[3], gy, C[4] * gz));
+                fy[q] = fmaf(C[3], gx, fmaf(C[1], gy, C[5] * gz));
+                fz[q] = fmaf(C[4], gx, fmaf(C[5], gy, C[2] * gz));
+            }
+            // the next group's factors and lattice entries travel while this group finishes
+            if (t + kW < n_groups) load_group(t + kW);
+            if (act) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    R1[9 * a + 3 * pb + pa] = fmaf(sfD(0, a), fx[0], fmaf(sfD(1, a), fx[1], sfD(2, a) * fx[2]));
+                    R1[27 + 9 * a + 3 * pb + pa] = fmaf(sfS(0, a), fy[0], fmaf(sfS(1, a), fy[1], sfS(2, a) * fy[2]));
+                    R1[54 + 9 * a + 3 * pb + pa] = fmaf(sfS(0, a), fz[0], fmaf(sfS(1, a), fz[1], sfS(2, a) * fz[2]));
+                }
+            }
+            __syncwarp();
+            // 4  lane (a, qz) = (pa, pb): transposed contraction over qy
+            float b1[3], b2[3], b3[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                b1[j] = R1[9 * pa + 3 * pb + j];
+                b2[j] = R1[27 + 9 * pa + 3 * pb + j];
+                b3[j] = R1[54 + 9 * pa + 3 * pb + j];
+            }
+            if (act) {
+#pragma unroll
+                for (int bb = 0; bb < 3; ++bb) {
+                    R2[9 * bb + 3 * pa + pb] =
+                        fmaf(sfS(0, bb), b1[0], fmaf(sfS(1, bb), b1[1], fmaf(sfS(2, bb), b1[2],
+                             fmaf(sfD(0, bb), b2[0], fmaf(sfD(1, bb), b2[1], sfD(2, bb) * b2[2])))));
+                    R2[27 + 9 * bb + 3 * pa + pb] = fmaf(sfS(0, bb), b3[0], fmaf(sfS(1, bb), b3[1], sfS(2, bb) * b3[2]));
+                }
+            }
+            __syncwarp();
+            // 5  lane (a, b) = (pa, pb): transposed contraction over qz, the products at c = 0..2
+            float e1[3], e2[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                e1[j] = R2[9 * pb + 3 * pa + j];
+                e2[j] = R2[27 + 9 * pb + 3 * pa + j];
+            }
+            if (act && cell < nb) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    sy[27 * cell + pp + 9 * c] =
+                        fmaf(sfS(0, c), e1[0], fmaf(sfS(1, c), e1[1], fmaf(sfS(2, c), e1[2],
+                             fmaf(sfD(0, c), e2[0], fmaf(sfD(1, c), e2[1], sfD(2, c) * e2[2])))));
+            }
+        }
+        __syncthreads();
     } else {
         for (int c = warp; c < nb; c += 2 * kW) {
             if (c + kW < nb) load_cell(c + kW, kB, lB);
@@ -764,11 +985,16 @@ void AmgDevice::set_level0_ebe(const EbeOperator* op) {
     ebe_.err = ebe_err_.get();
     // the cap is a property of the kernel, shared by every mesh: always the largest block's
     const int cap = (int)cb_smem_bytes(kCbMaxCells, kCbPer * kCb);
-    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0, kSrcKe>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1, kSrcKe>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    const int cap_g = (int)cb_geo_smem_bytes(kCbMaxCells, kCbPer * kCb);
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0, kSrcGeo>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_g));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1, kSrcGeo>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_g));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0, kSrcGeo16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_g));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1, kSrcGeo16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_g));
     const int cap_s = (int)cb_stream_smem_bytes(kCbMaxCells, kCbPer * kCb);
-    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_s));
-    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_s));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<0, kSrcRing>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_s));
+    FGB_CUDA(cudaFuncSetAttribute(k_cb_apply<1, kSrcRing>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap_s));
 }
 
 unsigned AmgDevice::level0_errors() {
@@ -786,7 +1012,8 @@ double AmgDevice::smoother_bytes() const {
     // id, item end, slot and the gathered x; per DoF: b, D^-1, d in and out, x out, the
     // Dirichlet flag; per slot: the partial written and read; per split
     // DoF: its id and slot range
-    return ebe_.n_cells * (378.0 * 4 + 110.0) + (double)ebe_.n_local * 14.0 + n * 21.0 + ebe_.n_slots * 8.0 +
+    const double per_cell = ebe_.geo_kind == 2 ? 324.0 : (ebe_.geo_kind == 1 ? 648.0 : 378.0 * 4);
+    return ebe_.n_cells * (per_cell + 110.0) + (double)ebe_.n_local * 14.0 + n * 21.0 + ebe_.n_slots * 8.0 +
            ebe_.n_bnd * 8.0;
 }
 
@@ -797,23 +1024,26 @@ void AmgDevice::level0_apply(int kind, const float* xin, float* xout, float c1, 
     const int g = grid_for(L.n, kB);
     if (ebe_on_) {
         const int gb = grid_for(ebe_.n_bnd, kB);
-        if (stream_ke_) {
-            const size_t smem = cb_stream_smem_bytes(ebe_.max_cells, ebe_.max_dofs);
-            if (kind == 0)
-                FGB_LAUNCH(k_cb_apply<0, true><<<ebe_.n_blocks, kCb + 32, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout,
-                                                                                          L.d.get(), c1, c2));
-            else
-                FGB_LAUNCH(k_cb_apply<1, true><<<ebe_.n_blocks, kCb + 32, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout,
-                                                                                          nullptr, 0.f, 0.f));
-        } else {
-            const size_t smem = cb_smem_bytes(ebe_.max_cells, ebe_.max_dofs);
-            if (kind == 0)
-                FGB_LAUNCH(k_cb_apply<0, false><<<ebe_.n_blocks, kCb, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout,
-                                                                                      L.d.get(), c1, c2));
-            else
-                FGB_LAUNCH(k_cb_apply<1, false><<<ebe_.n_blocks, kCb, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout,
-                                                                                      nullptr, 0.f, 0.f));
+        const int src = ebe_.geo_kind == 2 ? kSrcGeo16 : (ebe_.geo_kind == 1 ? kSrcGeo : (stream_ke_ ? kSrcRing : kSrcKe));
+        const size_t smem = src == kSrcRing ? cb_stream_smem_bytes(ebe_.max_cells, ebe_.max_dofs)
+                            : (src == kSrcGeo || src == kSrcGeo16) ? cb_geo_smem_bytes(ebe_.max_cells, ebe_.max_dofs)
+                                                                   : cb_smem_bytes(ebe_.max_cells, ebe_.max_dofs);
+        const int threads = src == kSrcRing ? kCb + 32 : kCb;
+        float* dd = kind == 0 ? L.d.get() : nullptr;
+        const float cc1 = kind == 0 ? c1 : 0.f, cc2 = kind == 0 ? c2 : 0.f;
+#define FGB_CB_APPLY(K, S) \
+    FGB_LAUNCH(k_cb_apply<K, S><<<ebe_.n_blocks, threads, smem, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, dd, cc1, cc2))
+        switch (src * 2 + kind) {
+            case kSrcKe * 2: FGB_CB_APPLY(0, kSrcKe); break;
+            case kSrcKe * 2 + 1: FGB_CB_APPLY(1, kSrcKe); break;
+            case kSrcRing * 2: FGB_CB_APPLY(0, kSrcRing); break;
+            case kSrcRing * 2 + 1: FGB_CB_APPLY(1, kSrcRing); break;
+            case kSrcGeo * 2: FGB_CB_APPLY(0, kSrcGeo); break;
+            case kSrcGeo * 2 + 1: FGB_CB_APPLY(1, kSrcGeo); break;
+            case kSrcGeo16 * 2: FGB_CB_APPLY(0, kSrcGeo16); break;
+            default: FGB_CB_APPLY(1, kSrcGeo16); break;
         }
+#undef FGB_CB_APPLY
         if (gb) {
             if (kind == 0)
                 FGB_LAUNCH(k_cb_finish<0><<<gb, kB, 0, stream_>>>(ebe_, L.dinv, L.bin, xin, xout, L.d.get(), c1, c2));

@@ -75,6 +75,12 @@ struct EbeOperator {
     const int8_t* fixed = nullptr;        // 1 on Dirichlet rows
     int64_t n_ke = 0;                     // floats in ke (378 per cell)
     unsigned* err = nullptr;              // bounded waits of the streamed kernel that timed out
+    int prefetch = 0;                     // element matrices prefetched into L2, cells ahead per warp
+    // geometric factors instead of the element matrices (0: element matrices; 1: FP32, 2: FP16):
+    // per position 81 pairs at [(qx, m), pencil] = 9 (3 qx + m) + qy + 3 qz, pair m = (C00, C11),
+    // (C22, C01), (C02, C12) of C_q = w_q |det J_q| J_q^-1 J_q^-T at Gauss point (qx, qy, qz)
+    const void* geo = nullptr;
+    int geo_kind = 0;
 };
 
 // Device side of the hierarchy and the V-cycle (amg.cu).
@@ -102,6 +108,11 @@ public:
     // level-0 element matrices streamed into a shared-memory ring by bulk copies (1) or loaded
     // by the warps that apply them (0, default: measured faster, see the design notes)
     void set_level0_stream(bool on) { stream_ke_ = on; }
+    void set_level0_prefetch(int cells) { ebe_.prefetch = cells; }
+    void set_level0_geo(const void* geo, int kind) {
+        ebe_.geo = geo;
+        ebe_.geo_kind = geo ? kind : 0;
+    }
     // nonzero when a bounded wait of the streamed kernel ran out (the result is then invalid)
     unsigned level0_errors();
     bool level0_ebe() const { return ebe_on_; }

@@ -485,20 +485,25 @@ __global__ void __launch_bounds__(kB) kb_dense(const int32_t* __restrict__ list,
     }
 }
 
-// WHILE condition: continue while an admitted mesh is unfinished and the cap is not reached
+// WHILE condition: continue while an admitted mesh is unfinished and the cap |loop[1]| is not
+// reached; a negative loop[1] also stops after an iteration in which an admitted mesh
+// finished (meshes finished before the launch are no longer admitted)
 __global__ void kb_continue(const int32_t* __restrict__ run, const int32_t* __restrict__ nrun, const BatchMeshState* st,
                             int32_t* loop, cudaGraphConditionalHandle handle, int use_handle) {
-    __shared__ int any;
-    if (threadIdx.x == 0) any = 0;
+    __shared__ int any, fin;
+    if (threadIdx.x == 0) any = fin = 0;
     __syncthreads();
     const int n = *nrun;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
         if (!st[run[i]].done) any = 1;
+        else fin = 1;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         const int it = loop[0] + 1;
         loop[0] = it;
-        const int go = (any && it < loop[1]) ? 1 : 0;
+        const int cap = loop[1] < 0 ? -loop[1] : loop[1];
+        const int go = (any && it < cap && !(loop[1] < 0 && fin)) ? 1 : 0;
         loop[2] = go;
         if (use_handle) cudaGraphSetConditional(handle, go);
     }
@@ -1179,7 +1184,7 @@ void BatchSolver::tune() {
     cudaEventDestroy(e1);
 }
 
-int BatchSolver::step(int max_iters) {
+int BatchSolver::step(int max_iters, bool stop_at_first) {
     std::lock_guard<std::mutex> lk(mu_);
     if (running_.empty()) return 0;
     ensure_capacity();
@@ -1204,7 +1209,7 @@ int BatchSolver::step(int max_iters) {
             capture();
             dirty_ = false;
         }
-        int loop[3] = {0, std::max(1, max_iters), 1};
+        int loop[3] = {0, std::max(1, max_iters) * (stop_at_first ? -1 : 1), 1};
         FGB_CUDA(cudaMemcpyAsync(d_->loop.get(), loop, 3 * sizeof(int), cudaMemcpyHostToDevice, stream_));
         FGB_CUDA(cudaGraphLaunch(exec_, stream_));
         FGB_CUDA(cudaMemcpyAsync(d_->h_loop, d_->loop.get(), 4 * sizeof(int), cudaMemcpyDeviceToHost, stream_));
@@ -1213,7 +1218,7 @@ int BatchSolver::step(int max_iters) {
         g_kernel_launches.fetch_add((long long)iters * body_kernels_);
     } else {
         dirty_ = false;
-        int loop[3] = {0, std::max(1, max_iters), 1};
+        int loop[3] = {0, std::max(1, max_iters) * (stop_at_first ? -1 : 1), 1};
         FGB_CUDA(cudaMemcpyAsync(d_->loop.get(), loop, 3 * sizeof(int), cudaMemcpyHostToDevice, stream_));
         cudaGraphConditionalHandle none{};
         while (true) {

@@ -95,8 +95,10 @@ public:
     // on the top as in PoissonSolver::setup); warm start from the slot's last solution.
     void admit(int slot, double E0, double rel_tol, int max_iter);
     // Run at most `max_iters` iterations of every admitted, unfinished mesh (one graph
-    // launch). Returns the number of admitted meshes still running afterwards.
-    int step(int max_iters);
+    // launch); with stop_at_first the launch also ends after the iteration in which a mesh
+    // finished, so that its result can be taken at once. Returns the number of admitted
+    // meshes still running afterwards.
+    int step(int max_iters, bool stop_at_first = false);
     // Slots whose solve finished since the last call (converged or failed), with results.
     std::vector<std::pair<int, BatchSolveResult>> collect_finished();
     bool idle() const { return running_.empty(); }

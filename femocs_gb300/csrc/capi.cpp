@@ -476,6 +476,14 @@ long long fgb_field_export_element_matrices(FGB_FIELD* f, double* out) {
 int fgb_field_set_level0_stream(FGB_FIELD* f, int on) {
     return guarded([&] { f->f->fem().set_level0_stream(on != 0); return 0; });
 }
+int fgb_field_set_level0_operator(FGB_FIELD* f, int kind) {
+    int used = -1;
+    const int rc = guarded([&] { used = f->f->fem().set_level0_operator(kind); return 0; });
+    return rc ? -1 : used;
+}
+int fgb_field_set_level0_prefetch(FGB_FIELD* f, int cells) {
+    return guarded([&] { f->f->fem().set_level0_prefetch(cells); return 0; });
+}
 int fgb_field_set_coarse_cycles(FGB_FIELD* f, int level, int cycles) {
     return guarded([&] { f->f->fem().set_coarse_cycles(level, cycles); return 0; });
 }
@@ -1014,6 +1022,9 @@ FGB_SERVER* fgb_server_create(FGB_BATCH* b, double rel_tol, int max_iter, int it
     return s;
 }
 void fgb_server_free(FGB_SERVER* s) { delete s; }
+int fgb_server_set_launch_policy(FGB_SERVER* s, int idle_iters, int stop_at_first) {
+    return guarded([&] { s->s->set_launch_policy(idle_iters, stop_at_first != 0); return 0; });
+}
 
 int fgb_server_add_run(FGB_SERVER* s, const FGB_MESH* m, const double* xyz, int n_atoms, unsigned long long seed) {
     int id = INT32_MIN;

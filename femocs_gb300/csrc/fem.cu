@@ -20,6 +20,7 @@
 //                      element matrices over the cell blocks (cell_blocks.h)
 //   k_ke_cyclic        Q2 element matrices into the cell blocks' FP32 (hi, lo) layout
 #include <algorithm>
+#include <cstring>
 #include <chrono>
 #include <omp.h>
 #include <cstdlib>
@@ -1489,6 +1490,11 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
         op.n_ke = 378LL * nc_;
         amg_->set_level0_ebe(&op);
         amg_->set_level0_stream(level0_stream_);
+        amg_->set_level0_prefetch(level0_prefetch_);
+        if (level0_geo_) {
+            ensure_geo();
+            amg_->set_level0_geo(geo_.get(), geo_built_);
+        }
     }
     phase("device hierarchy upload");
     amg_->smoother_timer.enabled = profiling_;
@@ -1582,6 +1588,8 @@ void FemDevice::set_cell_blocks(int cells_per_block, int max_dofs) {
     cb_cells_ = cells_per_block;
     cb_max_dofs_ = max_dofs;
     cb_.reset();
+    geo_built_ = geo_for_ = 0;  // block order changes: rebuilt on the next use
+    geo_.release();
     ke32_.release();
     ke32lo_.release();
     amg_.reset();
@@ -1611,6 +1619,51 @@ void FemDevice::export_element_matrices(double* out) {
 void FemDevice::set_level0_stream(bool on) {
     level0_stream_ = on;
     if (amg_) amg_->set_level0_stream(on);
+}
+
+void FemDevice::ensure_geo() {
+    if (geo_built_ && geo_for_ == level0_geo_) return;
+    ensure_cell_blocks();
+    const bool half = level0_geo_ == 2;
+    geo_.resize((size_t)nc_ * (half ? 324 : 648));
+    if (geo_max_.size() != 1) geo_max_.resize(1);
+    q2_geometric_factors(nc_, cb_->perm.get(), cell_dofs_.get(), dof_xyz_.get(), geo_.get(), half, geo_max_.get(),
+                         stream_);
+    geo_built_ = level0_geo_;
+    geo_for_ = level0_geo_;
+    if (half) {
+        unsigned h = 0;
+        FGB_CUDA(cudaMemcpyAsync(&h, geo_max_.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        float mx;
+        std::memcpy(&mx, &h, sizeof(mx));
+        if (!(mx < 6.0e4f)) {  // beyond FP16 (max 65504): the FP32 factors instead
+            geo_.resize((size_t)nc_ * 648);
+            q2_geometric_factors(nc_, cb_->perm.get(), cell_dofs_.get(), dof_xyz_.get(), geo_.get(), false, nullptr,
+                                 stream_);
+            geo_built_ = 1;
+        }
+    }
+}
+
+int FemDevice::set_level0_operator(int kind) {
+    FGB_REQUIRE(kind >= 0 && kind <= 2, "level-0 operator: 0 element matrices, 1 FP32 or 2 FP16 geometric factors");
+    FGB_REQUIRE(kind == 0 || fs_.order == 2, "geometric factors are for Q2 fields");
+    level0_geo_ = kind;
+    if (kind == 0) {
+        geo_built_ = geo_for_ = 0;
+        geo_.release();
+    } else {
+        ensure_geo();
+    }
+    if (amg_ && level0_ebe_) amg_->set_level0_geo(kind ? geo_.get() : nullptr, geo_built_);
+    return geo_built_;
+}
+
+void FemDevice::set_level0_prefetch(int cells) {
+    FGB_REQUIRE(cells >= 0 && cells <= 64, "level-0 prefetch depth: 0 (off) to 64 cells per warp");
+    level0_prefetch_ = cells;
+    if (amg_) amg_->set_level0_prefetch(cells);
 }
 
 void FemDevice::set_coarse_cycles(int level, int cycles) {

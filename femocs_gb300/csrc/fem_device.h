@@ -113,6 +113,11 @@ public:
     // Q2 level 0 by cell blocks: element matrices streamed by bulk copies or loaded by the
     // applying warps (default)
     void set_level0_stream(bool on);
+    void set_level0_prefetch(int cells);
+    // Q2 level 0 by cell blocks: element matrices (0) or geometric factors in FP32 (1) or
+    // FP16 (2), applied by sum factorisation; returns the kind in use (FP16 falls back to FP32
+    // when an entry is beyond its range)
+    int set_level0_operator(int kind);
     // multigrid: cycles of level+1 per coarse-grid correction at `level` (1 = V-cycle)
     void set_coarse_cycles(int level, int cycles);
     // Q2: apply the finest multigrid level element by element, by cell blocks (cell_blocks.h;
@@ -202,6 +207,14 @@ private:
     int smooth_degree_ = 0;
     std::vector<int> coarse_cycles_;
     bool level0_stream_ = false;
+    int level0_prefetch_ = 1;     // L2 prefetch one group ahead (measured best on config 2)
+    int level0_geo_ = 2;          // requested level-0 operator source (set_level0_operator):
+                                  // FP16 geometric factors (0.69 vs 0.89 ms per config-2 step)
+    int geo_built_ = 0;           // kind held in geo_ (0: none)
+    int geo_for_ = 0;             // kind requested when geo_ was built (2 may hold FP32: fallback)
+    DBuf<unsigned char> geo_;     // geometric factors in block order (q2_geometric_factors)
+    DBuf<unsigned> geo_max_;
+    void ensure_geo();
     bool ke_tensor_ = true;
     DBuf<unsigned char> tc_scratch_;  // tensor-core element matrices: slices per persistent CTA
     DBuf<unsigned> tc_err_;

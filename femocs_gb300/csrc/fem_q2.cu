@@ -14,11 +14,15 @@
 //                        search (fixed order: deterministic)
 //   k_q2_neumann_rows    3x3 Gauss on the bilinear top faces, biquadratic face shape functions
 //   k_sell_dirichlet     symmetric elimination on the SELL layout (FP64 + FP32 copies, D^-1)
+//   k_q2_geo             geometric factors w |det J| J^-1 J^-T per Gauss point for the
+//                        matrix-free level-0 smoother (FP32 or FP16, block order)
 // Lattice: node L = a + 3b + 9c at reference coordinates (a-1, b-1, c-1); 1-D quadratic
 // Lagrange l0(t) = t(t-1)/2, l1(t) = 1 - t^2, l2(t) = t(t+1)/2.
 #include <climits>
 #include <cmath>
 #include <mutex>
+
+#include <cuda_fp16.h>
 
 #include "fem_q2.h"
 
@@ -385,7 +389,71 @@ __global__ void k_sell_dirichlet(int n, const int64_t* __restrict__ sptr, const 
     dinv32[r] = (float)(1.0 / diag);
 }
 
+// geometric factors of the cell-block smoother: thread (p, q) takes cell perm[p], its corners
+// relative to corner 0 (FP64 differences, then FP32), J_q of the trilinear map, and writes
+// C_q = w_q |det J_q| J_q^-1 J_q^-T as pairs m = (C00, C11), (C22, C01), (C02, C12) at
+// [81 p + 9 (3 qx + m) + qy + 3 qz] (q = qx + 3 qy + 9 qz; the smoother's lane for pencil
+// (qy, qz) reads its three Gauss points' pairs 9 apart), in FP32 (T = float2) or FP16 (T = __half2; the largest |entry| is kept
+// in *cmax as float bits so that the host can refuse values beyond the FP16 range)
+template <typename T>
+__global__ void k_q2_geo(long long total, const int32_t* __restrict__ perm, const int32_t* __restrict__ cd,
+                         const double* __restrict__ dxyz, T* __restrict__ out, unsigned* __restrict__ cmax) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const long long p = idx / 27;
+    const int q = (int)(idx - 27 * p);
+    const int32_t* c = cd + 27 * (size_t)perm[p];
+    const double* x0 = dxyz + 3 * (size_t)c[c_q2_corner[0]];
+    float J[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    for (int k = 1; k < 8; ++k) {  // corner 0 contributes nothing relative to itself
+        const double* xk = dxyz + 3 * (size_t)c[c_q2_corner[k]];
+        for (int a = 0; a < 3; ++a) {
+            const float xa = (float)(xk[a] - x0[a]);
+            for (int b = 0; b < 3; ++b) J[a][b] = fmaf(xa, (float)c_q1_dN[(q * 8 + k) * 3 + b], J[a][b]);
+        }
+    }
+    // adjugate rows: J^-1 = adj / det
+    float A[3][3];
+    A[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    A[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    A[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    A[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    A[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    A[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    A[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    A[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    A[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    const float det = J[0][0] * A[0][0] + J[0][1] * A[1][0] + J[0][2] * A[2][0];
+    const float s = (float)c_q2_w[q] / fabsf(det);
+    auto C = [&](int r, int t) { return s * (A[r][0] * A[t][0] + A[r][1] * A[t][1] + A[r][2] * A[t][2]); };
+    const float v[6] = {C(0, 0), C(1, 1), C(2, 2), C(0, 1), C(0, 2), C(1, 2)};
+    T* o = out + 81 * (size_t)p + 27 * (q % 3) + q / 3;
+    if constexpr (sizeof(T) == sizeof(float2)) {
+        for (int m = 0; m < 3; ++m) o[9 * m] = make_float2(v[2 * m], v[2 * m + 1]);
+    } else {
+        float mx = 0.f;
+        for (int m = 0; m < 6; ++m) mx = fmaxf(mx, fabsf(v[m]));
+        if (!(mx <= 3.0e38f)) mx = 3.0e38f;  // NaN or inf: report as out of range
+        atomicMax(cmax, __float_as_uint(mx));
+        for (int m = 0; m < 3; ++m) o[9 * m] = __floats2half2_rn(v[2 * m], v[2 * m + 1]);
+    }
+}
+
 }  // namespace
+
+void q2_geometric_factors(long long n_pos, const int32_t* perm, const int32_t* cell_dofs, const double* dof_xyz,
+                          void* out, bool half, unsigned* cmax, cudaStream_t s) {
+    upload_tables();
+    const long long total = 27 * n_pos;
+    if (half) {
+        FGB_CUDA(cudaMemsetAsync(cmax, 0, sizeof(unsigned), s));
+        FGB_LAUNCH(k_q2_geo<__half2><<<grid_for(total, 256), 256, 0, s>>>(total, perm, cell_dofs, dof_xyz,
+                                                                         static_cast<__half2*>(out), cmax));
+    } else {
+        FGB_LAUNCH(k_q2_geo<float2><<<grid_for(total, 256), 256, 0, s>>>(total, perm, cell_dofs, dof_xyz,
+                                                                        static_cast<float2*>(out), cmax));
+    }
+}
 
 void q2_cell_stiffness(int nc, const int32_t* cd, const double* dxyz, double* ke, cudaStream_t s) {
     upload_tables();

@@ -14,6 +14,11 @@ void q2_cell_stiffness(int nc, const int32_t* cell_dofs, const double* dof_xyz, 
 // combined in FP64; scratch (per persistent CTA) and err are the caller's reusable buffers
 void q2_cell_stiffness_tc(int nc, const int32_t* cell_dofs, const double* dof_xyz, double* ke,
                           DBuf<unsigned char>& scratch, DBuf<unsigned>& err, cudaStream_t s);
+// geometric factors of the matrix-free level-0 smoother, block order (position p = cell
+// perm[p]): 81 pairs per position, FP32 (float2) or FP16 (half2); with half, *cmax (device)
+// receives the largest |entry| as float bits
+void q2_geometric_factors(long long n_pos, const int32_t* perm, const int32_t* cell_dofs, const double* dof_xyz,
+                          void* out, bool half, unsigned* cmax, cudaStream_t s);
 // one 128 x 48 x 32 BF16 tensor-core product of small integers on the device against the
 // host's: the largest absolute difference (0 when descriptors and TMEM layout are right)
 double tc_selftest();

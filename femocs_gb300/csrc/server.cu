@@ -155,6 +155,13 @@ void FieldServer::start() {
     th_ = std::thread([this] { loop(); });
 }
 
+void FieldServer::set_launch_policy(int idle_iters, bool stop_at_first) {
+    FGB_REQUIRE(!th_.joinable(), "the launch policy is set before the server starts");
+    FGB_REQUIRE(idle_iters >= 0, "idle iterations per launch must be >= 0");
+    opt_.idle_iters = idle_iters;
+    opt_.stop_at_first = stop_at_first;
+}
+
 void FieldServer::stop() {
     stop_ = true;
     qcv_.notify_all();
@@ -227,7 +234,16 @@ void FieldServer::loop() {
             for (auto& r : runs_) in_flight += r->stage != 0;
             max_in_flight_ = std::max(max_in_flight_, in_flight);
             if (!b_.idle()) {
-                b_.step(opt_.iters_per_launch);
+                // short launches while requests wait for admission (new arrivals or runs
+                // that are busy), long ones otherwise
+                bool waiting = false;
+                {
+                    std::lock_guard<std::mutex> lk(qmu_);
+                    waiting = !inbox_.empty();
+                }
+                for (auto& r : runs_) waiting = waiting || !r->queue.empty();
+                const int cap = !waiting && opt_.idle_iters > 0 ? opt_.idle_iters : opt_.iters_per_launch;
+                b_.step(cap, opt_.stop_at_first);
                 ++launches_;
                 for (auto& [slot, res] : b_.collect_finished()) {
                     Run& r = *runs_[slot2run[slot]];

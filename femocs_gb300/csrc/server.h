@@ -25,6 +25,8 @@ struct ServerOptions {
     double rel_tol = 1e-9;
     int max_iter = 500;
     int iters_per_launch = 4;     // solver iterations per graph launch between admissions
+    int idle_iters = 0;           // per launch while no request waits (0: iters_per_launch)
+    bool stop_at_first = false;   // end a launch after the iteration in which a solve finished
     int rank = 1;                 // interpolation rank (1 linear tet, 2 quadratic tet, 3 hex)
     bool smoothen = true;
     double hbm_reserve = 2e9;     // bytes left free when admitting a run's mesh
@@ -55,6 +57,9 @@ public:
     long long submit(int run, double E0, double sigma);
     void start();
     void stop();
+    // launch policy (before start): iterations per launch while no request waits, and whether
+    // a launch ends as soon as one of its solves finished
+    void set_launch_policy(int idle_iters, bool stop_at_first);
     // block until every submitted request has completed (or the timeout in seconds passes)
     bool drain(double timeout_s);
     // Poisson arrivals at `rate` per second, n requests, runs chosen uniformly, applied

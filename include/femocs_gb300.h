@@ -201,6 +201,16 @@ long long fgb_field_export_element_matrices(FGB_FIELD* f, double* out);
  * shared-memory ring filled by bulk copies from a producer warp (1) or by their own loads (0,
  * default: 0.86 against 1.19 ms per smoothing step on the 1.7e7-DoF benchmark mesh) */
 int fgb_field_set_level0_stream(FGB_FIELD* f, int on);
+/* Q2 level 0 by cell blocks: the operator from the element matrices (kind 0) or, matrix-free,
+ * from the geometric factors w_q |det J_q| J_q^-1 J_q^-T of the 27 Gauss points (kind 1: FP32,
+ * 648 bytes per hex; kind 2: FP16, 324 bytes; the default) applied by sum factorisation.
+ * Returns the kind in use (FP16 falls back to FP32 when a factor is beyond its range),
+ * negative on error */
+int fgb_field_set_level0_operator(FGB_FIELD* f, int kind);
+/* Q2 level 0 by cell blocks: each applying warp asks L2 for the operator data (element matrix
+ * or geometric factors) of the cells `cells` steps ahead of the ones it loads
+ * (cp.async.bulk.prefetch; 0 = off, 1 = the default, at most 64) */
+int fgb_field_set_level0_prefetch(FGB_FIELD* f, int cells);
 /* multigrid PCG: the coarse-grid correction of level `level` (0 = finest) runs `cycles` (1..8)
  * cycles of the next level, each on the residual left by the ones before (1 = V-cycle); the
  * preconditioner stays symmetric */
@@ -350,6 +360,10 @@ typedef struct FGB_SERVER FGB_SERVER;
 FGB_SERVER* fgb_server_create(FGB_BATCH* b, double rel_tol, int max_iter, int iters_per_launch, int rank, int smoothen,
                               double hbm_reserve);
 void fgb_server_free(FGB_SERVER* s);
+/* launch policy, before fgb_server_start: solver iterations per graph launch while no request
+ * waits for admission (idle_iters; 0 = iters_per_launch), and whether a launch ends after the
+ * iteration in which one of its solves finished (stop_at_first) */
+int fgb_server_set_launch_policy(FGB_SERVER* s, int idle_iters, int stop_at_first);
 /* register a run (mesh placed by fgb_server_place_pending or later by the scheduler) */
 int fgb_server_add_run(FGB_SERVER* s, const FGB_MESH* m, const double* xyz, int n_atoms, unsigned long long seed);
 /* n synthetic runs: nanotip meshes of specs[i], n_atoms points each (surface atoms, topped

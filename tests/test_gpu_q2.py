@@ -183,13 +183,14 @@ def test_q2_cell_block_limits_give_the_same_solve(anode):
 @pytest.mark.parametrize("cells,max_dofs", [(1, 27), (5, 150), (256, 4096)])
 def test_q2_streamed_element_matrices_are_bit_identical(cells, max_dofs):
     """The level-0 element matrices streamed through the bulk-copy ring and loaded by the
-    applying warps (the default) give bit-identical solves: the same products in the same order. Block
+    applying warps give bit-identical solves: the same products in the same order. Block
     limits cover one-cell blocks (every chunk partial, copies starting 8 bytes past a
     16-byte boundary for odd cells, the array's last bytes loaded plainly), blocks of five
     cells (odd chunk sizes) and the default blocks (full chunks, rings reused)."""
     m = fg.Mesh.synthetic(**SMALL)
     f = fg.Field(m, order=2)
     f.set_cell_blocks(cells, max_dofs)
+    assert f.set_level0_operator(0) == 0
     out = {}
     for stream in (False, True):
         f.set_level0_stream(stream)
@@ -200,3 +201,30 @@ def test_q2_streamed_element_matrices_are_bit_identical(cells, max_dofs):
         out[stream] = (st["iterations"], f.solution())
     assert out[True][0] == out[False][0]
     assert np.array_equal(out[True][1].view(np.int64), out[False][1].view(np.int64))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cells,max_dofs", [(1, 27), (5, 150), (256, 4096)])
+def test_q2_matrix_free_level0_matches_element_matrices(cells, max_dofs):
+    """The level-0 smoother applied matrix-free from the geometric factors (sum factorisation
+    over the hexes' pencils, three hexes per warp; FP32 and FP16 factors, with and without L2
+    prefetch) preconditions as well as the element matrices: the same iteration count within
+    one, the same true residual bound, and the same solution within the solve tolerance.
+    Block limits cover one-hex blocks (every three-hex group partial), five-hex blocks (a
+    partial last group) and the default blocks."""
+    m = fg.Mesh.synthetic(**SMALL)
+    f = fg.Field(m, order=2)
+    f.set_cell_blocks(cells, max_dofs)
+    res = {}
+    for kind, pf in ((0, 0), (1, 0), (2, 0), (2, 2)):
+        assert f.set_level0_operator(kind) == kind
+        f.set_level0_prefetch(pf)
+        f.setup(-E0)
+        f.assemble(True, False)
+        rc, st = f.solve(precision=2, rel_tol=1e-10)
+        assert rc > 0 and st["status"] == 1 and st["rel_residual"] <= 1e-10, (kind, st)
+        res[(kind, pf)] = (st["iterations"], f.solution())
+    it0, x0 = res[(0, 0)]
+    for key, (it, x) in res.items():
+        assert abs(it - it0) <= 1, (key, it, it0)
+        assert np.abs(x - x0).max() <= 2e3 * 1e-10 * np.abs(x0).max(), key
