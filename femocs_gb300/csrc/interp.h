@@ -75,6 +75,13 @@ public:
     const double* d_node_xyz() const { return xyz_.get(); }
     const int32_t* d_hexs() const { return hexs_.get(); }
     const double* d_hex_coeffs() const { return hexf_.get(); }
+    // keep the geometry-only factors of the nodal field and the smoothing on the device after
+    // the first extraction (112 B per node-hex incidence, 8 B per smoothing neighbour): later
+    // extractions only gather and sum, with bit-identical results. On by default.
+    void set_geometry_cache(bool on) {
+        geo_cache_ = on;
+        if (!on) { nodal_ids_.release(); nodal_coef_.release(); smooth_w_.release(); smooth_f_.release(); }
+    }
 
 private:
     void ensure_scratch(int n);
@@ -92,6 +99,9 @@ private:
     DBuf<int32_t> seed_, gptr_, gtets_;
     DBuf<double> gcxyz_;
     DBuf<double> sol_;
+    bool geo_cache_ = true;
+    DBuf<int32_t> nodal_ids_;
+    DBuf<double> nodal_coef_, smooth_w_, smooth_f_;
     // per-point scratch
     DBuf<int32_t> v_, nin_, f_, res_, dep_, counters_;
     int scratch_n_ = 0;

@@ -17,8 +17,12 @@
 //   k_nearest_ctr    exact nearest centroid (lowest index on ties) for points without V
 //   k_resolve        guess-independent points get their final cell in parallel
 //   k_chain_runs     each run of guess-dependent points replays the reference's chain
-//                    from the last independent point
+//                    from the last independent point (one warp per run, up to 32
+//                    point-in-tet tests of the guess and its neighbours at once)
 //   k_interpolate    shape functions of rank 1/2/3 and the weighted nodal solution
+//   k_nodal_field, k_smooth: the nodal field and its smoothing; their geometry-only factors
+//                    (k_nodal_coef, k_smooth_coef) are kept after a mesh's first
+//                    extraction, so later solves only gather and sum (k_*_cached)
 #include <climits>
 #include <cmath>
 #include <algorithm>
@@ -228,32 +232,46 @@ __global__ void k_resolve(int n, const int32_t* __restrict__ V, const int32_t* _
     else atomicAdd(&counters[2], 1);
 }
 
+// Runs of guess-dependent points replay the reference's chained search from the last
+// independent point (the guess, then the tets sharing its nodes in list order, then the scan
+// result), one warp per run: for each point lane 0 tests the guess and lanes 1..31 the guess's
+// neighbours in list order (further neighbours 31 at a time); the lowest lane whose tet
+// contains the point is the reference's first hit, so the result is that of the sequential
+// search, with up to 32 point-in-tet tests in flight instead of one
 __global__ void k_chain_runs(int n, Pts P, int g0, const double* __restrict__ det, const int32_t* __restrict__ nptr,
-                             const int32_t* __restrict__ nidx, const int32_t* __restrict__ V, const int32_t* __restrict__ F,
-                             const int32_t* __restrict__ dep, int32_t* __restrict__ res, int32_t* __restrict__ counters) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                                  const int32_t* __restrict__ nidx, const int32_t* __restrict__ V,
+                                  const int32_t* __restrict__ F, const int32_t* __restrict__ dep, int32_t* __restrict__ res,
+                                  int32_t* __restrict__ counters) {
+    const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wid >= n) return;  // whole warp leaves together
+    const int i = (int)wid;
     if (!dep[i] || (i > 0 && dep[i - 1])) return;
     int g = i == 0 ? g0 : abs(res[i - 1]);
     int j = i;
     for (; j < n && dep[j]; ++j) {
         double x, y, z;
         P.get(j, x, y, z);
-        int r;
-        if (pic(det, g, x, y, z)) {
-            r = g;
-        } else {
-            r = INT_MIN;
-            for (int k = nptr[g]; k < nptr[g + 1]; ++k) {
-                const int u = nidx[k];
-                if (pic(det, u, x, y, z)) { r = u; break; }
+        const int k0 = nptr[g], k1 = nptr[g + 1];
+        int r = INT_MIN;
+        // chunk 0: the guess (lane 0) and the first 31 neighbours; then 31 more per chunk
+        for (int base = k0 - 1; base < k1; base += 31) {
+            const int k = base + lane;  // lane 0 of chunk 0 is the guess itself
+            int cand = -1;
+            if (lane == 0) cand = base == k0 - 1 ? g : -1;
+            else if (k < k1) cand = nidx[k];
+            const bool hit = cand >= 0 && pic(det, cand, x, y, z);
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (m) {
+                r = __shfl_sync(0xffffffffu, cand, __ffs(m) - 1);
+                break;
             }
-            if (r == INT_MIN) r = V[j] >= 0 ? V[j] : -F[j];
         }
-        res[j] = r;
+        if (r == INT_MIN) r = V[j] >= 0 ? V[j] : -F[j];
+        if (lane == 0) res[j] = r;
         g = abs(r);
     }
-    atomicMax(&counters[3], j - i);
+    if (lane == 0) atomicMax(&counters[3], j - i);
 }
 
 // ---------------------------------------------------------------- surface triangles
@@ -713,6 +731,137 @@ __global__ void k_smooth(int n_tn, const int32_t* __restrict__ vptr, const int32
     }
 }
 
+// The geometry-only parts of k_nodal_field and k_smooth, evaluated once per mesh with the same
+// expressions (so the same FP64 values), and the per-solve kernels that use them: the same
+// sums in the same order, hence bit-identical results.
+//
+// k_nodal_coef: per (node, hex) item p of n2c, the four nonzero shape-function gradients of
+// the hex at that node in ascending local-node order: node ids ids[4p + j] and gradients
+// coef[12p + 3j + c]
+__global__ void k_nodal_coef(int n_items, const int32_t* __restrict__ n2c_item, const int32_t* __restrict__ hexs,
+                             const double* __restrict__ xyz, int32_t* __restrict__ ids, double* __restrict__ coef) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_items) return;
+    const int hex = n2c_item[p] >> 3, node = n2c_item[p] & 7;
+    const int32_t* hx = hexs + 8 * (size_t)hex;
+    const double uvw[3] = {(double)c_uvw[node][0], (double)c_uvw[node][1], (double)c_uvw[node][2]};
+    const int nn[3] = {c_nnn[node][0], c_nnn[node][1], c_nnn[node][2]};
+    const double* v0 = xyz + 3 * (size_t)hx[node];
+    double J[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double* vi = xyz + 3 * (size_t)hx[nn[i]];
+        const double f = uvw[i] * 0.5;
+        J[i][0] = (v0[0] - vi[0]) * f;
+        J[i][1] = (v0[1] - vi[1]) * f;
+        J[i][2] = (v0[2] - vi[2]) * f;
+    }
+    double Jdet = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) - J[1][0] * (J[0][1] * J[2][2] - J[2][1] * J[0][2]) +
+                  J[2][0] * (J[0][1] * J[1][2] - J[1][1] * J[0][2]);
+    Jdet = 1.0 / Jdet;
+    double Ji[3][3] = {
+        {J[1][1] * J[2][2] - J[2][1] * J[1][2], J[2][1] * J[0][2] - J[0][1] * J[2][2], J[0][1] * J[1][2] - J[1][1] * J[0][2]},
+        {J[2][0] * J[1][2] - J[1][0] * J[2][2], J[0][0] * J[2][2] - J[2][0] * J[0][2], J[1][0] * J[0][2] - J[0][0] * J[1][2]},
+        {J[1][0] * J[2][1] - J[2][0] * J[1][1], J[2][0] * J[0][1] - J[0][0] * J[2][1], J[0][0] * J[1][1] - J[1][0] * J[0][1]}};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Ji[i][j] *= Jdet;
+    double gs[3], gn[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        gs[i] = 0.5 * (Ji[i][0] * uvw[0] + Ji[i][1] * uvw[1] + Ji[i][2] * uvw[2]);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) gn[j][i] = -0.5 * Ji[i][j] * uvw[j];
+    }
+    int j = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const double* g;
+        if (k == node) g = gs;
+        else if (k == nn[0]) g = gn[0];
+        else if (k == nn[1]) g = gn[1];
+        else if (k == nn[2]) g = gn[2];
+        else continue;
+        ids[4 * (size_t)p + j] = hx[k];
+        double* o = coef + 12 * (size_t)p + 3 * j;
+        o[0] = g[0];
+        o[1] = g[1];
+        o[2] = g[2];
+        ++j;
+    }
+}
+
+// k_nodal_field from the per-item gradients of k_nodal_coef
+__global__ void k_nodal_field_cached(int n_nodes, const int32_t* __restrict__ n2c_ptr, const int32_t* __restrict__ ids,
+                                     const double* __restrict__ coef, double* __restrict__ sol) {
+    const int node_id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node_id >= n_nodes) return;
+    const int b = n2c_ptr[node_id], e = n2c_ptr[node_id + 1];
+    if (b == e) return;
+    double mx = 0.0, my = 0.0, mz = 0.0;
+    for (int p = b; p < e; ++p) {
+        double ex = 0.0, ey = 0.0, ez = 0.0;
+        const double* c = coef + 12 * (size_t)p;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const double ph = sol[5 * (size_t)ids[4 * (size_t)p + j] + 4];
+            ex -= c[3 * j] * ph;
+            ey -= c[3 * j + 1] * ph;
+            ez -= c[3 * j + 2] * ph;
+        }
+        mx += ex;
+        my += ey;
+        mz += ez;
+    }
+    const double f = 1.0 / (e - b);
+    double* s = sol + 5 * (size_t)node_id;
+    s[0] = mx * f;
+    s[1] = my * f;
+    s[2] = mz * f;
+}
+
+// k_smooth's weights exp(decay |x_i - x_nb|) per neighbour item and 1 / (their sum) per tet
+// vertex (-1 where the reference skips the vertex: no neighbours or a sum that is not positive)
+__global__ void k_smooth_coef(int n_tn, const int32_t* __restrict__ vptr, const int32_t* __restrict__ vidx,
+                              const double* __restrict__ xyz, double decay, double* __restrict__ w_out,
+                              double* __restrict__ f_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_tn) return;
+    const int b = vptr[i], e = vptr[i + 1];
+    const double px = xyz[3 * (size_t)i], py = xyz[3 * (size_t)i + 1], pz = xyz[3 * (size_t)i + 2];
+    double ws = 0;
+    for (int k = b; k < e; ++k) {
+        const int nb = vidx[k];
+        const double dx = px - xyz[3 * (size_t)nb], dy = py - xyz[3 * (size_t)nb + 1], dz = pz - xyz[3 * (size_t)nb + 2];
+        const double w = exp(decay * sqrt(dx * dx + dy * dy + dz * dz));
+        w_out[k] = w;
+        ws += w;
+    }
+    f_out[i] = (b != e && ws > 0) ? 1.0 / ws : -1.0;
+}
+
+// k_smooth from the weights of k_smooth_coef
+__global__ void k_smooth_cached(int n_tn, const int32_t* __restrict__ vptr, const int32_t* __restrict__ vidx,
+                                const double* __restrict__ wk, const double* __restrict__ fi, double* __restrict__ sol) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_tn) return;
+    const double f = fi[i];
+    if (f < 0) return;
+    const int b = vptr[i], e = vptr[i + 1];
+    double vx = 0, vy = 0, vz = 0;
+    for (int k = b; k < e; ++k) {
+        const int nb = vidx[k];
+        const double w = wk[k];
+        vx += sol[5 * (size_t)nb] * w;
+        vy += sol[5 * (size_t)nb + 1] * w;
+        vz += sol[5 * (size_t)nb + 2] * w;
+    }
+    sol[5 * (size_t)i] = vx * f;
+    sol[5 * (size_t)i + 1] = vy * f;
+    sol[5 * (size_t)i + 2] = vz * f;
+}
+
 __global__ void k_max_norm2(int n, const double* __restrict__ sol, unsigned long long* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1064,11 +1213,36 @@ void DeviceMesh::extract_solution(const double* d_phi, const int32_t* d_dof2node
     const int B = 256;
     sol_.zero(stream_);
     FGB_LAUNCH(k_scatter_solution<<<grid_for(n_dofs, B), B, 0, stream_>>>(n_dofs, d_phi, d_charge, d_dof2node, sol_.get()));
-    FGB_LAUNCH(k_nodal_field<<<grid_for(n_nodes_, B), B, 0, stream_>>>(n_nodes_, n2c_ptr_.get(), n2c_item_.get(), hexs_.get(), xyz_.get(),
-                                                            sol_.get()));
-    if (smoothen)
-        FGB_LAUNCH(k_smooth<<<grid_for(n_tetnodes_, B), B, 0, stream_>>>(n_tetnodes_, voro_ptr_.get(), voro_idx_.get(), xyz_.get(),
-                                                               decay_, sol_.get()));
+    if (geo_cache_) {
+        // the geometry-only factors are built at the first extraction of this mesh
+        if (!nodal_ids_.size()) {
+            const int n_items = (int)n2c_item_.size();
+            nodal_ids_.resize(4 * (size_t)std::max(1, n_items));
+            nodal_coef_.resize(12 * (size_t)std::max(1, n_items));
+            if (n_items > 0)
+                FGB_LAUNCH(k_nodal_coef<<<grid_for(n_items, B), B, 0, stream_>>>(n_items, n2c_item_.get(), hexs_.get(),
+                                                                                 xyz_.get(), nodal_ids_.get(),
+                                                                                 nodal_coef_.get()));
+            const int n_vor = (int)voro_idx_.size();
+            smooth_w_.resize(std::max(1, n_vor));
+            smooth_f_.resize(std::max(1, n_tetnodes_));
+            if (n_tetnodes_ > 0)
+                FGB_LAUNCH(k_smooth_coef<<<grid_for(n_tetnodes_, B), B, 0, stream_>>>(n_tetnodes_, voro_ptr_.get(),
+                                                                                     voro_idx_.get(), xyz_.get(), decay_,
+                                                                                     smooth_w_.get(), smooth_f_.get()));
+        }
+        FGB_LAUNCH(k_nodal_field_cached<<<grid_for(n_nodes_, B), B, 0, stream_>>>(n_nodes_, n2c_ptr_.get(), nodal_ids_.get(),
+                                                                                 nodal_coef_.get(), sol_.get()));
+        if (smoothen && n_tetnodes_ > 0)
+            FGB_LAUNCH(k_smooth_cached<<<grid_for(n_tetnodes_, B), B, 0, stream_>>>(n_tetnodes_, voro_ptr_.get(), voro_idx_.get(),
+                                                                                   smooth_w_.get(), smooth_f_.get(), sol_.get()));
+    } else {
+        FGB_LAUNCH(k_nodal_field<<<grid_for(n_nodes_, B), B, 0, stream_>>>(n_nodes_, n2c_ptr_.get(), n2c_item_.get(), hexs_.get(),
+                                                                          xyz_.get(), sol_.get()));
+        if (smoothen)
+            FGB_LAUNCH(k_smooth<<<grid_for(n_tetnodes_, B), B, 0, stream_>>>(n_tetnodes_, voro_ptr_.get(), voro_idx_.get(),
+                                                                            xyz_.get(), decay_, sol_.get()));
+    }
     FGB_CUDA(cudaGetLastError());
 }
 
@@ -1111,7 +1285,7 @@ void DeviceMesh::locate_interpolate(int n, const double* d_pts, int rank, int32_
     FGB_LAUNCH(k_resolve<<<grid_for(n, B), B, 0, stream_>>>(n, v_.get(), nin_.get(), f_.get(), res_.get(), dep_.get(), counters_.get()));
     // first guess of a fresh reader: abs(-1) = 1 for tets, abs(-1)/4 = 0 for hexes
     const int g0 = rank == 3 ? 0 : std::min(1, n_tets_ - 1);
-    FGB_LAUNCH(k_chain_runs<<<grid_for(n, B), B, 0, stream_>>>(n, P, g0, det_.get(), nbr_ptr_.get(), nbr_idx_.get(), v_.get(), f_.get(),
+    FGB_LAUNCH(k_chain_runs<<<grid_for(32LL * n, B), B, 0, stream_>>>(n, P, g0, det_.get(), nbr_ptr_.get(), nbr_idx_.get(), v_.get(), f_.get(),
                                                     dep_.get(), res_.get(), counters_.get()));
     FGB_LAUNCH(k_interpolate<<<grid_for(n, 128), 128, 0, stream_>>>(n, P, rank, 1, res_.get(), det_.get(), tet_nodes_.get(), quad_.get(),
                                                          hexs_.get(), hexf_.get(), sol_.get(), d_cells, d_out));
@@ -1156,7 +1330,7 @@ void DeviceMesh::locate_interpolate_noalloc(int n, const double* d_pts, int rank
                                                                     counters));
     FGB_LAUNCH(k_resolve<<<grid_for(n, B), B, 0, stream_>>>(n, V, nin, F, res, dep, counters));
     const int g0 = rank == 3 ? 0 : std::min(1, n_tets_ - 1);
-    FGB_LAUNCH(k_chain_runs<<<grid_for(n, B), B, 0, stream_>>>(n, P, g0, det_.get(), nbr_ptr_.get(), nbr_idx_.get(), V, F, dep,
+    FGB_LAUNCH(k_chain_runs<<<grid_for(32LL * n, B), B, 0, stream_>>>(n, P, g0, det_.get(), nbr_ptr_.get(), nbr_idx_.get(), V, F, dep,
                                                               res, counters));
     FGB_LAUNCH(k_interpolate<<<grid_for(n, 128), 128, 0, stream_>>>(n, P, rank, 1, res, det_.get(), tet_nodes_.get(),
                                                                     quad_.get(), hexs_.get(), hexf_.get(), sol_.get(), d_cells,
