@@ -827,7 +827,7 @@ def run_batch(args, world, rank, quiet=False):
 
     n_mesh = args.meshes or 256
     specs, fields = fg.batch_specs(n_mesh, seed=2024)
-    b = fg.Batch()
+    b = fg.Batch(persistent=args.persistent)
     t0 = time.perf_counter()
     slots = [int(v) for v in b.add_synthetic(specs)]
     build_s = time.perf_counter() - t0
@@ -885,7 +885,9 @@ def run_batch(args, world, rank, quiet=False):
         "vs_baseline": None, "dtype": "f64 CG / f32 multigrid preconditioner",
         "data": "synthetic (seeded random nanotips)",
         "config": {"workload": f"batch: {n_mesh} nanotips, radius 1-6 nm, aspect 2-8, field 0.5-3 GV/m, "
-                               "Q1 2e4-8e5 vacuum hexes log-uniform, one graph-captured launch",
+                               "Q1 2e4-8e5 vacuum hexes log-uniform, "
+                               + ("one persistent cooperative kernel per step" if args.persistent
+                                  else "one graph-captured launch per step"),
                    "n_meshes": n_mesh, "total_dofs": total, "rel_tol": REL_TOL,
                    "l2": "inputs larger than L2 (level-0 matrices %.1f GB)" % (total * 25 * 12 / 1e9)},
         "batch": {"solves_per_s": world * n_mesh * args.steps / (dev_ms * 1e-3), "converged": int(conv),
@@ -972,7 +974,7 @@ def run_serve(args, world, rank, quiet=False):
     rspecs, rfields = fg.batch_specs(n_runs - half, seed=4242)
     specs = [spec0] * half + rspecs
     base = np.r_[np.full(half, 0.1), rfields]
-    b = fg.Batch()
+    b = fg.Batch(persistent=args.persistent)
     srv = fg.Server(b, rel_tol=REL_TOL, max_iter=1000, iters_per_launch=args.iters_per_launch, rank=RANK)
     srv.set_launch_policy(args.idle_iters, args.stop_at_first)
     t0 = time.perf_counter()
@@ -1027,6 +1029,7 @@ def run_serve(args, world, rank, quiet=False):
         "config": {"workload": f"serve: {n_runs} MD runs ({half} config-0 tips, {n_runs - half} random tips), "
                                f"{args.atoms} atoms each, sigma 0.02 A per step, Poisson arrivals",
                    "total_dofs": int(dofs.sum()), "rates": args.rates, "iters_per_launch": args.iters_per_launch,
+                   "solver_launch": "persistent cooperative kernel" if args.persistent else "graph (WHILE node)",
                    "idle_iters": args.idle_iters, "stop_at_first": bool(args.stop_at_first)},
         "sweep": sweep, "build_s": build_s, "max_requests_in_flight": info["max_in_flight"],
         "solver_launches": info["solver_launches"], "plain_fp64_cg_served_one_at_a_time": plain,
@@ -1054,6 +1057,8 @@ def main():
     ap.add_argument("--iters-per-launch", type=int, default=4)
     ap.add_argument("--idle-iters", type=int, default=0,
                     help="serve: solver iterations per launch while no request waits (0: --iters-per-launch)")
+    ap.add_argument("--persistent", action="store_true",
+                    help="batch/serve: one persistent cooperative kernel per solver step instead of the graph")
     ap.add_argument("--stop-at-first", action="store_true",
                     help="serve: end a launch after the iteration in which a solve finished")
     ap.add_argument("--points", type=int, default=0)

@@ -609,8 +609,9 @@ class Batch:
     one CUDA graph launch per step). Solves: admit(slot, E0, ...) then step()/collect(), or
     solve_all(). Each slot keeps its last solution as the warm start of its next solve."""
 
-    def __init__(self, use_graph=True, autotune=True, grid_ctas=0):
-        self.h = load().fgb_batch_create(int(use_graph), int(autotune), int(grid_ctas))
+    def __init__(self, use_graph=True, autotune=True, grid_ctas=0, persistent=False):
+        mode = 2 if persistent else int(bool(use_graph))
+        self.h = load().fgb_batch_create(mode, int(autotune), int(grid_ctas))
         if not self.h:
             raise RuntimeError("batch creation failed: " + last_error())
         self._meshes = {}

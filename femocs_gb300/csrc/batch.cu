@@ -17,6 +17,9 @@
 #include <sstream>
 
 #include "batch.h"
+
+#include <cooperative_groups.h>
+namespace cg = cooperative_groups;
 #include "fem_device.h"
 
 namespace fgb {
@@ -290,7 +293,7 @@ __device__ __forceinline__ bool mesh_reduce(double (&v)[NV], double* partial, in
 }
 
 // ---- outer FP64 CG over level-0 blocks
-__global__ void __launch_bounds__(kB) kb_spmv_pq(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_spmv_pq(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                  const int32_t* __restrict__ bm, BatchMeshState* st,
                                                  const int64_t* __restrict__ sb, const int32_t* __restrict__ sl,
                                                  const int32_t* __restrict__ col, const double* __restrict__ v64,
@@ -312,6 +315,14 @@ __global__ void __launch_bounds__(kB) kb_spmv_pq(const int32_t* __restrict__ lis
         }
     }
 }
+__global__ void __launch_bounds__(kB) kb_spmv_pq(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                                 const int32_t* __restrict__ bm, BatchMeshState* st,
+                                                 const int64_t* __restrict__ sb, const int32_t* __restrict__ sl,
+                                                 const int32_t* __restrict__ col, const double* __restrict__ v64,
+                                                 const double* __restrict__ x, const double* __restrict__ p,
+                                                 double* __restrict__ q, double* partial) {
+    kbd_spmv_pq(list, count, bm, st, sb, sl, col, v64, x, p, q, partial);
+}
 
 __device__ __forceinline__ void batch_check(BatchMeshState* s, double rr) {
     s->rr = rr;
@@ -320,7 +331,7 @@ __device__ __forceinline__ void batch_check(BatchMeshState* s, double rr) {
     if (s->iter >= s->max_iter) { s->done = 1; s->status = -1; }
 }
 
-__global__ void __launch_bounds__(kB) kb_update(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_update(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                 const int32_t* __restrict__ bm, BatchMeshState* st,
                                                 double* __restrict__ x, const double* __restrict__ b,
                                                 double* __restrict__ r, const double* __restrict__ p,
@@ -349,8 +360,15 @@ __global__ void __launch_bounds__(kB) kb_update(const int32_t* __restrict__ list
         }
     }
 }
+__global__ void __launch_bounds__(kB) kb_update(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                                const int32_t* __restrict__ bm, BatchMeshState* st,
+                                                double* __restrict__ x, const double* __restrict__ b,
+                                                double* __restrict__ r, const double* __restrict__ p,
+                                                const double* __restrict__ q, float* __restrict__ r32, double* partial) {
+    kbd_update(list, count, bm, st, x, b, r, p, q, r32, partial);
+}
 
-__global__ void __launch_bounds__(kB) kb_rz(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_rz(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                             const int32_t* __restrict__ bm, BatchMeshState* st,
                                             const double* __restrict__ r, const float* __restrict__ z, double* partial) {
     const int cnt = *count;
@@ -371,8 +389,13 @@ __global__ void __launch_bounds__(kB) kb_rz(const int32_t* __restrict__ list, co
         }
     }
 }
+__global__ void __launch_bounds__(kB) kb_rz(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                            const int32_t* __restrict__ bm, BatchMeshState* st,
+                                            const double* __restrict__ r, const float* __restrict__ z, double* partial) {
+    kbd_rz(list, count, bm, st, r, z, partial);
+}
 
-__global__ void __launch_bounds__(kB) kb_direction(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_direction(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                    const int32_t* __restrict__ bm, BatchMeshState* st,
                                                    const float* __restrict__ z, double* __restrict__ p) {
     const int cnt = *count;
@@ -384,9 +407,14 @@ __global__ void __launch_bounds__(kB) kb_direction(const int32_t* __restrict__ l
         p[row] = beta == 0.0 ? (double)z[row] : (double)z[row] + beta * p[row];
     }
 }
+__global__ void __launch_bounds__(kB) kb_direction(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                                   const int32_t* __restrict__ bm, BatchMeshState* st,
+                                                   const float* __restrict__ z, double* __restrict__ p) {
+    kbd_direction(list, count, bm, st, z, p);
+}
 
 // ---- V-cycle kernels (any level)
-__global__ void __launch_bounds__(kB) kb_cheb_zero(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_cheb_zero(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                    const int32_t* __restrict__ bm, BatchMeshState* st,
                                                    const float* __restrict__ dinv, const float* __restrict__ b,
                                                    float* __restrict__ x, float* __restrict__ d, float inv_theta) {
@@ -400,10 +428,16 @@ __global__ void __launch_bounds__(kB) kb_cheb_zero(const int32_t* __restrict__ l
         x[row] = di;
     }
 }
+__global__ void __launch_bounds__(kB) kb_cheb_zero(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                                   const int32_t* __restrict__ bm, BatchMeshState* st,
+                                                   const float* __restrict__ dinv, const float* __restrict__ b,
+                                                   float* __restrict__ x, float* __restrict__ d, float inv_theta) {
+    kbd_cheb_zero(list, count, bm, st, dinv, b, x, d, inv_theta);
+}
 
 // c1 < 0: first step from a nonzero guess (d = c2 D^-1 r)
 template <int TPR>
-__global__ void __launch_bounds__(kB) kb_cheb_step(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_cheb_step(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                    const int32_t* __restrict__ bm, BatchMeshState* st, OpB A,
                                                    const float* __restrict__ dinv, const float* __restrict__ b,
                                                    const float* __restrict__ xin, float* __restrict__ xout,
@@ -424,9 +458,17 @@ __global__ void __launch_bounds__(kB) kb_cheb_step(const int32_t* __restrict__ l
         }
     }
 }
+template <int TPR>
+__global__ void __launch_bounds__(kB) kb_cheb_step(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                                   const int32_t* __restrict__ bm, BatchMeshState* st, OpB A,
+                                                   const float* __restrict__ dinv, const float* __restrict__ b,
+                                                   const float* __restrict__ xin, float* __restrict__ xout,
+                                                   float* __restrict__ d, float c1, float c2) {
+    kbd_cheb_step<TPR>(list, count, bm, st, A, dinv, b, xin, xout, d, c1, c2);
+}
 
 template <int TPR>
-__global__ void __launch_bounds__(kB) kb_residual(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_residual(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                   const int32_t* __restrict__ bm, BatchMeshState* st, OpB A,
                                                   const float* __restrict__ b, const float* __restrict__ x,
                                                   float* __restrict__ r) {
@@ -442,10 +484,17 @@ __global__ void __launch_bounds__(kB) kb_residual(const int32_t* __restrict__ li
         }
     }
 }
+template <int TPR>
+__global__ void __launch_bounds__(kB) kb_residual(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                                  const int32_t* __restrict__ bm, BatchMeshState* st, OpB A,
+                                                  const float* __restrict__ b, const float* __restrict__ x,
+                                                  float* __restrict__ r) {
+    kbd_residual<TPR>(list, count, bm, st, A, b, x, r);
+}
 
 // y = M x (accumulate: y += M x) over the rows of the listed blocks
 template <int TPR>
-__global__ void __launch_bounds__(kB) kb_csr_apply(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_csr_apply(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                    const int32_t* __restrict__ bm, BatchMeshState* st, OpB M,
                                                    const float* __restrict__ x, float* __restrict__ y, int accumulate) {
     constexpr int T = TPR == 0 ? 1 : TPR, RPP = kB / T;
@@ -460,9 +509,15 @@ __global__ void __launch_bounds__(kB) kb_csr_apply(const int32_t* __restrict__ l
         }
     }
 }
+template <int TPR>
+__global__ void __launch_bounds__(kB) kb_csr_apply(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                                   const int32_t* __restrict__ bm, BatchMeshState* st, OpB M,
+                                                   const float* __restrict__ x, float* __restrict__ y, int accumulate) {
+    kbd_csr_apply<TPR>(list, count, bm, st, M, x, y, accumulate);
+}
 
 // coarsest level: x = A_c^-1 b per mesh, one warp per row
-__global__ void __launch_bounds__(kB) kb_dense(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__device__ __forceinline__ void kbd_dense(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                const int32_t* __restrict__ bm, BatchMeshState* st,
                                                const float* __restrict__ dense, const float* __restrict__ b,
                                                float* __restrict__ x) {
@@ -483,6 +538,12 @@ __global__ void __launch_bounds__(kB) kb_dense(const int32_t* __restrict__ list,
             if (lane == 0) x[row] = acc;
         }
     }
+}
+__global__ void __launch_bounds__(kB) kb_dense(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+                                               const int32_t* __restrict__ bm, BatchMeshState* st,
+                                               const float* __restrict__ dense, const float* __restrict__ b,
+                                               float* __restrict__ x) {
+    kbd_dense(list, count, bm, st, dense, b, x);
 }
 
 // WHILE condition: continue while an admitted mesh is unfinished and the cap |loop[1]| is not
@@ -506,6 +567,125 @@ __global__ void kb_continue(const int32_t* __restrict__ run, const int32_t* __re
         const int go = (any && it < cap && !(loop[1] < 0 && fin)) ? 1 : 0;
         loop[2] = go;
         if (use_handle) cudaGraphSetConditional(handle, go);
+    }
+}
+
+// ---- the whole batched PCG as one persistent cooperative kernel: the iteration body of
+// launch_iteration / vcycle (the same phase bodies in the same order) with a grid-wide
+// barrier between phases, iterating until every admitted mesh has finished, the cap is
+// reached, or (negative cap) an admitted mesh finished in the last iteration. The phase
+// bodies reduce per 256-row block and per mesh in block order, so results are those of the
+// graph-captured launches bit for bit.
+constexpr int kMaxBatchLevels = 12;
+struct KbLevel {
+    const int32_t* S;      // smoothed-row blocks
+    const int32_t* D;      // dense-level blocks
+    const int32_t* T;      // restriction targets
+    const int32_t* bm;     // block -> mesh
+    const int32_t* cnt;    // counts of S, D, T
+    OpB A, R, P;           // level operator, restriction into this level, prolongation into it
+    const float* dinv;
+    float *b, *xa, *xb, *d, *rl;
+    int tpr, r_tpr, p_tpr;
+};
+struct KbParams {
+    int n_levels;
+    KbLevel lv[kMaxBatchLevels];
+    const int64_t* sb;
+    const int32_t* sl;
+    const int32_t* col;
+    const double* v64;
+    double *x, *bb, *r, *p, *q, *partial;
+    BatchMeshState* st;
+    const float* dense;
+    const int32_t* run;
+    int32_t* loop;  // [0] iterations, [1] cap (negative: stop after a mesh finished), [2] go, [3] running meshes
+    Cheb c;
+};
+
+#define FGB_KBD_TPR(FN, tpr, ...)                      \
+    do {                                               \
+        switch (tpr) {                                 \
+            case 0: FN<0>(__VA_ARGS__); break;         \
+            case 1: FN<1>(__VA_ARGS__); break;         \
+            case 4: FN<4>(__VA_ARGS__); break;         \
+            case 8: FN<8>(__VA_ARGS__); break;         \
+            case 16: FN<16>(__VA_ARGS__); break;       \
+            default: FN<32>(__VA_ARGS__); break;       \
+        }                                              \
+    } while (0)
+
+__device__ __forceinline__ float* kb_result(const KbLevel& L) { return (kDeg % 2 == 1) ? L.xa : L.xb; }
+
+__global__ void __launch_bounds__(kB) kb_persistent(const __grid_constant__ KbParams P) {
+    cg::grid_group grid = cg::this_grid();
+    BatchMeshState* st = P.st;
+    const int cap_raw = P.loop[1];
+    const int cap = cap_raw < 0 ? -cap_raw : cap_raw;
+    int it = 0;
+    while (true) {
+        const KbLevel& L0 = P.lv[0];
+        kbd_spmv_pq(L0.S, L0.cnt, L0.bm, st, P.sb, P.sl, P.col, P.v64, P.x, P.p, P.q, P.partial);
+        grid.sync();
+        kbd_update(L0.S, L0.cnt, L0.bm, st, P.x, P.bb, P.r, P.p, P.q, L0.b, P.partial);
+        grid.sync();
+        // V-cycle, down: pre-smoothing from zero (step k writes pre_buf(k), the last one xb),
+        // residual, restriction, the coarsest solve of the meshes whose dense level is next
+        for (int l = 0; l + 1 < P.n_levels; ++l) {
+            const KbLevel& L = P.lv[l];
+            const KbLevel& C = P.lv[l + 1];
+            auto pre_buf = [&](int k) { return ((kDeg - 1 - k) % 2 == 0) ? L.xb : L.xa; };
+            kbd_cheb_zero(L.S, L.cnt, L.bm, st, L.dinv, L.b, pre_buf(0), L.d, P.c.inv_theta);
+            grid.sync();
+            for (int k = 1; k < kDeg; ++k) {
+                FGB_KBD_TPR(kbd_cheb_step, L.tpr, L.S, L.cnt, L.bm, st, L.A, L.dinv, L.b, pre_buf(k - 1), pre_buf(k),
+                            L.d, P.c.c1[k], P.c.c2[k]);
+                grid.sync();
+            }
+            FGB_KBD_TPR(kbd_residual, L.tpr, L.S, L.cnt, L.bm, st, L.A, L.b, L.xb, L.rl);
+            grid.sync();
+            FGB_KBD_TPR(kbd_csr_apply, C.r_tpr, C.T, C.cnt + 2, C.bm, st, C.R, L.rl, C.b, 0);
+            grid.sync();
+            kbd_dense(C.D, C.cnt + 1, C.bm, st, P.dense, C.b, kb_result(C));
+            grid.sync();
+        }
+        // up: prolongation of the coarser result, post-smoothing (even steps write xa, odd xb)
+        for (int l = P.n_levels - 2; l >= 0; --l) {
+            const KbLevel& L = P.lv[l];
+            const KbLevel& C = P.lv[l + 1];
+            FGB_KBD_TPR(kbd_csr_apply, L.p_tpr, L.S, L.cnt, L.bm, st, L.P, kb_result(C), L.xb, 1);
+            grid.sync();
+            float* xin = L.xb;
+            for (int k = 0; k < kDeg; ++k) {
+                float* xout = (k % 2 == 0) ? L.xa : L.xb;
+                FGB_KBD_TPR(kbd_cheb_step, L.tpr, L.S, L.cnt, L.bm, st, L.A, L.dinv, L.b, xin, xout, L.d,
+                            k == 0 ? -1.f : P.c.c1[k], k == 0 ? P.c.inv_theta : P.c.c2[k]);
+                grid.sync();
+                xin = xout;
+            }
+        }
+        kbd_rz(L0.S, L0.cnt, L0.bm, st, P.r, kb_result(L0), P.partial);
+        grid.sync();
+        kbd_direction(L0.S, L0.cnt, L0.bm, st, kb_result(L0), P.p);
+        // every block takes the same decision from the states, which no phase before the next
+        // grid barrier changes
+        ++it;
+        __shared__ int any, fin;
+        if (threadIdx.x == 0) any = fin = 0;
+        __syncthreads();
+        const int n = P.loop[3];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            if (!((volatile BatchMeshState*)st)[P.run[i]].done) any = 1;
+            else fin = 1;
+        }
+        __syncthreads();
+        const bool go = any && it < cap && !(cap_raw < 0 && fin);
+        grid.sync();
+        if (!go) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.loop[0] = it;
+        P.loop[2] = 0;
     }
 }
 
@@ -1052,6 +1232,64 @@ void BatchSolver::launch_iteration() {
     FGB_LAUNCH(kb_direction<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, level_result(L), L.p.get()));
 }
 
+void BatchSolver::launch_persistent() {
+    FGB_REQUIRE(max_levels_ >= 2 && max_levels_ <= kMaxBatchLevels, "batch hierarchy depth out of range");
+    KbParams prm{};
+    prm.n_levels = max_levels_;
+    auto tp = [](const std::vector<int>& v, int l) { return l < (int)v.size() ? v[l] : 1; };
+    for (int l = 0; l < max_levels_; ++l) {
+        BatchLevelDev& L = *lv_[l];
+        KbLevel& k = prm.lv[l];
+        k.S = L.S.get();
+        k.D = L.D.get();
+        k.T = L.T.get();
+        k.bm = L.block_mesh.get();
+        k.cnt = d_->counts.get() + 3 * l;
+        k.A = l == 0 ? OpB{L.s_begin.get(), L.s_len.get(), L.a_col.get(), L.a_val.get()}
+                     : OpB{L.a_begin.get(), L.a_len.get(), L.a_col.get(), L.a_val.get()};
+        k.R = OpB{L.r_begin.get(), L.r_len.get(), L.r_col.get(), L.r_val.get()};
+        k.P = OpB{L.p_begin.get(), L.p_len.get(), L.p_col.get(), L.p_val.get()};
+        k.dinv = L.dinv.get();
+        k.b = L.b.get();
+        k.xa = L.xa.get();
+        k.xb = L.xb.get();
+        k.d = L.d.get();
+        k.rl = L.rl.get();
+        k.tpr = l == 0 ? 0 : tp(tpr_, l);
+        k.r_tpr = tp(r_tpr_, l);
+        k.p_tpr = tp(p_tpr_, l);
+    }
+    BatchLevelDev& L0 = *lv_[0];
+    prm.sb = L0.s_begin.get();
+    prm.sl = L0.s_len.get();
+    prm.col = L0.a_col.get();
+    prm.v64 = L0.v64.get();
+    prm.x = L0.x.get();
+    prm.bb = L0.bb.get();
+    prm.r = L0.r.get();
+    prm.p = L0.p.get();
+    prm.q = L0.q.get();
+    prm.partial = L0.partial.get();
+    prm.st = d_->st.get();
+    prm.dense = d_->dense.get();
+    prm.run = d_->run.get();
+    prm.loop = d_->loop.get();
+    prm.c = cheb_coefficients();
+    if (persistent_grid_ == 0) {
+        int dev = 0, sms = 0, per_sm = 0, coop = 0;
+        FGB_CUDA(cudaGetDevice(&dev));
+        FGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FGB_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        FGB_REQUIRE(coop, "device does not support cooperative launches");
+        FGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_persistent, kB, 0));
+        FGB_REQUIRE(per_sm > 0, "the persistent batch kernel does not fit on an SM");
+        persistent_grid_ = std::min(per_sm, 8) * sms;
+    }
+    void* args[] = {&prm};
+    FGB_CUDA(cudaLaunchCooperativeKernel((void*)kb_persistent, dim3(persistent_grid_), dim3(kB), args, 0, stream_));
+    g_kernel_launches.fetch_add(1);
+}
+
 void BatchSolver::capture() {
     if (exec_) { cudaGraphExecDestroy(exec_); exec_ = nullptr; }
     if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
@@ -1204,7 +1442,15 @@ int BatchSolver::step(int max_iters, bool stop_at_first) {
     }
     if (lists_dirty_) rebuild_lists();
     int iters = 0;
-    if (opt_.use_graph) {
+    if (opt_.persistent) {
+        dirty_ = false;
+        int loop[3] = {0, std::max(1, max_iters) * (stop_at_first ? -1 : 1), 1};
+        FGB_CUDA(cudaMemcpyAsync(d_->loop.get(), loop, 3 * sizeof(int), cudaMemcpyHostToDevice, stream_));
+        launch_persistent();
+        FGB_CUDA(cudaMemcpyAsync(d_->h_loop, d_->loop.get(), 4 * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        iters = d_->h_loop[0];
+    } else if (opt_.use_graph) {
         if (dirty_ || !exec_) {
             capture();
             dirty_ = false;

@@ -70,6 +70,7 @@ struct BatchSolveResult {
 struct BatchOptions {
     int grid_ctas = 0;          // CTAs of the work-list kernels (0: 8 per SM)
     bool use_graph = true;      // capture the iteration as a CUDA graph with a WHILE node
+    bool persistent = false;    // one persistent cooperative kernel per step instead (grid barriers between phases)
     bool autotune = true;       // pick threads-per-row of each coarse level by timing
 };
 
@@ -134,6 +135,8 @@ private:
     void rebuild_lists();
     void capture();
     void launch_iteration();      // one iteration body on stream_ (capture or fallback)
+    void launch_persistent();     // the whole step as one cooperative kernel (kb_persistent)
+    int persistent_grid_ = 0;
     void vcycle(int l);
     void tune();
 

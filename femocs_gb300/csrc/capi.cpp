@@ -851,6 +851,7 @@ FGB_BATCH* fgb_batch_create(int use_graph, int autotune, int grid_ctas) {
     const int rc = guarded([&] {
         BatchOptions o;
         o.use_graph = use_graph != 0;
+        o.persistent = use_graph == 2;
         o.autotune = autotune != 0;
         o.grid_ctas = grid_ctas;
         b->b.reset(new BatchSolver(o));

@@ -314,8 +314,10 @@ double fgb_nanotip_fit_spacing(const FgbNanotip* spec, double target_hexes);
  * admitted with an applied field (Neumann value -E0 on the top, phi = 0 on the metal, warm
  * start from the mesh's previous solution), stepped and collected. */
 typedef struct FGB_BATCH FGB_BATCH;
-/* use_graph: capture the iteration in a CUDA graph with a WHILE node (0: host loop);
- * autotune: time threads-per-row variants per level; grid_ctas: 0 = 8 per SM */
+/* use_graph: 1 = capture the iteration in a CUDA graph with a WHILE node, 2 = run each step as
+ * one persistent cooperative kernel (grid-wide barriers between the phases, same results bit
+ * for bit), 0 = host loop; autotune: time threads-per-row variants per level; grid_ctas:
+ * 0 = 8 per SM (the work-list kernels of modes 0 and 1) */
 FGB_BATCH* fgb_batch_create(int use_graph, int autotune, int grid_ctas);
 void fgb_batch_free(FGB_BATCH* b);
 /* slot >= 0; -1 when the free device memory minus hbm_reserve bytes does not admit the

@@ -118,6 +118,38 @@ def test_graph_and_host_loop_agree(meshes):
     assert st["kernels_per_iteration"] > 10
 
 
+def test_persistent_kernel_and_graph_bit_identical(meshes):
+    """One persistent cooperative kernel per step (grid-wide barriers between the phases of
+    the iteration) runs the same phase bodies in the same order as the graph-captured
+    launches, and every reduction is per 256-row block and per mesh in block order: the same
+    iterations and solutions bit for bit, cold and warm-started, with the autotuner on. A step
+    capped at 3 iterations stops there and the solve then continues to the same result."""
+    ref = None
+    for persistent in (False, True):
+        b, slots = batch_of(meshes, persistent=persistent)
+        res = b.solve_all(dict(zip(slots, FIELDS)), rel_tol=1e-10)
+        res2 = b.solve_all({s: 1.1 * f for s, f in zip(slots, FIELDS)}, rel_tol=1e-10)
+        out = ([res[s]["iterations"] for s in slots], [res2[s]["iterations"] for s in slots],
+               [b.phi_nodes(s) for s in slots])
+        for s in slots:
+            assert res[s]["status"] == 1 and res2[s]["status"] == 1
+        if ref is None:
+            ref = out
+        else:
+            assert out[0] == ref[0] and out[1] == ref[1]
+            for x, y in zip(out[2], ref[2]):
+                np.testing.assert_array_equal(x, y)
+    b1, slots = batch_of(meshes, persistent=True, autotune=False)
+    it_full = b1.solve_all({slots[0]: FIELDS[0]}, rel_tol=1e-10)[slots[0]]["iterations"]
+    b2, slots = batch_of(meshes, persistent=True, autotune=False)
+    b2.admit(slots[0], FIELDS[0], rel_tol=1e-10)
+    assert b2.step(3) == 1 and b2.stats()["last_iterations"] == 3
+    while b2.step(8):
+        pass
+    fin = b2.collect()
+    assert fin[slots[0]]["status"] == 1 and fin[slots[0]]["iterations"] == it_full
+
+
 def test_warm_start_iteration_cap_and_slot_reuse(meshes, oracle_phi):
     b, slots = batch_of(meshes)
     b.solve_all({0: FIELDS[0]}, rel_tol=1e-11)

@@ -228,3 +228,24 @@ def test_q2_matrix_free_level0_matches_element_matrices(cells, max_dofs):
     for key, (it, x) in res.items():
         assert abs(it - it0) <= 1, (key, it, it0)
         assert np.abs(x - x0).max() <= 2e3 * 1e-10 * np.abs(x0).max(), key
+
+
+@pytest.mark.gpu
+def test_q2_fp16_factors_fall_back_to_fp32_beyond_range():
+    """Geometric factors scale with the element size (w |det J| |J^-1|^2 ~ h / 3): on the small
+    tip scaled by 1e5 they exceed the FP16 range, so asking for FP16 factors gives the FP32
+    ones (the kind returned), and the solve matches the element-matrix smoother's."""
+    big = {k: (v if k == "growth" else v * 1e5) for k, v in SMALL.items()}
+    m = fg.Mesh.synthetic(**big)
+    f = fg.Field(m, order=2)
+    assert f.set_level0_operator(2) == 1
+    res = {}
+    for kind in (2, 0):
+        f.set_level0_operator(kind)
+        f.setup(-E0 * 1e-5)
+        f.assemble(True, False)
+        rc, st = f.solve(precision=2, rel_tol=1e-10)
+        assert rc > 0 and st["status"] == 1, (kind, st)
+        res[kind] = (st["iterations"], f.solution())
+    assert abs(res[2][0] - res[0][0]) <= 1, res
+    assert np.abs(res[2][1] - res[0][1]).max() <= 2e3 * 1e-10 * np.abs(res[0][1]).max()
