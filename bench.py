@@ -47,7 +47,7 @@ N_POINTS = {"config2": 1_000_000, "config1": 100_000, "probe": 200_000}
 # as config 2's Q2 rows; the cell-block step, k_cb_apply + k_cb_finish, from the element
 # matrices and matrix-free from the FP16 geometric factors); a launch's traffic scales with
 # its rows
-KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6, ("smoother_ebe", 2): 261.8, ("smoother_mf16", 2): 113.0}
+KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6, ("smoother_ebe", 2): 261.8, ("smoother_mf16", 2): 114.3}
 FALLBACK_HBM_GBS = 6800.0
 
 

@@ -316,7 +316,7 @@ __host__ __device__ inline size_t cb_stream_smem_bytes(int max_cells, int max_do
 //            cells' 1-D pencils (three cells per warp, see sfS / sfD).
 constexpr int kSrcKe = 0, kSrcRing = 1, kSrcGeo = 2, kSrcGeo16 = 3;
 template <int KIND, int SRC>
-__global__ void __launch_bounds__(SRC == kSrcRing ? kCb + 32 : kCb, SRC == kSrcRing ? 2 : 3)
+__global__ void __launch_bounds__(SRC == kSrcRing ? kCb + 32 : kCb, SRC == kSrcRing ? 2 : (SRC >= kSrcGeo ? 4 : 3))
     k_cb_apply(EbeOperator op, const float* __restrict__ dinv, const float* __restrict__ b,
                const float* __restrict__ xin, float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
     constexpr bool STREAM = SRC == kSrcRing;
@@ -655,12 +655,15 @@ __global__ void __launch_bounds__(SRC == kSrcRing ? kCb + 32 : kCb, SRC == kSrcR
         }
         __syncthreads();
     }
+    // phase C takes kCw entries per round: 4 in the geometric-factor variants, whose 64-register
+    // budget (4 CTAs per SM) the 8-entry rounds would spill
+    constexpr int kCw = GEO ? 4 : 8;
 #pragma unroll 1
-    for (int r0 = 0; r0 < kCbPer; r0 += 8) {
+    for (int r0 = 0; r0 < kCbPer; r0 += kCw) {
         if (tid + r0 * kCb >= nq) break;
-        int e0[8], e1[8], sl[8], g[8];
+        int e0[kCw], e1[kCw], sl[kCw], g[kCw];
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
+        for (int r = 0; r < kCw; ++r) {
             const int k = tid + (r0 + r) * kCb;
             const bool v = k < nq;
             e1[r] = v ? __ldg(op.item_end + q0 + k) : 0;
@@ -668,10 +671,10 @@ __global__ void __launch_bounds__(SRC == kSrcRing ? kCb + 32 : kCb, SRC == kSrcR
             sl[r] = v ? __ldg(op.slot + q0 + k) : -2;
             g[r] = v ? __ldg(op.dof_list + q0 + k) : 0;
         }
-        float ax[8], bv[8], dv[8], dd[8];
-        int fx[8];
+        float ax[kCw], bv[kCw], dv[kCw], dd[kCw];
+        int fx[kCw];
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
+        for (int r = 0; r < kCw; ++r) {
             const bool own = sl[r] == -1;
             bv[r] = own ? b[g[r]] : 0.f;
             dv[r] = own ? dinv[g[r]] : 1.f;
@@ -679,13 +682,13 @@ __global__ void __launch_bounds__(SRC == kSrcRing ? kCb + 32 : kCb, SRC == kSrcR
             fx[r] = own ? op.fixed[g[r]] : 0;
         }
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
+        for (int r = 0; r < kCw; ++r) {
             float a = 0.f;
             for (int e = e0[r]; e < e1[r]; ++e) a += sy[sit[e]];
             ax[r] = a;
         }
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
+        for (int r = 0; r < kCw; ++r) {
             if (sl[r] >= 0) {
                 op.partial[sl[r]] = ax[r];
             } else if (sl[r] == -1) {

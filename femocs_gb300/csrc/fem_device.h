@@ -235,7 +235,10 @@ private:
     DBuf<float2> cb_pair_;  // outer mode 2: partial (hi, lo) sums of the split DoFs
     DBuf<double> cb_dot_;   // outer mode 2: p.q partials
     bool cb_spmv_attr_ = false;
-    int cb_cells_ = 256, cb_max_dofs_ = 4096;
+    // cell blocks of at most 176 hexes / 2816 DoFs: the largest whose matrix-free smoother
+    // shared memory (56.4 KB) lets 4 CTAs of 64 registers share an SM (config 2: smoothing step
+    // 0.648 ms against 0.685 ms for 256 / 4096, outer product 1.70 against 1.77 ms)
+    int cb_cells_ = 176, cb_max_dofs_ = 2816;
     DBuf<int8_t> fixed_;    // 1 on Dirichlet rows of the current anode mode
     LaunchTimer spmv_timer_;
     int n_, nc_;
