@@ -726,15 +726,38 @@ __global__ void __launch_bounds__(kB) kb_true_residual(int row0, int n, const in
     }
 }
 
+// Work-list kernels walk their list with a fixed grid, every CTA taking an equal share, so
+// the grid must be resident in one wave: at most the CTAs of 256 threads that the kernel's
+// registers let an SM hold (8 at 32 registers, 5 at 40-48), times the SMs, capped by `cap`.
+int resident_grid(const void* fn, int cap) {
+    static std::mutex mu;
+    static std::map<const void*, int> per_sm;
+    static int sms = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!sms) {
+        int dev = 0;
+        FGB_CUDA(cudaGetDevice(&dev));
+        FGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    auto it = per_sm.find(fn);
+    if (it == per_sm.end()) {
+        int n = 0;
+        FGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kB, 0));
+        it = per_sm.emplace(fn, std::max(1, n)).first;
+    }
+    return std::max(1, std::min(cap, it->second * sms));
+}
+#define FGB_RG(KERNEL, cap) resident_grid((const void*)(KERNEL), (cap))
+
 #define FGB_BATCH_TPR(KERNEL, tpr, grid, stream, ...)                                                 \
     do {                                                                                              \
         switch (tpr) {                                                                                \
-            case 0: FGB_LAUNCH(KERNEL<0><<<grid, kB, 0, stream>>>(__VA_ARGS__)); break;               \
-            case 1: FGB_LAUNCH(KERNEL<1><<<grid, kB, 0, stream>>>(__VA_ARGS__)); break;               \
-            case 4: FGB_LAUNCH(KERNEL<4><<<grid, kB, 0, stream>>>(__VA_ARGS__)); break;               \
-            case 8: FGB_LAUNCH(KERNEL<8><<<grid, kB, 0, stream>>>(__VA_ARGS__)); break;               \
-            case 16: FGB_LAUNCH(KERNEL<16><<<grid, kB, 0, stream>>>(__VA_ARGS__)); break;             \
-            default: FGB_LAUNCH(KERNEL<32><<<grid, kB, 0, stream>>>(__VA_ARGS__)); break;             \
+            case 0: FGB_LAUNCH(KERNEL<0><<<FGB_RG(KERNEL<0>, grid), kB, 0, stream>>>(__VA_ARGS__)); break;               \
+            case 1: FGB_LAUNCH(KERNEL<1><<<FGB_RG(KERNEL<1>, grid), kB, 0, stream>>>(__VA_ARGS__)); break;               \
+            case 4: FGB_LAUNCH(KERNEL<4><<<FGB_RG(KERNEL<4>, grid), kB, 0, stream>>>(__VA_ARGS__)); break;               \
+            case 8: FGB_LAUNCH(KERNEL<8><<<FGB_RG(KERNEL<8>, grid), kB, 0, stream>>>(__VA_ARGS__)); break;               \
+            case 16: FGB_LAUNCH(KERNEL<16><<<FGB_RG(KERNEL<16>, grid), kB, 0, stream>>>(__VA_ARGS__)); break;             \
+            default: FGB_LAUNCH(KERNEL<32><<<FGB_RG(KERNEL<32>, grid), kB, 0, stream>>>(__VA_ARGS__)); break;             \
         }                                                                                             \
     } while (0)
 
@@ -1189,7 +1212,7 @@ void BatchSolver::vcycle(int l) {
                          : OpB{L.a_begin.get(), L.a_len.get(), L.a_col.get(), L.a_val.get()};
     // pre-smoothing from zero; step k writes pre_buf(k), the last one xb
     auto pre_buf = [&](int k) { return ((kDeg - 1 - k) % 2 == 0) ? L.xb.get() : L.xa.get(); };
-    FGB_LAUNCH(kb_cheb_zero<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.dinv.get(), L.b.get(),
+    FGB_LAUNCH(kb_cheb_zero<<<FGB_RG(kb_cheb_zero, grid_), kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.dinv.get(), L.b.get(),
                                                        pre_buf(0), L.d.get(), c.inv_theta));
     for (int k = 1; k < kDeg; ++k)
         FGB_BATCH_TPR(kb_cheb_step, tpr, grid_, stream_, L.S.get(), cS, L.block_mesh.get(), st, A, L.dinv.get(),
@@ -1201,7 +1224,7 @@ void BatchSolver::vcycle(int l) {
     const OpB R{C.r_begin.get(), C.r_len.get(), C.r_col.get(), C.r_val.get()};
     FGB_BATCH_TPR(kb_csr_apply, r_tpr_[l + 1], grid_, stream_, C.T.get(), cC + 2, C.block_mesh.get(), st, R, L.rl.get(),
                   C.b.get(), 0);
-    FGB_LAUNCH(kb_dense<<<grid_, kB, 0, stream_>>>(C.D.get(), cC + 1, C.block_mesh.get(), st, d_->dense.get(), C.b.get(),
+    FGB_LAUNCH(kb_dense<<<FGB_RG(kb_dense, grid_), kB, 0, stream_>>>(C.D.get(), cC + 1, C.block_mesh.get(), st, d_->dense.get(), C.b.get(),
                                                    level_result(C)));
     if (l + 2 < max_levels_) vcycle(l + 1);
     const OpB P{L.p_begin.get(), L.p_len.get(), L.p_col.get(), L.p_val.get()};
@@ -1221,15 +1244,15 @@ void BatchSolver::launch_iteration() {
     BatchLevelDev& L = *lv_[0];
     BatchMeshState* st = d_->st.get();
     const int32_t* cS = d_->counts.get();
-    FGB_LAUNCH(kb_spmv_pq<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.s_begin.get(), L.s_len.get(),
+    FGB_LAUNCH(kb_spmv_pq<<<FGB_RG(kb_spmv_pq, grid_), kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.s_begin.get(), L.s_len.get(),
                                                      L.a_col.get(), L.v64.get(), L.x.get(), L.p.get(), L.q.get(),
                                                      L.partial.get()));
-    FGB_LAUNCH(kb_update<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.x.get(), L.bb.get(), L.r.get(),
+    FGB_LAUNCH(kb_update<<<FGB_RG(kb_update, grid_), kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.x.get(), L.bb.get(), L.r.get(),
                                                     L.p.get(), L.q.get(), L.b.get(), L.partial.get()));
     vcycle(0);
-    FGB_LAUNCH(kb_rz<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.r.get(), level_result(L),
+    FGB_LAUNCH(kb_rz<<<FGB_RG(kb_rz, grid_), kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, L.r.get(), level_result(L),
                                                 L.partial.get()));
-    FGB_LAUNCH(kb_direction<<<grid_, kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, level_result(L), L.p.get()));
+    FGB_LAUNCH(kb_direction<<<FGB_RG(kb_direction, grid_), kB, 0, stream_>>>(L.S.get(), cS, L.block_mesh.get(), st, level_result(L), L.p.get()));
 }
 
 void BatchSolver::launch_persistent() {
