@@ -315,7 +315,7 @@ __device__ __forceinline__ void kbd_spmv_pq(const int32_t* __restrict__ list, co
         }
     }
 }
-__global__ void __launch_bounds__(kB) kb_spmv_pq(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_spmv_pq(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                  const int32_t* __restrict__ bm, BatchMeshState* st,
                                                  const int64_t* __restrict__ sb, const int32_t* __restrict__ sl,
                                                  const int32_t* __restrict__ col, const double* __restrict__ v64,
@@ -360,7 +360,7 @@ __device__ __forceinline__ void kbd_update(const int32_t* __restrict__ list, con
         }
     }
 }
-__global__ void __launch_bounds__(kB) kb_update(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_update(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                 const int32_t* __restrict__ bm, BatchMeshState* st,
                                                 double* __restrict__ x, const double* __restrict__ b,
                                                 double* __restrict__ r, const double* __restrict__ p,
@@ -389,7 +389,7 @@ __device__ __forceinline__ void kbd_rz(const int32_t* __restrict__ list, const i
         }
     }
 }
-__global__ void __launch_bounds__(kB) kb_rz(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_rz(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                             const int32_t* __restrict__ bm, BatchMeshState* st,
                                             const double* __restrict__ r, const float* __restrict__ z, double* partial) {
     kbd_rz(list, count, bm, st, r, z, partial);
@@ -407,7 +407,7 @@ __device__ __forceinline__ void kbd_direction(const int32_t* __restrict__ list, 
         p[row] = beta == 0.0 ? (double)z[row] : (double)z[row] + beta * p[row];
     }
 }
-__global__ void __launch_bounds__(kB) kb_direction(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_direction(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                    const int32_t* __restrict__ bm, BatchMeshState* st,
                                                    const float* __restrict__ z, double* __restrict__ p) {
     kbd_direction(list, count, bm, st, z, p);
@@ -428,7 +428,7 @@ __device__ __forceinline__ void kbd_cheb_zero(const int32_t* __restrict__ list, 
         x[row] = di;
     }
 }
-__global__ void __launch_bounds__(kB) kb_cheb_zero(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_cheb_zero(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                    const int32_t* __restrict__ bm, BatchMeshState* st,
                                                    const float* __restrict__ dinv, const float* __restrict__ b,
                                                    float* __restrict__ x, float* __restrict__ d, float inv_theta) {
@@ -459,7 +459,7 @@ __device__ __forceinline__ void kbd_cheb_step(const int32_t* __restrict__ list, 
     }
 }
 template <int TPR>
-__global__ void __launch_bounds__(kB) kb_cheb_step(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_cheb_step(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                    const int32_t* __restrict__ bm, BatchMeshState* st, OpB A,
                                                    const float* __restrict__ dinv, const float* __restrict__ b,
                                                    const float* __restrict__ xin, float* __restrict__ xout,
@@ -485,7 +485,7 @@ __device__ __forceinline__ void kbd_residual(const int32_t* __restrict__ list, c
     }
 }
 template <int TPR>
-__global__ void __launch_bounds__(kB) kb_residual(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_residual(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                   const int32_t* __restrict__ bm, BatchMeshState* st, OpB A,
                                                   const float* __restrict__ b, const float* __restrict__ x,
                                                   float* __restrict__ r) {
@@ -510,7 +510,7 @@ __device__ __forceinline__ void kbd_csr_apply(const int32_t* __restrict__ list, 
     }
 }
 template <int TPR>
-__global__ void __launch_bounds__(kB) kb_csr_apply(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_csr_apply(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                    const int32_t* __restrict__ bm, BatchMeshState* st, OpB M,
                                                    const float* __restrict__ x, float* __restrict__ y, int accumulate) {
     kbd_csr_apply<TPR>(list, count, bm, st, M, x, y, accumulate);
@@ -539,7 +539,7 @@ __device__ __forceinline__ void kbd_dense(const int32_t* __restrict__ list, cons
         }
     }
 }
-__global__ void __launch_bounds__(kB) kb_dense(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
+__global__ void __launch_bounds__(kB, 8) kb_dense(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                                const int32_t* __restrict__ bm, BatchMeshState* st,
                                                const float* __restrict__ dense, const float* __restrict__ b,
                                                float* __restrict__ x) {
@@ -728,7 +728,8 @@ __global__ void __launch_bounds__(kB) kb_true_residual(int row0, int n, const in
 
 // Work-list kernels walk their list with a fixed grid, every CTA taking an equal share, so
 // the grid must be resident in one wave: at most the CTAs of 256 threads that the kernel's
-// registers let an SM hold (8 at 32 registers, 5 at 40-48), times the SMs, capped by `cap`.
+// registers let an SM hold, times the SMs, capped by `cap`. The work-list kernels are built
+// for 8 CTAs per SM (32 registers; the level-0 SELL step and residual spill 8 and 4 bytes).
 int resident_grid(const void* fn, int cap) {
     static std::mutex mu;
     static std::map<const void*, int> per_sm;
