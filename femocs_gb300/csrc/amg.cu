@@ -136,8 +136,11 @@ __global__ void __launch_bounds__(kB) k_cheb_zero(int n, const float* __restrict
 }
 
 // c1 < 0 marks the first step from a nonzero guess: d = D^-1 r / theta (c2 = 1/theta)
+// the row kernels below are built for 8 CTAs of 256 threads per SM (32 registers; the SELL
+// variants spill 16 bytes): config 1's level-0 smoothing ran at 0.43 of the copy bandwidth
+// with 6 CTAs per SM (40 registers), 0.50 with 8
 template <int TPR>
-__global__ void __launch_bounds__(kB) k_cheb_step(Op A, const float* __restrict__ b, const float* __restrict__ xin,
+__global__ void __launch_bounds__(kB, 8) k_cheb_step(Op A, const float* __restrict__ b, const float* __restrict__ xin,
                                                   float* __restrict__ xout, float* __restrict__ d, float c1, float c2) {
     const int i = row_of<TPR>();
     if (TPR <= 1 && i >= A.n) return;
@@ -155,7 +158,7 @@ __global__ void k_add_f(int n, const float* __restrict__ y, float* __restrict__ 
 }
 
 template <int TPR>
-__global__ void __launch_bounds__(kB) k_residual(Op A, const float* __restrict__ b, const float* __restrict__ x,
+__global__ void __launch_bounds__(kB, 8) k_residual(Op A, const float* __restrict__ b, const float* __restrict__ x,
                                                  float* __restrict__ r) {
     const int i = row_of<TPR>();
     if (TPR <= 1 && i >= A.n) return;
@@ -166,7 +169,7 @@ __global__ void __launch_bounds__(kB) k_residual(Op A, const float* __restrict__
 
 // y = M x (accumulate: y += M x) for a CSR transfer operator
 template <int TPR>
-__global__ void __launch_bounds__(kB) k_csr_apply(int n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
+__global__ void __launch_bounds__(kB, 8) k_csr_apply(int n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
                                                   const float* __restrict__ val, const float* __restrict__ x,
                                                   float* __restrict__ y, int accumulate) {
     const int i = row_of<TPR>();
