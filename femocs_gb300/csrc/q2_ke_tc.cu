@@ -328,28 +328,31 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 J[a][1] = fma(F[21 + a], xi * ze, fma(F[18 + a], ze, fma(F[12 + a], xi, F[6 + a])));
                 J[a][2] = fma(F[21 + a], xi * eta, fma(F[18 + a], eta, fma(F[15 + a], xi, F[9 + a])));
             }
-            const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-            const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-            const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-            const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-            const double id = 1.0 / det;
-            double inv[3][3];  // J^-1, inv[k][a] = d xi_k / d x_a
-            inv[0][0] = c00 * id;
-            inv[1][0] = c01 * id;
-            inv[2][0] = c02 * id;
-            inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-            inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-            inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-            inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-            inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-            inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-            const double w = c_tc_w[q] * fabs(det);
+            // C = w |det J| J^-1 J^-T = (w / |det J|) adj(J) adj(J)^T: one reciprocal instead of a
+            // division and a scaled inverse, on GB300's reduced-rate FP64 pipe. 1 / |det J| by
+            // Newton-Raphson (y <- y (2 - a y), the error squares each step) from the FP32
+            // reciprocal: 2^-23, 2^-46, then FP64 rounding after two steps
+            double adj[3][3];  // J^-1 = adj / det, adj[k][a] for d xi_k / d x_a
+            adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+            adj[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+            adj[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+            adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+            adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+            adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+            adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+            adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+            adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+            const double ad = fabs(J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0]);
+            double y = (double)(1.0f / (float)ad);
+            y = y * fma(-ad, y, 2.0);
+            y = y * fma(-ad, y, 2.0);
+            const double sw = c_tc_w[q] * y;
             const int kk[6] = {0, 1, 2, 0, 0, 1}, ll[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
             for (int m = 0; m < 6; ++m) {
-                const double mk = inv[kk[m]][0] * inv[ll[m]][0] + inv[kk[m]][1] * inv[ll[m]][1] +
-                                  inv[kk[m]][2] * inv[ll[m]][2];
-                out[m] = w * mk;
+                const double mk = adj[kk[m]][0] * adj[ll[m]][0] + adj[kk[m]][1] * adj[ll[m]][1] +
+                                  adj[kk[m]][2] * adj[ll[m]][2];
+                out[m] = sw * mk;
             }
         }
         __syncthreads();
