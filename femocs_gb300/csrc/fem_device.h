@@ -6,7 +6,10 @@
 #include "device.h"
 #include "fem.h"
 
+#include <future>
 #include <memory>
+
+#include "cell_blocks.h"
 
 namespace fgb {
 
@@ -273,6 +276,15 @@ private:
     CgState* h_state_ = nullptr;  // pinned mirror
     double spmv64_ms_ = 0, spmv32_ms_ = 0;
     cudaEvent_t ev0_, ev1_, kev0_, kev1_;
+    // host work started at construction on other threads (declared last: destroyed, that is
+    // waited for, before the structure they read): the Q2 cell blocks of the default shape,
+    // and the Q1 structure of a Q2 field's coarse level (set_q1_structure)
+    std::future<CellBlocks> cb_host_;
+    int cb_host_cells_ = 0, cb_host_dofs_ = 0;
+    std::future<FemStructure> q1_fs_;
+
+public:
+    void set_q1_structure(std::future<FemStructure> f) { q1_fs_ = std::move(f); }
 };
 
 }  // namespace fgb

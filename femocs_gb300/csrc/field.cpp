@@ -1,5 +1,7 @@
 #include "field.h"
 
+#include <future>
+
 namespace fgb {
 
 Field::Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream, int order)
@@ -12,7 +14,16 @@ Field::Field(std::shared_ptr<const PreparedMesh> pm, cudaStream_t stream, int or
         FGB_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
         own_stream_ = true;
     }
-    fem_.reset(new FemDevice(*pm_, order == 2 ? build_q2_structure(*pm_, false) : build_fem_structure(*pm_), stream_));
+    if (order == 2) {
+        // the Q1 structure of the same mesh, the coarse level of the Q2 multigrid (needed at
+        // the first solve), is built on another host thread while the Q2 structure is built here
+        std::shared_ptr<const PreparedMesh> pm = pm_;
+        std::future<FemStructure> q1 = std::async(std::launch::async, [pm] { return build_fem_structure(*pm); });
+        fem_.reset(new FemDevice(*pm_, build_q2_structure(*pm_, false), stream_));
+        fem_->set_q1_structure(std::move(q1));
+    } else {
+        fem_.reset(new FemDevice(*pm_, build_fem_structure(*pm_), stream_));
+    }
     dm_.reset(new DeviceMesh(*pm_, stream_));
 }
 
