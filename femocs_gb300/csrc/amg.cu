@@ -772,15 +772,16 @@ void sell4_of(const CsrD& A, std::vector<int64_t>& sptr, std::vector<int32_t>& s
     const int n = A.n_rows, ns = (n + 31) / 32;
     sptr.assign(ns + 1, 0);
     slen.assign(ns, 0);
+#pragma omp parallel for schedule(static)
     for (int s = 0; s < ns; ++s) {
         int m = 0;
         for (int r = s * 32; r < std::min(n, s * 32 + 32); ++r) m = std::max<int>(m, (int)(A.ptr[r + 1] - A.ptr[r]));
-        m = (m + 3) / 4 * 4;
-        slen[s] = m;
-        sptr[s + 1] = sptr[s] + (int64_t)m * 32;
+        slen[s] = (m + 3) / 4 * 4;
     }
-    scol.assign(sptr[ns], 0);
-    val.assign(sptr[ns], 0.f);
+    for (int s = 0; s < ns; ++s) sptr[s + 1] = sptr[s] + (int64_t)slen[s] * 32;
+    scol.resize(sptr[ns]);
+    val.resize(sptr[ns]);
+#pragma omp parallel for schedule(dynamic, 64)
     for (int s = 0; s < ns; ++s)
         for (int lane = 0; lane < 32; ++lane) {
             const int r = s * 32 + lane;
@@ -801,7 +802,10 @@ void upload_csr32(const CsrD& M, DBuf<int64_t>& ptr, DBuf<int32_t>& col, DBuf<fl
     ptr.upload(M.ptr, s);
     if (M.nnz() > 0) {
         col.upload(M.col, s);
-        std::vector<float> v(M.val.begin(), M.val.end());
+        std::vector<float> v(M.val.size());
+        const long long nv = (long long)v.size();
+#pragma omp parallel for schedule(static)
+        for (long long k = 0; k < nv; ++k) v[k] = (float)M.val[k];
         val.upload(v, s);
     } else {
         col.resize(1);
@@ -831,6 +835,7 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
             lv->dinv = l0_dinv;
         } else if (l < L - 1) {
             std::vector<float> di(lv->n, 1.f);
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < lv->n; ++i)
                 for (int64_t k = hl.A.ptr[i]; k < hl.A.ptr[i + 1]; ++k)
                     if (hl.A.col[k] == i) di[i] = (float)(1.0 / hl.A.val[k]);

@@ -52,7 +52,8 @@ CsrD accumulate_rows(int n_rows, int n_cols, RowTerms row_terms) {
         std::vector<double> acc(n_cols, 0.0);
         std::vector<int32_t> mark(n_cols, -1), list;
         list.reserve(1024);
-#pragma omp for schedule(dynamic, 256)
+        // small chunks: the coarse levels have few rows, each with hundreds of terms
+#pragma omp for schedule(dynamic, 8)
         for (int i = 0; i < n_rows; ++i) {
             list.clear();
             row_terms(i, [&](int32_t c, double v) {

@@ -26,6 +26,16 @@ extern std::atomic<long long> g_kernel_launches;
                                ": " #call " -> " + cudaGetErrorString(e_));               \
     } while (0)
 
+// Host-to-device copy of pageable memory through pinned staging: chunks of the source are
+// copied (by all host threads) into two pinned buffers in turn, each sent by an async DMA on
+// `s` while the next is filled. Returns once the source may be reused; copies from several
+// host threads take turns. Large copies from pageable memory otherwise run at a few GB/s.
+void h2d_staged(void* dst, const void* src, size_t bytes, cudaStream_t s);
+constexpr size_t kStagedMinBytes = size_t(8) << 20;
+// the reverse: device to pageable host memory through the same double buffering; returns
+// once the data are in `dst` (synchronous with the host, like a pageable copy)
+void d2h_staged(void* dst, const void* src, size_t bytes, cudaStream_t s);
+
 // Owning device buffer (cudaMalloc'd, freed on destruction).
 template <typename T>
 class DBuf {
@@ -65,11 +75,13 @@ public:
     }
     void upload(const T* h, size_t n, cudaStream_t s = 0) {
         resize(n);
-        if (n) FGB_CUDA(cudaMemcpyAsync(p_, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+        if (n * sizeof(T) >= kStagedMinBytes) h2d_staged(p_, h, n * sizeof(T), s);
+        else if (n) FGB_CUDA(cudaMemcpyAsync(p_, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
     }
     void upload(const std::vector<T>& v, cudaStream_t s = 0) { upload(v.data(), v.size(), s); }
     void download(T* h, size_t n, cudaStream_t s = 0) const {
-        if (n) FGB_CUDA(cudaMemcpyAsync(h, p_, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+        if (n * sizeof(T) >= kStagedMinBytes) d2h_staged(h, p_, n * sizeof(T), s);
+        else if (n) FGB_CUDA(cudaMemcpyAsync(h, p_, n * sizeof(T), cudaMemcpyDeviceToHost, s));
     }
     std::vector<T> to_host(cudaStream_t s = 0) const {
         std::vector<T> v(n_);

@@ -20,6 +20,7 @@
 //                      element matrices over the cell blocks (cell_blocks.h)
 //   k_ke_cyclic        Q2 element matrices into the cell blocks' FP32 (hi, lo) layout
 #include <algorithm>
+#include <mutex>
 #include <cstring>
 #include <chrono>
 #include <omp.h>
@@ -43,6 +44,69 @@ struct FemDevice::CellBlocksDev {
 };
 
 std::atomic<long long> g_kernel_launches{0};
+
+void d2h_staged(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    constexpr size_t kChunk = size_t(32) << 20;
+    static std::mutex mu;
+    static unsigned char* stage[2] = {nullptr, nullptr};
+    static cudaEvent_t done[2];
+    std::lock_guard<std::mutex> lk(mu);
+    if (!stage[0])
+        for (int k = 0; k < 2; ++k) {
+            FGB_CUDA(cudaMallocHost(&stage[k], kChunk));
+            FGB_CUDA(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming));
+        }
+    const unsigned char* in = static_cast<const unsigned char*>(src);
+    unsigned char* out = static_cast<unsigned char*>(dst);
+    const size_t n_chunks = (bytes + kChunk - 1) / kChunk;
+    auto issue = [&](size_t c) {
+        const size_t off = c * kChunk, len = std::min(kChunk, bytes - off);
+        FGB_CUDA(cudaMemcpyAsync(stage[c & 1], in + off, len, cudaMemcpyDeviceToHost, s));
+        FGB_CUDA(cudaEventRecord(done[c & 1], s));
+    };
+    if (n_chunks) issue(0);
+    for (size_t c = 0; c < n_chunks; ++c) {
+        if (c + 1 < n_chunks) issue(c + 1);  // the next chunk travels while this one is copied out
+        FGB_CUDA(cudaEventSynchronize(done[c & 1]));
+        const size_t off = c * kChunk, len = std::min(kChunk, bytes - off);
+        const long long parts = (long long)((len + (size_t(1) << 20) - 1) >> 20);
+#pragma omp parallel for schedule(static)
+        for (long long q = 0; q < parts; ++q) {
+            const size_t a = (size_t)q << 20, b = std::min(len, a + (size_t(1) << 20));
+            std::memcpy(out + off + a, stage[c & 1] + a, b - a);
+        }
+    }
+}
+
+void h2d_staged(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    constexpr size_t kChunk = size_t(32) << 20;
+    static std::mutex mu;
+    static unsigned char* stage[2] = {nullptr, nullptr};
+    static cudaEvent_t done[2];
+    std::lock_guard<std::mutex> lk(mu);
+    if (!stage[0]) {
+        for (int k = 0; k < 2; ++k) {
+            FGB_CUDA(cudaMallocHost(&stage[k], kChunk));
+            FGB_CUDA(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming));
+            FGB_CUDA(cudaEventRecord(done[k], s));
+        }
+    }
+    const unsigned char* in = static_cast<const unsigned char*>(src);
+    unsigned char* out = static_cast<unsigned char*>(dst);
+    int k = 0;
+    for (size_t off = 0; off < bytes; off += kChunk, k ^= 1) {
+        const size_t len = std::min(kChunk, bytes - off);
+        FGB_CUDA(cudaEventSynchronize(done[k]));  // the DMA that last read this buffer is done
+        const long long parts = (long long)((len + (size_t(1) << 20) - 1) >> 20);
+#pragma omp parallel for schedule(static)
+        for (long long q = 0; q < parts; ++q) {
+            const size_t a = (size_t)q << 20, b = std::min(len, a + (size_t(1) << 20));
+            std::memcpy(stage[k] + a, in + off + a, b - a);
+        }
+        FGB_CUDA(cudaMemcpyAsync(out + off, stage[k], len, cudaMemcpyHostToDevice, s));
+        FGB_CUDA(cudaEventRecord(done[k], s));
+    }
+}
 
 namespace {
 
@@ -1138,28 +1202,21 @@ double FemDevice::time_spmv(int precision, int reps) {
 void FemDevice::download_matrix(std::vector<double>& vals, std::vector<double>& rhs) {
     // CSR order values after Dirichlet elimination, gathered back from the SELL layout
     std::vector<double> s = sell64_.to_host(stream_);
+    // row r's CSR entries start at off[r] (Q1: the structure's row pointer; Q2: the prefix of
+    // the row lengths); entry j of row r sits at its SELL position, rows in parallel
+    std::vector<int64_t> q2off;
     if (fs_.order == 2) {
-        vals.resize(fs_.nnz());
-        int64_t k = 0;
-        for (int r = 0; r < n_; ++r) {
-            const int sl = r / 32, lane = r % 32;
-            for (int j = 0; j < fs_.row_len[r]; ++j)
-                vals[k++] = s[fs_.slice_ptr[sl] + ((int64_t)(j / 4) * 32 + lane) * 4 + j % 4];
-        }
-        rhs = rhs_.to_host(stream_);
-        return;
+        q2off.assign(n_ + 1, 0);
+        for (int r = 0; r < n_; ++r) q2off[r + 1] = q2off[r] + fs_.row_len[r];
     }
-    std::vector<int64_t> c2s(fs_.nnz());
-    // rebuild the CSR->SELL map on the host (kept only on the device after upload)
+    const int64_t* off = fs_.order == 2 ? q2off.data() : fs_.rowptr.data();
+    vals.resize(off[n_]);
+#pragma omp parallel for schedule(dynamic, 1024)
     for (int r = 0; r < n_; ++r) {
         const int sl = r / 32, lane = r % 32;
-        for (int64_t k = fs_.rowptr[r]; k < fs_.rowptr[r + 1]; ++k) {
-            const int64_t j = k - fs_.rowptr[r];
-            c2s[k] = fs_.slice_ptr[sl] + ((j / 4) * 32 + lane) * 4 + j % 4;
-        }
+        const int64_t b = off[r], len = off[r + 1] - b;
+        for (int64_t j = 0; j < len; ++j) vals[b + j] = s[fs_.slice_ptr[sl] + ((j / 4) * 32 + lane) * 4 + j % 4];
     }
-    vals.resize(fs_.nnz());
-    for (int64_t k = 0; k < fs_.nnz(); ++k) vals[k] = s[c2s[k]];
     rhs = rhs_.to_host(stream_);
 }
 
