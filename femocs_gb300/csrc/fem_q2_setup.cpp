@@ -14,6 +14,8 @@
 #include <numeric>
 #include <parallel/algorithm>
 
+#include <omp.h>
+
 namespace fgb {
 
 namespace {
@@ -108,17 +110,45 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
     phase("entity keys");
     __gnu_parallel::sort(ek.begin(), ek.end());
     phase("entity sort");
+    // runs of equal keys in the sorted list are one entity each, numbered in order: run heads
+    // flagged and counted per thread block of the list, an exclusive scan over the blocks, then
+    // each record takes its run's id (the numbering of a sequential pass, in parallel)
+    const size_t ne = ek.size();
+    std::vector<int32_t> run_id(ne);
     int n_shared = 0;
-    std::vector<int32_t> face_count;  // occurrences of each face entity (boundary faces: 1)
-    std::vector<int32_t> ent_first;   // first (cell, L) of each shared entity
-    for (size_t i = 0; i < ek.size();) {
-        size_t j = i + 1;
-        while (j < ek.size() && ek[j].k == ek[i].k) ++j;
-        const int id = nvx + n_shared++;
-        for (size_t q = i; q < j; ++q) ent[27 * (size_t)ek[q].cell + ek[q].local] = id;
-        face_count.push_back(ek[i].k[2] == INT32_MAX ? 0 : (int32_t)(j - i));
-        ent_first.push_back(27 * ek[i].cell + ek[i].local);
-        i = j;
+    {
+        const int nt = std::max(1, omp_get_max_threads());
+        std::vector<int64_t> heads(nt + 1, 0);
+#pragma omp parallel num_threads(nt)
+        {
+            const int t = omp_get_thread_num();
+            const size_t a0 = ne * t / nt, a1 = ne * (t + 1) / nt;
+            int64_t h = 0;
+            for (size_t i = a0; i < a1; ++i) h += (i == 0 || !(ek[i].k == ek[i - 1].k));
+            heads[t + 1] = h;
+#pragma omp barrier
+#pragma omp single
+            for (int u = 0; u < nt; ++u) heads[u + 1] += heads[u];
+            int64_t id = heads[t] - 1;
+            for (size_t i = a0; i < a1; ++i) {
+                if (i == 0 || !(ek[i].k == ek[i - 1].k)) ++id;
+                run_id[i] = (int32_t)id;
+            }
+        }
+        n_shared = (int)heads[nt];
+    }
+    std::vector<int32_t> face_count(n_shared);  // occurrences of each face entity (boundary faces: 1)
+    std::vector<int32_t> ent_first(n_shared);   // first (cell, L) of each shared entity
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)ne; ++i) {
+        const int r = run_id[i];
+        ent[27 * (size_t)ek[i].cell + ek[i].local] = nvx + r;
+        if (i == 0 || run_id[i - 1] != r) {
+            size_t j = i + 1;
+            while (j < ne && run_id[j] == r) ++j;
+            face_count[r] = ek[i].k[2] == INT32_MAX ? 0 : (int32_t)(j - i);
+            ent_first[r] = 27 * ek[i].cell + ek[i].local;
+        }
     }
     ek.clear();
     ek.shrink_to_fit();
@@ -152,14 +182,36 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
 
     phase("entity positions");
     // entity -> cells
+    // counting sort of the (cell, L) items by entity, stable in item order: per-thread counts
+    // over contiguous item ranges, offsets (entity, thread) in that order, then the fills
     std::vector<int32_t> e2c_ptr(n_ent + 1, 0);
-    for (int32_t e : ent) e2c_ptr[e + 1]++;
-    for (int i = 0; i < n_ent; ++i) e2c_ptr[i + 1] += e2c_ptr[i];
-    std::vector<int32_t> e2c(e2c_ptr[n_ent]);
+    std::vector<int32_t> e2c(ent.size());
     {
-        std::vector<int32_t> pos(e2c_ptr.begin(), e2c_ptr.end() - 1);
-        for (int c = 0; c < nc; ++c)
-            for (int L = 0; L < 27; ++L) e2c[pos[ent[27 * (size_t)c + L]]++] = 27 * c + L;
+        const int nt = std::max(1, std::min(omp_get_max_threads(), 16));
+        const size_t ni = ent.size();
+        std::vector<int32_t> cnt((size_t)nt * n_ent, 0);
+#pragma omp parallel num_threads(nt)
+        {
+            const int t = omp_get_thread_num();
+            int32_t* ct = &cnt[(size_t)t * n_ent];
+            for (size_t i = ni * t / nt; i < ni * (t + 1) / nt; ++i) ct[ent[i]]++;
+        }
+        int64_t run = 0;
+        for (int e = 0; e < n_ent; ++e) {
+            e2c_ptr[e] = (int32_t)run;
+            for (int t = 0; t < nt; ++t) {
+                const int32_t c = cnt[(size_t)t * n_ent + e];
+                cnt[(size_t)t * n_ent + e] = (int32_t)run;
+                run += c;
+            }
+        }
+        e2c_ptr[n_ent] = (int32_t)run;
+#pragma omp parallel num_threads(nt)
+        {
+            const int t = omp_get_thread_num();
+            int32_t* ot = &cnt[(size_t)t * n_ent];
+            for (size_t i = ni * t / nt; i < ni * (t + 1) / nt; ++i) e2c[ot[ent[i]]++] = (int32_t)i;
+        }
     }
     phase("entity -> cells");
     // row length = number of distinct entities of the incident cells, counted with a stamped
