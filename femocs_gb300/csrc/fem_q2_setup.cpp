@@ -157,30 +157,6 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
     fs.n_dofs = n_ent;
 
     phase("entity ids");
-    // entity -> one (cell, L) and its position
-    std::vector<int32_t> e_cell(n_ent, -1);
-    std::vector<int8_t> e_loc(n_ent, 0);
-    for (int c = 0; c < nc; ++c)
-        for (int L = 0; L < 27; ++L) {
-            const int32_t e = ent[27 * (size_t)c + L];
-            if (e_cell[e] < 0) {
-                e_cell[e] = c;
-                e_loc[e] = (int8_t)L;
-            }
-        }
-    std::vector<double> exyz(3 * (size_t)n_ent);
-#pragma omp parallel for schedule(static)
-    for (int e = 0; e < n_ent; ++e) {
-        int cr[8];
-        const int n = corners_of(e_loc[e], cr);
-        for (int d = 0; d < 3; ++d) {
-            double s = 0.0;
-            for (int q = 0; q < n; ++q) s += X[3 * (size_t)cell_node(e_cell[e], cr[q]) + d];
-            exyz[3 * (size_t)e + d] = s / n;
-        }
-    }
-
-    phase("entity positions");
     // entity -> cells
     // counting sort of the (cell, L) items by entity, stable in item order: per-thread counts
     // over contiguous item ranges, offsets (entity, thread) in that order, then the fills
@@ -214,6 +190,29 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
         }
     }
     phase("entity -> cells");
+    // entity -> its first (cell, L) in item order (the head of its stable list) and position
+    std::vector<int32_t> e_cell(n_ent, -1);
+    std::vector<int8_t> e_loc(n_ent, 0);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < n_ent; ++e) {
+        if (e2c_ptr[e] == e2c_ptr[e + 1]) continue;
+        const int32_t item = e2c[e2c_ptr[e]];
+        e_cell[e] = item / 27;
+        e_loc[e] = (int8_t)(item % 27);
+    }
+    std::vector<double> exyz(3 * (size_t)n_ent);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < n_ent; ++e) {
+        int cr[8];
+        const int n = corners_of(e_loc[e], cr);
+        for (int d = 0; d < 3; ++d) {
+            double s = 0.0;
+            for (int q = 0; q < n; ++q) s += X[3 * (size_t)cell_node(e_cell[e], cr[q]) + d];
+            exyz[3 * (size_t)e + d] = s / n;
+        }
+    }
+
+    phase("entity positions");
     // row length = number of distinct entities of the incident cells, counted with a stamped
     // open-addressing set per thread (no sort: the columns themselves are built later)
     int max_inc = 1;
