@@ -193,9 +193,11 @@ class Field:
     def assemble(self, full_run=True, anode_dirichlet=False):
         self._ok(load().fgb_field_assemble(self.h, int(full_run), int(anode_dirichlet)))
 
-    def solve(self, precision=2, rel_tol=1e-9, abs_tol=0.0, max_iter=10000, inner_tol=0.1):
+    def solve(self, precision=2, rel_tol=1e-9, abs_tol=0.0, max_iter=10000, inner_tol=0.0):
         """precision 0: FP64 Jacobi-PCG; 1: FP32 Jacobi-PCG with FP64 refinement;
-        2: FP64 CG with an FP32 multigrid V-cycle as preconditioner."""
+        2: FP64 CG with an FP32 multigrid V-cycle as preconditioner; 3: FP32 CG with the
+        V-cycle and its level-0 operator, inside FP64 refinement. inner_tol: residual
+        reduction per refinement (0: 0.1 for precision 1, 1e-3 for precision 3)."""
         rc = load().fgb_field_solve(self.h, precision, rel_tol, abs_tol, max_iter, inner_tol, None)
         if rc == -(2 ** 31):
             raise RuntimeError(last_error())
@@ -263,6 +265,11 @@ class Field:
     def set_smoothing(self, degree=0, lo=0.0):
         """Chebyshev degree and interval of the finest multigrid level (0: defaults)."""
         self._ok(load().fgb_field_set_smoothing(self.h, int(degree), float(lo)))
+
+    def set_level_smoothing(self, level, degree=0, lo=0.0):
+        """Chebyshev degree and interval of coarser multigrid level `level` >= 1 (Q2: level 1
+        is the Q1 system); 0 restores the default, from the next solve, without a rebuild."""
+        self._ok(load().fgb_field_set_level_smoothing(self.h, int(level), int(degree), float(lo)))
 
     def set_profiling(self, on=True):
         """Record CUDA event pairs around the multigrid path's hot launches."""

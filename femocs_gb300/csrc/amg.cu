@@ -25,8 +25,8 @@ namespace fgb {
 
 struct AmgDevLevel {
     int n = 0, n_coarse = 0;
-    double lambda = 1.0, cheb_lo = 0.1;
-    int cheb_degree = 2;
+    double lambda = 1.0, cheb_lo = 0.1, built_lo = 0.1;
+    int cheb_degree = 2, built_degree = 2;  // built_*: the hierarchy's own choice
     const int64_t* sptr = nullptr;
     const int32_t* slen = nullptr;
     const int32_t* scol = nullptr;
@@ -825,8 +825,8 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
         auto lv = std::make_unique<AmgDevLevel>();
         lv->n = hl.A.n_rows;
         lv->lambda = hl.lambda;
-        lv->cheb_degree = std::max(1, hl.cheb_degree);
-        lv->cheb_lo = hl.cheb_lo;
+        lv->cheb_degree = lv->built_degree = std::max(1, hl.cheb_degree);
+        lv->cheb_lo = lv->built_lo = hl.cheb_lo;
         if (l == 0) {
             lv->sptr = l0_sptr;
             lv->slen = l0_slen;
@@ -895,6 +895,14 @@ void AmgDevice::set_coarse_cycles(int level, int cycles) {
     FGB_REQUIRE(level >= 0 && cycles >= 1 && cycles <= 8, "coarse cycles: level >= 0, 1..8 cycles");
     if ((int)coarse_cycles_.size() <= level) coarse_cycles_.resize(level + 1, 1);
     coarse_cycles_[level] = cycles;
+}
+
+void AmgDevice::set_level_smoothing(int level, int degree, double lo) {
+    FGB_REQUIRE(level >= 0 && level < (int)lv_.size() && degree >= 0 && degree <= 15 && lo >= 0 && lo < 1,
+                "level smoothing: an existing level, degree 0..15, interval 0..1");
+    AmgDevLevel& L = *lv_[level];
+    L.cheb_degree = degree > 0 ? degree : L.built_degree;
+    L.cheb_lo = lo > 0 ? lo : L.built_lo;
 }
 
 int AmgDevice::n_levels() const { return (int)lv_.size(); }
@@ -1109,6 +1117,14 @@ const float* AmgDevice::vcycle(const float* r) {
     cycle(0);
     FGB_CUDA(cudaGetLastError());
     return L0.x;
+}
+
+void AmgDevice::level0_residual(const float* b, const float* x, float* y) {
+    AmgDevLevel& L0 = *lv_[0];
+    const float* keep = L0.bin;
+    L0.bin = b;
+    level0_apply(1, x, y, 0.f, 0.f);
+    L0.bin = keep;
 }
 
 }  // namespace fgb

@@ -92,6 +92,9 @@ public:
     // z = V(r) on level 0 (FP32, length n0); z is the hierarchy's own buffer, valid until the
     // next cycle
     const float* vcycle(const float* r);
+    // y = b - A0 x with the level-0 operator the smoother applies (FP32: the SELL matrix, or
+    // for Q2 the element matrices or geometric factors by cell blocks); b may be all zeros
+    void level0_residual(const float* b, const float* x, float* y);
     int n_levels() const;
     // "rows:nnz" per level, coarsest marked dense
     std::string describe() const;
@@ -123,6 +126,9 @@ public:
     // (1: V-cycle; 2 at level 0: two Q1 cycles per Q2 correction). Each further cycle starts
     // from the residual of the sum so far, so the preconditioner stays symmetric.
     void set_coarse_cycles(int level, int cycles);
+    // Chebyshev degree and interval of one level's smoother (0: the hierarchy's own choice);
+    // only the polynomial changes, nothing is rebuilt (the coarsest level is solved densely)
+    void set_level_smoothing(int level, int degree, double lo);
 
 private:
     void cycle(int l);

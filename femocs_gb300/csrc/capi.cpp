@@ -429,6 +429,7 @@ int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol,
         o.abs_tol = abs_tol;
         o.max_iter = max_iter;
         if (inner_tol > 0) o.inner_tol = inner_tol;
+        else if (precision == 3) o.inner_tol = 1e-3;
         rc = f->f->fem().solve(o, &f->last);
         if (stats6) {
             stats6[0] = f->last.iterations;
@@ -486,6 +487,9 @@ int fgb_field_set_level0_prefetch(FGB_FIELD* f, int cells) {
 }
 int fgb_field_set_coarse_cycles(FGB_FIELD* f, int level, int cycles) {
     return guarded([&] { f->f->fem().set_coarse_cycles(level, cycles); return 0; });
+}
+int fgb_field_set_level_smoothing(FGB_FIELD* f, int level, int degree, double lo) {
+    return guarded([&] { f->f->fem().set_level_smoothing(level, degree, lo); return 0; });
 }
 int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo) {
     return guarded([&] { f->f->fem().set_smoothing(degree, lo); return 0; });

@@ -131,10 +131,11 @@ void FemocsFacade::read_params() {
     conf_.get("radius", radius_);
     // GPU-specific keys
     conf_.get("gpu_rel_tol", rel_tol_);
-    conf_.get("gpu_inner_tol", inner_tol_);
     std::string prec = "amg";
     conf_.get("gpu_precision", prec);
-    precision_ = prec == "fp64" ? 0 : (prec == "mixed" ? 1 : 2);
+    precision_ = prec == "fp64" ? 0 : (prec == "mixed" ? 1 : (prec == "amg_mixed" ? 3 : 2));
+    inner_tol_ = precision_ == 3 ? 1e-3 : 0.1;
+    conf_.get("gpu_inner_tol", inner_tol_);
     conf_.get("gpu_use_abs_tol", use_abs_tol_);
     conf_.get("gpu_element_order", element_order_);
     std::string prep = "device";

@@ -731,6 +731,84 @@ __global__ void __launch_bounds__(kBlock) k_pcg_direction(int n, const float* __
     }
 }
 
+// ---- FP32 inner CG of the mixed multigrid solve (precision 3): e (the correction), r, p and
+// q = -A p in FP32 with the level-0 operator of the V-cycle, sums in FP64, scalars in CgState
+
+// p = z, rz = r.z
+__global__ void __launch_bounds__(kBlock) k_mcg_start(int n, const float* __restrict__ z, const float* __restrict__ r,
+                                                      float* __restrict__ p, double* partial, CgState* st) {
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float zi = z[i];
+        p[i] = zi;
+        v[0] += (double)r[i] * zi;
+    }
+    if (grid_reduce<1>(v, partial, &st->ticket)) st->rz = v[0];
+}
+
+// p.q from q = -A p; alpha = rz / p.A p (a non-positive curvature ends the inner solve)
+__global__ void __launch_bounds__(kBlock) k_mcg_pq(int n, const float* __restrict__ p, const float* __restrict__ qn,
+                                                   double* partial, CgState* st) {
+    if (st->done) return;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[0] += (double)p[i] * qn[i];
+    if (grid_reduce<1>(v, partial, &st->ticket)) {
+        const double pq = -v[0];
+        st->pq = pq;
+        if (!(pq > 0.0)) {
+            st->done = 1;
+            st->status = -2;
+        } else {
+            st->alpha = st->rz / pq;
+        }
+    }
+}
+
+// e += alpha p, r -= alpha A p (= r + alpha q), rr and the stop test
+__global__ void __launch_bounds__(kBlock) k_mcg_update(int n, float* __restrict__ e, float* __restrict__ r,
+                                                       const float* __restrict__ p, const float* __restrict__ qn,
+                                                       double* partial, CgState* st) {
+    if (st->done) return;
+    const float alpha = (float)st->alpha;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        e[i] = fmaf(alpha, p[i], e[i]);
+        const float ri = fmaf(alpha, qn[i], r[i]);
+        r[i] = ri;
+        v[0] += (double)ri * ri;
+    }
+    if (grid_reduce<1>(v, partial, &st->ticket)) {
+        st->iter += 1;
+        cg_check(st, v[0]);
+    }
+}
+
+// beta = r.z / r.z_old
+__global__ void __launch_bounds__(kBlock) k_mcg_rz(int n, const float* __restrict__ z, const float* __restrict__ r,
+                                                   double* partial, CgState* st) {
+    if (st->done) return;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[0] += (double)r[i] * z[i];
+    if (grid_reduce<1>(v, partial, &st->ticket)) {
+        st->beta = v[0] / st->rz;
+        st->rz = v[0];
+    }
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(kBlock) k_mcg_direction(int n, const float* __restrict__ z, float* __restrict__ p,
+                                                          const CgState* st) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = fmaf((float)st->beta, p[i], z[i]);
+}
+
+// x += e (the FP32 correction into the FP64 solution)
+__global__ void k_add_correction(int n, double* __restrict__ x, const float* __restrict__ e) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += (double)e[i];
+}
+
 // ---- outer SpMV of the Q2 multigrid PCG by cell blocks (the level-0 smoother's blocks,
 // cell_blocks.h), FP64-accurate from FP32 pairs: q = A p and p.q. K_e as hi/lo pairs in the
 // cyclic-half layout; lane i < 27 of a warp owns row i of a cell, forms K(i, i+t) p_{i+t} with
@@ -1255,7 +1333,11 @@ int FemDevice::solve(const SolveOptions& opt, SolveStats* st) {
     if (!st) st = &local;
     *st = SolveStats();
     FGB_CUDA(cudaEventRecord(ev0_, stream_));
-    int rc = opt.precision == 0 ? solve_plain(opt, st) : (opt.precision == 1 ? solve_mixed(opt, st) : solve_amg(opt, st));
+    FGB_REQUIRE(opt.precision >= 0 && opt.precision <= 3, "precision 0..3");
+    int rc = opt.precision == 0   ? solve_plain(opt, st)
+             : opt.precision == 1 ? solve_mixed(opt, st)
+             : opt.precision == 2 ? solve_amg(opt, st)
+                                  : solve_amg_mixed(opt, st);
     FGB_CUDA(cudaEventRecord(ev1_, stream_));
     FGB_CUDA(cudaEventSynchronize(ev1_));
     float ms = 0;
@@ -1432,6 +1514,9 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     // the Q1 level is the coarse solve of the Q2 level: smooth it harder
     h1.levels[0].cheb_degree = 4;
     h1.levels[0].cheb_lo = 0.04;
+    // below it one Chebyshev step per side is enough: config 2 keeps its 96 PCG iterations
+    // (618 -> 609 ms per solve); degree 2 or 3 there, or 3 or 6 at the Q1 level, cost more
+    for (size_t l = 1; l < h1.levels.size(); ++l) h1.levels[l].cheb_degree = 1;
     h1.levels[0].A.col = f1.col;
     h1.levels[0].A.val = std::move(v1);
     // embedding: a free Q2 DoF takes the mean of the free Q1 values at its entity's corners
@@ -1472,10 +1557,11 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     l0.A.n_rows = l0.A.n_cols = n_;
     l0.A.ptr.assign(1, fs_.nnz());  // structure lives on the device; nnz for reporting
     l0.lambda = estimate_lambda(15);
-    // degree 2 on [0.1, 1.1]: more iterations than degree 3-4 but fewer passes over the big Q2
-    // matrix per cycle (config 2: 95 iterations / 1.11 s vs 84 / 1.23 s at degree 3)
+    // degree 2 on [0.06, 1.1]: more iterations than degree 3-4 but fewer passes over the big Q2
+    // matrix per cycle (config 2: 95 iterations / 1.11 s vs 84 / 1.23 s at degree 3); the lower
+    // end 0.06 against 0.1: 70 -> 68 iterations on a 2.2e6-DoF tip, 96 on config 2 either way
     l0.cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 2;
-    l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.1;
+    l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.06;
     phase("lambda_max (device)");
     l0.R.n_rows = P.n_cols;
     l0.R.n_cols = P.n_rows;
@@ -1745,6 +1831,13 @@ void FemDevice::set_coarse_cycles(int level, int cycles) {
     coarse_cycles_[level] = cycles;
 }
 
+void FemDevice::set_level_smoothing(int level, int degree, double lo) {
+    FGB_REQUIRE(level >= 1 && level < 16 && degree >= 0 && degree <= 15 && lo >= 0 && lo < 1,
+                "level smoothing: level 1..15, degree 0..15, interval 0..1");
+    if ((int)level_smooth_.size() <= level) level_smooth_.resize(level + 1, {0, 0.0});
+    level_smooth_[level] = {degree, lo};
+}
+
 void FemDevice::set_profiling(bool on) {
     profiling_ = on;
     spmv_timer_.enabled = on;
@@ -1755,10 +1848,17 @@ void FemDevice::set_profiling(bool on) {
     }
 }
 
-int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
+void FemDevice::prepare_amg(SolveStats* st) {
     ensure_amg(st);
     for (int l = 0; l < (int)coarse_cycles_.size(); ++l) amg_->set_coarse_cycles(l, coarse_cycles_[l]);
+    // levels the hierarchy has, short of the dense coarsest one
+    for (int l = 1; l < (int)level_smooth_.size() && l + 1 < amg_->n_levels(); ++l)
+        amg_->set_level_smoothing(l, level_smooth_[l].first, level_smooth_[l].second);
     st->levels = amg_->n_levels();
+}
+
+int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
+    prepare_amg(st);
     const int gb = grid_for(n_, kBlock);
     CgState* ds = state_.get();
     FGB_LAUNCH(k_norm2<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
@@ -1877,6 +1977,104 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     if (const unsigned e = amg_->level0_errors())
         throw Error("level-0 smoother: a bounded wait of the streamed element matrices ran out (code " +
                     std::to_string(e) + ")");
+    st->smoother_ms = amg_->smoother_timer.collect(&st->smoother_launches);
+    st->smoother_bytes = amg_->smoother_bytes();
+    st->spmv_ms = spmv_timer_.collect(&st->spmv_launches);
+    return st->status >= 1 ? it : -it;
+}
+
+// Mixed multigrid solve (precision 3): FP64 iterative refinement around an FP32 CG with the
+// level-0 operator of the V-cycle (the FP32 SELL matrix, or for Q2 the matrix-free cell-block
+// operator) preconditioned by the V-cycle. Each refinement forms the FP64 residual
+// r = b - A x of the assembled system (compensated near the FP64 floor), solves A e = r in
+// FP32 to a relative reduction inner_tol (or to what the outer tolerance still needs), and
+// adds e to x in FP64. The FP32 operator differs from A by its rounding (and the FP16
+// factors' 2^-11), which bounds what one refinement can gain: a few refinements reach 1e-9.
+int FemDevice::solve_amg_mixed(const SolveOptions& opt, SolveStats* st) {
+    prepare_amg(st);
+    const int gb = grid_for(n_, kBlock);
+    const int rg = reduce_grid(n_, kBlock);
+    CgState* ds = state_.get();
+    FGB_LAUNCH(k_norm2<<<rg, kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
+    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    const double bnorm = std::sqrt(h_state_->rr);
+    st->bnorm = bnorm;
+    const double tol2 = tol2_of(opt, bnorm);
+    const int comp = compensated_residual(opt);
+    float* r = r32_.get();
+    float* p = p32_.get();
+    float* q = q32_.get();
+    float* e = d32_.get();
+    float* zero = z32_.get();
+    z32_.zero(stream_);
+    // true FP64 residual of x into r64 (and rr, ff in the state)
+    auto true_residual = [&]() {
+        CgState init{};
+        init.tol2 = tol2;
+        FGB_CUDA(cudaMemcpyAsync(ds, &init, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
+        FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                           sell64_.get(), x_.get(), rhs_.get(), r64_.get(), partial_.get(),
+                                                           ds, comp));
+        FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        return *h_state_;
+    };
+    CgState tr = true_residual();
+    double rr_true = tr.rr;
+    int status = (rr_true <= tol2 || bnorm == 0) ? 1 : 0, it = 0, refinements = 0, stalled = 0;
+    const double eta = std::min(std::max(opt.inner_tol, 1e-6), 0.5);
+    while (status == 0) {
+        FGB_LAUNCH(k_to32<<<gb, kBlock, 0, stream_>>>(n_, r64_.get(), r));
+        FGB_CUDA(cudaMemsetAsync(e, 0, sizeof(float) * n_, stream_));
+        CgState in{};
+        // the inner residual starts at ||r64||: reduce it by eta, or to half the outer target
+        in.tol2 = std::max(eta * eta * rr_true, 0.25 * tol2);
+        in.max_iter = std::max(1, opt.max_iter - it);
+        FGB_CUDA(cudaMemcpyAsync(ds, &in, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
+        const float* z = amg_->vcycle(r);
+        FGB_LAUNCH(k_mcg_start<<<rg, kBlock, 0, stream_>>>(n_, z, r, p, partial_.get(), ds));
+        int inner_status = 0;
+        while (true) {
+            spmv_timer_.begin(stream_);
+            amg_->level0_residual(zero, p, q);
+            spmv_timer_.end(stream_);
+            FGB_LAUNCH(k_mcg_pq<<<rg, kBlock, 0, stream_>>>(n_, p, q, partial_.get(), ds));
+            FGB_LAUNCH(k_mcg_update<<<rg, kBlock, 0, stream_>>>(n_, e, r, p, q, partial_.get(), ds));
+            FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+            FGB_CUDA(cudaStreamSynchronize(stream_));
+            if (h_state_->done) {
+                inner_status = h_state_->status;
+                it += h_state_->iter;
+                break;
+            }
+            const float* zi = amg_->vcycle(r);
+            FGB_LAUNCH(k_mcg_rz<<<rg, kBlock, 0, stream_>>>(n_, zi, r, partial_.get(), ds));
+            FGB_LAUNCH(k_mcg_direction<<<gb, kBlock, 0, stream_>>>(n_, zi, p, ds));
+        }
+        FGB_LAUNCH(k_add_correction<<<gb, kBlock, 0, stream_>>>(n_, x_.get(), e));
+        ++refinements;
+        const double rr_prev = rr_true;
+        tr = true_residual();
+        rr_true = tr.rr;
+        if (!(rr_true == rr_true)) { status = -2; break; }
+        if (rr_true <= tol2) { status = 1; break; }
+        // a solution within twice the FP64 floor is as converged as FP64 can hold it
+        if (comp && rr_true <= 4.0 * kFloorScale2 * tr.ff) { status = kStatusFloor; break; }
+        if (inner_status == -2 && rr_true >= rr_prev) { status = -2; break; }
+        if (it >= opt.max_iter) { status = -1; break; }
+        // refinements that no longer halve the residual: the FP32 operator's limit
+        stalled = rr_true > 0.25 * rr_prev ? stalled + 1 : 0;
+        if (stalled >= 2) { status = -3; break; }
+    }
+    st->iterations = it;
+    st->outer = refinements;
+    const double rn = std::sqrt(rr_true);
+    st->rel_residual = bnorm > 0 ? rn / bnorm : rn;
+    st->status = bnorm == 0 ? 1 : status;
+    if (const unsigned er = amg_->level0_errors())
+        throw Error("level-0 smoother: a bounded wait of the streamed element matrices ran out (code " +
+                    std::to_string(er) + ")");
     st->smoother_ms = amg_->smoother_timer.collect(&st->smoother_launches);
     st->smoother_bytes = amg_->smoother_bytes();
     st->spmv_ms = spmv_timer_.collect(&st->spmv_launches);

@@ -123,6 +123,9 @@ public:
     int set_level0_operator(int kind);
     // multigrid: cycles of level+1 per coarse-grid correction at `level` (1 = V-cycle)
     void set_coarse_cycles(int level, int cycles);
+    // multigrid: Chebyshev degree and interval of level `level` >= 1 (Q2: level 1 is the Q1
+    // system; 0 = the hierarchy's default), applied from the next solve without a rebuild
+    void set_level_smoothing(int level, int degree, double lo);
     // Q2: apply the finest multigrid level element by element, by cell blocks (cell_blocks.h;
     // default: 4.3 vs 8.95 GB per smoothing step on config 2), or through the assembled SELL
     // matrix; the hierarchy is rebuilt at the next solve
@@ -195,6 +198,8 @@ private:
     int solve_plain(const SolveOptions& opt, SolveStats* st);
     int solve_mixed(const SolveOptions& opt, SolveStats* st);
     int solve_amg(const SolveOptions& opt, SolveStats* st);
+    int solve_amg_mixed(const SolveOptions& opt, SolveStats* st);
+    void prepare_amg(SolveStats* st);  // hierarchy on first use, per-level settings
     void run_cg(bool fp32, CgState* d_state, int max_iter, int chunk);
 
     FemStructure fs_;
@@ -209,6 +214,7 @@ private:
     bool profiling_ = false;
     int smooth_degree_ = 0;
     std::vector<int> coarse_cycles_;
+    std::vector<std::pair<int, double>> level_smooth_;  // per level (index 0 unused): degree, lo
     bool level0_stream_ = false;
     int level0_prefetch_ = 1;     // L2 prefetch one group ahead (measured best on config 2)
     int level0_geo_ = 2;          // requested level-0 operator source (set_level0_operator):

@@ -154,14 +154,17 @@ int fgb_field_setup(FGB_FIELD* f, double applied_field, double applied_potential
 /* PoissonSolver::assemble(full_run); anode_dirichlet selects anode_bc = dirichlet */
 int fgb_field_assemble(FGB_FIELD* f, int full_run, int anode_dirichlet);
 /* CG solve; precision 0 = plain FP64 Jacobi-PCG, 1 = FP32 inner + FP64 refinement,
- * 2 = FP64 CG preconditioned by an FP32 multigrid V-cycle (hierarchy built on first use).
- * inner_tol: residual reduction between FP64 refinements (<= 0: default 0.1).
+ * 2 = FP64 CG preconditioned by an FP32 multigrid V-cycle (hierarchy built on first use),
+ * 3 = FP32 CG with that V-cycle and its FP32 level-0 operator (for Q2 the matrix-free
+ * cell-block operator) inside FP64 iterative refinement on the assembled FP64 system.
+ * inner_tol: residual reduction between FP64 refinements (<= 0: default 0.1 for precision
+ * 1, 1e-3 for precision 3).
  * stats (may be NULL): iterations, refinements, status, rel_residual, bnorm, ms; a 7th slot
  * preset to -1 receives the device time of the solver kernel alone.
  * status: 1 converged; 2 converged to the FP64 floor (rel_tol below 1e-10 evaluates the true
  * residual compensated, and a solution whose residual is within twice 2^-53 |(|b| + |A||x|)|
  * is as accurate as an FP64 vector can be on that system); -1 iteration cap; -2 breakdown or
- * NaN; -3 FP64 refinements stopped reducing the residual (precision 1).
+ * NaN; -3 FP64 refinements stopped reducing the residual (precision 1 and 3).
  * Returns #iterations (>0) when the status is 1 or 2, else -#iterations. */
 int fgb_field_solve(FGB_FIELD* f, int precision, double rel_tol, double abs_tol, int max_iter, double inner_tol,
                     double* stats6);
@@ -188,8 +191,14 @@ int fgb_field_set_cell_blocks(FGB_FIELD* f, int cells_per_block, int max_dofs);
 double fgb_field_outer_spmv_bytes(const FGB_FIELD* f);
 /* Chebyshev smoothing of the finest multigrid level: steps before and after the coarse
  * correction (0: default, Q1 4, Q2 2) and the interval's lower end as a fraction of
- * lambda_max (0: default, Q1 0.04, Q2 0.1); the hierarchy is rebuilt at the next solve */
+ * lambda_max (0: default, Q1 0.04, Q2 0.06); the hierarchy is rebuilt at the next solve */
 int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo);
+/* Chebyshev smoothing of a coarser multigrid level `level` >= 1 (Q2 fields: level 1 is the
+ * Q1 system of the same mesh, default degree 4 on [0.04, 1.1], and the aggregation levels
+ * below it degree 1; Q1 fields: the aggregation levels, default 3 on [0.06, 1.1]); degree 0 /
+ * lo 0 = the default. Applied from the next
+ * solve without rebuilding the hierarchy; the dense coarsest level is left alone */
+int fgb_field_set_level_smoothing(FGB_FIELD* f, int level, int degree, double lo);
 /* Q2 fields: element matrices of the full assembly on the tensor cores (1, default: per-cell
  * factors in FP64, error-free BF16 slices, tcgen05 products accumulated exactly in FP32, levels
  * combined as FP32 pairs into FP64) or on the FP32 pipe as FP32 hi/lo pairs (0) */

@@ -45,17 +45,18 @@ def test_assembled_system_matches_oracle(tip, anode):
     np.testing.assert_allclose(b, s.rhs, rtol=0, atol=1e-12 * np.abs(s.rhs).max())
 
 
-@pytest.mark.parametrize("precision", [0, 1, 2])
+@pytest.mark.parametrize("precision", [0, 1, 2, 3])
 @pytest.mark.parametrize("tol", [1e-9, 1e-12])
 def test_solve_matches_oracle(tip, precision, tol):
     m, f = tip
     f.setup(0.1)
     f.assemble(True, False)
     rc, st = f.solve(precision=precision, rel_tol=tol, max_iter=20000)
-    assert rc > 0 and st["status"] == 1
-    # the mixed solver stops on the true FP64 residual; the FP64 recursions on the
-    # recursive one, which drifts from the true residual by rounding
-    assert st["rel_residual"] <= tol * (1.05 if precision == 1 else 2.0)
+    # the refinement solvers (1, 3) stop on the true FP64 residual, 3 also at the FP64 floor
+    # (status 2); the FP64 recursions on the recursive one, which drifts by rounding
+    assert rc > 0 and st["status"] in ((1, 2) if precision == 3 else (1,)), st
+    if st["status"] == 1:
+        assert st["rel_residual"] <= tol * (1.05 if precision in (1, 3) else 2.0)
     xyz, cells, v2n = vacuum_system_inputs(m)
     s = orc.System(xyz, cells, 0.1)
     it, x = s.ssor_cg(1.2, 1e-13 * np.linalg.norm(s.rhs), 50000)
