@@ -108,7 +108,26 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
             }
         }
     phase("entity keys");
-    __gnu_parallel::sort(ek.begin(), ek.end());
+    // sort by (corner nodes, cell): buckets by the smallest corner node (atomic counts and
+    // cursors), then each bucket by the full key. The order is total (a cell has one record
+    // per entity), so the result is the comparison sort's at any thread count.
+    {
+        const size_t ne0 = ek.size();
+        const int n_nodes = (int)(X.size() / 3);
+        FGB_REQUIRE(ne0 < (size_t)INT32_MAX, "Q2 structure: too many edge and face records");
+        std::vector<int32_t> bstart(n_nodes + 1, 0);
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < (long long)ne0; ++i) __atomic_fetch_add(&bstart[ek[i].k[0] + 1], 1, __ATOMIC_RELAXED);
+        for (int v = 0; v < n_nodes; ++v) bstart[v + 1] += bstart[v];
+        std::vector<int32_t> cur(bstart.begin(), bstart.end() - 1);
+        std::vector<EntityKey> sorted(ne0);
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < (long long)ne0; ++i)
+            sorted[__atomic_fetch_add(&cur[ek[i].k[0]], 1, __ATOMIC_RELAXED)] = ek[i];
+#pragma omp parallel for schedule(dynamic, 2048)
+        for (int v = 0; v < n_nodes; ++v) std::sort(sorted.begin() + bstart[v], sorted.begin() + bstart[v + 1]);
+        ek.swap(sorted);
+    }
     phase("entity sort");
     // runs of equal keys in the sorted list are one entity each, numbered in order: run heads
     // flagged and counted per thread block of the list, an exclusive scan over the blocks, then
@@ -150,45 +169,49 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
             ent_first[r] = 27 * ek[i].cell + ek[i].local;
         }
     }
-    ek.clear();
-    ek.shrink_to_fit();
     const int n_ent = nvx + n_shared + nc;
     for (int c = 0; c < nc; ++c) ent[27 * (size_t)c + 13] = nvx + n_shared + c;
     fs.n_dofs = n_ent;
 
     phase("entity ids");
-    // entity -> cells
-    // counting sort of the (cell, L) items by entity, stable in item order: per-thread counts
-    // over contiguous item ranges, offsets (entity, thread) in that order, then the fills
+    // entity -> cells: the (cell, L) items of each entity in ascending item order, entities in
+    // id order (vertices, edges and faces, interiors). Vertices: a counting sort of the 8 corner
+    // items per cell. Edges and faces: the runs of the sorted records, which are already in
+    // (entity, cell) order. Interiors: one item per cell.
     std::vector<int32_t> e2c_ptr(n_ent + 1, 0);
     std::vector<int32_t> e2c(ent.size());
     {
-        const int nt = std::max(1, std::min(omp_get_max_threads(), 16));
-        const size_t ni = ent.size();
-        std::vector<int32_t> cnt((size_t)nt * n_ent, 0);
-#pragma omp parallel num_threads(nt)
+        int corner_L[8], nl = 0;
+        for (int L = 0; L < 27; ++L)
+            if (n_corner[L] == 1) corner_L[nl++] = L;
+        FGB_REQUIRE(nl == 8, "Q2 lattice: 8 corner nodes per cell");
+        for (int c = 0; c < nc; ++c)
+            for (int j = 0; j < 8; ++j) e2c_ptr[ent[27 * (size_t)c + corner_L[j]] + 1]++;
+        for (int v = 0; v < nvx; ++v) e2c_ptr[v + 1] += e2c_ptr[v];
+        const int64_t nv_items = e2c_ptr[nvx];
+        FGB_REQUIRE(nv_items == 8 * (int64_t)nc, "Q2 structure: vertex items");
         {
-            const int t = omp_get_thread_num();
-            int32_t* ct = &cnt[(size_t)t * n_ent];
-            for (size_t i = ni * t / nt; i < ni * (t + 1) / nt; ++i) ct[ent[i]]++;
+            std::vector<int32_t> cur(e2c_ptr.begin(), e2c_ptr.begin() + nvx);
+            for (int c = 0; c < nc; ++c)
+                for (int j = 0; j < 8; ++j) {
+                    const int32_t item = 27 * c + corner_L[j];
+                    e2c[cur[ent[item]]++] = item;
+                }
         }
-        int64_t run = 0;
-        for (int e = 0; e < n_ent; ++e) {
-            e2c_ptr[e] = (int32_t)run;
-            for (int t = 0; t < nt; ++t) {
-                const int32_t c = cnt[(size_t)t * n_ent + e];
-                cnt[(size_t)t * n_ent + e] = (int32_t)run;
-                run += c;
-            }
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < (long long)ne; ++i) {
+            e2c[nv_items + i] = 27 * ek[i].cell + ek[i].local;
+            if (i == 0 || run_id[i - 1] != run_id[i]) e2c_ptr[nvx + run_id[i]] = (int32_t)(nv_items + i);
         }
-        e2c_ptr[n_ent] = (int32_t)run;
-#pragma omp parallel num_threads(nt)
-        {
-            const int t = omp_get_thread_num();
-            int32_t* ot = &cnt[(size_t)t * n_ent];
-            for (size_t i = ni * t / nt; i < ni * (t + 1) / nt; ++i) e2c[ot[ent[i]]++] = (int32_t)i;
+#pragma omp parallel for schedule(static)
+        for (int c = 0; c < nc; ++c) {
+            e2c_ptr[nvx + n_shared + c] = (int32_t)(nv_items + (int64_t)ne + c);
+            e2c[nv_items + ne + c] = 27 * c + 13;
         }
+        e2c_ptr[n_ent] = (int32_t)(nv_items + (int64_t)ne + nc);
     }
+    ek.clear();
+    ek.shrink_to_fit();
     phase("entity -> cells");
     // entity -> its first (cell, L) in item order (the head of its stable list) and position
     std::vector<int32_t> e_cell(n_ent, -1);
