@@ -867,10 +867,12 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
         if (l == 0) lv->tpr = 0;
         if (l < L - 1) {
             lv->n_coarse = hl.P.n_cols;
-            upload_csr32(hl.P, lv->p_ptr, lv->p_col, lv->p_val, stream);
-            upload_csr32(hl.R, lv->r_ptr, lv->r_col, lv->r_val, stream);
-            lv->p_tpr = transfer_tpr((double)hl.P.nnz() / std::max(1, hl.P.n_rows));
-            lv->r_tpr = transfer_tpr((double)hl.R.nnz() / std::max(1, hl.R.n_rows));
+            if (!hl.transfers_on_device) {
+                upload_csr32(hl.P, lv->p_ptr, lv->p_col, lv->p_val, stream);
+                upload_csr32(hl.R, lv->r_ptr, lv->r_col, lv->r_val, stream);
+                lv->p_tpr = transfer_tpr((double)hl.P.nnz() / std::max(1, hl.P.n_rows));
+                lv->r_tpr = transfer_tpr((double)hl.R.nnz() / std::max(1, hl.R.n_rows));
+            }
         }
         lv->b.resize(lv->n);
         lv->xa.resize(lv->n);
@@ -903,6 +905,22 @@ void AmgDevice::set_level_smoothing(int level, int degree, double lo) {
     AmgDevLevel& L = *lv_[level];
     L.cheb_degree = degree > 0 ? degree : L.built_degree;
     L.cheb_lo = lo > 0 ? lo : L.built_lo;
+}
+
+void AmgDevice::adopt_transfers(int level, DBuf<int64_t>&& p_ptr, DBuf<int32_t>&& p_col, DBuf<float>&& p_val,
+                                DBuf<int64_t>&& r_ptr, DBuf<int32_t>&& r_col, DBuf<float>&& r_val, int64_t nnz) {
+    FGB_REQUIRE(level >= 0 && level + 1 < (int)lv_.size(), "transfers: a level with a coarser one");
+    AmgDevLevel& L = *lv_[level];
+    FGB_REQUIRE(p_ptr.size() == (size_t)L.n + 1 && r_ptr.size() == (size_t)L.n_coarse + 1,
+                "transfers: row pointers of P (fine rows) and R (coarse rows)");
+    L.p_ptr = std::move(p_ptr);
+    L.p_col = std::move(p_col);
+    L.p_val = std::move(p_val);
+    L.r_ptr = std::move(r_ptr);
+    L.r_col = std::move(r_col);
+    L.r_val = std::move(r_val);
+    L.p_tpr = transfer_tpr((double)nnz / std::max(1, L.n));
+    L.r_tpr = transfer_tpr((double)nnz / std::max(1, L.n_coarse));
 }
 
 int AmgDevice::n_levels() const { return (int)lv_.size(); }

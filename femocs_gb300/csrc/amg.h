@@ -30,6 +30,9 @@ struct AmgHostLevel {
     double lambda = 1.0;  // estimate of the largest eigenvalue of D^-1 A
     int cheb_degree = 3;  // Chebyshev smoothing steps before and after the coarse correction
     double cheb_lo = 0.06; // smoothing interval [cheb_lo, 1.1] x lambda
+    // P and R were built on the device and are handed over with AmgDevice::adopt_transfers
+    // (P.n_rows / P.n_cols give the shape; the host arrays stay empty)
+    bool transfers_on_device = false;
 };
 
 struct AmgHost {
@@ -129,6 +132,10 @@ public:
     // Chebyshev degree and interval of one level's smoother (0: the hierarchy's own choice);
     // only the polynomial changes, nothing is rebuilt (the coarsest level is solved densely)
     void set_level_smoothing(int level, int degree, double lo);
+    // prolongation P (rows of this level) and restriction R (rows of the next) of `level`,
+    // built on the device in CSR with FP32 values; the hierarchy takes ownership
+    void adopt_transfers(int level, DBuf<int64_t>&& p_ptr, DBuf<int32_t>&& p_col, DBuf<float>&& p_val,
+                         DBuf<int64_t>&& r_ptr, DBuf<int32_t>&& r_col, DBuf<float>&& r_val, int64_t nnz);
 
 private:
     void cycle(int l);

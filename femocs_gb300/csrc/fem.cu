@@ -1519,39 +1519,26 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     for (size_t l = 1; l < h1.levels.size(); ++l) h1.levels[l].cheb_degree = 1;
     h1.levels[0].A.col = f1.col;
     h1.levels[0].A.val = std::move(v1);
-    // embedding: a free Q2 DoF takes the mean of the free Q1 values at its entity's corners
-    CsrD P;
-    P.n_rows = n_;
-    P.n_cols = f1.n_dofs;
-    P.ptr.assign(n_ + 1, 0);
-    // two passes (count, fill) over the rows in parallel; the row order fixes the layout
-    auto embed_row = [&](int d, int32_t* col, double* val) {
-        const bool fixed = fs_.bc_kind[d] == 1 || (anode && fs_.bc_kind[d] == 2);
-        if (fixed) return 0;
-        int cr[8];
-        const int nk = q2_entity_corners(fs_.dof_local[d], cr);
-        const int hex = pm_->vac.cells[fs_.dof_cell[d]];
-        int m = 0;
-        for (int q = 0; q < nk; ++q) {
-            const int v = f1.node2dof[pm_->hex.hexs[8 * (size_t)hex + cr[q]]];
-            if (v >= 0 && !fixed1[v]) {
-                if (col) {
-                    col[m] = v;
-                    val[m] = 1.0 / nk;
-                }
-                ++m;
-            }
+    // embedding P (a free Q2 DoF takes the mean of the free Q1 values at its entity's corners)
+    // and R = P^T, built on the device from the Q1 DoFs of the cell corners
+    DeviceCsr32 Pd, Rd;
+    {
+        std::vector<int32_t> cq1(8 * (size_t)nc_);
+#pragma omp parallel for schedule(static)
+        for (int c = 0; c < nc_; ++c) {
+            const size_t hex = (size_t)pm_->vac.cells[c];
+            for (int k = 0; k < 8; ++k) cq1[8 * (size_t)c + k] = f1.node2dof[pm_->hex.hexs[8 * hex + k]];
         }
-        return m;
-    };
-#pragma omp parallel for schedule(static)
-    for (int d = 0; d < n_; ++d) P.ptr[d + 1] = embed_row(d, nullptr, nullptr);
-    for (int d = 0; d < n_; ++d) P.ptr[d + 1] += P.ptr[d];
-    P.col.resize(P.ptr[n_]);
-    P.val.resize(P.ptr[n_]);
-#pragma omp parallel for schedule(static)
-    for (int d = 0; d < n_; ++d) embed_row(d, &P.col[P.ptr[d]], &P.val[P.ptr[d]]);
-    phase("embedding P");
+        DBuf<int32_t> d_cq1, d_cell;
+        DBuf<int8_t> d_loc, d_fixed1;
+        d_cq1.upload(cq1, stream_);
+        d_cell.upload(fs_.dof_cell, stream_);
+        d_loc.upload(fs_.dof_local, stream_);
+        d_fixed1.upload(fixed1, stream_);
+        q2_embedding(n_, f1.n_dofs, d_cell.get(), d_loc.get(), d_cq1.get(), fixed_.get(), d_fixed1.get(), Pd, Rd,
+                     stream_);
+    }
+    phase("embedding P, R = P^T (device)");
     AmgHost h;
     AmgHostLevel l0;
     l0.A.n_rows = l0.A.n_cols = n_;
@@ -1563,57 +1550,19 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     l0.cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 2;
     l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.06;
     phase("lambda_max (device)");
-    l0.R.n_rows = P.n_cols;
-    l0.R.n_cols = P.n_rows;
-    {
-        // R = P^T, rows of R in ascending P row order: each thread transposes a contiguous
-        // block of P rows into offsets counted per (column, block), so the result equals the
-        // sequential transpose
-        const int nt = std::max(1, omp_get_max_threads());
-        const int ncol = P.n_cols;
-        std::vector<int64_t> cnt((size_t)nt * ncol + 1, 0);  // [block][column]
-#pragma omp parallel num_threads(nt)
-        {
-            const int t = omp_get_thread_num();
-            const int r0 = (int)((int64_t)P.n_rows * t / nt), r1 = (int)((int64_t)P.n_rows * (t + 1) / nt);
-            int64_t* c = &cnt[(size_t)t * ncol];
-            for (int64_t k = P.ptr[r0]; k < P.ptr[r1]; ++k) c[P.col[k]]++;
-        }
-        l0.R.ptr.assign(ncol + 1, 0);
-        // column-major prefix over (column, block)
-        std::vector<int64_t> off((size_t)nt * ncol);
-        int64_t run = 0;
-        for (int c = 0; c < ncol; ++c) {
-            l0.R.ptr[c] = run;
-            for (int t = 0; t < nt; ++t) {
-                off[(size_t)t * ncol + c] = run;
-                run += cnt[(size_t)t * ncol + c];
-            }
-        }
-        l0.R.ptr[ncol] = run;
-        l0.R.col.resize(P.nnz());
-        l0.R.val.resize(P.nnz());
-#pragma omp parallel num_threads(nt)
-        {
-            const int t = omp_get_thread_num();
-            const int r0 = (int)((int64_t)P.n_rows * t / nt), r1 = (int)((int64_t)P.n_rows * (t + 1) / nt);
-            int64_t* o = &off[(size_t)t * ncol];
-            for (int i = r0; i < r1; ++i)
-                for (int64_t k = P.ptr[i]; k < P.ptr[i + 1]; ++k) {
-                    const int64_t q = o[P.col[k]]++;
-                    l0.R.col[q] = i;
-                    l0.R.val[q] = P.val[k];
-                }
-        }
-    }
-    phase("R = P^T");
-    l0.P = std::move(P);
+    l0.P.n_rows = n_;
+    l0.P.n_cols = f1.n_dofs;
+    l0.R.n_rows = f1.n_dofs;
+    l0.R.n_cols = n_;
+    l0.transfers_on_device = true;
     h.levels.push_back(std::move(l0));
     for (auto& lv : h1.levels) h.levels.push_back(std::move(lv));
     h.coarse_inv = std::move(h1.coarse_inv);
     h.n_coarse = h1.n_coarse;
     amg_.reset(new AmgDevice(h, stream_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell32_.get(),
                              dinv32_.get()));
+    amg_->adopt_transfers(0, std::move(Pd.ptr), std::move(Pd.col), std::move(Pd.val), std::move(Rd.ptr),
+                          std::move(Rd.col), std::move(Rd.val), Pd.nnz);
     if (level0_ebe_) {
         if (ke32_.size() != 378 * (size_t)nc_) refresh_ke32();
         CellBlocksDev& c = *cb_;

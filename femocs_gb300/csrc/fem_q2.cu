@@ -25,6 +25,7 @@
 #include <cuda_fp16.h>
 
 #include "fem_q2.h"
+#include "dprim.cuh"
 
 namespace fgb {
 
@@ -439,6 +440,61 @@ __global__ void k_q2_geo(long long total, const int32_t* __restrict__ perm, cons
     }
 }
 
+// lattice corners of each local node's entity (1, 2, 4 or 8) as a by-value kernel argument
+struct CornerTab {
+    int8_t c[27][8];
+    int8_t n[27];
+};
+
+// one Q2 DoF per thread: count pass (ptr == nullptr: cnt[d] = entries of row d) or fill pass
+__global__ void k_embed_rows(int n, const int32_t* __restrict__ dof_cell, const int8_t* __restrict__ dof_local,
+                             const int32_t* __restrict__ cq1, const int8_t* __restrict__ fixed2,
+                             const int8_t* __restrict__ fixed1, CornerTab tab, const int64_t* __restrict__ ptr,
+                             int64_t* __restrict__ cnt, int32_t* __restrict__ col, float* __restrict__ val,
+                             int32_t* __restrict__ rowof) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    int m = 0;
+    if (!fixed2[d]) {
+        const int L = dof_local[d];
+        const int64_t c = dof_cell[d];
+        const int nk = tab.n[L];
+        for (int q = 0; q < nk; ++q) {
+            const int v = cq1[8 * c + tab.c[L][q]];
+            if (v >= 0 && !fixed1[v]) {
+                if (ptr) {
+                    const int64_t k = ptr[d] + m;
+                    col[k] = v;
+                    val[k] = 1.f / (float)nk;  // nk is 1, 2, 4 or 8: exact
+                    rowof[k] = d;
+                }
+                ++m;
+            }
+        }
+    }
+    if (!ptr) cnt[d] = m;
+}
+
+__global__ void k_iota32(int64_t n, int32_t* __restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (int32_t)i;
+}
+
+__global__ void k_count_cols(int64_t n, const int32_t* __restrict__ col, int64_t* __restrict__ cnt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(reinterpret_cast<unsigned long long*>(cnt + col[i]), 1ull);
+}
+
+// R entry j: the P entry idx[j] (sorted by column, ascending P position within a column)
+__global__ void k_transpose_fill(int64_t n, const int32_t* __restrict__ idx, const int32_t* __restrict__ rowof,
+                                 const float* __restrict__ pval, int32_t* __restrict__ rcol, float* __restrict__ rval) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int32_t k = idx[j];
+    rcol[j] = rowof[k];
+    rval[j] = pval[k];
+}
+
 }  // namespace
 
 void q2_geometric_factors(long long n_pos, const int32_t* perm, const int32_t* cell_dofs, const double* dof_xyz,
@@ -503,6 +559,61 @@ void sell_dirichlet(int n, const int64_t* sptr, const int32_t* scol, const int32
                     double* rhs, double* x, cudaStream_t s) {
     FGB_LAUNCH(k_sell_dirichlet<<<grid_for(n, 256), 256, 0, s>>>(n, sptr, scol, row_len, kval, bc, anode, v0, s64, s32,
                                                                  dinv64, dinv32, rhs, x));
+}
+
+void q2_embedding(int n, int n1, const int32_t* dof_cell, const int8_t* dof_local, const int32_t* cq1,
+                  const int8_t* fixed2, const int8_t* fixed1, DeviceCsr32& P, DeviceCsr32& R, cudaStream_t s) {
+    CornerTab tab;
+    for (int L = 0; L < 27; ++L) {
+        int cr[8];
+        const int nk = q2_entity_corners(L, cr);
+        tab.n[L] = (int8_t)nk;
+        for (int q = 0; q < 8; ++q) tab.c[L][q] = (int8_t)(q < nk ? cr[q] : 0);
+    }
+    const int nb = 256;
+    // P: row counts, their scan, the fill
+    P.n_rows = n;
+    P.n_cols = n1;
+    P.ptr.resize((size_t)n + 1);
+    {
+        dprim::SBuf<int64_t> cnt((size_t)n + 1, s);
+        FGB_CUDA(cudaMemsetAsync(cnt.get() + n, 0, sizeof(int64_t), s));
+        if (n) FGB_LAUNCH(k_embed_rows<<<(n + nb - 1) / nb, nb, 0, s>>>(n, dof_cell, dof_local, cq1, fixed2, fixed1, tab,
+                                                                       nullptr, cnt.get(), nullptr, nullptr, nullptr));
+        P.nnz = dprim::exclusive_scan_total<int64_t>(cnt.get(), P.ptr.get(), (int64_t)n + 1, s);
+    }
+    FGB_REQUIRE(P.nnz < (int64_t)INT32_MAX, "Q2 embedding: too many entries");
+    const int64_t nz = P.nnz;
+    P.col.resize(std::max<int64_t>(nz, 1));
+    P.val.resize(std::max<int64_t>(nz, 1));
+    dprim::SBuf<int32_t> rowof(std::max<int64_t>(nz, 1), s);
+    if (n) FGB_LAUNCH(k_embed_rows<<<(n + nb - 1) / nb, nb, 0, s>>>(n, dof_cell, dof_local, cq1, fixed2, fixed1, tab,
+                                                                   P.ptr.get(), nullptr, P.col.get(), P.val.get(),
+                                                                   rowof.get()));
+    // R = P^T: the entries sorted by column with a stable radix sort (so ascending P position,
+    // i.e. ascending row, within a column), row pointers from per-column counts
+    R.n_rows = n1;
+    R.n_cols = n;
+    R.nnz = nz;
+    R.ptr.resize((size_t)n1 + 1);
+    R.col.resize(std::max<int64_t>(nz, 1));
+    R.val.resize(std::max<int64_t>(nz, 1));
+    {
+        dprim::SBuf<int64_t> cnt((size_t)n1 + 1, s);
+        cnt.fill_bytes(0);
+        const unsigned g = (unsigned)((nz + nb - 1) / nb);
+        if (nz) FGB_LAUNCH(k_count_cols<<<g, nb, 0, s>>>(nz, P.col.get(), cnt.get()));
+        dprim::exclusive_scan<int64_t>(cnt.get(), R.ptr.get(), (int64_t)n1 + 1, nullptr, s);
+        if (nz) {
+            dprim::SBuf<uint32_t> keys(nz, s);
+            dprim::SBuf<int32_t> idx(nz, s);
+            FGB_CUDA(cudaMemcpyAsync(keys.get(), P.col.get(), sizeof(int32_t) * nz, cudaMemcpyDeviceToDevice, s));
+            FGB_LAUNCH(k_iota32<<<g, nb, 0, s>>>(nz, idx.get()));
+            dprim::radix_sort<uint32_t>(keys, &idx, nz, dprim::bits_for((uint64_t)std::max(1, n1 - 1)), s);
+            FGB_LAUNCH(k_transpose_fill<<<g, nb, 0, s>>>(nz, idx.get(), rowof.get(), P.val.get(), R.col.get(), R.val.get()));
+        }
+    }
+    FGB_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace fgb

@@ -35,6 +35,20 @@ void q2_assemble_rows(int n, int max_len, const int64_t* sptr, const int32_t* sc
                       double* kval, cudaStream_t s);
 void q2_neumann_rows(int n, const int32_t* r2f_ptr, const int32_t* r2f_item, const int32_t* top, const double* dof_xyz,
                      double bc, const double* extra, double* rhs, cudaStream_t s);
+// CSR matrix with FP32 values on the device
+struct DeviceCsr32 {
+    DBuf<int64_t> ptr;
+    DBuf<int32_t> col;
+    DBuf<float> val;
+    int n_rows = 0, n_cols = 0;
+    int64_t nnz = 0;
+};
+// Q2 -> Q1 embedding on the device: row d of P holds the free Q1 DoFs at the corners of the
+// entity of Q2 DoF d (corners in the lattice order of its cell dof_cell[d], weight
+// 1 / #corners); rows of fixed Q2 DoFs are empty. cq1 = the Q1 DoF of each cell corner (8 per
+// cell, -1: none). R = P^T with each row in ascending P-row order.
+void q2_embedding(int n, int n1, const int32_t* dof_cell, const int8_t* dof_local, const int32_t* cq1,
+                  const int8_t* fixed2, const int8_t* fixed1, DeviceCsr32& P, DeviceCsr32& R, cudaStream_t s);
 // symmetric Dirichlet elimination on a SELL-layout matrix (any element order)
 void sell_dirichlet(int n, const int64_t* sptr, const int32_t* scol, const int32_t* row_len, const double* kval,
                     const int8_t* bc, int anode, double v0, double* s64, float* s32, double* dinv64, float* dinv32,
