@@ -833,6 +833,13 @@ AmgDevice::AmgDevice(const AmgHost& h, cudaStream_t stream, const int64_t* l0_sp
             lv->scol = l0_scol;
             lv->val = l0_val;
             lv->dinv = l0_dinv;
+        } else if (l < L - 1 && hl.dev_val) {
+            lv->sptr = hl.dev_sptr;
+            lv->slen = hl.dev_slen;
+            lv->scol = hl.dev_scol;
+            lv->val = hl.dev_val;
+            lv->dinv = hl.dev_dinv;
+            lv->tpr = 0;
         } else if (l < L - 1) {
             std::vector<float> di(lv->n, 1.f);
 #pragma omp parallel for schedule(static)

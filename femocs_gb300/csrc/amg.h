@@ -33,6 +33,14 @@ struct AmgHostLevel {
     // P and R were built on the device and are handed over with AmgDevice::adopt_transfers
     // (P.n_rows / P.n_cols give the shape; the host arrays stay empty)
     bool transfers_on_device = false;
+    // operator already on the device as SELL-32 with 4-wide chunks (FP32 values, the
+    // eliminated FP64 matrix rounded, and its FP32 inverse diagonal), owned by the caller and
+    // alive as long as the hierarchy: used instead of packing and uploading A
+    const int64_t* dev_sptr = nullptr;
+    const int32_t* dev_slen = nullptr;
+    const int32_t* dev_scol = nullptr;
+    const float* dev_val = nullptr;
+    const float* dev_dinv = nullptr;
 };
 
 struct AmgHost {

@@ -136,15 +136,25 @@ double lambda_max(const CsrRef& A, int iters = 15) {
         x[i] = (double)((s >> 11) & 0xfffff) / 1048576.0 - 0.5;
     }
     double lam = 1.0;
+    // ||y||^2 from partial sums over fixed chunks of rows, added in chunk order: the same
+    // value at any thread count and schedule
+    constexpr int kChunk = 4096;
+    const int nch = (n + kChunk - 1) / kChunk;
+    std::vector<double> part(nch);
     for (int it = 0; it < iters; ++it) {
-        double nrm = 0.0;
-#pragma omp parallel for reduction(+ : nrm) schedule(static)
-        for (int i = 0; i < n; ++i) {
-            double acc = 0.0;
-            for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) acc += A.val[k] * x[A.col[k]];
-            y[i] = acc / d[i];
-            nrm += y[i] * y[i];
+#pragma omp parallel for schedule(static)
+        for (int ch = 0; ch < nch; ++ch) {
+            double sq = 0.0;
+            for (int i = ch * kChunk; i < std::min(n, (ch + 1) * kChunk); ++i) {
+                double acc = 0.0;
+                for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) acc += A.val[k] * x[A.col[k]];
+                y[i] = acc / d[i];
+                sq += y[i] * y[i];
+            }
+            part[ch] = sq;
         }
+        double nrm = 0.0;
+        for (int ch = 0; ch < nch; ++ch) nrm += part[ch];
         nrm = std::sqrt(nrm);
         if (nrm == 0) return 1.0;
         double xn = 0.0;

@@ -1509,16 +1509,10 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     for (int d = 0; d < f1.n_dofs; ++d) fixed1[d] = f1.bc_kind[d] == 1 || (anode && f1.bc_kind[d] == 2);
     AmgOptions ao1;
     ao1.level0_lambda = q1_->estimate_lambda(15, kAmgLambdaSeed);
+    // (built on a second host thread while the device worked on the embedding, the hierarchy
+    // took longer than the device work saved: two OpenMP teams on the same cores)
     AmgHost h1 = build_amg(*pm_, f1, v1, fixed1, ao1);
     phase("Q1 hierarchy (host)");
-    // the Q1 level is the coarse solve of the Q2 level: smooth it harder
-    h1.levels[0].cheb_degree = 4;
-    h1.levels[0].cheb_lo = 0.04;
-    // below it one Chebyshev step per side is enough: config 2 keeps its 96 PCG iterations
-    // (618 -> 609 ms per solve); degree 2 or 3 there, or 3 or 6 at the Q1 level, cost more
-    for (size_t l = 1; l < h1.levels.size(); ++l) h1.levels[l].cheb_degree = 1;
-    h1.levels[0].A.col = f1.col;
-    h1.levels[0].A.val = std::move(v1);
     // embedding P (a free Q2 DoF takes the mean of the free Q1 values at its entity's corners)
     // and R = P^T, built on the device from the Q1 DoFs of the cell corners
     DeviceCsr32 Pd, Rd;
@@ -1550,6 +1544,21 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     l0.cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 2;
     l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.06;
     phase("lambda_max (device)");
+    // the Q1 level is the coarse solve of the Q2 level: smooth it harder
+    h1.levels[0].cheb_degree = 4;
+    h1.levels[0].cheb_lo = 0.04;
+    // below it one Chebyshev step per side is enough: config 2 keeps its 96 PCG iterations
+    // (618 -> 609 ms per solve); degree 2 or 3 there, or 3 or 6 at the Q1 level, cost more
+    for (size_t l = 1; l < h1.levels.size(); ++l) h1.levels[l].cheb_degree = 1;
+    h1.levels[0].A.col = f1.col;
+    h1.levels[0].A.val = std::move(v1);
+    // the Q1 level applies the Q1 system's own device SELL matrix (the same FP32 values and
+    // layout the hierarchy would pack and upload)
+    h1.levels[0].dev_sptr = q1_->slice_ptr_.get();
+    h1.levels[0].dev_slen = q1_->slice_len_.get();
+    h1.levels[0].dev_scol = q1_->sell_col_.get();
+    h1.levels[0].dev_val = q1_->sell32_.get();
+    h1.levels[0].dev_dinv = q1_->dinv32_.get();
     l0.P.n_rows = n_;
     l0.P.n_cols = f1.n_dofs;
     l0.R.n_rows = f1.n_dofs;
