@@ -138,7 +138,7 @@ double lambda_max(const CsrRef& A, int iters = 15) {
     double lam = 1.0;
     // ||y||^2 from partial sums over fixed chunks of rows, added in chunk order: the same
     // value at any thread count and schedule
-    constexpr int kChunk = 4096;
+    constexpr int kChunk = 256;  // coarse levels have a few thousand dense-ish rows
     const int nch = (n + kChunk - 1) / kChunk;
     std::vector<double> part(nch);
     for (int it = 0; it < iters; ++it) {
