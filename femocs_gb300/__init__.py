@@ -266,6 +266,11 @@ class Field:
         """Chebyshev degree and interval of the finest multigrid level (0: defaults)."""
         self._ok(load().fgb_field_set_smoothing(self.h, int(degree), float(lo)))
 
+    def set_lazy_matrix(self, on=True):
+        """Q2: form the assembled SELL matrices only when something reads them (default) or
+        at every assembly (False); results are the same."""
+        self._ok(load().fgb_field_set_lazy_matrix(self.h, int(bool(on))))
+
     def set_level_smoothing(self, level, degree=0, lo=0.0):
         """Chebyshev degree and interval of coarser multigrid level `level` >= 1 (Q2: level 1
         is the Q1 system); 0 restores the default, from the next solve, without a rebuild."""

@@ -100,6 +100,7 @@ _PROTOS = {
     "fgb_field_export_element_matrices": (C.c_longlong, [vp, dp]),
     "fgb_field_set_smoothing": (C.c_int, [vp, C.c_int, C.c_double]),
     "fgb_field_set_level_smoothing": (C.c_int, [vp, C.c_int, C.c_int, C.c_double]),
+    "fgb_field_set_lazy_matrix": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_level0_ebe": (C.c_int, [vp, C.c_int]),
     "fgb_field_set_outer_spmv": (C.c_int, [vp, C.c_int]),
     "fgb_field_outer_spmv_bytes": (C.c_double, [vp]),

@@ -488,6 +488,9 @@ int fgb_field_set_level0_prefetch(FGB_FIELD* f, int cells) {
 int fgb_field_set_coarse_cycles(FGB_FIELD* f, int level, int cycles) {
     return guarded([&] { f->f->fem().set_coarse_cycles(level, cycles); return 0; });
 }
+int fgb_field_set_lazy_matrix(FGB_FIELD* f, int on) {
+    return guarded([&] { f->f->fem().set_lazy_matrix(on != 0); return 0; });
+}
 int fgb_field_set_level_smoothing(FGB_FIELD* f, int level, int degree, double lo) {
     return guarded([&] { f->f->fem().set_level_smoothing(level, degree, lo); return 0; });
 }

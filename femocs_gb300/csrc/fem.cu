@@ -832,6 +832,7 @@ struct CbSpmvArgs {
     float2* pair;   // partial (hi, lo) sums of the split DoFs, one per slot
     double* dot;    // p.q partials: one per block, then one per CTA of the finishing kernel
 };
+
 constexpr int kCbT = 256;
 __host__ __device__ inline size_t cbdf_smem_bytes(int max_cells, int max_dofs) {
     return 56 * (size_t)max_cells + 8 * (size_t)max_dofs + 216 * (size_t)max_cells;
@@ -1149,6 +1150,7 @@ void FemDevice::setup(double applied_field, double applied_potential) {
     applied_field_ = applied_field;
     applied_potential_ = applied_potential;
     x_.zero(stream_);  // solution = dirichlet_bc_value (0), src/DealSolver.cpp:384
+    x_zero_ = true;
 }
 
 double* FemDevice::space_charge_buffer(bool accumulate) {
@@ -1191,8 +1193,12 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
                 q2_cell_stiffness_tc(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), tc_scratch_, tc_err_, stream_);
             else
                 q2_cell_stiffness(nc_, cell_dofs_.get(), dof_xyz_.get(), ke_.get(), stream_);
-            q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
-                             r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
+            kval_valid_ = false;
+            if (!lazy_matrix_) {
+                q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
+                                 r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
+                kval_valid_ = true;
+            }
             if (level0_ebe_ || outer_mode_ == 2) refresh_ke32();
         }
         fixed_.resize(n_);
@@ -1200,9 +1206,21 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
         const double bc = anode_dirichlet ? 0.0 : applied_field_;
         q2_neumann_rows(n_, r2f_ptr_.get(), r2f_item_.get(), top_faces_.get(), dof_xyz_.get(), bc,
                         has_extra_ ? rhs_extra_.get() : nullptr, rhs_.get(), stream_);
-        sell_dirichlet(n_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), kval_.get(), bc_.get(),
-                       anode_dirichlet ? 1 : 0, applied_potential_, sell64_.get(), sell32_.get(), dinv64_.get(),
-                       dinv32_.get(), rhs_.get(), x_.get(), stream_);
+        if (lazy_matrix_ && (!anode_dirichlet || applied_potential_ == 0.0)) {
+            q2_dirichlet_zero(n_, r2c_ptr_.get(), r2c_item_.get(), ke_.get(), bc_.get(), anode_dirichlet ? 1 : 0,
+                              dinv64_.get(), dinv32_.get(), rhs_.get(), x_.get(), stream_);
+            sell_valid_ = false;
+        } else {
+            if (!kval_valid_) {
+                q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
+                                 r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
+                kval_valid_ = true;
+            }
+            sell_dirichlet(n_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), kval_.get(), bc_.get(),
+                           anode_dirichlet ? 1 : 0, applied_potential_, sell64_.get(), sell32_.get(), dinv64_.get(),
+                           dinv32_.get(), rhs_.get(), x_.get(), stream_);
+            sell_valid_ = true;
+        }
         FGB_CUDA(cudaGetLastError());
         return;
     }
@@ -1240,12 +1258,49 @@ void FemDevice::assemble_q1_rows(bool matrix, bool anode_dirichlet) {
     FGB_CUDA(cudaGetLastError());
 }
 
+void FemDevice::ensure_sell() {
+    if (fs_.order != 2 || sell_valid_) return;
+    if (!kval_valid_) {
+        q2_assemble_rows(n_, max_row_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), r2c_ptr_.get(),
+                         r2c_item_.get(), cell_dofs_.get(), ke_.get(), kval_.get(), stream_);
+        kval_valid_ = true;
+    }
+    // the eliminated values only: D^-1, the right-hand side and x are those of the assembly
+    sell_dirichlet(n_, slice_ptr_.get(), sell_col_.get(), row_len_.get(), kval_.get(), bc_.get(),
+                   anode_dirichlet_ ? 1 : 0, applied_potential_, sell64_.get(), sell32_.get(), nullptr, nullptr,
+                   nullptr, nullptr, stream_);
+    sell_valid_ = true;
+    split_valid_ = false;
+}
+
+double FemDevice::cells_true_residual() {
+    FGB_REQUIRE(fs_.order == 2, "residual from element matrices: Q2 fields");
+    if (res_state_.size() != 1) res_state_.resize(1);
+    CgState* rs = res_state_.get();
+    FGB_CUDA(cudaMemsetAsync(rs, 0, sizeof(CgState), stream_));
+    cell_y_.resize(27 * (size_t)nc_);
+    q2_residual_cells(n_, nc_, r2c_ptr_.get(), r2c_item_.get(), cell_dofs_.get(), ke_.get(), fixed_.get(),
+                      dinv64_.get(), x_.get(), rhs_.get(), cell_y_.get(), r64_.get(), stream_);
+    FGB_LAUNCH(k_norm2<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, r64_.get(), partial_.get(), rs));
+    CgState h{};
+    FGB_CUDA(cudaMemcpyAsync(&h, rs, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+    FGB_CUDA(cudaStreamSynchronize(stream_));
+    return h.rr;
+}
+
+void FemDevice::set_lazy_matrix(bool on) {
+    if (!on) ensure_sell();
+    lazy_matrix_ = on;
+}
+
 void FemDevice::spmv64(const double* x, double* y) {
+    ensure_sell();
     FGB_LAUNCH(k_sell_spmv<double><<<grid_for(n_, kBlock), kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
                                                                       sell64_.get(), x, y));
 }
 
 double FemDevice::time_spmv(int precision, int reps) {
+    ensure_sell();
     if (precision == 2) {
         ensure_amg(nullptr);
         return amg_->time_smoother(reps);
@@ -1278,6 +1333,7 @@ double FemDevice::time_spmv(int precision, int reps) {
 }
 
 void FemDevice::download_matrix(std::vector<double>& vals, std::vector<double>& rhs) {
+    ensure_sell();
     // CSR order values after Dirichlet elimination, gathered back from the SELL layout
     std::vector<double> s = sell64_.to_host(stream_);
     // row r's CSR entries start at off[r] (Q1: the structure's row pointer; Q2: the prefix of
@@ -1328,16 +1384,22 @@ void FemDevice::run_cg(bool fp32, CgState* d_state, int max_iter, int chunk) {
     FGB_CUDA(cudaGetLastError());
 }
 
+static int compensated_residual(const SolveOptions& opt);
+
 int FemDevice::solve(const SolveOptions& opt, SolveStats* st) {
     SolveStats local;
     if (!st) st = &local;
     *st = SolveStats();
     FGB_CUDA(cudaEventRecord(ev0_, stream_));
     FGB_REQUIRE(opt.precision >= 0 && opt.precision <= 3, "precision 0..3");
+    // the multigrid PCG over the cell blocks takes its FP64 true residual from the element
+    // matrices when the assembled matrix is not current; everything else reads that matrix
+    if (opt.precision != 2 || outer_mode_ != 2 || !level0_ebe_ || compensated_residual(opt)) ensure_sell();
     int rc = opt.precision == 0   ? solve_plain(opt, st)
              : opt.precision == 1 ? solve_mixed(opt, st)
              : opt.precision == 2 ? solve_amg(opt, st)
                                   : solve_amg_mixed(opt, st);
+    x_zero_ = false;
     FGB_CUDA(cudaEventRecord(ev1_, stream_));
     FGB_CUDA(cudaEventSynchronize(ev1_));
     float ms = 0;
@@ -1458,6 +1520,7 @@ void FemDevice::ensure_amg(SolveStats* st) {
 }
 
 double FemDevice::estimate_lambda(int iters, uint64_t seed) {
+    ensure_sell();
     // power iteration on D^-1 A from a fixed pseudo-random start, FP64 on the device
     std::vector<double> h(n_);
     uint64_t sd = seed;
@@ -1631,6 +1694,7 @@ void FemDevice::download_pattern(std::vector<int64_t>& rowptr, std::vector<int32
 std::string FemDevice::amg_levels() const { return amg_ ? amg_->describe() : std::string(); }
 
 void FemDevice::ensure_split() {
+    ensure_sell();
     if (split_valid_) return;
     const long long ne = (long long)fs_.slice_ptr.back();
     sell_lo_.resize(ne);
@@ -1822,31 +1886,22 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
     FGB_LAUNCH(k_norm2<<<reduce_grid(n_, kBlock), kBlock, 0, stream_>>>(n_, rhs_.get(), partial_.get(), ds));
     FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
     FGB_CUDA(cudaStreamSynchronize(stream_));
-    const double bnorm = std::sqrt(h_state_->rr);
+    const double bb = h_state_->rr, bnorm = std::sqrt(bb);
     st->bnorm = bnorm;
     CgState init{};
     init.tol2 = tol2_of(opt, bnorm);
     init.max_iter = opt.max_iter;
     FGB_CUDA(cudaMemcpyAsync(ds, &init, sizeof(CgState), cudaMemcpyHostToDevice, stream_));
-    // r = b - A x (FP64), stop if already converged
-    FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(), sell64_.get(),
-                                                       x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds,
-                                                       compensated_residual(opt)));
-    FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
-    FGB_CUDA(cudaStreamSynchronize(stream_));
-    int status = 0, it = 0, restarts = 0;
-    double rr_true = h_state_->rr;
-    if (rr_true <= init.tol2 || bnorm == 0) status = 1;
     const int mode = outer_mode_;
     const bool df = mode >= 1;
     CbSpmvArgs ca{};
     int cb_grid = 1;
     size_t cb_smem = 0;
-    if (df && status == 0) {
+    if (df) {
         if (mode == 1) ensure_split();
         p2_.resize(n_);
     }
-    if (mode == 2 && status == 0) {
+    if (mode == 2) {
         ensure_cell_blocks();
         if (ke32_.size() != 378 * (size_t)nc_ || ke32lo_.size() != 378 * (size_t)nc_) refresh_ke32();
         CellBlocksDev& c = *cb_;
@@ -1865,6 +1920,36 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
                         c.dof_start.get(), c.dof_list.get(), c.slot.get(), c.bnd_dofs.get(), c.bnd_ptr.get(),
                         c.item_end.get(), c.loc.get(), c.items.get(), fixed_.get(), cb_pair_.get(), cb_dot_.get()};
     }
+    // true FP64 residual b - A x into r64: the assembled matrix when it is current, else (Q2,
+    // not compensated: solve() formed the matrix for every other case) the FP64 element
+    // matrices row by row
+    const bool cell_residual = !sell_valid_;
+    FGB_REQUIRE(!cell_residual || (fs_.order == 2 && !compensated_residual(opt)),
+                "true residual without the assembled matrix");
+    auto true_residual = [&](double* ff) {
+        if (cell_residual) {
+            *ff = 0.0;
+            return cells_true_residual();
+        }
+        FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
+                                                           sell64_.get(), x_.get(), rhs_.get(), r64_.get(), partial_.get(),
+                                                           ds, compensated_residual(opt)));
+        FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
+        FGB_CUDA(cudaStreamSynchronize(stream_));
+        *ff = h_state_->ff;
+        return h_state_->rr;
+    };
+    // r = b - A x, stop if already converged; from the zero vector of setup() (every Dirichlet
+    // value zero on this path) r is b itself
+    double ff_true = 0.0, rr_true = 0.0;
+    if (cell_residual && x_zero_) {
+        FGB_CUDA(cudaMemcpyAsync(r64_.get(), rhs_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, stream_));
+        rr_true = bb;
+    } else {
+        rr_true = true_residual(&ff_true);
+    }
+    int status = 0, it = 0, restarts = 0;
+    if (rr_true <= init.tol2 || bnorm == 0) status = 1;
     float2* p2 = df ? p2_.get() : nullptr;
     // Convergence is declared on the FP64 true residual b - A x: when the recursion reports
     // convergence, r is recomputed exactly and CG restarts from it if it is still above the
@@ -1902,15 +1987,10 @@ int FemDevice::solve_amg(const SolveOptions& opt, SolveStats* st) {
             FGB_LAUNCH(k_pcg_direction<<<gb, kBlock, 0, stream_>>>(n_, zi, p64_.get(), p2, ds));
         }
         // true FP64 residual of the current x (also the restart residual)
-        FGB_LAUNCH(k_residual64<<<gb, kBlock, 0, stream_>>>(n_, slice_ptr_.get(), slice_len_.get(), sell_col_.get(),
-                                                           sell64_.get(), x_.get(), rhs_.get(), r64_.get(), partial_.get(), ds,
-                                                           compensated_residual(opt)));
-        FGB_CUDA(cudaMemcpyAsync(h_state_, ds, sizeof(CgState), cudaMemcpyDeviceToHost, stream_));
-        FGB_CUDA(cudaStreamSynchronize(stream_));
-        rr_true = h_state_->rr;
+        rr_true = true_residual(&ff_true);
         // with a compensated residual, a solution within twice the FP64 floor is as converged
         // as FP64 can hold it: success (kStatusFloor), no restart on rounding noise
-        const bool at_floor = compensated_residual(opt) && rr_true <= 4.0 * kFloorScale2 * h_state_->ff;
+        const bool at_floor = !cell_residual && compensated_residual(opt) && rr_true <= 4.0 * kFloorScale2 * ff_true;
         if (status == 1 && rr_true > init.tol2 && at_floor) {
             status = kStatusFloor;
             break;

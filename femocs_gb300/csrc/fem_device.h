@@ -130,6 +130,9 @@ public:
     // default: 4.3 vs 8.95 GB per smoothing step on config 2), or through the assembled SELL
     // matrix; the hierarchy is rebuilt at the next solve
     void set_level0_ebe(bool on);
+    // Q2: form the assembled SELL matrices at every assembly (false) or only when read (true,
+    // the default); results are the same
+    void set_lazy_matrix(bool on);
     // outer SpMV of the multigrid PCG: 1 = the SELL matrix as FP32 hi/lo pairs with error-free
     // products (Q1 default; FP64-accurate to ~2^-48 per term, off the FP64 pipe), 2 = the same
     // arithmetic element by element over the cell blocks (Q2 default: half the bytes of the
@@ -171,7 +174,10 @@ public:
 
     // solution by dof / by mesh node
     const double* d_solution() const { return x_.get(); }
-    double* d_solution() { return x_.get(); }
+    double* d_solution() {  // writable: the solution is no longer known to be zero
+        x_zero_ = false;
+        return x_.get();
+    }
     const FemStructure& structure() const { return fs_; }
     int n_dofs() const { return fs_.n_dofs; }
     int64_t nnz() const { return fs_.nnz(); }
@@ -232,6 +238,19 @@ private:
     bool level0_ebe_ = false;
     int outer_mode_ = 1;
     bool split_valid_ = false;
+    // Q2: the assembled SELL values (kval_, then sell64_/sell32_) are formed only when a
+    // consumer needs them (ensure_sell): with all Dirichlet values zero, D^-1, the right-hand
+    // side and x come from the element matrices directly, and the multigrid PCG over the cell
+    // blocks reads neither matrix
+    bool lazy_matrix_ = true;
+    bool kval_valid_ = false;   // kval_ holds the rows of the current element matrices
+    bool sell_valid_ = true;    // sell64_/sell32_ hold the current eliminated values
+    void ensure_sell();
+    // r64 = b - A x from the FP64 element matrices (Q2, no assembled matrix), returns |r|^2
+    double cells_true_residual();
+    DBuf<CgState> res_state_;
+    DBuf<double> cell_y_;       // K_e x_e per cell (27 per cell) for that residual
+    bool x_zero_ = true;        // x is the zero vector of setup() (no solve or write since)
     DBuf<float> sell_lo_;  // low FP32 part of the matrix values (high part: sell32_)
     DBuf<float2> p2_;      // p as interleaved FP32 (hi, lo) pairs
     void ensure_split();

@@ -369,10 +369,12 @@ __global__ void k_sell_dirichlet(int n, const int64_t* __restrict__ sptr, const 
             s64[q] = a;
             s32[q] = (float)a;
         }
-        rhs[r] = gr * diag;
-        x[r] = gr;
+        if (rhs) {
+            rhs[r] = gr * diag;
+            x[r] = gr;
+        }
     } else {
-        double acc = rhs[r];
+        double acc = rhs ? rhs[r] : 0.0;
         for (int j = 0; j < len; ++j) {
             const int64_t q = pos(j);
             const int c = scol[q];
@@ -384,7 +386,77 @@ __global__ void k_sell_dirichlet(int n, const int64_t* __restrict__ sptr, const 
             s64[q] = a;
             s32[q] = (float)a;
         }
-        rhs[r] = acc;
+        if (rhs) rhs[r] = acc;
+    }
+    if (!rhs) return;  // values only: the right-hand side, x and D^-1 are already in place
+    dinv64[r] = 1.0 / diag;
+    dinv32[r] = (float)(1.0 / diag);
+}
+
+// r = b - A x of the eliminated system without the assembled matrix, in FP64, in two passes.
+// Cells: y_e = K_e x_e, one warp per cell with the cell's 378 packed entries and its 27 x
+// values (zero for fixed DoFs: their columns are zero in the eliminated matrix) staged in
+// shared memory, lane i < 27 forming row i. Rows: r = b - the sum of the row's y entries over
+// its cells (r2c order; item 27 c + L indexes y directly); a fixed row's residual is b - diag x.
+__global__ void __launch_bounds__(32 * kQ2Warps) k_q2_cell_products(int nc, const int32_t* __restrict__ cd,
+                                                                    const double* __restrict__ ke,
+                                                                    const int8_t* __restrict__ fixed,
+                                                                    const double* __restrict__ x,
+                                                                    double* __restrict__ y) {
+    __shared__ double sk[kQ2Warps][378];
+    __shared__ double sx[kQ2Warps][27];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kQ2Warps + wid;
+    if (c >= nc) return;  // whole warp leaves together
+    const double* K = ke + 378 * (size_t)c;
+    for (int k = lane; k < 378; k += 32) sk[wid][k] = K[k];
+    if (lane < 27) {
+        const int d = cd[27 * (size_t)c + lane];
+        sx[wid][lane] = fixed[d] ? 0.0 : x[d];
+    }
+    __syncwarp();
+    if (lane < 27) {
+        double acc = 0.0;
+        for (int j = 0; j < 27; ++j) acc = fma(sk[wid][sym27(lane, j)], sx[wid][j], acc);
+        y[27 * (size_t)c + lane] = acc;
+    }
+}
+
+__global__ void k_q2_residual_rows(int n, const int32_t* __restrict__ r2c_ptr, const int32_t* __restrict__ r2c_item,
+                                   const double* __restrict__ y, const int8_t* __restrict__ fixed,
+                                   const double* __restrict__ dinv, const double* __restrict__ x,
+                                   const double* __restrict__ b, double* __restrict__ r) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    if (fixed[row]) {
+        r[row] = b[row] - x[row] / dinv[row];
+        return;
+    }
+    double acc = 0.0;
+    for (int p = r2c_ptr[row]; p < r2c_ptr[row + 1]; ++p) acc += y[r2c_item[p]];
+    r[row] = b[row] - acc;
+}
+
+// The eliminated system's D^-1, right-hand side and x without the matrix, when every
+// Dirichlet value is zero: the diagonal is the same sum of element-matrix diagonals, in the
+// same cell order, as the assembled one (k_q2_assemble_rows); fixed rows get rhs = x = 0; the
+// lift of the boundary values onto the free rows vanishes
+__global__ void k_q2_dirichlet_zero(int n, const int32_t* __restrict__ r2c_ptr, const int32_t* __restrict__ r2c_item,
+                                    const double* __restrict__ ke, const int8_t* __restrict__ bc, int anode,
+                                    double* __restrict__ dinv64, float* __restrict__ dinv32, double* __restrict__ rhs,
+                                    double* __restrict__ x) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double diag = 0.0;
+    for (int p = r2c_ptr[r]; p < r2c_ptr[r + 1]; ++p) {
+        const int item = r2c_item[p];
+        const int c = item / 27, li = item - 27 * c;
+        diag += ke[378 * (size_t)c + sym27(li, li)];
+    }
+    if (r2c_ptr[r] == r2c_ptr[r + 1]) diag = 1.0;
+    if (fixed_kind(bc[r], anode)) {
+        rhs[r] = 0.0;
+        x[r] = 0.0;
     }
     dinv64[r] = 1.0 / diag;
     dinv32[r] = (float)(1.0 / diag);
@@ -559,6 +631,19 @@ void sell_dirichlet(int n, const int64_t* sptr, const int32_t* scol, const int32
                     double* rhs, double* x, cudaStream_t s) {
     FGB_LAUNCH(k_sell_dirichlet<<<grid_for(n, 256), 256, 0, s>>>(n, sptr, scol, row_len, kval, bc, anode, v0, s64, s32,
                                                                  dinv64, dinv32, rhs, x));
+}
+
+void q2_residual_cells(int n, int nc, const int32_t* r2c_ptr, const int32_t* r2c_item, const int32_t* cd,
+                       const double* ke, const int8_t* fixed, const double* dinv, const double* x, const double* b,
+                       double* y, double* r, cudaStream_t s) {
+    if (nc) FGB_LAUNCH(k_q2_cell_products<<<(nc + kQ2Warps - 1) / kQ2Warps, 32 * kQ2Warps, 0, s>>>(nc, cd, ke, fixed, x, y));
+    if (n) FGB_LAUNCH(k_q2_residual_rows<<<grid_for(n, 256), 256, 0, s>>>(n, r2c_ptr, r2c_item, y, fixed, dinv, x, b, r));
+}
+
+void q2_dirichlet_zero(int n, const int32_t* r2c_ptr, const int32_t* r2c_item, const double* ke, const int8_t* bc,
+                       int anode, double* dinv64, float* dinv32, double* rhs, double* x, cudaStream_t s) {
+    FGB_LAUNCH(k_q2_dirichlet_zero<<<grid_for(n, 256), 256, 0, s>>>(n, r2c_ptr, r2c_item, ke, bc, anode, dinv64, dinv32,
+                                                                    rhs, x));
 }
 
 void q2_embedding(int n, int n1, const int32_t* dof_cell, const int8_t* dof_local, const int32_t* cq1,

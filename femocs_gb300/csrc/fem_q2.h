@@ -49,9 +49,19 @@ struct DeviceCsr32 {
 // cell, -1: none). R = P^T with each row in ascending P-row order.
 void q2_embedding(int n, int n1, const int32_t* dof_cell, const int8_t* dof_local, const int32_t* cq1,
                   const int8_t* fixed2, const int8_t* fixed1, DeviceCsr32& P, DeviceCsr32& R, cudaStream_t s);
-// symmetric Dirichlet elimination on a SELL-layout matrix (any element order)
+// symmetric Dirichlet elimination on a SELL-layout matrix (any element order); rhs == nullptr
+// writes the eliminated values s64/s32 only (rhs, x and D^-1 untouched)
 void sell_dirichlet(int n, const int64_t* sptr, const int32_t* scol, const int32_t* row_len, const double* kval,
                     const int8_t* bc, int anode, double v0, double* s64, float* s32, double* dinv64, float* dinv32,
                     double* rhs, double* x, cudaStream_t s);
+// r = b - A x of the eliminated Q2 system from the FP64 element matrices (no assembled
+// matrix): y (27 per cell, scratch) = K_e x_e per cell, then per row the sum over its cells
+void q2_residual_cells(int n, int nc, const int32_t* r2c_ptr, const int32_t* r2c_item, const int32_t* cd,
+                       const double* ke, const int8_t* fixed, const double* dinv, const double* x, const double* b,
+                       double* y, double* r, cudaStream_t s);
+// D^-1, right-hand side and x of the eliminated Q2 system when every Dirichlet value is zero,
+// without the matrix: the diagonal from the element matrices in the assembled summation order
+void q2_dirichlet_zero(int n, const int32_t* r2c_ptr, const int32_t* r2c_item, const double* ke, const int8_t* bc,
+                       int anode, double* dinv64, float* dinv32, double* rhs, double* x, cudaStream_t s);
 
 }  // namespace fgb

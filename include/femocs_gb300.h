@@ -199,6 +199,12 @@ int fgb_field_set_smoothing(FGB_FIELD* f, int degree, double lo);
  * lo 0 = the default. Applied from the next
  * solve without rebuilding the hierarchy; the dense coarsest level is left alone */
 int fgb_field_set_level_smoothing(FGB_FIELD* f, int level, int degree, double lo);
+/* Q2 fields: form the assembled SELL matrices (FP64 and FP32 values of the eliminated system)
+ * at every assembly (0) or only when something reads them (1, the default): the system
+ * export, the Jacobi-preconditioned solvers, precision 3, a compensated true residual
+ * (rel_tol below 1e-10), a nonzero Dirichlet value. The default multigrid PCG over the cell
+ * blocks takes D^-1 and its FP64 true residual from the element matrices */
+int fgb_field_set_lazy_matrix(FGB_FIELD* f, int on);
 /* Q2 fields: element matrices of the full assembly on the tensor cores (1, default: per-cell
  * factors in FP64, error-free BF16 slices, tcgen05 products accumulated exactly in FP32, levels
  * combined as FP32 pairs into FP64) or on the FP32 pipe as FP32 hi/lo pairs (0) */
