@@ -272,12 +272,18 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
 
     phase("row lengths");
     // ---- numbering: Morton order, then windows of 256 by decreasing row length
-    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
-    for (int e = 0; e < n_ent; ++e)
-        for (int d = 0; d < 3; ++d) {
-            mn[d] = std::min(mn[d], exyz[3 * (size_t)e + d]);
-            mx[d] = std::max(mx[d], exyz[3 * (size_t)e + d]);
-        }
+    double mn0 = 1e300, mn1 = 1e300, mn2 = 1e300, mx0 = -1e300, mx1 = -1e300, mx2 = -1e300;
+#pragma omp parallel for schedule(static) reduction(min : mn0, mn1, mn2) reduction(max : mx0, mx1, mx2)
+    for (int e = 0; e < n_ent; ++e) {
+        const double* p = &exyz[3 * (size_t)e];
+        mn0 = std::min(mn0, p[0]);
+        mn1 = std::min(mn1, p[1]);
+        mn2 = std::min(mn2, p[2]);
+        mx0 = std::max(mx0, p[0]);
+        mx1 = std::max(mx1, p[1]);
+        mx2 = std::max(mx2, p[2]);
+    }
+    const double mn[3] = {mn0, mn1, mn2}, mx[3] = {mx0, mx1, mx2};
     std::vector<std::pair<uint64_t, int32_t>> key(n_ent);
 #pragma omp parallel for schedule(static)
     for (int e = 0; e < n_ent; ++e) {
@@ -292,6 +298,7 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
     }
     __gnu_parallel::sort(key.begin(), key.end());
     std::vector<int32_t> dof2e(n_ent), e2dof(n_ent);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n_ent; ++i) dof2e[i] = key[i].second;
     key.clear();
     key.shrink_to_fit();
@@ -335,8 +342,29 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
 
     phase("dof tables");
     // row -> (cell, local), ascending cell
+    // row pointers: lengths in parallel, then a blocked prefix sum (per-block totals, a scan
+    // over the blocks, each block offset by its predecessors)
     fs.r2c_ptr.assign(n_ent + 1, 0);
-    for (int d = 0; d < n_ent; ++d) fs.r2c_ptr[d + 1] = fs.r2c_ptr[d] + (e2c_ptr[dof2e[d] + 1] - e2c_ptr[dof2e[d]]);
+    {
+        const int nt = std::max(1, omp_get_max_threads());
+        std::vector<int64_t> bsum(nt + 1, 0);
+#pragma omp parallel num_threads(nt)
+        {
+            const int t = omp_get_thread_num();
+            const int d0 = (int)((int64_t)n_ent * t / nt), d1 = (int)((int64_t)n_ent * (t + 1) / nt);
+            int64_t run = 0;
+            for (int d = d0; d < d1; ++d) {
+                run += e2c_ptr[dof2e[d] + 1] - e2c_ptr[dof2e[d]];
+                fs.r2c_ptr[d + 1] = (int32_t)run;
+            }
+            bsum[t + 1] = run;
+#pragma omp barrier
+#pragma omp single
+            for (int u = 0; u < nt; ++u) bsum[u + 1] += bsum[u];
+            const int32_t off = (int32_t)bsum[t];
+            for (int d = d0; d < d1; ++d) fs.r2c_ptr[d + 1] += off;
+        }
+    }
     fs.r2c_item.resize(fs.r2c_ptr[n_ent]);
 #pragma omp parallel for schedule(static)
     for (int d = 0; d < n_ent; ++d) {
