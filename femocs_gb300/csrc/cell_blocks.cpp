@@ -135,19 +135,64 @@ CellBlocks build_cell_blocks(const FemStructure& fs, int cells_per_block, int ma
             }
 
     // slots renumbered by DoF: the slots of boundary DoF j are bnd_ptr[j] .. bnd_ptr[j+1]-1 in
-    // ascending block order (block-order slot s ascends with the block)
+    // ascending block order (block-order slot s ascends with the block). Counts per DoF, the
+    // DoFs with slots compacted in ascending order (blocked scan), the slots bucketed by DoF
+    // (atomic cursors) and each bucket sorted: the numbering of a sequential pass.
     std::vector<int32_t> cnt(n, 0);
-    for (int s = 0; s < cb.n_slots; ++s) ++cnt[slot_dof[s]];
+#pragma omp parallel for schedule(static)
+    for (int s = 0; s < cb.n_slots; ++s) __atomic_fetch_add(&cnt[slot_dof[s]], 1, __ATOMIC_RELAXED);
     std::vector<int32_t> first(n, -1);
-    cb.bnd_ptr.push_back(0);
-    for (int d = 0; d < n; ++d)
-        if (cnt[d]) {
-            first[d] = cb.bnd_ptr.back();
-            cb.bnd_dofs.push_back(d);
-            cb.bnd_ptr.push_back(cb.bnd_ptr.back() + cnt[d]);
+    {
+        const int nt = std::max(1, omp_get_max_threads());
+        std::vector<int64_t> tn(nt + 1, 0), ts(nt + 1, 0);
+        int n_bnd = 0;
+#pragma omp parallel num_threads(nt)
+        {
+            const int t = omp_get_thread_num();
+            const int d0 = (int)((int64_t)n * t / nt), d1 = (int)((int64_t)n * (t + 1) / nt);
+            int64_t a = 0, b = 0;
+            for (int d = d0; d < d1; ++d)
+                if (cnt[d]) {
+                    ++a;
+                    b += cnt[d];
+                }
+            tn[t + 1] = a;
+            ts[t + 1] = b;
+#pragma omp barrier
+#pragma omp single
+            {
+                for (int u = 0; u < nt; ++u) {
+                    tn[u + 1] += tn[u];
+                    ts[u + 1] += ts[u];
+                }
+                n_bnd = (int)tn[nt];
+                cb.bnd_dofs.resize(n_bnd);
+                cb.bnd_ptr.resize(n_bnd + 1);
+                cb.bnd_ptr[n_bnd] = (int32_t)ts[nt];
+            }
+            int64_t j = tn[t], off = ts[t];
+            for (int d = d0; d < d1; ++d)
+                if (cnt[d]) {
+                    cb.bnd_dofs[j] = d;
+                    cb.bnd_ptr[j] = (int32_t)off;
+                    first[d] = (int32_t)off;
+                    off += cnt[d];
+                    ++j;
+                }
         }
-    std::vector<int32_t> renum(cb.n_slots);
-    for (int s = 0; s < cb.n_slots; ++s) renum[s] = first[slot_dof[s]]++;
+        FGB_REQUIRE(cb.bnd_ptr[n_bnd] == cb.n_slots, "cell blocks: slot count");
+    }
+    std::vector<int32_t> order(cb.n_slots), renum(cb.n_slots);
+    {
+        std::vector<int32_t>& cur = first;  // bucket cursors from here on
+#pragma omp parallel for schedule(static)
+        for (int s = 0; s < cb.n_slots; ++s) order[__atomic_fetch_add(&cur[slot_dof[s]], 1, __ATOMIC_RELAXED)] = s;
+        const int n_bnd = (int)cb.bnd_dofs.size();
+#pragma omp parallel for schedule(dynamic, 4096)
+        for (int j = 0; j < n_bnd; ++j) std::sort(order.begin() + cb.bnd_ptr[j], order.begin() + cb.bnd_ptr[j + 1]);
+#pragma omp parallel for schedule(static)
+        for (int p = 0; p < cb.n_slots; ++p) renum[order[p]] = p;
+    }
 #pragma omp parallel for schedule(static)
     for (int64_t q = 0; q < ne; ++q)
         if (cb.slot[q] >= 0) cb.slot[q] = renum[cb.slot[q]];
