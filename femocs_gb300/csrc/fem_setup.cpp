@@ -186,11 +186,28 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
             b.cell = c;
             b.face = (int8_t)f;
         }
-    __gnu_parallel::sort(faces.begin(), faces.end(), [](const BFace& a, const BFace& b) {
-        for (int k = 0; k < 4; ++k)
-            if (a.s[k] != b.s[k]) return a.s[k] < b.s[k];
-        return a.cell < b.cell;
-    });
+    // sorted by (corner DoFs, cell): buckets by the smallest corner DoF (atomic counts and
+    // cursors), then each bucket by the full key; the order is total, so the result is the
+    // comparison sort's at any thread count
+    {
+        auto face_less = [](const BFace& a, const BFace& b) {
+            for (int k = 0; k < 4; ++k)
+                if (a.s[k] != b.s[k]) return a.s[k] < b.s[k];
+            return a.cell < b.cell;
+        };
+        const long long nf = (long long)faces.size();
+        std::vector<int32_t> bstart(nv + 1, 0);
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < nf; ++i) __atomic_fetch_add(&bstart[faces[i].s[0] + 1], 1, __ATOMIC_RELAXED);
+        for (int v = 0; v < nv; ++v) bstart[v + 1] += bstart[v];
+        std::vector<int32_t> cur(bstart.begin(), bstart.end() - 1);
+        std::vector<BFace> sorted(faces.size());
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < nf; ++i) sorted[__atomic_fetch_add(&cur[faces[i].s[0]], 1, __ATOMIC_RELAXED)] = faces[i];
+#pragma omp parallel for schedule(dynamic, 2048)
+        for (int v = 0; v < nv; ++v) std::sort(sorted.begin() + bstart[v], sorted.begin() + bstart[v + 1], face_less);
+        faces.swap(sorted);
+    }
     std::vector<BFace> bnd;
     for (size_t i = 0; i < faces.size();) {
         size_t j = i + 1;
