@@ -144,7 +144,8 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
         fs.node2dof[fs.dof2node[d]] = d;
     }
     fs.cell_dofs.resize(8 * (size_t)nc);
-    for (size_t i = 0; i < cv.size(); ++i) fs.cell_dofs[i] = v2dof[cv[i]];
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)cv.size(); ++i) fs.cell_dofs[i] = v2dof[cv[i]];
 
     // CSR in dof numbering
     fs.rowptr.assign(nv + 1, 0);
@@ -169,6 +170,7 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     fs.r2c_ptr.assign(nv + 1, 0);
     for (int d = 0; d < nv; ++d) fs.r2c_ptr[d + 1] = fs.r2c_ptr[d] + (v2c_ptr[dof2v[d] + 1] - v2c_ptr[dof2v[d]]);
     fs.r2c_item.resize(fs.r2c_ptr[nv]);
+#pragma omp parallel for schedule(static)
     for (int d = 0; d < nv; ++d) {
         const int v = dof2v[d];
         std::copy(v2c.begin() + v2c_ptr[v], v2c.begin() + v2c_ptr[v + 1], fs.r2c_item.begin() + fs.r2c_ptr[d]);
