@@ -88,32 +88,56 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     }
 
     phase("vertex -> cells");
-    // neighbour sets (vertex numbering) and degrees
+    // neighbour sets (vertex numbering) and degrees, as one flat array: the sorted, unique
+    // vertices of each vertex's cells, counted in a first pass and written in a second
     std::vector<int32_t> deg(nv);
-    std::vector<std::vector<int32_t>> nb(nv);
-#pragma omp parallel for schedule(dynamic, 1024)
-    for (int v = 0; v < nv; ++v) {
-        std::vector<int32_t>& l = nb[v];
-        l.reserve(8 * (v2c_ptr[v + 1] - v2c_ptr[v]));
+    auto neighbours = [&](int v, std::vector<int32_t>& l) {
+        l.clear();
         for (int p = v2c_ptr[v]; p < v2c_ptr[v + 1]; ++p) {
             const int c = v2c[p] / 8;
             for (int k = 0; k < 8; ++k) l.push_back(cv[8 * (size_t)c + k]);
         }
         std::sort(l.begin(), l.end());
         l.erase(std::unique(l.begin(), l.end()), l.end());
-        deg[v] = (int32_t)l.size();
+    };
+#pragma omp parallel
+    {
+        std::vector<int32_t> l;
+#pragma omp for schedule(dynamic, 1024)
+        for (int v = 0; v < nv; ++v) {
+            neighbours(v, l);
+            deg[v] = (int32_t)l.size();
+        }
+    }
+    std::vector<int64_t> nb_ptr(nv + 1, 0);
+    for (int v = 0; v < nv; ++v) nb_ptr[v + 1] = nb_ptr[v] + deg[v];
+    std::vector<int32_t> nb_col(nb_ptr[nv]);
+#pragma omp parallel
+    {
+        std::vector<int32_t> l;
+#pragma omp for schedule(dynamic, 1024)
+        for (int v = 0; v < nv; ++v) {
+            neighbours(v, l);
+            std::copy(l.begin(), l.end(), nb_col.begin() + nb_ptr[v]);
+        }
     }
 
     phase("neighbour sets");
     // Morton order, then windows of 256 sorted by decreasing degree
-    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
-    for (int v = 0; v < nv; ++v)
-        for (int c = 0; c < 3; ++c) {
-            const double x = X[3 * (size_t)rcs.vertex2node[v] + c];
-            mn[c] = std::min(mn[c], x);
-            mx[c] = std::max(mx[c], x);
-        }
+    double mn0 = 1e300, mn1 = 1e300, mn2 = 1e300, mx0 = -1e300, mx1 = -1e300, mx2 = -1e300;
+#pragma omp parallel for schedule(static) reduction(min : mn0, mn1, mn2) reduction(max : mx0, mx1, mx2)
+    for (int v = 0; v < nv; ++v) {
+        const double* p = &X[3 * (size_t)rcs.vertex2node[v]];
+        mn0 = std::min(mn0, p[0]);
+        mn1 = std::min(mn1, p[1]);
+        mn2 = std::min(mn2, p[2]);
+        mx0 = std::max(mx0, p[0]);
+        mx1 = std::max(mx1, p[1]);
+        mx2 = std::max(mx2, p[2]);
+    }
+    const double mn[3] = {mn0, mn1, mn2}, mx[3] = {mx0, mx1, mx2};
     std::vector<std::pair<uint64_t, int32_t>> key(nv);
+#pragma omp parallel for schedule(static)
     for (int v = 0; v < nv; ++v) {
         uint64_t code = 0;
         for (int c = 0; c < 3; ++c) {
@@ -126,8 +150,10 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     }
     __gnu_parallel::sort(key.begin(), key.end());
     std::vector<int32_t> dof2v(nv);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nv; ++i) dof2v[i] = key[i].second;
     const int W = 256;
+#pragma omp parallel for schedule(dynamic, 64)
     for (int w0 = 0; w0 < nv; w0 += W) {
         const int w1 = std::min(nv, w0 + W);
         std::stable_sort(dof2v.begin() + w0, dof2v.begin() + w1,
@@ -157,13 +183,13 @@ FemStructure build_fem_structure(const PreparedMesh& pm, int region) {
     fs.col.resize(fs.rowptr[nv]);
 #pragma omp parallel for schedule(dynamic, 1024)
     for (int d = 0; d < nv; ++d) {
-        const std::vector<int32_t>& l = nb[dof2v[d]];
+        const int v = dof2v[d];
+        const int64_t b = nb_ptr[v], len = nb_ptr[v + 1] - b;
         int32_t* o = &fs.col[fs.rowptr[d]];
-        for (size_t k = 0; k < l.size(); ++k) o[k] = v2dof[l[k]];
-        std::sort(o, o + l.size());
+        for (int64_t k = 0; k < len; ++k) o[k] = v2dof[nb_col[b + k]];
+        std::sort(o, o + len);
     }
-    nb.clear();
-    nb.shrink_to_fit();
+    std::vector<int32_t>().swap(nb_col);
 
     phase("CSR columns");
     // row -> (cell, local), ascending cell
