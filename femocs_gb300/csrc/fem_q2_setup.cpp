@@ -296,7 +296,23 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
         }
         key[e] = {code, e};
     }
-    __gnu_parallel::sort(key.begin(), key.end());
+    // sorted by (code, entity): buckets by the top 16 bits of the 63-bit code (atomic counts
+    // and cursors), then each bucket; the keys are unique, so the order is the full sort's
+    {
+        constexpr int kBits = 16, kShift = 63 - kBits;
+        std::vector<int32_t> bstart((1 << kBits) + 1, 0);
+#pragma omp parallel for schedule(static)
+        for (int e = 0; e < n_ent; ++e) __atomic_fetch_add(&bstart[(key[e].first >> kShift) + 1], 1, __ATOMIC_RELAXED);
+        for (int b = 0; b < (1 << kBits); ++b) bstart[b + 1] += bstart[b];
+        std::vector<int32_t> cur(bstart.begin(), bstart.end() - 1);
+        std::vector<std::pair<uint64_t, int32_t>> sorted(n_ent);
+#pragma omp parallel for schedule(static)
+        for (int e = 0; e < n_ent; ++e)
+            sorted[__atomic_fetch_add(&cur[key[e].first >> kShift], 1, __ATOMIC_RELAXED)] = key[e];
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int b = 0; b < (1 << kBits); ++b) std::sort(sorted.begin() + bstart[b], sorted.begin() + bstart[b + 1]);
+        key.swap(sorted);
+    }
     std::vector<int32_t> dof2e(n_ent), e2dof(n_ent);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n_ent; ++i) dof2e[i] = key[i].second;
