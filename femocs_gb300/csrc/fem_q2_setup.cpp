@@ -93,20 +93,32 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
     }
     std::vector<EntityKey> ek(18 * (size_t)nc);
 #pragma omp parallel for schedule(static)
-    for (int c = 0; c < nc; ++c)
+    for (int c = 0; c < nc; ++c) {
+        int32_t cn[8];  // the cell's corner nodes, read once
+        for (int k = 0; k < 8; ++k) cn[k] = cell_node(c, k);
         for (int L = 0; L < 27; ++L) {
             const int n = n_corner[L];
             if (n == 1) {
-                ent[27 * (size_t)c + L] = pm.vac.node2vertex[cell_node(c, corner_tab[L][0])];
+                ent[27 * (size_t)c + L] = pm.vac.node2vertex[cn[corner_tab[L][0]]];
             } else if (n == 2 || n == 4) {
                 EntityKey& e = ek[18 * (size_t)c + slot_of[L]];
-                e.k = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MAX};
-                for (int q = 0; q < n; ++q) e.k[q] = cell_node(c, corner_tab[L][q]);
-                std::sort(e.k.begin(), e.k.end());
+                int32_t k[4] = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MAX};
+                for (int q = 0; q < n; ++q) k[q] = cn[corner_tab[L][q]];
+                // four keys in ascending order (a five-exchange sorting network)
+                auto cx = [&](int a, int b) {
+                    if (k[b] < k[a]) std::swap(k[a], k[b]);
+                };
+                cx(0, 1);
+                cx(2, 3);
+                cx(0, 2);
+                cx(1, 3);
+                cx(1, 2);
+                e.k = {k[0], k[1], k[2], k[3]};
                 e.cell = c;
                 e.local = (int8_t)L;
             }
         }
+    }
     phase("entity keys");
     // sort by (corner nodes, cell): buckets by the smallest corner node (atomic counts and
     // cursors), then each bucket by the full key. The order is total (a cell has one record
