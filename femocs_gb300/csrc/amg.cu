@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(kB) k_cheb_zero(int n, const float* __restrict
 
 // c1 < 0 marks the first step from a nonzero guess: d = D^-1 r / theta (c2 = 1/theta)
 // the row kernels below are built for 8 CTAs of 256 threads per SM (32 registers; the SELL
-// variants spill 16 bytes): config 1's level-0 smoothing ran at 0.43 of the copy bandwidth
+// variants spill 16 bytes): the 2.8e5-DoF Q1 nanotip's level-0 smoothing ran at 0.43 of the copy bandwidth
 // with 6 CTAs per SM (40 registers), 0.50 with 8
 template <int TPR>
 __global__ void __launch_bounds__(kB, 8) k_cheb_step(Op A, const float* __restrict__ b, const float* __restrict__ xin,

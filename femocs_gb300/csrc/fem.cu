@@ -1055,8 +1055,8 @@ FemDevice::FemDevice(const PreparedMesh& pm, FemStructure&& fs, cudaStream_t str
     : fs_(std::move(fs)), pm_(&pm), stream_(stream), n_(fs_.n_dofs), nc_(fs_.n_cells) {
     cudaStream_t s = stream_;
     if (fs_.order == 2) {
-        // the cell blocks (host, ~0.3 s on config 2) are built while the uploads below run and
-        // until the first assembly needs them
+        // the cell blocks (host, ~0.3 s on the 1.7e7-DoF Q2 nanotip) are built while the
+        // uploads below run and until the first assembly needs them
         cb_host_cells_ = cb_cells_;
         cb_host_dofs_ = cb_max_dofs_;
         cb_host_ = std::async(std::launch::async, [this] { return build_cell_blocks(fs_, cb_host_cells_, cb_host_dofs_); });
@@ -1602,16 +1602,18 @@ void FemDevice::build_q2_amg(int anode, SolveStats* st) {
     l0.A.ptr.assign(1, fs_.nnz());  // structure lives on the device; nnz for reporting
     l0.lambda = estimate_lambda(15);
     // degree 2 on [0.06, 1.1]: more iterations than degree 3-4 but fewer passes over the big Q2
-    // matrix per cycle (config 2: 95 iterations / 1.11 s vs 84 / 1.23 s at degree 3); the lower
-    // end 0.06 against 0.1: 70 -> 68 iterations on a 2.2e6-DoF tip, 96 on config 2 either way
+    // matrix per cycle (1.7e7-DoF Q2 nanotip: 95 iterations / 1.11 s vs 84 / 1.23 s at degree 3);
+    // the lower end 0.06 against 0.1: 70 -> 68 iterations on a 2.2e6-DoF tip, 96 on the
+    // 1.7e7-DoF one either way
     l0.cheb_degree = smooth_degree_ > 0 ? smooth_degree_ : 2;
     l0.cheb_lo = smooth_lo_ > 0 ? smooth_lo_ : 0.06;
     phase("lambda_max (device)");
     // the Q1 level is the coarse solve of the Q2 level: smooth it harder
     h1.levels[0].cheb_degree = 4;
     h1.levels[0].cheb_lo = 0.04;
-    // below it one Chebyshev step per side is enough: config 2 keeps its 96 PCG iterations
-    // (618 -> 609 ms per solve); degree 2 or 3 there, or 3 or 6 at the Q1 level, cost more
+    // below it one Chebyshev step per side is enough: the 1.7e7-DoF Q2 nanotip keeps its 96 PCG
+    // iterations (618 -> 609 ms per solve); degree 2 or 3 there, or 3 or 6 at the Q1 level,
+    // cost more
     for (size_t l = 1; l < h1.levels.size(); ++l) h1.levels[l].cheb_degree = 1;
     h1.levels[0].A.col = f1.col;
     h1.levels[0].A.val = std::move(v1);

@@ -127,8 +127,8 @@ public:
     // system; 0 = the hierarchy's default), applied from the next solve without a rebuild
     void set_level_smoothing(int level, int degree, double lo);
     // Q2: apply the finest multigrid level element by element, by cell blocks (cell_blocks.h;
-    // default: 4.3 vs 8.95 GB per smoothing step on config 2), or through the assembled SELL
-    // matrix; the hierarchy is rebuilt at the next solve
+    // default: 4.3 vs 8.95 GB per smoothing step on the 1.7e7-DoF Q2 nanotip), or through the
+    // assembled SELL matrix; the hierarchy is rebuilt at the next solve
     void set_level0_ebe(bool on);
     // Q2: form the assembled SELL matrices at every assembly (false) or only when read (true,
     // the default); results are the same
@@ -222,9 +222,11 @@ private:
     std::vector<int> coarse_cycles_;
     std::vector<std::pair<int, double>> level_smooth_;  // per level (index 0 unused): degree, lo
     bool level0_stream_ = false;
-    int level0_prefetch_ = 1;     // L2 prefetch one group ahead (measured best on config 2)
-    int level0_geo_ = 2;          // requested level-0 operator source (set_level0_operator):
-                                  // FP16 geometric factors (0.69 vs 0.89 ms per config-2 step)
+    // L2 prefetch one group ahead (measured best on the 1.7e7-DoF Q2 nanotip)
+    int level0_prefetch_ = 1;
+    // requested level-0 operator source (set_level0_operator): FP16 geometric factors (0.69 vs
+    // 0.89 ms per step on the 1.7e7-DoF Q2 nanotip)
+    int level0_geo_ = 2;
     int geo_built_ = 0;           // kind held in geo_ (0: none)
     int geo_for_ = 0;             // kind requested when geo_ was built (2 may hold FP32: fallback)
     DBuf<unsigned char> geo_;     // geometric factors in block order (q2_geometric_factors)
@@ -264,8 +266,9 @@ private:
     DBuf<double> cb_dot_;   // outer mode 2: p.q partials
     bool cb_spmv_attr_ = false;
     // cell blocks of at most 176 hexes / 2816 DoFs: the largest whose matrix-free smoother
-    // shared memory (56.4 KB) lets 4 CTAs of 64 registers share an SM (config 2: smoothing step
-    // 0.648 ms against 0.685 ms for 256 / 4096, outer product 1.70 against 1.77 ms)
+    // shared memory (56.4 KB) lets 4 CTAs of 64 registers share an SM (1.7e7-DoF Q2 nanotip:
+    // smoothing step 0.648 ms against 0.685 ms for 256 / 4096, outer product 1.70 against
+    // 1.77 ms)
     int cb_cells_ = 176, cb_max_dofs_ = 2816;
     DBuf<int8_t> fixed_;    // 1 on Dirichlet rows of the current anode mode
     LaunchTimer spmv_timer_;
