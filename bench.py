@@ -44,7 +44,7 @@ RANK = 1           # interpolation_rank default of the reference (src/Config.cpp
 N_POINTS = {"config2": 1_000_000, "config1": 100_000, "probe": 200_000}
 # DRAM bytes (read + write) per row of one launch of the hot multigrid kernels, from ncu
 # captures of the Q2 probe workload (the SELL level-0 Chebyshev step at 61.9 nonzeros per row,
-# as config 2's Q2 rows; the cell-block step, k_cb_apply + k_cb_finish, from the element
+# as the R = 5 nm nanotip's Q2 rows; the cell-block step, k_cb_apply + k_cb_finish, from the element
 # matrices and matrix-free from the FP16 geometric factors); a launch's traffic scales with
 # its rows
 KERNEL_TRAFFIC_PER_ROW = {("smoother", 2): 551.6, ("smoother_ebe", 2): 261.8, ("smoother_mf16", 2): 114.3}
@@ -52,7 +52,8 @@ FALLBACK_HBM_GBS = 6800.0
 
 
 def element_order(args):
-    """config 2 is quoted with Q2 elements, config 1 with Q1 (the reference's element)"""
+    """the R = 5 nm nanotip (`config2`) is quoted with Q2 elements, the R = 2 nm one (`config1`)
+    with Q1 (the reference's element)"""
     if args.order:
         return args.order
     return 2 if args.workload in ("config2", "probe") else 1
@@ -60,7 +61,7 @@ def element_order(args):
 
 def spec_of(workload):
     import femocs_gb300 as fg
-    if workload == "probe":  # config-2 geometry on a coarser grid, small enough for full ncu captures
+    if workload == "probe":  # the R = 5 nm geometry on a coarser grid, small enough for full ncu captures
         return dict(fg.CONFIG2, h=22.0, growth=1.3)
     return dict(fg.CONFIG2 if workload == "config2" else fg.CONFIG1)
 
@@ -547,7 +548,7 @@ def run_ours(args, world, rank):
         "mixed_jacobi_cg": ({"p50_ms": statistics.median(mixed_ms), "iterations": mixed[-1]["iterations"],
                              "refinements": mixed[-1]["outer"], "kernel_ms": mixed[-1]["kernel_ms"],
                              "rel_residual": mixed[-1]["rel_residual"]} if mixed else
-                            "not timed on Q2 (~1e4 iterations, 83 s per solve on config 2)"),
+                            "not timed on Q2 (~1e4 iterations, 83 s per solve on the 1.7e7-DoF nanotip)"),
         "e2e": {"value": n * world / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": 24 * n_points,
                 "d2h_bytes_per_step": 36 * n_points,
                 "note": "femocs_run + femocs_interpolate_elfield through the C ABI, host arrays"},
@@ -958,7 +959,7 @@ def serve_plain_baseline(specs, base, n_atoms, runs, steps=3, seed=5):
 
 
 def run_serve(args, world, rank, quiet=False):
-    """64 concurrent MD runs (half the config-0 tip, half random batch-style tips), ~5e4
+    """64 concurrent MD runs (half the R = 2 nm, H = 8 nm tip, half random batch-style tips), ~5e4
     atoms each, resident; Poisson arrivals swept over rates; each request displaces its run's
     atoms by N(0, 0.02 A), re-solves warm-started with an applied field within 1% of the
     run's base field, recovers the nodal field and interpolates E and phi at the atoms, and
@@ -1017,7 +1018,7 @@ def run_serve(args, world, rank, quiet=False):
     srv.stop()
     info = srv.info()
     # like-for-like: the same requests one at a time with the plain FP64 Jacobi-PCG, on runs of
-    # both halves (config-1 tips and random batch tips)
+    # both halves (R = 2 nm tips and random batch tips)
     sample_runs = sorted(set([0, 1, half, half + 1, n_runs - 1]))
     plain = serve_plain_baseline(specs, base, args.atoms, sample_runs)
     best = max(sweep, key=lambda d: d["solves_per_s"])
@@ -1026,7 +1027,7 @@ def run_serve(args, world, rank, quiet=False):
         "value": best["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": len(args.rates),
         "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 CG / f32 multigrid preconditioner", "data": "synthetic (seeded nanotips, FCC surface atoms)",
-        "config": {"workload": f"serve: {n_runs} MD runs ({half} config-0 tips, {n_runs - half} random tips), "
+        "config": {"workload": f"serve: {n_runs} MD runs ({half} R=2 nm H=8 nm tips, {n_runs - half} random tips), "
                                f"{args.atoms} atoms each, sigma 0.02 A per step, Poisson arrivals",
                    "total_dofs": int(dofs.sum()), "rates": args.rates, "iters_per_launch": args.iters_per_launch,
                    "solver_launch": "persistent cooperative kernel" if args.persistent else "graph (WHILE node)",
