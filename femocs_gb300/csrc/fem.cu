@@ -1220,6 +1220,7 @@ void FemDevice::assemble(bool full_run, bool anode_dirichlet) {
                            anode_dirichlet ? 1 : 0, applied_potential_, sell64_.get(), sell32_.get(), dinv64_.get(),
                            dinv32_.get(), rhs_.get(), x_.get(), stream_);
             sell_valid_ = true;
+            if (anode_dirichlet && applied_potential_ != 0.0) x_zero_ = false;  // x holds the anode value
         }
         FGB_CUDA(cudaGetLastError());
         return;
@@ -1256,6 +1257,8 @@ void FemDevice::assemble_q1_rows(bool matrix, bool anode_dirichlet) {
                                                  applied_potential_, dirichlet_value_, csr2sell_.get(), sell64_.get(),
                                                  sell32_.get(), dinv64_.get(), dinv32_.get(), rhs_.get(), x_.get()));
     FGB_CUDA(cudaGetLastError());
+    // x holds the boundary values on the Dirichlet rows
+    if (dirichlet_value_ != 0.0 || (anode_dirichlet && applied_potential_ != 0.0)) x_zero_ = false;
 }
 
 void FemDevice::ensure_sell() {
