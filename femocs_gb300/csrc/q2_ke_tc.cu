@@ -29,8 +29,9 @@
 //      complete_tx) and issues tcgen05.mma (M = 128, N = 48, K = 16, BF16 in, FP32 in TMEM);
 //      tcgen05.commit signals when a C slot may be refilled and when the N-tile is done;
 //   3  the eight warps read the six level accumulators with tcgen05.ld (warp w: TMEM lanes
-//      32 (w % 4) .., i.e. 32 cells, and half of the N-tile's columns), combine them in FP64 and
-//      store the 378 packed FP64 entries per cell.
+//      32 (w % 4) .., i.e. 32 cells, and half of the N-tile's columns), combine them into an
+//      FP32 pair (TwoSum), scale it into FP64 on the integer pipes and store the 378 packed
+//      FP64 entries per cell.
 // Every mbarrier wait is bounded; a wait that runs out sets an error word (checked by the host
 // after the launch) and the kernel finishes without further tensor-core work, freeing its TMEM.
 #include <cuda_bf16.h>
@@ -254,6 +255,19 @@ __global__ void __launch_bounds__(128) k_tc_selftest(float* __restrict__ out, un
 }
 
 
+// f 2^k as an FP64 value on the integer pipes: the float's sign, exponent and mantissa moved
+// into the double layout (exact); zeros, subnormals and exponents that would leave the normal
+// range take the FP64 conversion and scaling instead. -1022 <= k <= 1023.
+__device__ __forceinline__ double tc_scaled_f64(float f, int k) {
+    const uint32_t u = __float_as_uint(f);
+    const int e = (int)((u >> 23) & 0xffu);
+    const int ed = e - 127 + 1023 + k;
+    if (e == 0 || e == 255 || ed <= 0 || ed >= 2047)
+        return (double)f * __longlong_as_double((long long)(k + 1023) << 52);
+    const uint64_t d = ((uint64_t)(u >> 31) << 63) | ((uint64_t)ed << 52) | ((uint64_t)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)d);
+}
+
 // ------------------------------------------------------------------ element matrices
 // the six packed symmetric M entries in K order: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2)
 __global__ void __launch_bounds__(kTcThreads, 1)
@@ -466,8 +480,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         for (int j = 0; j < 8; ++j) {
                             const int e = nt * kTcN + col + j;
                             if (e < 378) {
-                                const double scale = __longlong_as_double((long long)(e_c + __ldg(texp + e) + 1023) << 52);
-                                ke[378 * (size_t)c + e] = ((double)hi[j] + (double)lo[j]) * scale;
+                                // (hi + lo) 2^k: both parts scaled exactly, one FP64 add (exact:
+                                // the pair spans fewer than 53 bits)
+                                const int k = e_c + __ldg(texp + e);
+                                ke[378 * (size_t)c + e] = tc_scaled_f64(hi[j], k) + tc_scaled_f64(lo[j], k);
                             }
                         }
                 }
