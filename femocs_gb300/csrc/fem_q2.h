@@ -9,9 +9,10 @@ namespace fgb {
 
 // 378 packed upper-triangle entries per cell
 void q2_cell_stiffness(int nc, const int32_t* cell_dofs, const double* dof_xyz, double* ke, cudaStream_t s);
-// the same 378 entries per cell on the tensor cores (q2_ke_tc.cu): per-cell factors in FP64,
-// error-free BF16 slices, tcgen05 products with FP32 accumulators in tensor memory, levels
-// combined in FP64; scratch (per persistent CTA) and err are the caller's reusable buffers
+// the same 378 entries per cell on the tensor cores (q2_ke_tc.cu): per-point factors in
+// double-float arithmetic, error-free BF16 slices, tcgen05 products with FP32 accumulators in
+// tensor memory, levels combined into FP64; scratch (per persistent CTA) and err are the
+// caller's reusable buffers
 void q2_cell_stiffness_tc(int nc, const int32_t* cell_dofs, const double* dof_xyz, double* ke,
                           DBuf<unsigned char>& scratch, DBuf<unsigned>& err, cudaStream_t s);
 // geometric factors of the matrix-free level-0 smoother, block order (position p = cell

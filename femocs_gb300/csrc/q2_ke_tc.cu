@@ -20,10 +20,11 @@
 // gives 5e-14 of max |K_e| on the nanotip meshes).
 //
 // One persistent CTA (256 threads) per SM, tiles of 128 cells:
-//   1  the threads compute C in FP64 (Jacobians of the trilinear map at the 27 Gauss points),
-//      keep it in shared memory, find each row's exponent and write the six BF16 slices of
-//      their rows into this CTA's global scratch, already in the K-major core-matrix layout
-//      the MMA reads (8 rows x 16 bytes per core matrix, no swizzle);
+//   1  the threads compute C (Jacobians of the trilinear map at the 27 Gauss points, in
+//      double-float arithmetic on FP32 pairs, ~48 bits: GB300's FP64 pipe runs at 1/64 of
+//      FP32), keep it in shared memory as FP64, find each row's exponent and write the six
+//      BF16 slices of their rows into this CTA's global scratch, already in the K-major
+//      core-matrix layout the MMA reads (8 rows x 16 bytes per core matrix, no swizzle);
 //   2  for each of 8 N-tiles of 48 entries, one thread moves the N-tile's six T slices and, one
 //      after another, the six C slices into shared memory with cp.async.bulk (mbarrier
 //      complete_tx) and issues tcgen05.mma (M = 128, N = 48, K = 16, BF16 in, FP32 in TMEM);
@@ -73,11 +74,14 @@ constexpr size_t kTcOffExp = kTcOffD1;                                  // 19148
 constexpr size_t kTcOffBar = kTcOffExp + kTcM * sizeof(int);            // 197184
 constexpr size_t kTcOffTmem = kTcOffBar + 8 * sizeof(uint64_t);         // 197248
 constexpr size_t kTcSmem = kTcOffTmem + 16;
-// phase 1 keeps C (128 x 162) and the cells' trilinear coefficients (128 x 24) in the T and C regions
-static_assert(kTcM * (162 + 24) * sizeof(double) <= kTcOffD1, "phase 1 data in the T and C regions");
+// phase 1 keeps C (128 x 162) and the cells' scaled trilinear coefficients (128 x 21 pairs) in the
+// T and C regions
+static_assert(kTcM * (162 * sizeof(double) + 21 * sizeof(float2) + sizeof(int)) <= kTcOffD1,
+              "phase 1 data in the T and C regions");
 static_assert(kTcSmem <= 232448, "shared memory per CTA");
 
 __constant__ double c_tc_w[27];
+__constant__ float2 c_tc_wdf[27];        // the same weights as FP32 (hi, lo) pairs
 __constant__ int c_tc_corner[8];         // lattice index of femocs corner k
 
 // ------------------------------------------------------------------ PTX wrappers
@@ -255,6 +259,39 @@ __global__ void __launch_bounds__(128) k_tc_selftest(float* __restrict__ out, un
 }
 
 
+// ---- double-float arithmetic (an FP32 pair hi + lo, ~48 bits) for the per-point factors:
+// error-free sums (Knuth's TwoSum) and products (FMA), renormalised after each operation.
+// The intrinsics keep the compiler from contracting the error terms.
+struct Df {
+    float h, l;
+};
+__device__ __forceinline__ Df df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ Df df_fast_two_sum(float a, float b) {  // |a| >= |b| or a = 0
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ Df df_add(Df a, Df b) {
+    Df s = df_two_sum(a.h, b.h);
+    const Df t = df_two_sum(a.l, b.l);
+    s = df_fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+    return df_fast_two_sum(s.h, __fadd_rn(s.l, t.l));
+}
+__device__ __forceinline__ Df df_neg(Df a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ Df df_mul(Df a, Df b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return df_fast_two_sum(p, e);
+}
+// a b - c d
+__device__ __forceinline__ Df df_mul_sub(Df a, Df b, Df c, Df d) { return df_add(df_mul(a, b), df_neg(df_mul(c, d))); }
+// s a for s in {-1, 0, 1} (exact)
+__device__ __forceinline__ Df df_sgn(int s, Df a) { return s > 0 ? a : (s < 0 ? df_neg(a) : Df{0.f, 0.f}); }
+
 // f 2^k as an FP64 value on the integer pipes: the float's sign, exponent and mantissa moved
 // into the double layout (exact); zeros, subnormals and exponents that would leave the normal
 // range take the FP64 conversion and scaling instead. -1022 <= k <= 1023.
@@ -278,7 +315,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     unsigned char* sT = sm + kTcOffT;
     unsigned char* sA = sm + kTcOffA;
     double* sC = reinterpret_cast<double*>(sm);  // phase 1 only: 128 x 162 over the T and C regions
-    double* sF = sC + kTcM * 162;  // phase 1: trilinear coefficients f0..f7 (x, y, z) per cell
+    // phase 1: per cell the trilinear coefficients f1..f7 (x, y, z), scaled by 2^-s with s the
+    // exponent of the largest, as FP32 pairs, and s
+    float2* sFd = reinterpret_cast<float2*>(sC + kTcM * 162);
+    int* sFs = reinterpret_cast<int*>(sFd + kTcM * 21);
     int* sExp = reinterpret_cast<int*>(sm + kTcOffExp);
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kTcOffBar);  // 0 T, 1-2 C full, 3-4 C free, 5 done
     uint32_t* sTmem = reinterpret_cast<uint32_t*>(sm + kTcOffTmem);
@@ -301,11 +341,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const int c0 = tile * kTcM;
         // ---- 1a: the trilinear map x = f0 + f1 xi + f2 eta + f3 zeta + f4 xi eta + f5 xi zeta +
-        // f6 eta zeta + f7 xi eta zeta of each cell (femocs corner signs), then C in FP64 per
-        // (cell, Gauss point): J columns d x / d xi = f1 + f4 eta + f5 zeta + f7 eta zeta, ...
+        // f6 eta zeta + f7 xi eta zeta of each cell (femocs corner signs) in FP64, scaled and
+        // kept as FP32 pairs; then C per (cell, Gauss point)
         if (tid < kTcM) {
             const int c = c0 + tid;
-            double* F = sF + 24 * tid;
+            double F[24];
+#pragma unroll
             for (int r = 0; r < 24; ++r) F[r] = 0.0;
             if (c < nc) {
                 const int hx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, hy[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
@@ -323,6 +364,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     }
                 }
             }
+            // scale by the largest |f1..f7| (its exponent, by the bit pattern), then FP32 pairs
+            unsigned long long mx = 0;
+#pragma unroll
+            for (int r = 3; r < 24; ++r)
+                mx = max(mx, (unsigned long long)__double_as_longlong(F[r]) & 0x7FFFFFFFFFFFFFFFull);
+            const int sc = mx == 0 ? 0 : (int)(mx >> 52) - 1023;
+            const double down = __longlong_as_double((long long)(1023 - sc) << 52);
+#pragma unroll
+            for (int r = 3; r < 24; ++r) {
+                const double v = F[r] * down;
+                const float h = (float)v;
+                sFd[21 * tid + r - 3] = make_float2(h, (float)(v - (double)h));
+            }
+            sFs[tid] = sc;
         }
         __syncthreads();
         for (int it = tid; it < kTcM * 27; it += kTcThreads) {
@@ -332,41 +387,57 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 for (int m = 0; m < 6; ++m) out[m] = 0.0;
                 continue;
             }
-            const double g = 0.77459666924148337704;  // sqrt(3/5)
-            const double xi = (q % 3 - 1) * g, eta = ((q / 3) % 3 - 1) * g, ze = (q / 9 - 1) * g;
-            const double* F = sF + 24 * cl;
-            double J[3][3];
+            // per (cell, Gauss point) in double-float, on the scaled coefficients f' = f 2^-s:
+            // J columns d x / d xi = f1 + f4 eta + f5 zeta + f7 eta zeta, ... with the Gauss
+            // coordinates sx g, sy g, sz g (g = sqrt(3/5), s in {-1, 0, 1}); then
+            // C = w |det J| J^-1 J^-T = (w / |det J|) adj(J) adj(J)^T, which scales as a length:
+            // C = C' 2^s
+            const int sx = q % 3 - 1, sy = (q / 3) % 3 - 1, sz = q / 9 - 1;
+            // sqrt(3/5) and 3/5 as FP32 pairs (hi = the FP32 rounding, lo = the remainder)
+            const Df g = {0x1.8c97f0p-1f, -0x1.7811b8p-26f}, g2 = {0x1.333334p-1f, -0x1.99999ap-26f};
+            const float2* Fp = sFd + 21 * cl;
+            auto f = [&](int r, int a) {  // coefficient f_r, component a
+                const float2 v = Fp[3 * (r - 1) + a];
+                return Df{v.x, v.y};
+            };
+            Df J[3][3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                J[a][0] = fma(F[21 + a], eta * ze, fma(F[15 + a], ze, fma(F[12 + a], eta, F[3 + a])));
-                J[a][1] = fma(F[21 + a], xi * ze, fma(F[18 + a], ze, fma(F[12 + a], xi, F[6 + a])));
-                J[a][2] = fma(F[21 + a], xi * eta, fma(F[18 + a], eta, fma(F[15 + a], xi, F[9 + a])));
+                // d/d xi: f1 + g (sy f4 + sz f5) + g^2 sy sz f7, and the same pattern for eta, zeta
+                J[a][0] = df_add(df_add(f(1, a), df_mul(g, df_add(df_sgn(sy, f(4, a)), df_sgn(sz, f(5, a))))),
+                                 df_mul(g2, df_sgn(sy * sz, f(7, a))));
+                J[a][1] = df_add(df_add(f(2, a), df_mul(g, df_add(df_sgn(sx, f(4, a)), df_sgn(sz, f(6, a))))),
+                                 df_mul(g2, df_sgn(sx * sz, f(7, a))));
+                J[a][2] = df_add(df_add(f(3, a), df_mul(g, df_add(df_sgn(sx, f(5, a)), df_sgn(sy, f(6, a))))),
+                                 df_mul(g2, df_sgn(sx * sy, f(7, a))));
             }
-            // C = w |det J| J^-1 J^-T = (w / |det J|) adj(J) adj(J)^T: one reciprocal instead of a
-            // division and a scaled inverse, on GB300's reduced-rate FP64 pipe. 1 / |det J| by
-            // Newton-Raphson (y <- y (2 - a y), the error squares each step) from the FP32
-            // reciprocal: 2^-23, 2^-46, then FP64 rounding after two steps
-            double adj[3][3];  // J^-1 = adj / det, adj[k][a] for d xi_k / d x_a
-            adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-            adj[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-            adj[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-            adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
-            adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
-            adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
-            adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
-            adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
-            adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-            const double ad = fabs(J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0]);
-            double y = (double)(1.0f / (float)ad);
-            y = y * fma(-ad, y, 2.0);
-            y = y * fma(-ad, y, 2.0);
-            const double sw = c_tc_w[q] * y;
+            Df adj[3][3];  // J^-1 = adj / det, adj[k][a] for d xi_k / d x_a
+            adj[0][0] = df_mul_sub(J[1][1], J[2][2], J[1][2], J[2][1]);
+            adj[1][0] = df_mul_sub(J[1][2], J[2][0], J[1][0], J[2][2]);
+            adj[2][0] = df_mul_sub(J[1][0], J[2][1], J[1][1], J[2][0]);
+            adj[0][1] = df_mul_sub(J[0][2], J[2][1], J[0][1], J[2][2]);
+            adj[1][1] = df_mul_sub(J[0][0], J[2][2], J[0][2], J[2][0]);
+            adj[2][1] = df_mul_sub(J[0][1], J[2][0], J[0][0], J[2][1]);
+            adj[0][2] = df_mul_sub(J[0][1], J[1][2], J[0][2], J[1][1]);
+            adj[1][2] = df_mul_sub(J[0][2], J[1][0], J[0][0], J[1][2]);
+            adj[2][2] = df_mul_sub(J[0][0], J[1][1], J[0][1], J[1][0]);
+            Df det = df_add(df_add(df_mul(J[0][0], adj[0][0]), df_mul(J[0][1], adj[1][0])), df_mul(J[0][2], adj[2][0]));
+            if (det.h < 0.f) det = df_neg(det);
+            // 1 / |det J|: the FP32 reciprocal, then one Newton-Raphson step in double-float
+            // (y + y (1 - d y); the error squares: 2^-23 -> 2^-46)
+            const Df y0 = {__frcp_rn(det.h), 0.f};
+            const Df e1 = df_add(Df{1.f, 0.f}, df_neg(df_mul(det, y0)));
+            const Df y = df_add(y0, df_mul(y0, e1));
+            const float2 wq = c_tc_wdf[q];
+            const Df sw = df_mul(Df{wq.x, wq.y}, y);
             const int kk[6] = {0, 1, 2, 0, 0, 1}, ll[6] = {0, 1, 2, 1, 2, 2};
+            const int sc = sFs[cl];
 #pragma unroll
             for (int m = 0; m < 6; ++m) {
-                const double mk = adj[kk[m]][0] * adj[ll[m]][0] + adj[kk[m]][1] * adj[ll[m]][1] +
-                                  adj[kk[m]][2] * adj[ll[m]][2];
-                out[m] = sw * mk;
+                const Df mk = df_add(df_add(df_mul(adj[kk[m]][0], adj[ll[m]][0]), df_mul(adj[kk[m]][1], adj[ll[m]][1])),
+                                     df_mul(adj[kk[m]][2], adj[ll[m]][2]));
+                const Df v = df_mul(sw, mk);
+                out[m] = tc_scaled_f64(v.h, sc) + tc_scaled_f64(v.l, sc);
             }
         }
         __syncthreads();
@@ -583,6 +654,12 @@ TcTables& tc_tables() {
         t->tsl.upload(tsl);
         t->texp.upload(texp);
         FGB_CUDA(cudaMemcpyToSymbol(c_tc_w, w.data(), sizeof(double) * w.size()));
+        std::vector<float2> wdf(w.size());
+        for (size_t q = 0; q < w.size(); ++q) {
+            const float h = (float)w[q];
+            wdf[q] = make_float2(h, (float)(w[q] - (double)h));
+        }
+        FGB_CUDA(cudaMemcpyToSymbol(c_tc_wdf, wdf.data(), sizeof(float2) * wdf.size()));
         FGB_CUDA(cudaMemcpyToSymbol(c_tc_corner, corner.data(), sizeof(int) * corner.size()));
         FGB_CUDA(cudaFuncSetAttribute(k_q2_ke_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
         FGB_CUDA(cudaDeviceSynchronize());

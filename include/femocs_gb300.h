@@ -205,9 +205,10 @@ int fgb_field_set_level_smoothing(FGB_FIELD* f, int level, int degree, double lo
  * (rel_tol below 1e-10), a nonzero Dirichlet value. The default multigrid PCG over the cell
  * blocks takes D^-1 and its FP64 true residual from the element matrices */
 int fgb_field_set_lazy_matrix(FGB_FIELD* f, int on);
-/* Q2 fields: element matrices of the full assembly on the tensor cores (1, default: per-cell
- * factors in FP64, error-free BF16 slices, tcgen05 products accumulated exactly in FP32, levels
- * combined as FP32 pairs into FP64) or on the FP32 pipe as FP32 hi/lo pairs (0) */
+/* Q2 fields: element matrices of the full assembly on the tensor cores (1, default: per-point
+ * factors in double-float arithmetic (~48 bits), error-free BF16 slices, tcgen05 products
+ * accumulated exactly in FP32, levels combined as FP32 pairs into FP64) or on the FP32 pipe as
+ * FP32 hi/lo pairs (0) */
 int fgb_field_set_ke_tensor(FGB_FIELD* f, int on);
 /* element matrices of the last full assembly (Q1: 64 per cell; Q2: 378 packed upper-triangle
  * entries per cell, row by row); returns the number of values (out may be NULL), -1 on error */
