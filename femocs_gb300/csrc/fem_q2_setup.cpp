@@ -238,11 +238,12 @@ FemStructure build_q2_structure(const PreparedMesh& pm, bool sell_columns) {
     std::vector<double> exyz(3 * (size_t)n_ent);
 #pragma omp parallel for schedule(static)
     for (int e = 0; e < n_ent; ++e) {
-        int cr[8];
-        const int n = corners_of(e_loc[e], cr);
+        const int L = e_loc[e], n = n_corner[L];  // the lattice corners of L, tabulated above
+        int32_t nd[8];
+        for (int q = 0; q < n; ++q) nd[q] = cell_node(e_cell[e], corner_tab[L][q]);
         for (int d = 0; d < 3; ++d) {
             double s = 0.0;
-            for (int q = 0; q < n; ++q) s += X[3 * (size_t)cell_node(e_cell[e], cr[q]) + d];
+            for (int q = 0; q < n; ++q) s += X[3 * (size_t)nd[q] + d];
             exyz[3 * (size_t)e + d] = s / n;
         }
     }
