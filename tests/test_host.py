@@ -142,6 +142,10 @@ def test_structure_builders_do_not_depend_on_thread_count():
         outs.append(subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True,
                                    timeout=300).stdout.strip())
     assert outs[0] == outs[1] and outs[0].startswith("[")
+    # and the structures themselves are pinned: the numbering (Morton order, windows by row
+    # length) and every table of this mesh, for Q1 vacuum, Q1 bulk and Q2
+    pinned = [0x91bc05e014367b7f, 0x45728c20f1713063, 0xe384d55500756846]
+    assert [int(v) & 0xffffffffffffffff for v in eval(outs[0])] == pinned
 
 
 @pytest.mark.parametrize("cells,max_dofs", [(256, 4096), (64, 1024), (16, 200), (1, 27)])
